@@ -1,0 +1,555 @@
+// CPU oracle for the batched alignment solve -- TEST INFRASTRUCTURE ONLY.
+//
+// A plain scalar C++ restatement of the recurrences, tie rules, seeds, traceback walk,
+// path compression and all-optimal DFS of pyalign's DP core (pyalign/algorithm/solver.h,
+// pyalign 0.4.4).  It is the checker for the CUDA path: only tests/, the smoke check and
+// the CPU-baseline leg of bench.py load it.  Nothing in the product links or calls it.
+//
+// Parity pin: the reference's own known-answer tests (pyalign/tests/*.py) run on this
+// oracle through oracle/algorithm.py (tests/golden/make_golden.py); global/local linear,
+// affine (max and min), general (log) gap and lane batching are pinned that way.
+// Semiglobal, DTW, score-only and the Solution codomain are pinned only by this
+// restatement (the reference's tests do not cover them).
+//
+// Every value is a float32, as in the reference (module.cpp:11-14 instantiates
+// Options<float, int16_t/int32_t>); both optimisation directions are implemented natively
+// (no negation trick), so the oracle independently checks the GPU path's
+// "minimize == -maximize(-x)" rewrite.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <stack>
+#include <unordered_set>
+#include <vector>
+
+namespace {
+
+constexpr int32_t NO_TB = std::numeric_limits<int32_t>::min();  // solver.h:182-185
+
+struct Pt {
+	int32_t u, v;
+	bool operator==(const Pt &o) const { return u == o.u && v == o.v; }
+};
+
+enum { DIR_MIN = 0, DIR_MAX = 1 };                       // enum.h:13-16
+enum { LOC_LOCAL = 0, LOC_GLOBAL = 1, LOC_SEMIGLOBAL = 2 };  // enum.h:28-32
+enum { GAP_LINEAR = 0, GAP_AFFINE = 1, GAP_GENERAL = 2 };
+enum { TYPE_ALIGNMENT = 0, TYPE_DTW = 1 };
+enum { GOAL_SCORE = 0, GOAL_ONE = 1, GOAL_ALL = 2 };     // solver.h:13-39
+
+}  // namespace
+
+extern "C" {
+
+// Options as resolved by the reference's FactoryCreator (factory.h:1036-1241).
+typedef struct {
+	int32_t type;        // 0 alignment, 1 dtw
+	int32_t direction;   // 0 minimize, 1 maximize
+	int32_t detail;      // 0 score, 1 alignment, 2 solution
+	int32_t count;       // 0 one, 1 all
+	int32_t locality;    // 0 local, 1 global, 2 semiglobal
+	int32_t remove_dup;  // options.h:21 (= not return_dup)
+	int32_t gap_kind;    // 0 linear, 1 affine, 2 general (factory.h:1112-1135)
+	float linear_s, linear_t;
+	float affine_u_s, affine_v_s, affine_u_t, affine_v_t;  // Gotoh w(k) = u k + v (solver.h:2858-2881)
+	const float *general_s;  // cap_s + 1 costs (GapCost.costs(n), factory.h:20-31)
+	const float *general_t;  // cap_t + 1 costs
+	int32_t cap_s, cap_t;    // solver capacity (create_solver max_len_s/max_len_t)
+} pao_options;
+
+}  // extern "C"
+
+namespace {
+
+struct Dir {
+	bool maximize;
+	float worst() const {  // solver.h:62-65, 88-91
+		return maximize ? -std::numeric_limits<float>::infinity() : std::numeric_limits<float>::infinity();
+	}
+	bool is_opt(float a, float b) const { return maximize ? (a > b) : (a < b); }  // solver.h:53-56, 79-82
+	float opt(float a, float b) const { return is_opt(a, b) ? a : b; }
+	float sgn() const { return maximize ? -1.0f : 1.0f; }  // gap_sgn, solver.h:2807
+};
+
+// One traceback cell.  In "one" mode (traceback_1, solver.h:196-278) the list holds at most
+// one point and a cleared cell is {NO_TB, NO_TB} with size 0; in "all" mode (traceback_n,
+// solver.h:280-374) it is a list that can hold {NO_TB, NO_TB} as a real entry (the local
+// zero candidate, solver.h:2006-2011).
+struct TB {
+	std::vector<Pt> pts;
+};
+
+// A layer of values and traceback cells with the reference's (-1)-shifted indexing.
+struct Layer {
+	int32_t ls = 0, lt = 0;
+	std::vector<float> val;
+	std::vector<TB> tb;
+	void init(int32_t s, int32_t t, float fill) {
+		ls = s; lt = t;
+		val.assign(size_t(s + 1) * size_t(t + 1), fill);
+		tb.assign(size_t(s + 1) * size_t(t + 1), TB());
+	}
+	size_t idx(int32_t i, int32_t j) const { return size_t(i + 1) * size_t(lt + 1) + size_t(j + 1); }
+	float &V(int32_t i, int32_t j) { return val[idx(i, j)]; }
+	float V(int32_t i, int32_t j) const { return val[idx(i, j)]; }
+	TB &T(int32_t i, int32_t j) { return tb[idx(i, j)]; }
+	const TB &T(int32_t i, int32_t j) const { return tb[idx(i, j)]; }
+};
+
+// The accumulators of solver.h:1226-1427: the first push initialises, later pushes replace
+// only when strictly better (direction::opt_q); in "all" mode, equal values append.
+struct Acc {
+	const Dir &dir;
+	int goal;
+	float &val;
+	TB &tb;
+
+	void init(float v, Pt p) {
+		val = v;
+		if (goal != GOAL_SCORE) {
+			tb.pts.clear();
+			if (goal == GOAL_ALL || p.u != NO_TB) tb.pts.push_back(p);
+		}
+	}
+	void init(float v, const TB &t) {
+		val = v;
+		if (goal != GOAL_SCORE) tb.pts = t.pts;
+	}
+	void push(float v, Pt p) {
+		if (goal == GOAL_SCORE) {
+			val = dir.opt(v, val);
+			return;
+		}
+		if (dir.is_opt(v, val)) {
+			init(v, p);
+		} else if (goal == GOAL_ALL && v == val) {
+			tb.pts.push_back(p);
+		}
+	}
+	void push(float v, const TB &t) {
+		if (goal == GOAL_SCORE) {
+			val = dir.opt(v, val);
+			return;
+		}
+		if (dir.is_opt(v, val)) {
+			init(v, t);
+		} else if (goal == GOAL_ALL && v == val) {
+			for (const auto &p : t.pts) tb.pts.push_back(p);
+		}
+	}
+};
+
+// xt::linspace<float>(start, stop, n): start + step * i, step = (stop - start) / (n - 1).
+// This is the assumed semantics of the xtensor generator used by AffineCost::vector
+// (solver.h:2876-2880); it is exact for integer costs.
+std::vector<float> affine_vector(float u, float v, size_t n) {
+	std::vector<float> w(n);
+	const float stop = float(n - 1) * u;
+	const float step = n > 1 ? (stop - 0.0f) / float(n - 1) : 0.0f;
+	for (size_t i = 0; i < n; i++) w[i] = (0.0f + step * float(i)) + v;
+	if (n > 0) w[0] = 0;
+	return w;
+}
+
+struct Alignment {
+	bool has = false;    // false when the traceback iterator produced nothing
+	int32_t ls = 0, lt = 0;
+	float score = 0;
+	std::vector<int32_t> map;  // s_to_t if ls <= lt else t_to_s (factory.h:149-170)
+	std::vector<Pt> path;      // build_path (solver.h:858-938)
+};
+
+// path_compressor (solver.h:809-847): emits the previous point when a step changes both
+// coordinates and that point is non-negative.
+void compress_path(const std::vector<Pt> &path, Alignment &a) {
+	a.map.assign(a.ls <= a.lt ? size_t(a.ls) : size_t(a.lt), -1);
+	bool empty = true;
+	Pt last{0, 0};
+	for (const auto &p : path) {
+		if (empty) {
+			empty = false;
+		} else if (p.u != last.u && p.v != last.v) {
+			if (last.u >= 0 && last.v >= 0) {
+				if (a.ls <= a.lt) a.map[size_t(last.u)] = last.v;
+				else a.map[size_t(last.v)] = last.u;
+			}
+		}
+		last = p;
+	}
+}
+
+std::vector<Pt> compressed_points(const std::vector<Pt> &path) {
+	std::vector<Pt> out;
+	bool empty = true;
+	Pt last{0, 0};
+	for (const auto &p : path) {
+		if (empty) {
+			empty = false;
+		} else if (p.u != last.u && p.v != last.v) {
+			if (last.u >= 0 && last.v >= 0) out.push_back(last);
+		}
+		last = p;
+	}
+	return out;
+}
+
+struct PathHash {
+	size_t operator()(const std::vector<Pt> &v) const {
+		size_t seed = 0;
+		for (const auto &p : v) {
+			seed ^= std::hash<int32_t>()(p.u) + 0x9e3779b9 + (seed << 6) + (seed >> 2);
+			seed ^= std::hash<int32_t>()(p.v) + 0x9e3779b9 + (seed << 6) + (seed >> 2);
+		}
+		return seed;
+	}
+};
+
+struct Problem {
+	pao_options o;
+	Dir dir;
+	int goal;
+	int32_t ls, lt;
+	std::vector<float> sim;  // ls x lt row-major
+	std::vector<float> gen_s, gen_t;
+	std::vector<Layer> layers;  // D (, P, Q)
+
+	// traceback strategy (solver.h:2094-2124, 2190-2220, 2296-2326)
+	bool cont1(int32_t u, int32_t v) const { return u >= 0 && v >= 0; }
+	bool cont2(float val) const {
+		if (o.type == TYPE_ALIGNMENT && o.locality == LOC_LOCAL) return dir.is_opt(val, 0.0f);
+		return true;
+	}
+	bool has_trace() const { return goal != GOAL_SCORE; }
+	float s(int32_t i, int32_t j) const { return sim[size_t(i) * size_t(lt) + size_t(j)]; }
+
+	// seeds pushed onto a LIFO stack (solver.h:1937-2092, 2174-2188, 2266-2294)
+	std::vector<Pt> seeds() const {
+		std::vector<Pt> out;
+		const Layer &D = layers[0];
+		const int loc = o.type == TYPE_DTW ? LOC_GLOBAL : o.locality;
+		if (loc == LOC_GLOBAL) {
+			out.push_back(Pt{ls - 1, lt - 1});
+		} else if (loc == LOC_LOCAL && goal == GOAL_ALL) {
+			float best = 0.0f;
+			for (int32_t i = ls - 1; i >= 0; i--)
+				for (int32_t j = lt - 1; j >= 0; j--) best = dir.opt(D.V(i, j), best);
+			for (int32_t i = ls - 1; i >= 0; i--)
+				for (int32_t j = lt - 1; j >= 0; j--) {
+					const float x = D.V(i, j);
+					if (x == best && dir.is_opt(x, 0.0f)) out.push_back(Pt{i, j});
+				}
+		} else {
+			// Optima: strict replacement in scan order
+			float best = dir.worst();
+			Pt bp{0, 0};
+			auto add = [&](int32_t i, int32_t j) {
+				const float x = D.V(i, j);
+				if (dir.is_opt(x, best)) { best = x; bp = Pt{i, j}; }
+			};
+			if (loc == LOC_LOCAL) {
+				for (int32_t i = ls - 1; i >= 0; i--)
+					for (int32_t j = lt - 1; j >= 0; j--) add(i, j);
+			} else {
+				for (int32_t j = 0; j < lt; j++) add(ls - 1, j);
+				for (int32_t i = 0; i < ls; i++) add(i, lt - 1);
+			}
+			if (dir.is_opt(best, dir.worst())) out.push_back(bp);
+		}
+		return out;
+	}
+
+	void build_layers() {
+		const bool dtw = o.type == TYPE_DTW;
+		const int loc = dtw ? LOC_GLOBAL : o.locality;
+		const float sgn = dir.sgn();
+		const float worst = dir.worst();
+		const int nlayers = (!dtw && o.gap_kind == GAP_AFFINE) ? 3 : 1;
+		layers.assign(size_t(nlayers), Layer());
+		for (auto &L : layers) L.init(ls, lt, 0.0f);
+		Layer &D = layers[0];
+
+		if (dtw) {  // solver.h:3205-3210
+			for (auto &x : D.val) x = worst;
+			D.V(-1, -1) = 0.0f;
+		} else if (o.gap_kind == GAP_LINEAR) {  // solver.h:2806-2814
+			for (int32_t i = -1; i < ls; i++)
+				D.V(i, -1) = loc == LOC_GLOBAL ? (float(i + 1) * o.linear_s) * sgn : 0.0f;
+			for (int32_t j = -1; j < lt; j++)
+				D.V(-1, j) = loc == LOC_GLOBAL ? (float(j + 1) * o.linear_t) * sgn : 0.0f;
+		} else if (o.gap_kind == GAP_AFFINE) {  // solver.h:2918-2967
+			Layer &P = layers[1], &Q = layers[2];
+			const auto ws = affine_vector(o.affine_u_s, o.affine_v_s, size_t(o.cap_s) + 1);
+			const auto wt = affine_vector(o.affine_u_t, o.affine_v_t, size_t(o.cap_t) + 1);
+			for (int32_t i = -1; i < ls; i++) Q.V(i, -1) = worst;
+			for (int32_t j = -1; j < lt; j++) P.V(-1, j) = worst;
+			for (int32_t i = -1; i < ls; i++) {
+				const float x = loc == LOC_GLOBAL ? ws[size_t(i + 1)] * sgn : 0.0f;
+				D.V(i, -1) = x;
+				P.V(i, -1) = x;
+			}
+			for (int32_t j = -1; j < lt; j++) {
+				const float x = loc == LOC_GLOBAL ? wt[size_t(j + 1)] * sgn : 0.0f;
+				D.V(-1, j) = x;
+				Q.V(-1, j) = x;
+			}
+		} else {  // solver.h:3116-3125
+			for (int32_t i = -1; i < ls; i++)
+				D.V(i, -1) = loc == LOC_GLOBAL ? gen_s[size_t(i + 1)] * sgn : 0.0f;
+			for (int32_t j = -1; j < lt; j++)
+				D.V(-1, j) = loc == LOC_GLOBAL ? gen_t[size_t(j + 1)] * sgn : 0.0f;
+		}
+	}
+
+	void solve() {
+		build_layers();
+		const bool dtw = o.type == TYPE_DTW;
+		const bool local = !dtw && o.locality == LOC_LOCAL;
+		const float sgn = dir.sgn();
+		Layer &D = layers[0];
+
+		auto start = [&](float &val, TB &tb) {
+			Acc a{dir, goal, val, tb};
+			return a;
+		};
+
+		for (int32_t u = 0; u < ls; u++) {
+			for (int32_t v = 0; v < lt; v++) {
+				if (dtw) {  // solver.h:3233-3250
+					Acc a = start(D.V(u, v), D.T(u, v));
+					a.init(D.V(u - 1, v - 1), Pt{u - 1, v - 1});
+					a.push(D.V(u - 1, v), Pt{u - 1, v});
+					a.push(D.V(u, v - 1), Pt{u, v - 1});
+					D.V(u, v) += s(u, v);
+				} else if (o.gap_kind == GAP_LINEAR) {  // solver.h:2837-2854
+					Acc a = start(D.V(u, v), D.T(u, v));
+					bool first = true;
+					if (local) { a.init(0.0f, Pt{NO_TB, NO_TB}); first = false; }
+					const float dg = D.V(u - 1, v - 1) + s(u, v);
+					if (first) a.init(dg, Pt{u - 1, v - 1}); else a.push(dg, Pt{u - 1, v - 1});
+					a.push(D.V(u - 1, v) + o.linear_s * sgn, Pt{u - 1, v});
+					a.push(D.V(u, v - 1) + o.linear_t * sgn, Pt{u, v - 1});
+				} else if (o.gap_kind == GAP_AFFINE) {  // solver.h:2989-3035
+					Layer &P = layers[1], &Q = layers[2];
+					const float w1s = o.affine_u_s + o.affine_v_s;
+					const float w1t = o.affine_u_t + o.affine_v_t;
+					{
+						Acc a = start(P.V(u, v), P.T(u, v));
+						a.init(D.V(u - 1, v) + w1s * sgn, Pt{u - 1, v});
+						a.push(P.V(u - 1, v) + o.affine_u_s * sgn, P.T(u - 1, v));
+					}
+					{
+						Acc a = start(Q.V(u, v), Q.T(u, v));
+						a.init(D.V(u, v - 1) + w1t * sgn, Pt{u, v - 1});
+						a.push(Q.V(u, v - 1) + o.affine_u_t * sgn, Q.T(u, v - 1));
+					}
+					{
+						Acc a = start(D.V(u, v), D.T(u, v));
+						bool first = true;
+						if (local) { a.init(0.0f, Pt{NO_TB, NO_TB}); first = false; }
+						const float dg = D.V(u - 1, v - 1) + s(u, v);
+						if (first) a.init(dg, Pt{u - 1, v - 1}); else a.push(dg, Pt{u - 1, v - 1});
+						a.push(P.V(u, v), P.T(u, v));
+						a.push(Q.V(u, v), Q.T(u, v));
+					}
+				} else {  // solver.h:3153-3182
+					Acc a = start(D.V(u, v), D.T(u, v));
+					bool first = true;
+					if (local) { a.init(0.0f, Pt{NO_TB, NO_TB}); first = false; }
+					const float dg = D.V(u - 1, v - 1) + s(u, v);
+					if (first) a.init(dg, Pt{u - 1, v - 1}); else a.push(dg, Pt{u - 1, v - 1});
+					for (int32_t k = -1; k < u; k++)
+						a.push(D.V(k, v) + gen_s[size_t(u - k)] * sgn, Pt{k, v});
+					for (int32_t k = -1; k < v; k++)
+						a.push(D.V(u, k) + gen_t[size_t(v - k)] * sgn, Pt{u, k});
+				}
+			}
+		}
+	}
+
+	// TracebackIterators<false>::Iterator::next (solver.h:1497-1536) for one seed.
+	bool walk_one(Pt seed, float &score, std::vector<Pt> &path) const {
+		const Layer &D = layers[0];
+		int32_t u = seed.u, v = seed.v;
+		score = D.V(u, v);
+		path.clear();
+		if (!has_trace()) return true;
+		path.push_back(Pt{u, v});
+		while (cont1(u, v) && cont2(D.V(u, v))) {
+			const TB &t = D.T(u, v);
+			const int32_t nu = t.pts.empty() ? NO_TB : t.pts[0].u;
+			const int32_t nv = t.pts.empty() ? NO_TB : t.pts[0].v;
+			u = nu; v = nv;
+			path.push_back(Pt{u, v});
+		}
+		return true;
+	}
+
+	// --- all-optimal DFS state (solver.h:1582-1716) ---
+	struct Entry {
+		float path_val;
+		Pt cur;
+		int32_t path_len;
+	};
+	std::stack<Entry> stk;
+	std::vector<Pt> dfs_path;
+	std::unordered_set<std::vector<Pt>, PathHash> emitted;
+	bool iter_one_done = false;   // for max-degree-1 iterators (TracebackIterators<false>)
+	std::vector<Pt> one_seeds;
+
+	void init_iterator() {
+		const auto sd = seeds();
+		if (goal == GOAL_ALL) {
+			for (const auto &p : sd) stk.push(Entry{layers[0].V(p.u, p.v), p, 0});
+		} else {
+			one_seeds = sd;  // Stack1 keeps only the last pushed seed (solver.h:1429-1449)
+			if (one_seeds.size() > 1) one_seeds.erase(one_seeds.begin(), one_seeds.end() - 1);
+		}
+	}
+
+	bool next(float &score, std::vector<Pt> &path) {
+		if (goal != GOAL_ALL) {
+			if (one_seeds.empty()) return false;
+			const Pt sd = one_seeds.back();
+			one_seeds.pop_back();
+			walk_one(sd, score, path);
+			return true;
+		}
+		const Layer &D = layers[0];
+		while (!stk.empty()) {
+			const Entry e = stk.top();
+			stk.pop();
+			if (e.path_len == 0) dfs_path.clear();
+			else dfs_path.resize(size_t(e.path_len));
+			dfs_path.push_back(e.cur);
+			const int32_t u1 = e.cur.u, v1 = e.cur.v;
+			if (cont1(u1, v1) && cont2(D.V(u1, v1))) {
+				const TB &t = D.T(u1, v1);
+				const int32_t psize = int32_t(dfs_path.size());
+				if (!t.pts.empty()) {
+					for (const auto &p : t.pts) stk.push(Entry{e.path_val, p, psize});
+				} else {
+					stk.push(Entry{e.path_val, Pt{NO_TB, NO_TB}, psize});
+				}
+			} else {
+				if (o.remove_dup) {
+					auto cp = compressed_points(dfs_path);
+					if (emitted.count(cp)) continue;
+					emitted.insert(std::move(cp));
+				}
+				score = e.path_val;
+				path = dfs_path;
+				return true;
+			}
+		}
+		return false;
+	}
+};
+
+}  // namespace
+
+extern "C" {
+
+struct pao_result {
+	Problem p;
+	// result of the one-shot codomains
+	Alignment one;
+	float score = 0;
+	bool iterator = false;
+	// last iterator result
+	Alignment cur;
+	// solution data: values and traceback of the reported layers
+	int32_t sol_layers = 0;
+};
+
+// Solve one pair.  `sim` is the ls x lt similarity (or distance) matrix, row-major.
+pao_result *pao_solve(const pao_options *o, int32_t ls, int32_t lt, const float *sim) {
+	auto *r = new pao_result();
+	Problem &p = r->p;
+	p.o = *o;
+	p.dir = Dir{o->direction == DIR_MAX};
+	if (o->type == TYPE_DTW) p.goal = GOAL_ONE;  // factory.h:1055-1099
+	else if (o->count == 1) p.goal = GOAL_ALL;   // factory.h:1219-1233
+	else p.goal = o->detail == 0 ? GOAL_SCORE : GOAL_ONE;  // factory.h:1198-1216
+	p.ls = ls;
+	p.lt = lt;
+	p.sim.assign(sim, sim + size_t(ls) * size_t(lt));
+	if (o->type == TYPE_ALIGNMENT && o->gap_kind == GAP_GENERAL) {
+		p.gen_s.assign(o->general_s, o->general_s + o->cap_s + 1);
+		p.gen_t.assign(o->general_t, o->general_t + o->cap_t + 1);
+	}
+	p.solve();
+	p.init_iterator();
+	return r;
+}
+
+void pao_free(pao_result *r) { delete r; }
+
+int32_t pao_goal(const pao_result *r) { return r->p.goal; }
+int32_t pao_layer_count(const pao_result *r) { return int32_t(r->p.layers.size()); }
+
+// Advance the traceback iterator of this pair.  Returns 1 and fills score, the alignment
+// map (min(ls, lt) entries) and the full path (path_len points, up to ls + lt + 2) when a
+// result exists, 0 when exhausted.  For Score/Alignment/Solution (count ONE) this is the
+// single next() of Solver::score/alignment/solution (solver.h:2593-2705).
+int32_t pao_next(pao_result *r, float *score, int32_t *map, int32_t *path, int32_t *path_len) {
+	float sc = 0;
+	std::vector<Pt> pth;
+	if (!r->p.next(sc, pth)) return 0;
+	Alignment a;
+	a.ls = r->p.ls;
+	a.lt = r->p.lt;
+	compress_path(pth, a);
+	*score = sc;
+	if (map) std::memcpy(map, a.map.data(), a.map.size() * sizeof(int32_t));
+	if (path) {
+		for (size_t k = 0; k < pth.size(); k++) { path[2 * k] = pth[k].u; path[2 * k + 1] = pth[k].v; }
+	}
+	if (path_len) *path_len = int32_t(pth.size());
+	return 1;
+}
+
+float pao_worst(const pao_result *r) { return r->p.dir.worst(); }
+
+// Values of layer k, (ls+1) x (lt+1) row-major, including the border row/column.
+void pao_values(const pao_result *r, int32_t k, float *out) {
+	const auto &L = r->p.layers[size_t(k)];
+	std::memcpy(out, L.val.data(), L.val.size() * sizeof(float));
+}
+
+// First traceback entry per cell of layer k ((ls+1) x (lt+1) x 2), NO_TB where empty
+// (solver.h:2413-2431).
+void pao_tb_matrix(const pao_result *r, int32_t k, int32_t *out) {
+	const auto &L = r->p.layers[size_t(k)];
+	for (size_t c = 0; c < L.tb.size(); c++) {
+		const auto &t = L.tb[c];
+		out[2 * c] = t.pts.empty() ? NO_TB : t.pts[0].u;
+		out[2 * c + 1] = t.pts.empty() ? NO_TB : t.pts[0].v;
+	}
+}
+
+// All traceback entries of layer k as (n, 2, 2) edges ((i-1, j-1) -> (u, v)), in the
+// order of solver.h:2445-2479.  Call with out == nullptr to get n.
+int64_t pao_tb_edges(const pao_result *r, int32_t k, int32_t *out) {
+	const auto &L = r->p.layers[size_t(k)];
+	int64_t n = 0;
+	for (int32_t i = 0; i <= L.ls; i++) {
+		for (int32_t j = 0; j <= L.lt; j++) {
+			const auto &t = L.tb[size_t(i) * size_t(L.lt + 1) + size_t(j)];
+			for (const auto &p : t.pts) {
+				if (out) {
+					out[4 * n + 0] = i - 1;
+					out[4 * n + 1] = j - 1;
+					out[4 * n + 2] = p.u;
+					out[4 * n + 3] = p.v;
+				}
+				n++;
+			}
+		}
+	}
+	return n;
+}
+
+}  // extern "C"
