@@ -1,0 +1,254 @@
+/*
+ * pyalign_gb300 -- C ABI of the GB300 (sm_103a) batched alignment solve.
+ *
+ * This library replaces the native core of pyalign 0.4.4: the pybind11 module
+ * `pyalign.algorithm.<variant>.algorithm` (pyalign/algorithm/module.cpp:7-18), whose
+ * Solver interface is declared in pyalign/algorithm/factory.h:414-508 and registered in
+ * pyalign/algorithm/pyalign.h:17-77.  Each entry point below names the reference
+ * function it replaces.  All arguments are plain pointers and sizes; no torch or numpy
+ * types cross this boundary.  The Python binding (pyalign_gb300/algorithm.py, ctypes)
+ * re-exports the reference's Python names on top of it.
+ *
+ * Conventions
+ *  - Every function that can fail returns a pa_status; pa_last_error() gives the
+ *    message of the last failure on the calling thread.  PA_ERR_INVALID_ARGUMENT maps
+ *    to the reference's std::invalid_argument (Python ValueError); PA_ERR_LENGTH to its
+ *    exceeded_*_length exceptions (solver.h:95-152, Python RuntimeError).
+ *  - Arrays follow the reference's layouts: codes a/b are (batch, n_s) and (batch, n_t)
+ *    uint32 row-major (solve.py:402-404); a dense similarity is (n_s, n_t, batch) float32,
+ *    lane-minor (solve.py:349); lengths are (2, batch) int32: row 0 = |s|, row 1 = |t|.
+ *  - Values are float32 as in the reference (module.cpp:11-14); alignment maps, paths
+ *    and traceback matrices are int32 (the Python layer narrows them for m16).
+ *  - A solver is not re-entrant (like the reference, factory.h:682-973); results and
+ *    iterators own their data and stay valid after later solve calls.
+ *  - All device work of a solver runs on its CUDA stream (pa_solver_set_stream).
+ */
+#ifndef PYALIGN_GB300_H
+#define PYALIGN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t pa_status;
+#define PA_OK 0
+#define PA_ERR_INVALID_ARGUMENT 1
+#define PA_ERR_LENGTH 2
+#define PA_ERR_CUDA 3
+#define PA_ERR_NO_DEVICE 4
+#define PA_ERR_INTERNAL 5
+#define PA_ERR_TIMEOUT 6
+#define PA_ERR_UNSUPPORTED 7
+
+/* enums: values identical to pyalign/algorithm/enum.h:8-33 */
+#define PA_TYPE_ALIGNMENT 0
+#define PA_TYPE_DTW 1
+#define PA_MINIMIZE 0
+#define PA_MAXIMIZE 1
+#define PA_DETAIL_SCORE 0
+#define PA_DETAIL_ALIGNMENT 1
+#define PA_DETAIL_SOLUTION 2
+#define PA_COUNT_ONE 0
+#define PA_COUNT_ALL 1
+#define PA_LOCAL 0
+#define PA_GLOBAL 1
+#define PA_SEMIGLOBAL 2
+
+/* gap cost kinds, as resolved by FactoryCreator::resolve_gap_type (factory.h:1106-1136) */
+#define PA_GAP_LINEAR 0
+#define PA_GAP_AFFINE 1
+#define PA_GAP_GENERAL 2
+
+/* where caller buffers live */
+#define PA_HOST 0
+#define PA_DEVICE 1
+
+typedef struct pa_options {
+	int32_t type;        /* PA_TYPE_* (options.h:14-21) */
+	int32_t direction;   /* PA_MINIMIZE / PA_MAXIMIZE */
+	int32_t detail;      /* PA_DETAIL_* (options.h:25-36) */
+	int32_t count;       /* PA_COUNT_* */
+	int32_t locality;    /* PA_LOCAL / PA_GLOBAL / PA_SEMIGLOBAL */
+	int32_t remove_dup;  /* = not return_dup (options.h:21) */
+	int32_t batch;       /* options "batch" (solve.py:181) */
+	int32_t batch_size;  /* lanes per solve call when batch != 0; 0 = library default */
+	int32_t index_bits;  /* 16 for m16, 32 for m32 (module.cpp:10-14) */
+	int32_t gap_kind;    /* PA_GAP_*; ignored for DTW */
+	float linear_s, linear_t;                 /* linear: w(k) = g k */
+	float affine_u_s, affine_v_s;             /* affine, Gotoh form w(k) = u k + v (solver.h:2858-2881) */
+	float affine_u_t, affine_v_t;
+	const float *general_s;  /* general: GapCost.costs(max_len_s + 1) (factory.h:20-31), copied */
+	const float *general_t;  /* general: GapCost.costs(max_len_t + 1), copied */
+} pa_options;
+
+typedef struct pa_solver pa_solver;
+typedef struct pa_result pa_result;
+typedef struct pa_iterator pa_iterator;
+
+/* Last error message of the calling thread ("" if none). */
+const char *pa_last_error(void);
+
+/* Library version string. */
+const char *pa_version(void);
+
+/* Number of usable CUDA devices (0 when none: every solve then fails with
+ * PA_ERR_NO_DEVICE -- there is no CPU fallback). */
+int32_t pa_device_count(void);
+
+/* Replaces create_solver<Options> (factory.h:1268-1278): a solver for sequences up to
+ * max_len_s x max_len_t.  Fails with PA_ERR_LENGTH past the index type's limit
+ * (solver.h:496-503). */
+pa_status pa_solver_create(const pa_options *options, int64_t max_len_s, int64_t max_len_t,
+                           pa_solver **out);
+void pa_solver_destroy(pa_solver *solver);
+
+/* Replaces Solver::batch_size (factory.h:422, pyalign.h:25). */
+int32_t pa_solver_batch_size(const pa_solver *solver);
+
+/* Run the solver's device work on `stream` (a cudaStream_t; NULL = the solver's own
+ * non-blocking stream). */
+pa_status pa_solver_set_stream(pa_solver *solver, void *stream);
+
+/* ---- the 15 solve entry points (factory.h:424-507; pyalign.h:26-40) ----
+ * sim (dense): n_s x n_t x batch float32; a: batch x n_s, b: batch x n_t uint32;
+ * table: table_rows x table_cols float32; length: 2 x batch int32 (host memory).
+ * Score variants write `batch` float32 scores; all others return a pa_result.     */
+
+pa_status pa_solve_for_score(pa_solver *s, const float *sim, int64_t n_s, int64_t n_t,
+                             int64_t batch, const int32_t *length, float *scores);
+pa_status pa_solve_indexed_for_score(pa_solver *s, const uint32_t *a, const uint32_t *b,
+                                     int64_t batch, int64_t n_s, int64_t n_t,
+                                     const float *table, int64_t table_rows, int64_t table_cols,
+                                     const int32_t *length, float *scores);
+pa_status pa_solve_binary_for_score(pa_solver *s, const uint32_t *a, const uint32_t *b,
+                                    int64_t batch, int64_t n_s, int64_t n_t, float eq, float ne,
+                                    const int32_t *length, float *scores);
+
+pa_status pa_solve_for_alignment(pa_solver *s, const float *sim, int64_t n_s, int64_t n_t,
+                                 int64_t batch, const int32_t *length, pa_result **out);
+pa_status pa_solve_indexed_for_alignment(pa_solver *s, const uint32_t *a, const uint32_t *b,
+                                         int64_t batch, int64_t n_s, int64_t n_t,
+                                         const float *table, int64_t table_rows,
+                                         int64_t table_cols, const int32_t *length,
+                                         pa_result **out);
+pa_status pa_solve_binary_for_alignment(pa_solver *s, const uint32_t *a, const uint32_t *b,
+                                        int64_t batch, int64_t n_s, int64_t n_t, float eq,
+                                        float ne, const int32_t *length, pa_result **out);
+
+pa_status pa_solve_for_alignment_iterator(pa_solver *s, const float *sim, int64_t n_s,
+                                          int64_t n_t, int64_t batch, const int32_t *length,
+                                          pa_result **out);
+pa_status pa_solve_indexed_for_alignment_iterator(pa_solver *s, const uint32_t *a,
+                                                  const uint32_t *b, int64_t batch, int64_t n_s,
+                                                  int64_t n_t, const float *table,
+                                                  int64_t table_rows, int64_t table_cols,
+                                                  const int32_t *length, pa_result **out);
+pa_status pa_solve_binary_for_alignment_iterator(pa_solver *s, const uint32_t *a,
+                                                 const uint32_t *b, int64_t batch, int64_t n_s,
+                                                 int64_t n_t, float eq, float ne,
+                                                 const int32_t *length, pa_result **out);
+
+pa_status pa_solve_for_solution(pa_solver *s, const float *sim, int64_t n_s, int64_t n_t,
+                                int64_t batch, const int32_t *length, pa_result **out);
+pa_status pa_solve_indexed_for_solution(pa_solver *s, const uint32_t *a, const uint32_t *b,
+                                        int64_t batch, int64_t n_s, int64_t n_t,
+                                        const float *table, int64_t table_rows,
+                                        int64_t table_cols, const int32_t *length,
+                                        pa_result **out);
+pa_status pa_solve_binary_for_solution(pa_solver *s, const uint32_t *a, const uint32_t *b,
+                                       int64_t batch, int64_t n_s, int64_t n_t, float eq,
+                                       float ne, const int32_t *length, pa_result **out);
+
+pa_status pa_solve_for_solution_iterator(pa_solver *s, const float *sim, int64_t n_s,
+                                         int64_t n_t, int64_t batch, const int32_t *length,
+                                         pa_result **out);
+pa_status pa_solve_indexed_for_solution_iterator(pa_solver *s, const uint32_t *a,
+                                                 const uint32_t *b, int64_t batch, int64_t n_s,
+                                                 int64_t n_t, const float *table,
+                                                 int64_t table_rows, int64_t table_cols,
+                                                 const int32_t *length, pa_result **out);
+pa_status pa_solve_binary_for_solution_iterator(pa_solver *s, const uint32_t *a,
+                                                const uint32_t *b, int64_t batch, int64_t n_s,
+                                                int64_t n_t, float eq, float ne,
+                                                const int32_t *length, pa_result **out);
+
+/* ---- results: one per solve call, `batch` lanes ---- */
+void pa_result_destroy(pa_result *r);
+int64_t pa_result_size(const pa_result *r);
+int64_t pa_result_len_s(const pa_result *r, int64_t lane);
+int64_t pa_result_len_t(const pa_result *r, int64_t lane);
+
+/* Alignment of a lane (codomain Alignment or Solution): Alignment::score/s_to_t/t_to_s
+ * (factory.h:130-193).  `map` receives min(|s|, |t|) entries: s_to_t when |s| <= |t|,
+ * else t_to_s, -1 where unaligned.  has_alignment is 0 when the reference's traceback
+ * iterator yields nothing (local/semiglobal problems without cells); the score is then
+ * the direction's worst value. */
+int32_t pa_result_has_alignment(const pa_result *r, int64_t lane);
+float pa_result_score(const pa_result *r, int64_t lane);
+pa_status pa_result_alignment(const pa_result *r, int64_t lane, int32_t *map);
+
+/* Bulk export of all lanes: scores[batch]; maps concatenated at map_offsets[lane]
+ * (caller-computed prefix sums of min(|s|, |t|)). */
+pa_status pa_result_export(const pa_result *r, float *scores, int32_t *maps,
+                           const int64_t *map_offsets);
+
+/* Solution of a lane (core::Solution, solver.h:2329-2507; SolutionImpl factory.h:284-352).
+ * values: layers x (|s|+1) x (|t|+1) float32, the border row/column included.
+ * tb_matrix: layers x (|s|+1) x (|t|+1) x 2, first traceback entry per cell, INT32_MIN
+ * where none.  tb_edges: (n, 2, 2) per layer ((i-1, j-1) -> (u, v)); pass NULL to get n.
+ * path: (n, 2) points of the traceback walk (build_path, solver.h:858-938). */
+int32_t pa_result_layers(const pa_result *r, int64_t lane);
+int32_t pa_result_max_degree_1(const pa_result *r);
+pa_status pa_result_values(const pa_result *r, int64_t lane, float *values);
+pa_status pa_result_tb_matrix(const pa_result *r, int64_t lane, int32_t *tb);
+int64_t pa_result_tb_edges(const pa_result *r, int64_t lane, int32_t layer, int32_t *edges);
+int64_t pa_result_path(const pa_result *r, int64_t lane, int32_t *path);
+
+/* Solver metadata (AlgorithmMetaData, solver.h:154-177): name, runtime, memory. */
+const char *pa_result_algorithm(const pa_result *r, int32_t field);
+
+/* ---- iterators over all optimal alignments of a lane (AlignmentIterator,
+ * SolutionIterator: solver.h:1783-1888; TracebackIterators<true> 1568-1743).
+ * The iterator keeps the result alive.  next() returns 1 and fills score, map
+ * (min(|s|,|t|) entries) and, if path != NULL, the walk (path_len points, at most
+ * |s| + |t| + 2); 0 when exhausted. */
+pa_status pa_result_iterator(pa_result *r, int64_t lane, pa_iterator **out);
+int32_t pa_iterator_next(pa_iterator *it, float *score, int32_t *map, int32_t *path,
+                         int64_t *path_len);
+void pa_iterator_destroy(pa_iterator *it);
+
+/* ---- batched form: the whole bag in one call (no per-lane objects) ----
+ * Score plus one optimal traceback for `batch` pairs of uneven lengths, the throughput
+ * path behind ProblemBatch.  Inputs and outputs are host or device memory
+ * (`location`); lengths (2 x batch int32) are always host memory.  Outputs: scores
+ * (batch) and the maps concatenated at map_offsets (host array of batch entries,
+ * prefix sums of min(|s|, |t|)); maps may be NULL for score only. */
+typedef struct pa_batch {
+	int32_t form;       /* 0 dense, 1 indexed, 2 binary */
+	int32_t location;   /* PA_HOST or PA_DEVICE for a, b, table, sim, scores, maps */
+	int64_t batch, n_s, n_t;
+	const uint32_t *a;
+	const uint32_t *b;
+	const float *sim;   /* dense (n_s, n_t, batch) */
+	const float *table; /* indexed */
+	int64_t table_rows, table_cols;
+	float eq, ne;       /* binary */
+	const int32_t *length;  /* host (2, batch) */
+} pa_batch;
+
+pa_status pa_solve_batch(pa_solver *s, const pa_batch *batch, float *scores, int32_t *maps,
+                         const int64_t *map_offsets);
+
+/* Device time of the phases of the last solve on this solver, in milliseconds
+ * (0: upload, 1: DP kernels, 2: traceback kernels, 3: download), and the number of
+ * kernels launched.  Measured with CUDA events on the solver's stream. */
+pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYALIGN_GB300_H */

@@ -144,6 +144,7 @@ class Options:
         self.batch = bool(d["batch"])
         self.direction = Direction(int(d["direction"]))
         self.remove_dup = not bool(d["return_dup"])
+        self.batch_size = d.get("batch_size") if hasattr(d, "get") else None
         if self.type == Type.ALIGNMENT:
             cod = d["codomain"]
             self.detail = Detail(int(cod.detail))
@@ -350,7 +351,7 @@ class Solver:
                     f"requested maximum length {n} for {name} exceeds maximum supported "
                     f"sequence length in this implementation {lim}")
         self._cap_s, self._cap_t = int(max_len_s), int(max_len_t)
-        self._batch_size = self.LANES if options.batch else 1
+        self._batch_size = (int(options.batch_size or self.LANES)) if options.batch else 1
         o = options
         kinds = (o.gap_s[0], o.gap_t[0])
         if o.type == Type.DTW:

@@ -1,0 +1,666 @@
+"""Drop-in replacement for pyalign's native ``algorithm`` module, backed by the GB300 library.
+
+pyalign 0.4.4 obtains its compute core as ``algorithm = import_algorithm()``
+(pyalign/solve.py:18, pyalign/cpu.py:21-47), a pybind11 module whose names are registered
+in pyalign/algorithm/pyalign.h:17-102 and module.cpp:7-18.  This module exports the same
+names -- the enums, ``Algorithm``, and the ``m16``/``m32`` submodules with
+``create_options``/``create_solver``, ``Solver`` (15 ``solve_*`` methods, ``batch_size``,
+``options``), ``Alignment``, ``AlignmentIterator``, ``Solution``, ``SolutionIterator`` --
+with the same argument meaning and errors (ValueError for std::invalid_argument,
+RuntimeError for the length exceptions), over the C ABI of include/pyalign_gb300.h.
+
+Every solve runs on the GPU.  If the library is not built or no CUDA device is present,
+calls fail loudly; there is no CPU fallback.
+"""
+
+import ctypes
+import enum
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libpyalign_gb300.so")
+
+PA_OK, PA_ERR_INVALID_ARGUMENT, PA_ERR_LENGTH = 0, 1, 2
+
+_c_i32, _c_i64, _c_f32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_float
+_P = ctypes.c_void_p
+_PF = ctypes.POINTER(ctypes.c_float)
+_PI = ctypes.POINTER(ctypes.c_int32)
+_PU = ctypes.POINTER(ctypes.c_uint32)
+_PL = ctypes.POINTER(ctypes.c_int64)
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [
+        ("type", _c_i32), ("direction", _c_i32), ("detail", _c_i32), ("count", _c_i32),
+        ("locality", _c_i32), ("remove_dup", _c_i32), ("batch", _c_i32), ("batch_size", _c_i32),
+        ("index_bits", _c_i32), ("gap_kind", _c_i32),
+        ("linear_s", _c_f32), ("linear_t", _c_f32),
+        ("affine_u_s", _c_f32), ("affine_v_s", _c_f32), ("affine_u_t", _c_f32), ("affine_v_t", _c_f32),
+        ("general_s", _PF), ("general_t", _PF),
+    ]
+
+
+class Batch(ctypes.Structure):
+    """pa_batch of the C ABI (the bag-at-once form)."""
+    _fields_ = [
+        ("form", _c_i32), ("location", _c_i32), ("batch", _c_i64), ("n_s", _c_i64), ("n_t", _c_i64),
+        ("a", _PU), ("b", _PU), ("sim", _PF), ("table", _PF), ("table_rows", _c_i64),
+        ("table_cols", _c_i64), ("eq", _c_f32), ("ne", _c_f32), ("length", _PI),
+    ]
+
+
+_lib = None
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def lib():
+    """The loaded C library (built by pyalign_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise ImportError(
+                f"{_LIB_PATH} is missing: build it with `python -m pyalign_gb300.build` "
+                "(there is no CPU fallback)")
+        L = ctypes.CDLL(_LIB_PATH)
+        L.pa_last_error.restype = ctypes.c_char_p
+        L.pa_version.restype = ctypes.c_char_p
+        L.pa_device_count.restype = _c_i32
+        L.pa_solver_create.restype = _c_i32
+        L.pa_solver_create.argtypes = [ctypes.POINTER(_Options), _c_i64, _c_i64, ctypes.POINTER(_P)]
+        L.pa_solver_destroy.argtypes = [_P]
+        L.pa_solver_batch_size.restype = _c_i32
+        L.pa_solver_batch_size.argtypes = [_P]
+        L.pa_solver_set_stream.argtypes = [_P, _P]
+        L.pa_solver_last_timings.argtypes = [_P, _PF, _PI]
+        dense = [_P, _PF, _c_i64, _c_i64, _c_i64, _PI]
+        indexed = [_P, _PU, _PU, _c_i64, _c_i64, _c_i64, _PF, _c_i64, _c_i64, _PI]
+        binary = [_P, _PU, _PU, _c_i64, _c_i64, _c_i64, _c_f32, _c_f32, _PI]
+        for codomain in ("score", "alignment", "alignment_iterator", "solution", "solution_iterator"):
+            out = [_PF] if codomain == "score" else [ctypes.POINTER(_P)]
+            for prefix, args in (("pa_solve_for_", dense), ("pa_solve_indexed_for_", indexed),
+                                 ("pa_solve_binary_for_", binary)):
+                f = getattr(L, prefix + codomain)
+                f.restype = _c_i32
+                f.argtypes = args + out
+        L.pa_solve_batch.restype = _c_i32
+        L.pa_solve_batch.argtypes = [_P, ctypes.POINTER(Batch), _P, _P, _PL]
+        L.pa_result_destroy.argtypes = [_P]
+        L.pa_result_size.restype = _c_i64
+        L.pa_result_size.argtypes = [_P]
+        for f in ("pa_result_len_s", "pa_result_len_t"):
+            getattr(L, f).restype = _c_i64
+            getattr(L, f).argtypes = [_P, _c_i64]
+        L.pa_result_has_alignment.restype = _c_i32
+        L.pa_result_has_alignment.argtypes = [_P, _c_i64]
+        L.pa_result_score.restype = _c_f32
+        L.pa_result_score.argtypes = [_P, _c_i64]
+        L.pa_result_alignment.argtypes = [_P, _c_i64, _PI]
+        L.pa_result_export.argtypes = [_P, _PF, _PI, _PL]
+        L.pa_result_layers.restype = _c_i32
+        L.pa_result_layers.argtypes = [_P, _c_i64]
+        L.pa_result_max_degree_1.restype = _c_i32
+        L.pa_result_max_degree_1.argtypes = [_P]
+        L.pa_result_values.argtypes = [_P, _c_i64, _PF]
+        L.pa_result_tb_matrix.argtypes = [_P, _c_i64, _PI]
+        L.pa_result_tb_edges.restype = _c_i64
+        L.pa_result_tb_edges.argtypes = [_P, _c_i64, _c_i32, _PI]
+        L.pa_result_path.restype = _c_i64
+        L.pa_result_path.argtypes = [_P, _c_i64, _PI]
+        L.pa_result_algorithm.restype = ctypes.c_char_p
+        L.pa_result_algorithm.argtypes = [_P, _c_i32]
+        L.pa_result_iterator.argtypes = [_P, _c_i64, ctypes.POINTER(_P)]
+        L.pa_iterator_next.restype = _c_i32
+        L.pa_iterator_next.argtypes = [_P, _PF, _PI, _PI, _PL]
+        L.pa_iterator_destroy.argtypes = [_P]
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status == PA_OK:
+        return
+    msg = lib().pa_last_error().decode()
+    if status == PA_ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    raise RuntimeError(msg)
+
+
+def _fp(a):
+    return a.ctypes.data_as(_PF)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_PI)
+
+
+def _up(a):
+    return a.ctypes.data_as(_PU)
+
+
+# --- enums (enum.h:8-33, pyalign.h:80-102) ---
+
+class Type(enum.IntEnum):
+    ALIGNMENT = 0
+    DTW = 1
+
+
+class Direction(enum.IntEnum):
+    MINIMIZE = 0
+    MAXIMIZE = 1
+
+
+class Detail(enum.IntEnum):
+    SCORE = 0
+    ALIGNMENT = 1
+    SOLUTION = 2
+
+
+class Count(enum.IntEnum):
+    ONE = 0
+    ALL = 1
+
+
+class Locality(enum.IntEnum):
+    LOCAL = 0
+    GLOBAL = 1
+    SEMIGLOBAL = 2
+
+
+class Algorithm:
+    """Solver metadata (AlgorithmMetaData, solver.h:154-177; pyalign.h:72-78)."""
+
+    def __init__(self, name, runtime, memory):
+        self._v = (name, runtime, memory)
+
+    name = property(lambda self: self._v[0])
+    runtime = property(lambda self: self._v[1])
+    memory = property(lambda self: self._v[2])
+
+
+DEFAULT_BATCH_SIZE = int(os.environ.get("PYALIGN_GB300_BATCH_SIZE", "2048"))
+
+
+def _gap_spec(g):
+    """GapCostOptions (factory.h:33-65) for one side of the gap cost."""
+    if g is None:
+        return ("linear", np.float32(0.0))
+    sc = g.to_special_case()
+    if "affine" in sc:
+        t = sc["affine"]
+        # factory.h:42-52: (u, v) of w(k) = u + v k become Gotoh's w(k) = u' k + v'
+        return ("affine", (np.float32(t[1]), np.float32(t[0])))
+    if "linear" in sc:
+        return ("linear", np.float32(sc["linear"]))
+    return ("general", g)
+
+
+class Options:
+    """Parsed solver options (options.h:9-117)."""
+
+    def __init__(self, d, index_bits):
+        self._d = d
+        self.index_bits = index_bits
+        self.type = Type(int(d["solver"]))
+        self.batch = bool(d["batch"])
+        self.direction = Direction(int(d["direction"]))
+        self.remove_dup = not bool(d["return_dup"])
+        self.batch_size = int(d.get("batch_size", DEFAULT_BATCH_SIZE)) if hasattr(d, "get") else DEFAULT_BATCH_SIZE
+        if self.type == Type.ALIGNMENT:
+            cod = d["codomain"]
+            self.detail = Detail(int(cod.detail))
+            self.count = Count(int(cod.count))
+            self.locality = Locality(int(d["locality"])) if "locality" in d else Locality.LOCAL
+            gc = d["gap_cost"] if "gap_cost" in d else None
+            if isinstance(gc, dict):
+                gs, gt = gc.get("s"), gc.get("t")
+            else:
+                gs, gt = gc, gc
+            self.gap_s, self.gap_t = _gap_spec(gs), _gap_spec(gt)
+        else:
+            self.detail, self.count, self.locality = Detail.ALIGNMENT, Count.ONE, Locality.GLOBAL
+            self.gap_s = self.gap_t = ("linear", np.float32(0.0))
+
+    def to_dict(self):
+        return self._d
+
+
+def _general_costs(spec, n):
+    kind, val = spec
+    if kind == "general":
+        c = np.ascontiguousarray(val.costs(n), dtype=np.float32)
+        if c.shape != (n,):
+            raise ValueError(f"expected gap cost tensor length of {n}, got {c.shape[0]}")
+        return c
+    if kind == "linear":
+        return (np.arange(n, dtype=np.float32) * np.float32(val)).astype(np.float32)
+    u, v = val  # affine in Gotoh form
+    w = (np.arange(n, dtype=np.float32) * u + v).astype(np.float32)
+    w[0] = 0
+    return w
+
+
+# --- results ---
+
+class _Result:
+    """Owner of a pa_result handle (one solve call)."""
+
+    __slots__ = ("ptr",)
+
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        if self.ptr and _lib is not None:
+            _lib.pa_result_destroy(self.ptr)
+            self.ptr = None
+
+
+def _narrow(a, dtype):
+    a = np.asarray(a)
+    if dtype == np.int16:
+        lo = np.iinfo(np.int16).min
+        return np.where(a == np.iinfo(np.int32).min, lo, a).astype(np.int16)
+    return a.astype(np.int32, copy=False)
+
+
+class Alignment:
+    """Alignment (factory.h:130-193): score plus s_to_t / t_to_s, -1 where unaligned."""
+
+    __slots__ = ("_ls", "_lt", "_score", "_s_to_t", "_t_to_s", "_dtype")
+
+    def __init__(self, ls, lt, score, mp, index_dtype):
+        self._ls, self._lt = ls, lt
+        self._score = float(score)
+        self._dtype = index_dtype
+        mp = _narrow(mp, index_dtype)
+        if ls <= lt:
+            self._s_to_t, self._t_to_s = mp, None
+        else:
+            self._s_to_t, self._t_to_s = None, mp
+
+    @property
+    def score(self):
+        return self._score
+
+    @staticmethod
+    def _invert(src, n, dtype):  # factory.h:110-128
+        out = np.full((n,), -1, dtype=dtype)
+        idx = np.nonzero(src >= 0)[0]
+        out[src[idx]] = idx
+        return out
+
+    @property
+    def s_to_t(self):
+        if self._s_to_t is None:
+            self._s_to_t = self._invert(self._t_to_s, self._ls, self._dtype)
+        return self._s_to_t
+
+    @property
+    def t_to_s(self):
+        if self._t_to_s is None:
+            self._t_to_s = self._invert(self._s_to_t, self._lt, self._dtype)
+        return self._t_to_s
+
+
+class Solution:
+    """Solution (SolutionImpl, factory.h:284-352; core::Solution solver.h:2329-2507)."""
+
+    def __init__(self, res, lane, ls, lt, dtype, step=None, algorithm=True):
+        self._res, self._lane, self._ls, self._lt, self._dtype = res, lane, ls, lt, dtype
+        self._step = step  # (score, map, path) of an iterator step, or None
+        self._with_algorithm = algorithm
+        self._cache = {}
+
+    def _get(self, key, fn):
+        if key not in self._cache:
+            self._cache[key] = fn()
+        return self._cache[key]
+
+    @property
+    def values(self):
+        def f():
+            L = lib()
+            k = L.pa_result_layers(self._res.ptr, self._lane)
+            out = np.zeros((k, self._ls + 1, self._lt + 1), dtype=np.float32)
+            check(L.pa_result_values(self._res.ptr, self._lane, _fp(out)))
+            return out
+        return self._get("values", f)
+
+    @property
+    def traceback_has_max_degree_1(self):
+        return bool(lib().pa_result_max_degree_1(self._res.ptr))
+
+    @property
+    def traceback_as_matrix(self):
+        def f():
+            L = lib()
+            k = L.pa_result_layers(self._res.ptr, self._lane)
+            out = np.zeros((k, self._ls + 1, self._lt + 1, 2), dtype=np.int32)
+            check(L.pa_result_tb_matrix(self._res.ptr, self._lane, _ip(out)))
+            return _narrow(out, self._dtype)
+        return self._get("tbm", f)
+
+    @property
+    def traceback_as_edges(self):
+        def f():
+            L = lib()
+            k = L.pa_result_layers(self._res.ptr, self._lane)
+            out = []
+            for layer in range(k):
+                n = L.pa_result_tb_edges(self._res.ptr, self._lane, layer, None)
+                e = np.zeros((n, 2, 2), dtype=np.int32)
+                if n:
+                    L.pa_result_tb_edges(self._res.ptr, self._lane, layer, _ip(e))
+                out.append(_narrow(e, self._dtype))
+            return out
+        return list(self._get("edges", f))
+
+    def _walk(self):
+        def f():
+            if self._step is not None:
+                return self._step
+            L = lib()
+            if not L.pa_result_has_alignment(self._res.ptr, self._lane):
+                return None
+            path = np.zeros((self._ls + self._lt + 4, 2), dtype=np.int32)
+            n = L.pa_result_path(self._res.ptr, self._lane, _ip(path))
+            mp = np.zeros((min(self._ls, self._lt),), dtype=np.int32)
+            L.pa_result_alignment(self._res.ptr, self._lane, _ip(mp))
+            sc = L.pa_result_score(self._res.ptr, self._lane)
+            return (float(sc), mp, path[:max(n, 0)].copy() if n >= 0 else None)
+        return self._get("walk", f)
+
+    @property
+    def path(self):
+        w = self._walk()
+        if w is None or w[2] is None:
+            return None
+        return _narrow(w[2], self._dtype)
+
+    @property
+    def score(self):
+        w = self._walk()
+        return None if w is None else float(w[0])
+
+    @property
+    def alignment(self):
+        w = self._walk()
+        if w is None:
+            return None
+        return Alignment(self._ls, self._lt, w[0], w[1], self._dtype)
+
+    @property
+    def algorithm(self):
+        if not self._with_algorithm:
+            return None
+        L = lib()
+        return Algorithm(*(L.pa_result_algorithm(self._res.ptr, k).decode() for k in range(3)))
+
+
+class _Iter:
+    def __init__(self, res, lane, ls, lt, dtype):
+        self._res, self._lane, self._ls, self._lt, self._dtype = res, lane, ls, lt, dtype
+        h = _P()
+        check(lib().pa_result_iterator(res.ptr, lane, ctypes.byref(h)))
+        self._it = h
+
+    def __del__(self):
+        if getattr(self, "_it", None) and _lib is not None:
+            _lib.pa_iterator_destroy(self._it)
+            self._it = None
+
+    def _next(self):
+        sc = ctypes.c_float(0)
+        mp = np.zeros((min(self._ls, self._lt),), dtype=np.int32)
+        path = np.zeros((self._ls + self._lt + 4, 2), dtype=np.int32)
+        n = ctypes.c_int64(0)
+        if not lib().pa_iterator_next(self._it, ctypes.byref(sc), _ip(mp), _ip(path), ctypes.byref(n)):
+            return None
+        return float(sc.value), mp, path[:n.value].copy()
+
+
+class AlignmentIterator(_Iter):
+    """AlignmentIterator (factory.h:218-245): next() -> Alignment or None."""
+
+    def next(self):
+        r = self._next()
+        if r is None:
+            return None
+        return Alignment(self._ls, self._lt, r[0], r[1], self._dtype)
+
+
+class SolutionIterator(_Iter):
+    """SolutionIterator (factory.h:271-385): next() -> Solution or None."""
+
+    def next(self):
+        r = self._next()
+        if r is None:
+            return None
+        return Solution(self._res, self._lane, self._ls, self._lt, self._dtype, step=r, algorithm=False)
+
+
+# --- solver ---
+
+class Solver:
+    """Solver (factory.h:414-508) running on the GPU."""
+
+    def __init__(self, max_len_s, max_len_t, options):
+        o = options
+        self._opts = o
+        self._index_dtype = np.int16 if o.index_bits == 16 else np.int32
+        c = _Options()
+        c.type, c.direction = int(o.type), int(o.direction)
+        c.detail, c.count, c.locality = int(o.detail), int(o.count), int(o.locality)
+        c.remove_dup, c.batch, c.batch_size = int(o.remove_dup), int(o.batch), int(o.batch_size)
+        c.index_bits = int(o.index_bits)
+        kinds = (o.gap_s[0], o.gap_t[0])
+        self._keep = []
+        if o.type == Type.DTW or kinds == ("linear", "linear"):
+            c.gap_kind = 0
+            c.linear_s, c.linear_t = float(o.gap_s[1]), float(o.gap_t[1])
+        elif kinds == ("affine", "affine"):
+            c.gap_kind = 1
+            c.affine_u_s, c.affine_v_s = float(o.gap_s[1][0]), float(o.gap_s[1][1])
+            c.affine_u_t, c.affine_v_t = float(o.gap_t[1][0]), float(o.gap_t[1][1])
+        else:
+            c.gap_kind = 2
+            gs = _general_costs(o.gap_s, int(max_len_s) + 1)
+            gt = _general_costs(o.gap_t, int(max_len_t) + 1)
+            self._keep += [gs, gt]
+            c.general_s, c.general_t = _fp(gs), _fp(gt)
+        h = _P()
+        check(lib().pa_solver_create(ctypes.byref(c), int(max_len_s), int(max_len_t), ctypes.byref(h)))
+        self._h = h
+        self._batch_size = lib().pa_solver_batch_size(h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pa_solver_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def options(self):
+        return self._opts.to_dict()
+
+    @property
+    def batch_size(self):
+        return self._batch_size
+
+    def last_timings(self):
+        ms = (ctypes.c_float * 4)()
+        n = ctypes.c_int32(0)
+        lib().pa_solver_last_timings(self._h, ms, ctypes.byref(n))
+        return list(ms), n.value
+
+    # --- argument marshalling (pytensor casts of factory.h:424-507)
+    @staticmethod
+    def _len(length):
+        return np.ascontiguousarray(length, dtype=np.int32)
+
+    @staticmethod
+    def _codes(x):
+        return np.ascontiguousarray(x, dtype=np.uint32)
+
+    def _call(self, name, form, args):
+        L = lib()
+        if form == "dense":
+            sim, length = args
+            sim = np.ascontiguousarray(sim, dtype=np.float32)
+            if sim.ndim != 3:
+                raise ValueError("similarity must be a 3-d array (len_s, len_t, batch)")
+            ln = self._len(length)
+            head = [self._h, _fp(sim), sim.shape[0], sim.shape[1], sim.shape[2], _ip(ln)]
+            keep = (sim, ln)
+            lens = ln
+        elif form == "indexed":
+            a, b, sim, length = args
+            a, b = self._codes(a), self._codes(b)
+            sim = np.ascontiguousarray(sim, dtype=np.float32)
+            ln = self._len(length)
+            if a.shape[0] != b.shape[0]:
+                raise ValueError(f"problem of batch size {b.shape[0]} given to solver that was "
+                                 f"configured to batch size {self._batch_size}")
+            head = [self._h, _up(a), _up(b), a.shape[0], a.shape[1], b.shape[1], _fp(sim),
+                    sim.shape[0], sim.shape[1], _ip(ln)]
+            keep = (a, b, sim, ln)
+            lens = ln
+        else:
+            a, b, eq, ne, length = args
+            a, b = self._codes(a), self._codes(b)
+            ln = self._len(length)
+            if a.shape[0] != b.shape[0]:
+                raise ValueError(f"problem of batch size {b.shape[0]} given to solver that was "
+                                 f"configured to batch size {self._batch_size}")
+            head = [self._h, _up(a), _up(b), a.shape[0], a.shape[1], b.shape[1], float(eq), float(ne), _ip(ln)]
+            keep = (a, b, ln)
+            lens = ln
+        if lens.ndim != 2 or lens.shape[0] != 2 or lens.shape[1] != self._batch_size:
+            raise ValueError(f"m_length has shape {tuple(lens.shape)}, expected (2, {self._batch_size})")
+        prefix = {"dense": "pa_solve_for_", "indexed": "pa_solve_indexed_for_", "binary": "pa_solve_binary_for_"}[form]
+        fn = getattr(L, prefix + name)
+        if name == "score":
+            out = np.zeros((self._batch_size,), dtype=np.float32)
+            check(fn(*head, _fp(out)))
+            del keep
+            return out
+        h = _P()
+        check(fn(*head, ctypes.byref(h)))
+        del keep
+        return _Result(h)
+
+    def _lanes(self, res):
+        L = lib()
+        n = L.pa_result_size(res.ptr)
+        ls = [L.pa_result_len_s(res.ptr, k) for k in range(n)]
+        lt = [L.pa_result_len_t(res.ptr, k) for k in range(n)]
+        return n, ls, lt
+
+    def _alignments(self, res):
+        n, ls, lt = self._lanes(res)
+        sizes = np.minimum(np.asarray(ls, dtype=np.int64), np.asarray(lt, dtype=np.int64))
+        offs = np.zeros((n,), dtype=np.int64)
+        if n > 1:
+            offs[1:] = np.cumsum(sizes)[:-1]
+        maps = np.zeros((int(sizes.sum()),), dtype=np.int32)
+        scores = np.zeros((n,), dtype=np.float32)
+        check(lib().pa_result_export(res.ptr, _fp(scores), _ip(maps), offs.ctypes.data_as(_PL)))
+        return tuple(Alignment(ls[k], lt[k], scores[k], maps[offs[k]:offs[k] + sizes[k]], self._index_dtype)
+                     for k in range(n))
+
+    def _iterators(self, res, cls):
+        n, ls, lt = self._lanes(res)
+        return tuple(cls(res, k, ls[k], lt[k], self._index_dtype) for k in range(n))
+
+    def _solutions(self, res):
+        n, ls, lt = self._lanes(res)
+        return tuple(Solution(res, k, ls[k], lt[k], self._index_dtype) for k in range(n))
+
+    def _dispatch(self, codomain, form, args):
+        if codomain == "score":
+            return self._call("score", form, args)
+        res = self._call(codomain, form, args)
+        if codomain == "alignment":
+            return self._alignments(res)
+        if codomain == "alignment_iterator":
+            return self._iterators(res, AlignmentIterator)
+        if codomain == "solution":
+            return self._solutions(res)
+        return self._iterators(res, SolutionIterator)
+
+    def solve_for_score(self, sim, length):
+        return self._dispatch("score", "dense", (sim, length))
+
+    def solve_indexed_for_score(self, a, b, sim, length):
+        return self._dispatch("score", "indexed", (a, b, sim, length))
+
+    def solve_binary_for_score(self, a, b, eq, ne, length):
+        return self._dispatch("score", "binary", (a, b, eq, ne, length))
+
+    def solve_for_alignment(self, sim, length):
+        return self._dispatch("alignment", "dense", (sim, length))
+
+    def solve_for_alignment_iterator(self, sim, length):
+        return self._dispatch("alignment_iterator", "dense", (sim, length))
+
+    def solve_indexed_for_alignment(self, a, b, sim, length):
+        return self._dispatch("alignment", "indexed", (a, b, sim, length))
+
+    def solve_indexed_for_alignment_iterator(self, a, b, sim, length):
+        return self._dispatch("alignment_iterator", "indexed", (a, b, sim, length))
+
+    def solve_binary_for_alignment(self, a, b, eq, ne, length):
+        return self._dispatch("alignment", "binary", (a, b, eq, ne, length))
+
+    def solve_binary_for_alignment_iterator(self, a, b, eq, ne, length):
+        return self._dispatch("alignment_iterator", "binary", (a, b, eq, ne, length))
+
+    def solve_for_solution(self, sim, length):
+        return self._dispatch("solution", "dense", (sim, length))
+
+    def solve_for_solution_iterator(self, sim, length):
+        return self._dispatch("solution_iterator", "dense", (sim, length))
+
+    def solve_indexed_for_solution(self, a, b, sim, length):
+        return self._dispatch("solution", "indexed", (a, b, sim, length))
+
+    def solve_indexed_for_solution_iterator(self, a, b, sim, length):
+        return self._dispatch("solution_iterator", "indexed", (a, b, sim, length))
+
+    def solve_binary_for_solution(self, a, b, eq, ne, length):
+        return self._dispatch("solution", "binary", (a, b, eq, ne, length))
+
+    def solve_binary_for_solution_iterator(self, a, b, eq, ne, length):
+        return self._dispatch("solution_iterator", "binary", (a, b, eq, ne, length))
+
+
+class _IndexModule:
+    """The ``m16``/``m32`` submodules (module.cpp:10-14)."""
+
+    def __init__(self, bits):
+        self._bits = bits
+        self.Solver = Solver
+        self.Alignment = Alignment
+        self.AlignmentIterator = AlignmentIterator
+        self.Solution = Solution
+        self.SolutionIterator = SolutionIterator
+        self.Options = Options
+
+    def create_options(self, d):
+        return Options(d, self._bits)
+
+    def create_solver(self, max_len_s, max_len_t, options):
+        return Solver(max_len_s, max_len_t, options)
+
+
+m16 = _IndexModule(16)
+m32 = _IndexModule(32)

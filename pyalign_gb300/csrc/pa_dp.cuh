@@ -1,0 +1,570 @@
+// Wavefront DP kernels for the batched alignment solve (sm_103a).
+//
+// Recurrences restated from pyalign/algorithm/solver.h (pyalign 0.4.4):
+//   linear  (NW/SW)  LinearGapCostSolver::solve   solver.h:2825-2855
+//   affine  (Gotoh)  AffineGapCostSolver::solve   solver.h:2970-3036
+//   DTW              DynamicTimeSolver::solve     solver.h:3213-3251
+// with the tie rule of Accumulator/TracingAccumulator (solver.h:1226-1427): the first
+// candidate pushed wins unless a later one is strictly better; "all optimal" keeps every
+// candidate equal to the maximum.  Seeds follow Local/Global/Semiglobal
+// (solver.h:1980-2327).
+//
+// Everything runs in the "maximize" form: the host negates similarities for minimize
+// problems (min f == -max(-f) exactly in IEEE arithmetic), and gap costs enter as
+// negative addends.
+//
+// Mapping to the GPU.  A pair is solved by a group of G lanes (G = 4..32) of one warp;
+// each lane owns R = 8 consecutive rows of a stripe of G*R rows and the group sweeps the
+// columns of t as a skewed wavefront (lane k works on column s-k at step s).  The
+// boundary (D, P) of a lane's last row travels to the next lane by __shfl_up_sync; the
+// last lane writes it to a per-group scratch row that feeds the next stripe.  Per cell,
+// the traceback is a 4-bit nibble (one optimal path: 2-bit D source, P-extend bit,
+// Q-extend bit) or a 16-bit word (all optimal paths: every tied predecessor), stored
+// as one coalesced 32-bit (or 128-bit) word per lane per step.
+//
+// Integer scoring runs on int32 "tagged" values: every value is scaled by 4 and the low
+// two bits of each candidate carry its push priority (zero 3 > diag 2 > P/up 1 > Q/left
+// 0), so a single max chain yields the value and the reference's tie winner at once.
+
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+namespace pa {
+
+enum GapKind { GAP_LINEAR = 0, GAP_AFFINE = 1, GAP_DTW = 2, GAP_GENERAL = 3 };
+enum LocKind { LOC_LOCAL = 0, LOC_GLOBAL = 1, LOC_SEMI = 2 };
+enum TbKind { TB_NONE = 0, TB_ONE = 1, TB_ALL = 2 };
+enum SubKind { SUB_TABLE = 0, SUB_BINARY = 1, SUB_DENSE = 2 };
+
+constexpr int R = 8;              // rows per lane
+constexpr int BLOCK = 128;        // threads per block
+constexpr int WARPS = BLOCK / 32;
+constexpr int MAX_SMEM_TABLE = 64;  // alphabet size kept in shared memory
+
+// status bits written by kernels (host turns them into errors)
+constexpr int ST_BAD_CODE = 1;
+
+template <typename V>
+struct DpParams {
+	int32_t npairs;
+	const int32_t *order;   // processing order (host sorted by cost)
+	const int32_t *len_s;   // per pair
+	const int32_t *len_t;
+	// sequences (SUB_TABLE / SUB_BINARY)
+	const uint32_t *a;
+	const uint32_t *b;
+	int64_t a_stride, b_stride;
+	// substitution
+	int32_t sub_kind;
+	const V *table;         // table_rows x table_cols, prepared by the host (scaled/tagged)
+	int32_t table_rows, table_cols;
+	V eq, ne;               // binary, prepared
+	const float *dense;     // S(k,i,j) = dense[dense_off[k] + i*dense_si + j*dense_sj]
+	const int64_t *dense_off;
+	int64_t dense_si, dense_sj;
+	float dense_sign;       // +1 maximize, -1 minimize
+	// gap addends (negative), prepared by the host
+	V c_up, c_left;         // linear: vertical / horizontal step
+	V c_open_s, c_ext_s;    // affine P (vertical): from D, from P
+	V c_open_t, c_ext_t;    // affine Q (horizontal)
+	// borders: left_D[i+1] = D(i,-1), top_D[j+1] = D(-1,j)  (i, j >= -1)
+	const V *left_D;
+	const V *top_D;
+	const V *left_P;        // values output only: P(i,-1)
+	const V *top_Q;         // values output only: Q(-1,j)
+	V neg_inf;
+	int32_t G;              // lanes per pair group
+	// outputs
+	float *score;           // reference-domain score
+	int32_t *seed;          // (i, j) per pair
+	int32_t *has_seed;
+	float out_sign;         // +1 maximize, -1 minimize
+	void *masks;            // TB_ONE: uint32 words; TB_ALL: uint4
+	const int64_t *mask_off;  // per pair, in store elements
+	const float *best_in;   // TB_ALL + local: optimum per pair (reference domain)
+	// solution values (optional): per pair layers x (ls+1) x (lt+1) floats
+	float *values;
+	const int64_t *val_off;
+	// scratch: per group slot, 2 buffers of max_lt (D, P) pairs
+	void *scratch;
+	int64_t scratch_stride;  // elements per slot
+	int32_t *work_counter;
+	int32_t *status;
+};
+
+template <typename V>
+struct V2T;
+template <>
+struct V2T<int32_t> { typedef int2 type; };
+template <>
+struct V2T<float> { typedef float2 type; };
+
+__device__ __forceinline__ int32_t vmax(int32_t a, int32_t b) { return max(a, b); }
+__device__ __forceinline__ float vmax(float a, float b) { return fmaxf(a, b); }
+
+template <typename V>
+__device__ __forceinline__ float to_ref(V x, bool tagged, float sign);
+
+template <>
+__device__ __forceinline__ float to_ref<int32_t>(int32_t x, bool tagged, float sign) {
+	if (x < -(1 << 28)) return -INFINITY * sign;
+	const int32_t v = tagged ? (x >> 2) : x;
+	return float(v) * sign;
+}
+
+template <>
+__device__ __forceinline__ float to_ref<float>(float x, bool, float sign) {
+	return x * sign;
+}
+
+// Substitution value of (query code qa at row i, subject code tb at column j).
+template <typename V>
+struct SubCtx {
+	const V *table;  // shared or global
+	int32_t cols;
+	V eq, ne;
+};
+
+template <typename V, int GAP, int LOC, int TB>
+__global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
+	constexpr bool ISINT = std::is_same<V, int32_t>::value;
+	constexpr bool TAG = ISINT && TB != TB_ALL;  // int32 tagged values
+	typedef typename V2T<V>::type V2;
+
+	extern __shared__ unsigned char smem_raw[];
+	V *stab = reinterpret_cast<V *>(smem_raw);
+	const bool table_in_smem = p.sub_kind == SUB_TABLE && p.table_rows <= MAX_SMEM_TABLE &&
+	                           p.table_cols <= MAX_SMEM_TABLE;
+	if (table_in_smem) {
+		const int n = p.table_rows * p.table_cols;
+		for (int k = threadIdx.x; k < n; k += blockDim.x) stab[k] = p.table[k];
+	}
+	__syncthreads();
+	const V *tab = table_in_smem ? stab : p.table;
+
+	const int G = p.G;
+	const int lane = threadIdx.x & 31;
+	const int sub = lane % G;          // lane within the group
+	const int grp = lane / G;          // group within the warp
+	const int gpw = 32 / G;            // groups per warp
+	const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int slot = warp_global * gpw + grp;
+	V2 *scr = reinterpret_cast<V2 *>(p.scratch) + int64_t(slot) * p.scratch_stride;
+	const int64_t half = p.scratch_stride / 2;
+	const V NEG = p.neg_inf;
+	const int rpp = G * R;  // rows per pass
+
+	for (;;) {
+		int base = 0;
+		if (lane == 0) base = atomicAdd(p.work_counter, gpw);
+		base = __shfl_sync(0xffffffffu, base, 0);
+		if (base >= p.npairs) break;
+		const int w = base + grp;
+		const int pair = w < p.npairs ? p.order[w] : -1;
+		const int ls = pair >= 0 ? p.len_s[pair] : 0;
+		const int lt = pair >= 0 ? p.len_t[pair] : 0;
+		const bool empty = ls == 0 || lt == 0;
+		const int npass = empty ? 0 : (ls + rpp - 1) / rpp;
+		const int nsteps_pair = lt + G - 1;
+		int wpass = npass, wsteps = empty ? 0 : nsteps_pair;
+		for (int o = 16; o > 0; o >>= 1) {
+			wpass = max(wpass, __shfl_xor_sync(0xffffffffu, wpass, o));
+			wsteps = max(wsteps, __shfl_xor_sync(0xffffffffu, wsteps, o));
+		}
+
+		const uint32_t *arow = p.a ? p.a + int64_t(pair < 0 ? 0 : pair) * p.a_stride : nullptr;
+		const uint32_t *brow = p.b ? p.b + int64_t(pair < 0 ? 0 : pair) * p.b_stride : nullptr;
+		const float *drow = p.dense ? p.dense + (pair >= 0 ? p.dense_off[pair] : 0) : nullptr;
+		const V best_in = (TB == TB_ALL && LOC == LOC_LOCAL && pair >= 0)
+		                      ? V(p.best_in[pair] * p.out_sign)
+		                      : V(0);
+		float *vals = (p.values && pair >= 0) ? p.values + p.val_off[pair] : nullptr;
+		const int64_t lstride = int64_t(lt + 1);
+		const int64_t layer_sz = int64_t(ls + 1) * lstride;
+
+		// --- solution values: borders (solver.h:2806-2814, 2918-2967, 3116-3125, 3205-3210)
+		if (vals) {
+			const bool tg = TAG;
+			for (int j = sub - 1; j < lt; j += G) {
+				vals[j + 1] = to_ref(p.top_D[j + 1], tg, p.out_sign);
+				if (GAP == GAP_AFFINE) {
+					vals[layer_sz + (j + 1)] = (j < 0) ? to_ref(p.left_P[0], tg, p.out_sign)
+					                                   : -INFINITY * p.out_sign;
+					vals[2 * layer_sz + (j + 1)] = to_ref(p.top_Q[j + 1], tg, p.out_sign);
+				}
+			}
+			for (int i = sub; i < ls; i += G) {
+				vals[int64_t(i + 1) * lstride] = to_ref(p.left_D[i + 1], tg, p.out_sign);
+				if (GAP == GAP_AFFINE) {
+					vals[layer_sz + int64_t(i + 1) * lstride] = to_ref(p.left_P[i + 1], tg, p.out_sign);
+					vals[2 * layer_sz + int64_t(i + 1) * lstride] = -INFINITY * p.out_sign;
+				}
+			}
+		}
+
+		// seed tracking state
+		V l_best = NEG;              // local: best value of this lane
+		int l_bi = -1, l_bj = -1;
+		V row_best = NEG;            // semiglobal: last row (first max in ascending j)
+		int row_bj = -1;
+		V col_best = NEG;            // semiglobal: last column (first max in ascending i)
+		int col_bi = -1;
+		V glob = NEG;                // global: D(ls-1, lt-1)
+		bool have_glob = false;
+
+		for (int q = 0; q < wpass; q++) {
+			const bool pass_active = q < npass;
+			const int row0 = q * rpp + sub * R;
+			const int nvalid = ls - row0;  // rows of this lane that are < ls (may be <= 0 or >= R)
+			const V2 *bin = scr + (q & 1) * half;
+			V2 *bout = scr + ((q + 1) & 1) * half;
+			const bool write_boundary = sub == G - 1 && q + 1 < npass;
+
+			uint32_t qa[R];
+#pragma unroll
+			for (int r = 0; r < R; r++) {
+				const int i = row0 + r;
+				qa[r] = 0;
+				if (pass_active && i < ls && arow) qa[r] = arow[i];
+			}
+			if (p.sub_kind == SUB_TABLE && pass_active) {
+#pragma unroll
+				for (int r = 0; r < R; r++) {
+					if (row0 + r < ls && int32_t(qa[r]) >= p.table_rows) atomicOr(p.status, ST_BAD_CODE);
+				}
+			}
+
+			V Dl[R], Ql[R];
+#pragma unroll
+			for (int r = 0; r < R; r++) {
+				const int i = row0 + r;
+				Dl[r] = (pass_active && i < ls) ? p.left_D[i + 1] : NEG;
+				Ql[r] = NEG;
+			}
+			// (D, P) of this lane's last row as seen by the next lane; column -1 initially
+			V outD = Dl[R - 1], outP = NEG;
+			V prev_up = (pass_active && row0 <= ls) ? p.left_D[row0] : NEG;  // D(row0-1, -1)
+
+			// traceback state of the best per row (local, one optimal path)
+			V bv[(TB == TB_ONE && LOC == LOC_LOCAL) ? R : 1];
+			int bj[(TB == TB_ONE && LOC == LOC_LOCAL) ? R : 1];
+			if (TB == TB_ONE && LOC == LOC_LOCAL) {
+#pragma unroll
+				for (int r = 0; r < R; r++) { bv[r] = NEG; bj[r] = -1; }
+			}
+			const bool last_row_lane = pass_active && nvalid >= 1 && nvalid <= R;
+			const int r_last = nvalid - 1;
+
+			for (int s = 0; s < wsteps; s++) {
+				const int j = s - sub;
+				V upD = __shfl_up_sync(0xffffffffu, outD, 1, G);
+				V upP = __shfl_up_sync(0xffffffffu, outP, 1, G);
+				const bool act = pass_active && j >= 0 && j < lt;
+				if (sub == 0 && act) {
+					if (q == 0) {
+						upD = p.top_D[j + 1];
+						upP = NEG;
+					} else {
+						const V2 bv2 = bin[j];
+						upD = bv2.x;
+						upP = bv2.y;
+					}
+				}
+				if (act) {
+					// substitution values of the R rows at column j
+					V S[R];
+					if (p.sub_kind == SUB_DENSE) {
+#pragma unroll
+						for (int r = 0; r < R; r++) {
+							const int i = min(row0 + r, ls - 1);
+							const float x = drow[int64_t(i) * p.dense_si + int64_t(j) * p.dense_sj] * p.dense_sign;
+							S[r] = V(x);
+						}
+					} else {
+						const uint32_t tb = brow[j];
+						if (p.sub_kind == SUB_BINARY) {
+#pragma unroll
+							for (int r = 0; r < R; r++) S[r] = (qa[r] == tb) ? p.eq : p.ne;
+						} else {
+							const int tcol = int(tb) < p.table_cols ? int(tb) : 0;
+							if (int(tb) >= p.table_cols) atomicOr(p.status, ST_BAD_CODE);
+#pragma unroll
+							for (int r = 0; r < R; r++) {
+								const int rr = int(qa[r]) < p.table_rows ? int(qa[r]) : 0;
+								S[r] = tab[rr * p.table_cols + tcol];
+							}
+						}
+					}
+
+					uint32_t mword = 0;
+					uint32_t mall[4] = {0, 0, 0, 0};
+					V dsave = prev_up;  // D(i-1, j-1) for the first row
+					V uD = upD, uP = upP;
+#pragma unroll
+					for (int r = 0; r < R; r++) {
+						const V old = Dl[r];
+						V D, P = NEG, Q = NEG;
+						if (TAG) {
+							// ---- int32 tagged: one max chain gives value and tie winner
+							int32_t key;
+							if (GAP == GAP_AFFINE) {
+								const V oP = uD + p.c_open_s, eP = uP + p.c_ext_s;
+								P = vmax(oP, eP);
+								const V oQ = old + p.c_open_t, eQ = Ql[r] + p.c_ext_t;
+								Q = vmax(oQ, eQ);
+								key = vmax(vmax(dsave + S[r], P), Q);
+								if (LOC == LOC_LOCAL) key = vmax(key, 3);
+								D = key & ~3;
+								if (TB == TB_ONE)
+									mword |= (uint32_t(key & 3) | (uint32_t(eP > oP) << 2) | (uint32_t(eQ > oQ) << 3)) << (4 * r);
+							} else if (GAP == GAP_LINEAR) {
+								key = vmax(vmax(dsave + S[r], uD + p.c_up), old + p.c_left);
+								if (LOC == LOC_LOCAL) key = vmax(key, 3);
+								D = key & ~3;
+								if (TB == TB_ONE) mword |= uint32_t(key & 3) << (4 * r);
+							} else {  // DTW
+								key = vmax(vmax(dsave + 2, uD + 1), old);
+								D = (key & ~3) + S[r];
+								if (TB == TB_ONE) mword |= uint32_t(key & 3) << (4 * r);
+							}
+						} else {
+							// ---- explicit compares (float, or int32 for all-optimal masks)
+							uint32_t cell = 0;
+							V best;
+							int code;
+							if (GAP == GAP_AFFINE) {
+								const V oP = uD + p.c_open_s, eP = uP + p.c_ext_s;
+								const bool bP = eP > oP;
+								P = bP ? eP : oP;
+								const V oQ = old + p.c_open_t, eQ = Ql[r] + p.c_ext_t;
+								const bool bQ = eQ > oQ;
+								Q = bQ ? eQ : oQ;
+								const V dg = dsave + S[r];
+								if (LOC == LOC_LOCAL) {
+									best = V(0); code = 3;
+									if (dg > best) { best = dg; code = 2; }
+								} else {
+									best = dg; code = 2;
+								}
+								if (P > best) { best = P; code = 1; }
+								if (Q > best) { best = Q; code = 0; }
+								D = best;
+								if (TB == TB_ONE) {
+									cell = uint32_t(code) | (uint32_t(bP) << 2) | (uint32_t(bQ) << 3);
+								} else if (TB == TB_ALL) {
+									cell = (LOC == LOC_LOCAL && best == V(0) ? 1u : 0u) | (dg == best ? 2u : 0u) |
+									       (P == best ? 4u : 0u) | (Q == best ? 8u : 0u) |
+									       (oP == P ? 16u : 0u) | (eP == P ? 32u : 0u) |
+									       (oQ == Q ? 64u : 0u) | (eQ == Q ? 128u : 0u);
+								}
+							} else if (GAP == GAP_LINEAR) {
+								const V dg = dsave + S[r];
+								const V up = uD + p.c_up;
+								const V lf = old + p.c_left;
+								if (LOC == LOC_LOCAL) {
+									best = V(0); code = 3;
+									if (dg > best) { best = dg; code = 2; }
+								} else {
+									best = dg; code = 2;
+								}
+								if (up > best) { best = up; code = 1; }
+								if (lf > best) { best = lf; code = 0; }
+								D = best;
+								if (TB == TB_ONE) {
+									cell = uint32_t(code);
+								} else if (TB == TB_ALL) {
+									cell = (LOC == LOC_LOCAL && best == V(0) ? 1u : 0u) | (dg == best ? 2u : 0u) |
+									       (up == best ? 4u : 0u) | (lf == best ? 8u : 0u);
+								}
+							} else {  // DTW
+								best = dsave; code = 2;
+								if (uD > best) { best = uD; code = 1; }
+								if (old > best) { best = old; code = 0; }
+								if (TB == TB_ALL) {
+									cell = (dsave == best ? 2u : 0u) | (uD == best ? 4u : 0u) | (old == best ? 8u : 0u);
+								}
+								D = best + S[r];
+								if (TB == TB_ONE) cell = uint32_t(code);
+							}
+							if (TB == TB_ONE) mword |= cell << (4 * r);
+							if (TB == TB_ALL) {
+								if (LOC == LOC_LOCAL && r < nvalid && best_in > V(0) && D == best_in) cell |= 256u;
+								mall[r >> 1] |= cell << (16 * (r & 1));
+							}
+						}
+
+						// seeds
+						if (LOC == LOC_LOCAL) {
+							if (TB == TB_ONE) {
+								if (r < nvalid && D >= bv[r]) { bv[r] = D; bj[r] = j; }
+							} else if (TB == TB_NONE) {
+								if (r < nvalid) l_best = vmax(l_best, D);
+							}
+						}
+						if (vals && r < nvalid) {
+							const int64_t c = int64_t(row0 + r + 1) * lstride + (j + 1);
+							vals[c] = to_ref(D, TAG, p.out_sign);
+							if (GAP == GAP_AFFINE) {
+								vals[layer_sz + c] = to_ref(P, TAG, p.out_sign);
+								vals[2 * layer_sz + c] = to_ref(Q, TAG, p.out_sign);
+							}
+						}
+						dsave = old;
+						Dl[r] = D;
+						if (GAP == GAP_AFFINE) Ql[r] = Q;
+						uD = D;
+						uP = P;
+					}
+					outD = uD;
+					outP = uP;
+					if (write_boundary) bout[j] = V2{outD, outP};
+
+					if (TB == TB_ONE) {
+						uint32_t *m = reinterpret_cast<uint32_t *>(p.masks) + p.mask_off[pair];
+						m[(int64_t(q) * nsteps_pair + s) * G + sub] = mword;
+					} else if (TB == TB_ALL) {
+						uint4 *m = reinterpret_cast<uint4 *>(p.masks) + p.mask_off[pair];
+						m[(int64_t(q) * nsteps_pair + s) * G + sub] = make_uint4(mall[0], mall[1], mall[2], mall[3]);
+					}
+
+					if (LOC == LOC_SEMI || LOC == LOC_GLOBAL) {
+						if (last_row_lane && q == npass - 1) {
+							V x = Dl[0];
+#pragma unroll
+							for (int r = 1; r < R; r++)
+								if (r == r_last) x = Dl[r];
+							if (LOC == LOC_SEMI) {
+								if (x > row_best) { row_best = x; row_bj = j; }
+							} else if (j == lt - 1) {
+								glob = x;
+								have_glob = true;
+							}
+						}
+						if (LOC == LOC_SEMI && j == lt - 1) {
+#pragma unroll
+							for (int r = 0; r < R; r++)
+								if (r < nvalid && Dl[r] > col_best) { col_best = Dl[r]; col_bi = row0 + r; }
+						}
+					}
+				}
+				prev_up = upD;
+			}
+			if (TB == TB_ONE && LOC == LOC_LOCAL) {
+				// fold the per-row bests: larger value, then larger i (rows ascend), then the
+				// row's own largest j (solver.h:2048-2056 scans i, j descending, strict)
+#pragma unroll
+				for (int r = 0; r < R; r++) {
+					if (bj[r] >= 0 && bv[r] >= l_best) { l_best = bv[r]; l_bi = row0 + r; l_bj = bj[r]; }
+				}
+			}
+			__syncwarp();
+		}
+
+		// ---- group reductions and outputs
+		if (LOC == LOC_LOCAL) {
+			for (int o = 1; o < G; o <<= 1) {
+				const V ov = __shfl_xor_sync(0xffffffffu, l_best, o, G);
+				const int oi = __shfl_xor_sync(0xffffffffu, l_bi, o, G);
+				const int oj = __shfl_xor_sync(0xffffffffu, l_bj, o, G);
+				const bool take = ov > l_best || (ov == l_best && (oi > l_bi || (oi == l_bi && oj > l_bj)));
+				if (take) { l_best = ov; l_bi = oi; l_bj = oj; }
+			}
+		} else if (LOC == LOC_SEMI) {
+			for (int o = 1; o < G; o <<= 1) {
+				const V orv = __shfl_xor_sync(0xffffffffu, row_best, o, G);
+				const int orj = __shfl_xor_sync(0xffffffffu, row_bj, o, G);
+				if (orj >= 0 && (row_bj < 0 || orv > row_best)) { row_best = orv; row_bj = orj; }
+				const V ocv = __shfl_xor_sync(0xffffffffu, col_best, o, G);
+				const int oci = __shfl_xor_sync(0xffffffffu, col_bi, o, G);
+				if (oci >= 0 && (col_bi < 0 || ocv > col_best || (ocv == col_best && oci < col_bi))) {
+					col_best = ocv; col_bi = oci;
+				}
+			}
+		} else {
+			for (int o = 1; o < G; o <<= 1) {
+				const V og = __shfl_xor_sync(0xffffffffu, glob, o, G);
+				const int oh = __shfl_xor_sync(0xffffffffu, int(have_glob), o, G);
+				if (oh && !have_glob) { glob = og; have_glob = true; }
+			}
+		}
+
+		if (sub == 0 && pair >= 0) {
+			int si = -1, sj = -1, has = 0;
+			float sc = -INFINITY * p.out_sign;
+			if (!empty) {
+				if (LOC == LOC_LOCAL) {
+					if (TB == TB_ALL) {
+						has = 1;
+						sc = p.best_in[pair];
+					} else if (l_best > NEG) {
+						has = 1; si = l_bi; sj = l_bj;
+						sc = to_ref(l_best, TAG, p.out_sign);
+					}
+				} else if (LOC == LOC_SEMI) {
+					has = 1;
+					if (row_bj >= 0 && (col_bi < 0 || !(col_best > row_best))) {
+						si = ls - 1; sj = row_bj; sc = to_ref(row_best, TAG, p.out_sign);
+					} else {
+						si = col_bi; sj = lt - 1; sc = to_ref(col_best, TAG, p.out_sign);
+					}
+				} else {
+					has = 1; si = ls - 1; sj = lt - 1;
+					sc = to_ref(glob, TAG, p.out_sign);
+				}
+			} else {
+				// no cells: the seed is a border cell or does not exist
+				if (LOC == LOC_GLOBAL) {
+					has = 1; si = ls - 1; sj = lt - 1;
+					const V x = ls == 0 ? p.top_D[lt] : p.left_D[ls];
+					sc = to_ref(x, TAG, p.out_sign);
+				} else if (LOC == LOC_SEMI) {
+					// Optima over D(ls-1, 0..lt-1) then D(0..ls-1, lt-1) (solver.h:2284-2292)
+					V b = NEG;
+					for (int jj = 0; jj < lt; jj++) {
+						const V x = p.top_D[jj + 1];
+						if (x > b) { b = x; si = ls - 1; sj = jj; }
+					}
+					for (int ii = 0; ii < ls; ii++) {
+						const V x = p.left_D[ii + 1];
+						if (x > b) { b = x; si = ii; sj = lt - 1; }
+					}
+					if (b > NEG) { has = 1; sc = to_ref(b, TAG, p.out_sign); }
+				}
+			}
+			p.score[pair] = sc;
+			p.seed[2 * pair] = si;
+			p.seed[2 * pair + 1] = sj;
+			p.has_seed[pair] = has;
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------
+// Traceback walk for one optimal path (TracebackIterators<false>::Iterator::next,
+// solver.h:1497-1536), one thread per pair, over the 4-bit masks.  The walk emits the
+// alignment map: a point is an edge when the next step moves diagonally
+// (path_compressor, solver.h:809-847); P/Q steps jump to the gap-open cell.
+struct WalkParams {
+	int32_t npairs;
+	const int32_t *len_s;
+	const int32_t *len_t;
+	const int32_t *seed;
+	const int32_t *has_seed;
+	const uint32_t *masks;
+	const int64_t *mask_off;
+	int32_t G;
+	int32_t gap;    // GapKind
+	int32_t local;  // 1: stop at value-0 cells
+	int32_t *maps;  // min(ls, lt) per pair at map_off
+	const int64_t *map_off;
+	int32_t *paths;  // optional: 2 ints per point, ls + lt + 2 points per pair at path_off
+	const int64_t *path_off;
+	int32_t *path_len;
+};
+
+__global__ void walk_kernel(WalkParams p);
+
+}  // namespace pa

@@ -1,0 +1,1484 @@
+// Host runtime and C ABI of the GB300 alignment solve (include/pyalign_gb300.h).
+//
+// One pa_solver per reference Solver (factory.h:682-973): it owns the options, the border
+// vectors of its capacity (computed exactly as the reference's constructors do), a CUDA
+// stream and a set of growable device buffers.  A solve call uploads one batch, runs the
+// DP kernels and the traceback kernel on the stream, downloads the results and wraps
+// them in a pa_result that outlives later calls.  There is no CPU fallback: without a
+// device every solve fails with PA_ERR_NO_DEVICE.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <stack>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pyalign_gb300.h"
+#include "pa_dp.cuh"
+#include "pa_launch.h"
+#include "pa_wsb.h"
+
+using namespace pa;
+
+namespace {
+
+thread_local std::string g_err;
+
+pa_status fail(pa_status st, const std::string &msg) {
+	g_err = msg;
+	return st;
+}
+
+#define PA_CUDA(call)                                                                       \
+	do {                                                                                    \
+		cudaError_t e_ = (call);                                                            \
+		if (e_ != cudaSuccess)                                                              \
+			return fail(PA_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e_) + \
+			                             " at " #call);                                     \
+	} while (0)
+
+constexpr int32_t NO_TB = INT32_MIN;
+
+struct DevBuf {
+	void *p = nullptr;
+	size_t cap = 0;
+	~DevBuf() {
+		if (p) cudaFree(p);
+	}
+	cudaError_t ensure(size_t n) {
+		if (n <= cap && p) return cudaSuccess;
+		if (p) cudaFree(p);
+		p = nullptr;
+		cap = 0;
+		const size_t want = std::max<size_t>(n + n / 4, 256);
+		cudaError_t e = cudaMalloc(&p, want);
+		if (e == cudaSuccess) cap = want;
+		return e;
+	}
+	template <typename T>
+	T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct PinBuf {
+	void *p = nullptr;
+	size_t cap = 0;
+	~PinBuf() {
+		if (p) cudaFreeHost(p);
+	}
+	cudaError_t ensure(size_t n) {
+		if (n <= cap && p) return cudaSuccess;
+		if (p) cudaFreeHost(p);
+		p = nullptr;
+		cap = 0;
+		const size_t want = std::max<size_t>(n + n / 4, 256);
+		cudaError_t e = cudaMallocHost(&p, want);
+		if (e == cudaSuccess) cap = want;
+		return e;
+	}
+	template <typename T>
+	T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// Goals of solver.h:13-39 as selected by FactoryCreator (factory.h:1195-1240).
+enum Goal { GOAL_SCORE = 0, GOAL_ONE = 1, GOAL_ALL = 2 };
+// Output shapes of the 15 solve methods (factory.h:699-808).
+enum Method { M_SCORE = 0, M_ALIGNMENT = 1, M_ALIGNMENT_ITER = 2, M_SOLUTION = 3, M_SOLUTION_ITER = 4 };
+enum Form { F_DENSE = 0, F_INDEXED = 1, F_BINARY = 2 };
+
+struct Input {
+	int form;
+	int location;  // where a/b/sim/table live
+	int64_t batch, n_s, n_t;
+	const uint32_t *a, *b;
+	const float *sim;
+	const float *table;
+	int64_t table_rows, table_cols;
+	float eq, ne;
+	const int32_t *length;  // host (2, batch)
+};
+
+// xt::linspace<float>(0, (n-1)*u, n) + v with w[0] = 0 -- AffineCost::vector
+// (solver.h:2876-2880), assuming the generator start + step * i, step = (stop - start)/(n-1).
+std::vector<float> affine_vector(float u, float v, size_t n) {
+	std::vector<float> w(n);
+	const float stop = float(n - 1) * u;
+	const float step = n > 1 ? (stop - 0.0f) / float(n - 1) : 0.0f;
+	for (size_t i = 0; i < n; i++) w[i] = (0.0f + step * float(i)) + v;
+	if (n) w[0] = 0.0f;
+	return w;
+}
+
+bool integral(float x) { return std::isfinite(x) && std::nearbyint(x) == x; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// Results
+
+struct ResultData {
+	int64_t batch = 0;
+	std::vector<int32_t> ls, lt;
+	int goal = GOAL_ONE, gap = GAP_LINEAR, loc = LOC_GLOBAL, type = PA_TYPE_ALIGNMENT;
+	int remove_dup = 1;
+	int layers = 1;
+	int method = 0;
+	float sign = 1.0f;
+	int G = 32;
+	float worst = -INFINITY;
+	std::vector<float> scores;
+	std::vector<int32_t> has;     // has_alignment per lane
+	std::vector<int32_t> seeds;   // 2 per lane
+	std::vector<int64_t> map_off;
+	std::vector<int32_t> maps;
+	std::vector<int64_t> path_off;
+	std::vector<int32_t> paths, path_len;
+	std::vector<int64_t> mask_off;
+	std::vector<uint32_t> masks_one;  // TB_ONE words (solutions)
+	std::vector<uint32_t> masks_all;  // TB_ALL: 4 words per lane-step
+	std::vector<int64_t> val_off;
+	std::vector<float> values;
+	// general (WSB) gap: traceback codes and values per lane
+	std::vector<int64_t> wsb_off;
+	std::vector<int32_t> wsb_tb;
+	std::vector<float> wsb_vals;
+	std::vector<float> gen_s, gen_t;  // normalised gap costs for all-optimal WSB ties
+	bool has_algorithm = true;
+	std::string alg[3];
+
+	// ---- mask access
+	uint32_t nib(int64_t lane, int i, int j) const {
+		const int rpp = G * R;
+		const int q = i / rpp, rem = i - q * rpp, sb = rem / R, r = rem - sb * R;
+		const int64_t S = lt[lane] + G - 1;
+		const uint32_t w = masks_one[size_t(mask_off[lane] + (int64_t(q) * S + (j + sb)) * G + sb)];
+		return (w >> (4 * r)) & 15u;
+	}
+	uint32_t cell(int64_t lane, int i, int j) const {
+		const int rpp = G * R;
+		const int q = i / rpp, rem = i - q * rpp, sb = rem / R, r = rem - sb * R;
+		const int64_t S = lt[lane] + G - 1;
+		const size_t e = size_t(mask_off[lane] + (int64_t(q) * S + (j + sb)) * G + sb);
+		const uint32_t w = masks_all[4 * e + size_t(r >> 1)];
+		return (w >> (16 * (r & 1))) & 0xffffu;
+	}
+	// WSB one-optimal traceback code of D(i, j): kind (0 none, 1 diag, 2 vertical k, 3 horizontal k)
+	int32_t wsb(int64_t lane, int i, int j) const {
+		return wsb_tb[size_t(wsb_off[lane] + int64_t(i) * lt[lane] + j)];
+	}
+	float wsb_val(int64_t lane, int i, int j) const {  // normalised D(i, j), i, j >= -1
+		return wsb_vals[size_t(wsb_voff[lane] + int64_t(i + 1) * (lt[lane] + 1) + (j + 1))];
+	}
+	std::vector<int64_t> wsb_voff;
+
+	// traceback list of D(i, j) in push order (solver.h:1328-1369): all-optimal masks
+	void tb_list_all(int64_t lane, int i, int j, std::vector<std::pair<int, int>> &out, int layer = 0) const {
+		out.clear();
+		if (gap == GAP_GENERAL) {
+			wsb_list(lane, i, j, out);
+			return;
+		}
+		const uint32_t c0 = cell(lane, i, j);
+		// layer 1 (P) / 2 (Q): only that gap's own list (solver.h:2995-3016)
+		const uint32_t c = layer == 0 ? c0 : (layer == 1 ? 4u : 8u);
+		if (c & 1u) out.push_back({NO_TB, NO_TB});
+		if (c & 2u) out.push_back({i - 1, j - 1});
+		if (c & 4u) {
+			if (gap == GAP_AFFINE) {
+				for (int k = i;; k--) {
+					const uint32_t ck = cell(lane, k, j);
+					if (ck & 16u) out.push_back({k - 1, j});
+					if ((ck & 32u) && k > 0) continue;
+					break;
+				}
+			} else {
+				out.push_back({i - 1, j});
+			}
+		}
+		if (c & 8u) {
+			if (gap == GAP_AFFINE) {
+				for (int k = j;; k--) {
+					const uint32_t ck = cell(lane, i, k);
+					if (ck & 64u) out.push_back({i, k - 1});
+					if ((ck & 128u) && k > 0) continue;
+					break;
+				}
+			} else {
+				out.push_back({i, j - 1});
+			}
+		}
+	}
+	// WSB ties recomputed from the device values with the reference's float operations
+	// (solver.h:3157-3180)
+	void wsb_list(int64_t lane, int i, int j, std::vector<std::pair<int, int>> &out) const {
+		const float d = wsb_val(lane, i, j);
+		const bool local = loc == LOC_LOCAL;
+		if (local && d == 0.0f) out.push_back({NO_TB, NO_TB});
+		const float dg = wsb_val(lane, i - 1, j - 1) + wsb_diag(lane, i, j);
+		if (dg == d) out.push_back({i - 1, j - 1});
+		for (int k = -1; k < i; k++)
+			if (wsb_val(lane, k, j) + (-gen_s[size_t(i - k)]) == d) out.push_back({k, j});
+		for (int k = -1; k < j; k++)
+			if (wsb_val(lane, i, k) + (-gen_t[size_t(j - k)]) == d) out.push_back({i, k});
+	}
+	std::vector<float> wsb_sub;  // normalised similarity per lane cell (all-optimal WSB)
+	std::vector<int64_t> wsb_sub_off;
+	float wsb_diag(int64_t lane, int i, int j) const {
+		return wsb_sub[size_t(wsb_sub_off[lane] + int64_t(i) * lt[lane] + j)];
+	}
+
+	bool cont2_all(int64_t lane, int i, int j) const {
+		if (loc != LOC_LOCAL) return true;
+		if (gap == GAP_GENERAL) return wsb_val(lane, i, j) > 0.0f;
+		return !(cell(lane, i, j) & 1u);
+	}
+};
+
+struct pa_result {
+	std::shared_ptr<ResultData> d;
+};
+
+struct pa_iterator {
+	std::shared_ptr<ResultData> d;
+	int64_t lane = 0;
+	bool one_done = false;
+	// DFS state (solver.h:1582-1716)
+	struct Entry {
+		int u, v;
+		int32_t path_len;
+	};
+	std::stack<Entry> stk;
+	std::vector<std::pair<int, int>> path;
+	struct Hash {
+		size_t operator()(const std::vector<int32_t> &v) const {
+			size_t seed = 0;
+			for (auto x : v) seed ^= std::hash<int32_t>()(x) + 0x9e3779b9 + (seed << 6) + (seed >> 2);
+			return seed;
+		}
+	};
+	std::unordered_set<std::vector<int32_t>, Hash> emitted;
+	std::vector<std::pair<int, int>> scratch;
+};
+
+// ---------------------------------------------------------------------------------------
+// Solver
+
+struct pa_solver {
+	pa_options opt{};
+	std::vector<float> gen_s, gen_t;  // general gap costs (reference domain)
+	int64_t cap_s = 0, cap_t = 0;
+	int32_t batch_size = 1;
+	int gap = GAP_LINEAR;  // GapKind, or GAP_GENERAL
+	int goal = GOAL_ONE;
+	int loc = LOC_GLOBAL;
+	float sign = 1.0f;     // +1 maximize, -1 minimize
+	// normalised (maximize-form) borders, float: index k = cell -1 + k
+	std::vector<float> left_D, left_P, top_D, top_Q;
+	std::string alg[3];
+
+	int device = -1;
+	int sm_count = 0;
+	cudaStream_t own_stream = nullptr;
+	cudaStream_t stream = nullptr;
+	cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+	float last_ms[4] = {0, 0, 0, 0};
+	int32_t last_launches = 0;
+
+	DevBuf d_a, d_b, d_tab, d_dense, d_dense_off, d_ls, d_lt, d_order, d_mask_off, d_score, d_seed, d_has,
+	    d_masks, d_scratch, d_counter, d_status, d_border, d_maps, d_map_off, d_paths, d_path_off,
+	    d_path_len, d_vals, d_val_off, d_best, d_gen, d_wsb_off, d_wsb_tb, d_wsb_vals, d_wsb_sub,
+	    d_wsb_sub_off;
+	PinBuf h_stage, h_out;
+
+	~pa_solver() {
+		for (auto &e : ev)
+			if (e) cudaEventDestroy(e);
+		if (own_stream) cudaStreamDestroy(own_stream);
+	}
+};
+
+namespace {
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+pa_status ensure_device(pa_solver *s) {
+	if (s->device >= 0) return PA_OK;
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+		cudaGetLastError();
+		return fail(PA_ERR_NO_DEVICE, "no CUDA device: pyalign_gb300 has no CPU fallback");
+	}
+	PA_CUDA(cudaGetDevice(&s->device));
+	PA_CUDA(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
+	PA_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
+	if (!s->stream) s->stream = s->own_stream;
+	for (auto &e : s->ev) PA_CUDA(cudaEventCreate(&e));
+	return PA_OK;
+}
+
+// Per-call plan of the DP launch.
+struct Plan {
+	bool use_int = false;
+	int tb = TB_ONE;
+	int G = 32;
+	int64_t max_ls = 0, max_lt = 0;
+};
+
+int choose_G(int64_t max_ls) {
+	// rows per lane R = 8: the group height G*R covers the typical length in few passes
+	if (max_ls <= 32) return 4;
+	if (max_ls <= 64) return 8;
+	if (max_ls <= 128) return 16;
+	return 32;
+}
+
+template <typename V>
+V cvt(float x, bool use_int, int scale, int tag) {
+	if (use_int) {
+		if (!std::isfinite(x)) return V(-(1 << 29));
+		return V(int32_t(std::nearbyint(x)) * scale + tag);
+	}
+	return V(x);
+}
+
+template <typename V>
+pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const int32_t *h_ls,
+                 const int32_t *h_lt, int64_t npairs, bool want_values, const float *best_in_dev,
+                 int *launches) {
+	const bool ISINT = std::is_same<V, int32_t>::value;
+	const bool tag = ISINT && tb != TB_ALL;
+	const int scale = tag ? 4 : 1;
+	cudaStream_t st = s->stream;
+	DpParams<V> p{};
+	p.npairs = int32_t(npairs);
+	p.order = s->d_order.as<int32_t>();
+	p.len_s = s->d_ls.as<int32_t>();
+	p.len_t = s->d_lt.as<int32_t>();
+	p.sub_kind = in.form == F_DENSE ? SUB_DENSE : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
+	p.neg_inf = ISINT ? V(-(1 << 29)) : V(-INFINITY);
+	p.G = plan.G;
+	p.out_sign = s->sign;
+	const int gk = s->gap;  // GAP_LINEAR / GAP_AFFINE / GAP_DTW
+	const int diag_tag = (tag && gk != GAP_DTW) ? 2 : 0;
+
+	// ---- sequences and substitution
+	if (in.form != F_DENSE) {
+		p.a = in.location == PA_DEVICE ? in.a : s->d_a.as<uint32_t>();
+		p.b = in.location == PA_DEVICE ? in.b : s->d_b.as<uint32_t>();
+		p.a_stride = in.n_s;
+		p.b_stride = in.n_t;
+	}
+	std::vector<V> tabv;
+	if (in.form == F_INDEXED) {
+		p.table_rows = int32_t(in.table_rows);
+		p.table_cols = int32_t(in.table_cols);
+		p.table = s->d_tab.as<V>();
+	} else if (in.form == F_BINARY) {
+		p.eq = cvt<V>(in.eq * s->sign, ISINT, scale, diag_tag);
+		p.ne = cvt<V>(in.ne * s->sign, ISINT, scale, diag_tag);
+	} else {
+		p.dense = in.location == PA_DEVICE ? in.sim : s->d_dense.as<float>();
+		p.dense_off = s->d_dense_off.as<int64_t>();
+		p.dense_si = in.n_t * in.batch;
+		p.dense_sj = in.batch;
+		p.dense_sign = s->sign;
+	}
+	// ---- gaps (negative addends, maximize form)
+	const pa_options &o = s->opt;
+	if (gk == GAP_LINEAR) {
+		p.c_up = cvt<V>(-o.linear_s, ISINT, scale, tag ? 1 : 0);
+		p.c_left = cvt<V>(-o.linear_t, ISINT, scale, 0);
+	} else if (gk == GAP_AFFINE) {
+		const float w1s = o.affine_u_s + o.affine_v_s, w1t = o.affine_u_t + o.affine_v_t;
+		p.c_open_s = cvt<V>(-w1s, ISINT, scale, tag ? 1 : 0);
+		p.c_ext_s = cvt<V>(-o.affine_u_s, ISINT, scale, 0);
+		p.c_open_t = cvt<V>(-w1t, ISINT, scale, 0);
+		p.c_ext_t = cvt<V>(-o.affine_u_t, ISINT, scale, 0);
+	}
+	// ---- borders
+	{
+		const size_t ns = s->left_D.size(), nt = s->top_D.size();
+		std::vector<V> bv(2 * ns + 2 * nt);
+		for (size_t k = 0; k < ns; k++) {
+			bv[k] = cvt<V>(s->left_D[k], ISINT, scale, 0);
+			bv[ns + k] = cvt<V>(s->left_P[k], ISINT, scale, tag ? 1 : 0);
+		}
+		for (size_t k = 0; k < nt; k++) {
+			bv[2 * ns + k] = cvt<V>(s->top_D[k], ISINT, scale, 0);
+			bv[2 * ns + nt + k] = cvt<V>(s->top_Q[k], ISINT, scale, 0);
+		}
+		PA_CUDA(s->d_border.ensure(bv.size() * sizeof(V)));
+		PA_CUDA(cudaMemcpyAsync(s->d_border.p, bv.data(), bv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
+		V *b = s->d_border.as<V>();
+		p.left_D = b;
+		p.left_P = b + ns;
+		p.top_D = b + 2 * ns;
+		p.top_Q = b + 2 * ns + nt;
+		if (in.form == F_INDEXED) {
+			// the table is uploaded as floats; convert on the host here (small)
+			std::vector<float> ht(size_t(in.table_rows * in.table_cols));
+			if (in.location == PA_DEVICE) {
+				PA_CUDA(cudaMemcpyAsync(ht.data(), in.table, ht.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+				PA_CUDA(cudaStreamSynchronize(st));
+			} else {
+				std::memcpy(ht.data(), in.table, ht.size() * sizeof(float));
+			}
+			tabv.resize(ht.size());
+			for (size_t k = 0; k < ht.size(); k++) tabv[k] = cvt<V>(ht[k] * s->sign, ISINT, scale, diag_tag);
+			PA_CUDA(s->d_tab.ensure(tabv.size() * sizeof(V)));
+			PA_CUDA(cudaMemcpyAsync(s->d_tab.p, tabv.data(), tabv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
+			p.table = s->d_tab.as<V>();
+			PA_CUDA(cudaStreamSynchronize(st));  // tabv/bv are host temporaries
+		} else {
+			PA_CUDA(cudaStreamSynchronize(st));
+		}
+	}
+	// ---- outputs
+	p.score = s->d_score.as<float>();
+	p.seed = s->d_seed.as<int32_t>();
+	p.has_seed = s->d_has.as<int32_t>();
+	p.masks = s->d_masks.p;
+	p.mask_off = s->d_mask_off.as<int64_t>();
+	p.best_in = best_in_dev;
+	p.values = want_values ? s->d_vals.as<float>() : nullptr;
+	p.val_off = s->d_val_off.as<int64_t>();
+	p.work_counter = s->d_counter.as<int32_t>();
+	p.status = s->d_status.as<int32_t>();
+
+	// ---- grid and scratch
+	const size_t smem = (in.form == F_INDEXED && in.table_rows <= MAX_SMEM_TABLE && in.table_cols <= MAX_SMEM_TABLE)
+	                        ? size_t(in.table_rows * in.table_cols) * sizeof(V)
+	                        : 0;
+	int bps = 0;
+	cudaError_t e;
+	const int loc = s->loc;
+	if (ISINT) {
+		e = gk == GAP_LINEAR ? occupancy_dp_i_linear(loc, tb, smem, &bps)
+		    : gk == GAP_AFFINE ? occupancy_dp_i_affine(loc, tb, smem, &bps)
+		                       : occupancy_dp_i_dtw(loc, tb, smem, &bps);
+	} else {
+		e = gk == GAP_LINEAR ? occupancy_dp_f_linear(loc, tb, smem, &bps)
+		    : gk == GAP_AFFINE ? occupancy_dp_f_affine(loc, tb, smem, &bps)
+		                       : occupancy_dp_f_dtw(loc, tb, smem, &bps);
+	}
+	PA_CUDA(e);
+	bps = std::max(bps, 1);
+	const int gpw = 32 / plan.G;
+	const int64_t groups_needed = (npairs + gpw - 1) / gpw;  // warps needed
+	int64_t grid = int64_t(s->sm_count) * bps;
+	grid = std::min<int64_t>(grid, (groups_needed + WARPS - 1) / WARPS);
+	grid = std::max<int64_t>(grid, 1);
+	const int64_t slots = grid * WARPS * gpw;
+	p.scratch_stride = 2 * std::max<int64_t>(plan.max_lt, 1);
+	PA_CUDA(s->d_scratch.ensure(size_t(slots * p.scratch_stride) * 2 * sizeof(V)));
+	p.scratch = s->d_scratch.p;
+
+	PA_CUDA(cudaMemsetAsync(s->d_counter.p, 0, sizeof(int32_t), st));
+	if (ISINT) {
+		e = gk == GAP_LINEAR ? launch_dp_i_linear(loc, tb, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
+		    : gk == GAP_AFFINE ? launch_dp_i_affine(loc, tb, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
+		                       : launch_dp_i_dtw(loc, tb, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st);
+	} else {
+		e = gk == GAP_LINEAR ? launch_dp_f_linear(loc, tb, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
+		    : gk == GAP_AFFINE ? launch_dp_f_affine(loc, tb, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
+		                       : launch_dp_f_dtw(loc, tb, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st);
+	}
+	PA_CUDA(e);
+	(*launches)++;
+	(void)h_ls;
+	(void)h_lt;
+	return PA_OK;
+}
+
+// Validation shared by all entry points (factory.h:387-394, 526-533, 602-614;
+// solver.h:487-503, 719-728).
+pa_status validate(pa_solver *s, const Input &in) {
+	if (in.batch != s->batch_size)
+		return fail(PA_ERR_INVALID_ARGUMENT, "problem of batch size " + std::to_string(in.batch) +
+		                                         " given to solver that was configured to batch size " +
+		                                         std::to_string(s->batch_size));
+	if (in.n_s > s->cap_s)
+		return fail(PA_ERR_LENGTH, "sequence s of length " + std::to_string(in.n_s) +
+		                               " exceeds configured maximum length " + std::to_string(s->cap_s));
+	if (in.n_t > s->cap_t)
+		return fail(PA_ERR_LENGTH, "sequence t of length " + std::to_string(in.n_t) +
+		                               " exceeds configured maximum length " + std::to_string(s->cap_t));
+	if (!in.length) return fail(PA_ERR_INVALID_ARGUMENT, "length array missing");
+	if (in.form == F_INDEXED && in.location == PA_HOST) {
+		uint32_t ma = 0, mb = 0;
+		for (int64_t k = 0; k < in.batch * in.n_s; k++) ma = std::max(ma, in.a[k]);
+		for (int64_t k = 0; k < in.batch * in.n_t; k++) mb = std::max(mb, in.b[k]);
+		if (in.batch * in.n_s > 0 && int64_t(ma) >= in.table_rows)
+			return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a");
+		if (in.batch * in.n_t > 0 && int64_t(mb) >= in.table_cols)
+			return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in b");
+	}
+	return PA_OK;
+}
+
+// Decide int32 (exact, faster) vs float32 arithmetic.  Integer mode is used when every
+// similarity, gap cost and border is an integer and every reachable value stays below
+// 2^23 in magnitude, which also means the reference's float32 arithmetic is exact.
+bool int_mode_ok(const pa_solver *s, const Input &in, int64_t max_ls, int64_t max_lt) {
+	if (in.form == F_DENSE) return false;
+	if (s->gap == GAP_GENERAL) return false;
+	double m = 0;
+	auto chk = [&](float x) {
+		if (!integral(x)) return false;
+		m = std::max(m, double(std::fabs(x)));
+		return true;
+	};
+	const pa_options &o = s->opt;
+	if (s->gap == GAP_LINEAR && !(chk(o.linear_s) && chk(o.linear_t))) return false;
+	if (s->gap == GAP_AFFINE &&
+	    !(chk(o.affine_u_s) && chk(o.affine_v_s) && chk(o.affine_u_t) && chk(o.affine_v_t) &&
+	      chk(o.affine_u_s + o.affine_v_s) && chk(o.affine_u_t + o.affine_v_t)))
+		return false;
+	if (in.form == F_BINARY) {
+		if (!(chk(in.eq) && chk(in.ne))) return false;
+	} else {
+		if (in.location == PA_DEVICE) return false;  // table not inspected on the host
+		for (int64_t k = 0; k < in.table_rows * in.table_cols; k++)
+			if (!chk(in.table[k])) return false;
+	}
+	double mb = 0;
+	for (size_t k = 0; k <= size_t(std::min<int64_t>(max_ls, int64_t(s->left_D.size()) - 1)); k++) {
+		if (std::isfinite(s->left_D[k])) {
+			if (!integral(s->left_D[k])) return false;
+			mb = std::max(mb, double(std::fabs(s->left_D[k])));
+		}
+	}
+	for (size_t k = 0; k <= size_t(std::min<int64_t>(max_lt, int64_t(s->top_D.size()) - 1)); k++) {
+		if (std::isfinite(s->top_D[k])) {
+			if (!integral(s->top_D[k])) return false;
+			mb = std::max(mb, double(std::fabs(s->top_D[k])));
+		}
+	}
+	const double bound = double(max_ls + max_lt + 2) * m + mb;
+	return bound < double(1 << 23);
+}
+
+// General gap costs: one CTA per pair (pa_wsb.cu); values, traceback codes and the
+// similarity of every cell come back to the host for the traceback.
+pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls, const std::vector<int32_t> &lt,
+                  int *launches, ResultData &res) {
+	cudaStream_t st = s->stream;
+	const int64_t B = in.batch;
+	std::vector<int64_t> voff(size_t(B) + 1, 0), toff(size_t(B) + 1, 0);
+	for (int64_t k = 0; k < B; k++) {
+		voff[size_t(k) + 1] = voff[size_t(k)] + int64_t(ls[size_t(k)] + 1) * (lt[size_t(k)] + 1);
+		toff[size_t(k) + 1] = toff[size_t(k)] + int64_t(ls[size_t(k)]) * lt[size_t(k)];
+	}
+	res.wsb_voff = voff;
+	res.wsb_off = toff;
+	res.wsb_sub_off = toff;
+	const size_t ns = s->left_D.size(), nt = s->top_D.size();
+	std::vector<float> host(2 * ns + 2 * nt);
+	std::copy(s->left_D.begin(), s->left_D.end(), host.begin());
+	std::copy(s->top_D.begin(), s->top_D.end(), host.begin() + ns);
+	std::copy(s->gen_s.begin(), s->gen_s.end(), host.begin() + ns + nt);
+	std::copy(s->gen_t.begin(), s->gen_t.end(), host.begin() + 2 * ns + nt);
+	PA_CUDA(s->d_gen.ensure(host.size() * 4));
+	PA_CUDA(cudaMemcpyAsync(s->d_gen.p, host.data(), host.size() * 4, cudaMemcpyHostToDevice, st));
+	PA_CUDA(s->d_wsb_off.ensure(voff.size() * 8));
+	PA_CUDA(cudaMemcpyAsync(s->d_wsb_off.p, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, st));
+	PA_CUDA(s->d_wsb_sub_off.ensure(toff.size() * 8));
+	PA_CUDA(cudaMemcpyAsync(s->d_wsb_sub_off.p, toff.data(), toff.size() * 8, cudaMemcpyHostToDevice, st));
+	PA_CUDA(s->d_wsb_vals.ensure(size_t(voff[size_t(B)]) * 4));
+	PA_CUDA(s->d_wsb_tb.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
+	PA_CUDA(s->d_wsb_sub.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
+	std::vector<float> tab;
+	WsbParams w{};
+	w.npairs = int32_t(B);
+	w.len_s = s->d_ls.as<int32_t>();
+	w.len_t = s->d_lt.as<int32_t>();
+	w.local = s->loc;
+	w.sub_kind = in.form == F_DENSE ? SUB_DENSE : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
+	if (in.form != F_DENSE) {
+		w.a = in.location == PA_DEVICE ? in.a : s->d_a.as<uint32_t>();
+		w.b = in.location == PA_DEVICE ? in.b : s->d_b.as<uint32_t>();
+		w.a_stride = in.n_s;
+		w.b_stride = in.n_t;
+	}
+	if (in.form == F_INDEXED) {
+		const size_t n = size_t(in.table_rows * in.table_cols) * 4;
+		PA_CUDA(s->d_tab.ensure(n));
+		PA_CUDA(cudaMemcpyAsync(s->d_tab.p, in.table, n, in.location == PA_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+		w.table = s->d_tab.as<float>();
+		w.table_rows = int32_t(in.table_rows);
+		w.table_cols = int32_t(in.table_cols);
+	}
+	w.eq = in.eq;
+	w.ne = in.ne;
+	if (in.form == F_DENSE) {
+		w.dense = in.location == PA_DEVICE ? in.sim : s->d_dense.as<float>();
+		w.dense_si = in.n_t * in.batch;
+		w.dense_sj = in.batch;
+	}
+	w.sign = s->sign;
+	const float *g = s->d_gen.as<float>();
+	w.left_D = g;
+	w.top_D = g + ns;
+	w.gap_s = g + ns + nt;
+	w.gap_t = g + 2 * ns + nt;
+	w.vals = s->d_wsb_vals.as<float>();
+	w.vals_off = s->d_wsb_off.as<int64_t>();
+	w.tb = s->d_wsb_tb.as<int32_t>();
+	w.tb_off = s->d_wsb_sub_off.as<int64_t>();
+	w.sub = s->d_wsb_sub.as<float>();
+	w.score = s->d_score.as<float>();
+	w.seed = s->d_seed.as<int32_t>();
+	w.has_seed = s->d_has.as<int32_t>();
+	w.status = s->d_status.as<int32_t>();
+	PA_CUDA(launch_wsb(w, st));
+	(*launches)++;
+	PA_CUDA(cudaStreamSynchronize(st));  // host vectors above are temporaries
+	return PA_OK;
+}
+
+pa_status download_wsb(pa_solver *s, ResultData &res) {
+	cudaStream_t st = s->stream;
+	const int64_t B = res.batch;
+	res.wsb_vals.resize(size_t(res.wsb_voff[size_t(B)]));
+	res.wsb_tb.resize(size_t(res.wsb_off[size_t(B)]));
+	res.wsb_sub.resize(size_t(res.wsb_off[size_t(B)]));
+	if (!res.wsb_vals.empty())
+		PA_CUDA(cudaMemcpyAsync(res.wsb_vals.data(), s->d_wsb_vals.p, res.wsb_vals.size() * 4, cudaMemcpyDeviceToHost, st));
+	if (!res.wsb_tb.empty()) {
+		PA_CUDA(cudaMemcpyAsync(res.wsb_tb.data(), s->d_wsb_tb.p, res.wsb_tb.size() * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(cudaMemcpyAsync(res.wsb_sub.data(), s->d_wsb_sub.p, res.wsb_sub.size() * 4, cudaMemcpyDeviceToHost, st));
+	}
+	return PA_OK;
+}
+
+pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_out, pa_result **out,
+                     int32_t *maps_out = nullptr, const int64_t *map_offsets = nullptr) {
+	if (pa_status st = ensure_device(s)) return st;
+	if (pa_status st = validate(s, in)) return st;
+	cudaStream_t st = s->stream;
+	const int64_t B = in.batch;
+
+	// per-lane lengths, clamped to the batch arrays (stale lanes of a partial batch carry
+	// lengths beyond the master shape; the reference computes them from padding and the
+	// Python layer discards them, solve.py:382-396, 554-560)
+	std::vector<int32_t> ls(static_cast<size_t>(B)), lt(static_cast<size_t>(B));
+	int64_t max_ls = 0, max_lt = 0;
+	for (int64_t k = 0; k < B; k++) {
+		ls[size_t(k)] = int32_t(std::min<int64_t>(std::max(in.length[k], 0), in.n_s));
+		lt[size_t(k)] = int32_t(std::min<int64_t>(std::max(in.length[B + k], 0), in.n_t));
+		max_ls = std::max<int64_t>(max_ls, ls[size_t(k)]);
+		max_lt = std::max<int64_t>(max_lt, lt[size_t(k)]);
+	}
+
+	auto R_ = std::make_shared<ResultData>();
+	ResultData &res = *R_;
+	res.batch = B;
+	res.ls = ls;
+	res.lt = lt;
+	res.goal = s->goal;
+	res.gap = s->gap;
+	res.loc = s->loc;
+	res.type = s->opt.type;
+	res.remove_dup = s->opt.remove_dup;
+	res.layers = s->gap == GAP_AFFINE ? 3 : 1;
+	res.worst = -INFINITY * s->sign;
+	res.method = method;
+	res.sign = s->sign;
+	for (int k = 0; k < 3; k++) res.alg[k] = s->alg[k];
+	res.gen_s = s->gen_s;
+	res.gen_t = s->gen_t;
+
+	// what the method needs from the goal (factory.h:699-808, solver.h:2593-2740)
+	const int goal = s->goal;
+	int tb;
+	if (goal == GOAL_SCORE) tb = TB_NONE;
+	else if (goal == GOAL_ONE) tb = (method == M_SCORE) ? TB_NONE : TB_ONE;
+	else tb = method == M_SCORE ? TB_NONE : TB_ALL;
+	const bool want_values = (method == M_SOLUTION || method == M_SOLUTION_ITER) && s->gap != GAP_GENERAL;
+	const bool want_paths = method == M_SOLUTION || (goal == GOAL_ONE && method == M_SOLUTION_ITER) ||
+	                        (goal == GOAL_ONE && method == M_ALIGNMENT_ITER);
+
+	cudaEventRecord(s->ev[0], st);
+	int launches = 0;
+
+	// ---- upload inputs
+	if (in.location == PA_HOST) {
+		if (in.form == F_DENSE) {
+			const size_t n = size_t(in.n_s * in.n_t * B) * sizeof(float);
+			PA_CUDA(s->d_dense.ensure(n));
+			if (n) PA_CUDA(cudaMemcpyAsync(s->d_dense.p, in.sim, n, cudaMemcpyHostToDevice, st));
+		} else {
+			const size_t na = size_t(B * in.n_s) * sizeof(uint32_t), nb = size_t(B * in.n_t) * sizeof(uint32_t);
+			PA_CUDA(s->d_a.ensure(na));
+			PA_CUDA(s->d_b.ensure(nb));
+			if (na) PA_CUDA(cudaMemcpyAsync(s->d_a.p, in.a, na, cudaMemcpyHostToDevice, st));
+			if (nb) PA_CUDA(cudaMemcpyAsync(s->d_b.p, in.b, nb, cudaMemcpyHostToDevice, st));
+		}
+	}
+	// per-pair metadata
+	Plan plan;
+	plan.max_ls = max_ls;
+	plan.max_lt = max_lt;
+	plan.G = choose_G(max_ls);
+	plan.tb = tb;
+	res.G = plan.G;
+	std::vector<int32_t> order(static_cast<size_t>(B));
+	std::iota(order.begin(), order.end(), 0);
+	std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+		return int64_t(ls[size_t(x)]) * lt[size_t(x)] > int64_t(ls[size_t(y)]) * lt[size_t(y)];
+	});
+	std::vector<int64_t> mask_off(size_t(B) + 1, 0), map_off(size_t(B) + 1, 0), path_off(size_t(B) + 1, 0),
+	    val_off(size_t(B) + 1, 0), dense_off(size_t(B), 0);
+	const int rpp = plan.G * R;
+	for (int64_t k = 0; k < B; k++) {
+		const int64_t a = ls[size_t(k)], b = lt[size_t(k)];
+		const int64_t npass = (a == 0 || b == 0) ? 0 : (a + rpp - 1) / rpp;
+		mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * (b + plan.G - 1) * plan.G;
+		map_off[size_t(k) + 1] = map_off[size_t(k)] + std::min(a, b);
+		path_off[size_t(k) + 1] = path_off[size_t(k)] + 2 * (a + b + 2);
+		val_off[size_t(k) + 1] = val_off[size_t(k)] + int64_t(res.layers) * (a + 1) * (b + 1);
+		dense_off[size_t(k)] = k;
+	}
+	auto up = [&](DevBuf &d, const void *h, size_t n) -> cudaError_t {
+		cudaError_t e = d.ensure(n);
+		if (e != cudaSuccess || n == 0) return e;
+		return cudaMemcpyAsync(d.p, h, n, cudaMemcpyHostToDevice, st);
+	};
+	// the host vectors above must live until the copies complete: synchronise below
+	PA_CUDA(up(s->d_ls, ls.data(), ls.size() * 4));
+	PA_CUDA(up(s->d_lt, lt.data(), lt.size() * 4));
+	PA_CUDA(up(s->d_order, order.data(), order.size() * 4));
+	PA_CUDA(up(s->d_mask_off, mask_off.data(), mask_off.size() * 8));
+	PA_CUDA(up(s->d_map_off, map_off.data(), map_off.size() * 8));
+	PA_CUDA(up(s->d_path_off, path_off.data(), path_off.size() * 8));
+	PA_CUDA(up(s->d_val_off, val_off.data(), val_off.size() * 8));
+	PA_CUDA(up(s->d_dense_off, dense_off.data(), dense_off.size() * 8));
+	PA_CUDA(s->d_score.ensure(size_t(B) * 4));
+	PA_CUDA(s->d_seed.ensure(size_t(B) * 8));
+	PA_CUDA(s->d_has.ensure(size_t(B) * 4));
+	PA_CUDA(s->d_counter.ensure(4));
+	PA_CUDA(s->d_status.ensure(4));
+	PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, st));
+	const size_t mask_elem = tb == TB_ALL ? 16 : 4;
+	if (tb != TB_NONE) PA_CUDA(s->d_masks.ensure(size_t(mask_off[size_t(B)]) * mask_elem));
+	if (want_values) PA_CUDA(s->d_vals.ensure(size_t(val_off[size_t(B)]) * 4));
+	PA_CUDA(cudaEventRecord(s->ev[1], st));
+
+	// ---- DP
+	if (s->gap == GAP_GENERAL) {
+		if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
+	} else {
+		const bool use_int = int_mode_ok(s, in, max_ls, max_lt);
+		plan.use_int = use_int;
+		if (tb == TB_ALL && s->loc == LOC_LOCAL) {
+			// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
+			pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, TB_NONE, ls.data(), lt.data(), B, false, nullptr, &launches)
+			                       : run_dp<float>(s, in, plan, TB_NONE, ls.data(), lt.data(), B, false, nullptr, &launches);
+			if (e2) return e2;
+			PA_CUDA(s->d_best.ensure(size_t(B) * 4));
+			PA_CUDA(cudaMemcpyAsync(s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
+		}
+		pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, tb, ls.data(), lt.data(), B, want_values,
+		                                         s->d_best.as<float>(), &launches)
+		                       : run_dp<float>(s, in, plan, tb, ls.data(), lt.data(), B, want_values,
+		                                       s->d_best.as<float>(), &launches);
+		if (e2) return e2;
+	}
+	PA_CUDA(cudaEventRecord(s->ev[2], st));
+
+	// ---- traceback walk (one optimal path)
+	const bool need_walk = tb == TB_ONE && s->gap != GAP_GENERAL &&
+	                       (method == M_ALIGNMENT || method == M_ALIGNMENT_ITER || method == M_SOLUTION ||
+	                        method == M_SOLUTION_ITER);
+	if (need_walk) {
+		const bool to_user = maps_out && in.location == PA_DEVICE;
+		PA_CUDA(s->d_maps.ensure(size_t(map_off[size_t(B)]) * 4));
+		if (want_paths) {
+			PA_CUDA(s->d_paths.ensure(size_t(path_off[size_t(B)]) * 4));
+			PA_CUDA(s->d_path_len.ensure(size_t(B) * 4));
+		}
+		WalkParams w{};
+		w.npairs = int32_t(B);
+		w.len_s = s->d_ls.as<int32_t>();
+		w.len_t = s->d_lt.as<int32_t>();
+		w.seed = s->d_seed.as<int32_t>();
+		w.has_seed = s->d_has.as<int32_t>();
+		w.masks = s->d_masks.as<uint32_t>();
+		w.mask_off = s->d_mask_off.as<int64_t>();
+		w.G = plan.G;
+		w.gap = s->gap;
+		w.local = s->loc == LOC_LOCAL;
+		w.maps = to_user ? maps_out : s->d_maps.as<int32_t>();
+		w.map_off = s->d_map_off.as<int64_t>();
+		if (to_user && map_offsets) {
+			PA_CUDA(up(s->d_map_off, map_offsets, size_t(B) * 8));
+		}
+		w.paths = want_paths ? s->d_paths.as<int32_t>() : nullptr;
+		w.path_off = s->d_path_off.as<int64_t>();
+		w.path_len = want_paths ? s->d_path_len.as<int32_t>() : nullptr;
+		walk_kernel<<<int((B + 127) / 128), 128, 0, st>>>(w);
+		PA_CUDA(cudaGetLastError());
+		launches++;
+	}
+	PA_CUDA(cudaEventRecord(s->ev[3], st));
+
+	// ---- download
+	res.scores.resize(size_t(B));
+	res.has.resize(size_t(B));
+	res.seeds.resize(size_t(2 * B));
+	int32_t status = 0;
+	PA_CUDA(cudaMemcpyAsync(res.scores.data(), s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+	PA_CUDA(cudaMemcpyAsync(res.has.data(), s->d_has.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+	PA_CUDA(cudaMemcpyAsync(res.seeds.data(), s->d_seed.p, size_t(B) * 8, cudaMemcpyDeviceToHost, st));
+	PA_CUDA(cudaMemcpyAsync(&status, s->d_status.p, 4, cudaMemcpyDeviceToHost, st));
+	res.map_off = map_off;
+	res.mask_off = mask_off;
+	if (need_walk) {
+		if (maps_out && in.location == PA_DEVICE) {
+			// results stay on the device
+		} else if (maps_out) {
+			PA_CUDA(cudaMemcpyAsync(maps_out, s->d_maps.p, size_t(map_off[size_t(B)]) * 4, cudaMemcpyDeviceToHost, st));
+		} else {
+			res.maps.resize(size_t(map_off[size_t(B)]));
+			PA_CUDA(cudaMemcpyAsync(res.maps.data(), s->d_maps.p, res.maps.size() * 4, cudaMemcpyDeviceToHost, st));
+		}
+		if (want_paths) {
+			res.path_off = path_off;
+			res.paths.resize(size_t(path_off[size_t(B)]));
+			res.path_len.resize(size_t(B));
+			PA_CUDA(cudaMemcpyAsync(res.paths.data(), s->d_paths.p, res.paths.size() * 4, cudaMemcpyDeviceToHost, st));
+			PA_CUDA(cudaMemcpyAsync(res.path_len.data(), s->d_path_len.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+		}
+	}
+	if (tb == TB_ALL && s->gap != GAP_GENERAL) {
+		res.masks_all.resize(size_t(mask_off[size_t(B)]) * 4);
+		PA_CUDA(cudaMemcpyAsync(res.masks_all.data(), s->d_masks.p, res.masks_all.size() * 4, cudaMemcpyDeviceToHost, st));
+	}
+	if (tb == TB_ONE && want_values && s->gap != GAP_GENERAL) {
+		res.masks_one.resize(size_t(mask_off[size_t(B)]));
+		PA_CUDA(cudaMemcpyAsync(res.masks_one.data(), s->d_masks.p, res.masks_one.size() * 4, cudaMemcpyDeviceToHost, st));
+	}
+	if (want_values) {
+		res.val_off = val_off;
+		res.values.resize(size_t(val_off[size_t(B)]));
+		PA_CUDA(cudaMemcpyAsync(res.values.data(), s->d_vals.p, res.values.size() * 4, cudaMemcpyDeviceToHost, st));
+	}
+	if (s->gap == GAP_GENERAL) {
+		if (pa_status e = download_wsb(s, res)) return e;
+	}
+	PA_CUDA(cudaEventRecord(s->ev[4], st));
+	PA_CUDA(cudaStreamSynchronize(st));
+	for (int k = 0; k < 4; k++) cudaEventElapsedTime(&s->last_ms[k], s->ev[k], s->ev[k + 1]);
+	s->last_launches = launches;
+	if (status & ST_BAD_CODE) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a or b");
+
+	// ---- codomain semantics on the host side
+	if (goal == GOAL_ALL && method == M_SCORE) {
+		// Solver::score with all-optimal goal: first DFS result (solver.h:2593-2608);
+		// local problems without a positive optimum have no seed -> worst value
+		for (int64_t k = 0; k < B; k++) {
+			const bool pos = s->loc != LOC_LOCAL || (res.scores[size_t(k)] * s->sign > 0.0f);
+			if (!pos || ls[size_t(k)] == 0 || lt[size_t(k)] == 0) {
+				if (s->loc == LOC_LOCAL) res.scores[size_t(k)] = res.worst;
+			}
+		}
+	}
+	if (scores_out) std::memcpy(scores_out, res.scores.data(), size_t(B) * 4);
+	if (out) {
+		*out = new pa_result{R_};
+	}
+	return PA_OK;
+}
+
+// ---- host DFS over all-optimal masks (TracebackIterators<true>, solver.h:1647-1716)
+
+void iterator_init(pa_iterator *it) {
+	const ResultData &d = *it->d;
+	const int64_t k = it->lane;
+	const int ls = d.ls[size_t(k)], lt = d.lt[size_t(k)];
+	if (d.goal != GOAL_ALL) return;
+	if (d.loc == LOC_LOCAL) {
+		// all cells equal to a strictly positive optimum, pushed in reverse scan order
+		// (solver.h:2066-2091)
+		const float best = d.scores[size_t(k)] * d.sign;  // normalised optimum
+		if (!(best > 0.0f) || ls == 0 || lt == 0) return;
+		for (int i = ls - 1; i >= 0; i--)
+			for (int j = lt - 1; j >= 0; j--) {
+				bool seed;
+				if (d.gap == GAP_GENERAL) seed = d.wsb_val(k, i, j) == best;
+				else seed = (d.cell(k, i, j) & 256u) != 0;
+				if (seed) it->stk.push({i, j, 0});
+			}
+	} else {
+		if (d.has[size_t(k)]) it->stk.push({d.seeds[size_t(2 * k)], d.seeds[size_t(2 * k + 1)], 0});
+	}
+}
+
+// compressed path = the points emitted by path_compressor (solver.h:809-847)
+void compress(const std::vector<std::pair<int, int>> &path, std::vector<int32_t> &cp) {
+	cp.clear();
+	bool empty = true;
+	int lu = 0, lv = 0;
+	for (const auto &pt : path) {
+		if (empty) empty = false;
+		else if (pt.first != lu && pt.second != lv) {
+			if (lu >= 0 && lv >= 0) {
+				cp.push_back(lu);
+				cp.push_back(lv);
+			}
+		}
+		lu = pt.first;
+		lv = pt.second;
+	}
+}
+
+bool iterator_next_all(pa_iterator *it, std::vector<std::pair<int, int>> &path_out) {
+	const ResultData &d = *it->d;
+	const int64_t k = it->lane;
+	std::vector<int32_t> cp;
+	while (!it->stk.empty()) {
+		const auto e = it->stk.top();
+		it->stk.pop();
+		if (e.path_len == 0) it->path.clear();
+		else it->path.resize(size_t(e.path_len));
+		it->path.push_back({e.u, e.v});
+		if (e.u >= 0 && e.v >= 0 && d.cont2_all(k, e.u, e.v)) {
+			d.tb_list_all(k, e.u, e.v, it->scratch);
+			const int32_t psize = int32_t(it->path.size());
+			if (!it->scratch.empty()) {
+				for (const auto &pt : it->scratch) it->stk.push({pt.first, pt.second, psize});
+			} else {
+				it->stk.push({NO_TB, NO_TB, psize});
+			}
+		} else {
+			if (d.remove_dup) {
+				compress(it->path, cp);
+				if (it->emitted.count(cp)) continue;
+				it->emitted.insert(cp);
+			}
+			path_out = it->path;
+			return true;
+		}
+	}
+	return false;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// WSB (general gap) glue lives in pa_wsb.cu; it needs these accessors.
+namespace pa {
+pa_status wsb_fail(pa_status st, const std::string &m) { return fail(st, m); }
+}  // namespace pa
+
+// ---------------------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+const char *pa_last_error(void) { return g_err.c_str(); }
+
+const char *pa_version(void) { return "pyalign_gb300 0.1 (sm_103a)"; }
+
+int32_t pa_device_count(void) {
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess) {
+		cudaGetLastError();
+		return 0;
+	}
+	return n;
+}
+
+pa_status pa_solver_create(const pa_options *o, int64_t max_len_s, int64_t max_len_t, pa_solver **out) {
+	if (!o || !out) return fail(PA_ERR_INVALID_ARGUMENT, "null argument");
+	const int bits = o->index_bits == 16 ? 16 : 32;
+	const int64_t lim = (bits == 16 ? int64_t(INT16_MAX) : int64_t(INT32_MAX)) >> 1;  // solver.h:496-503
+	if (max_len_s < 0 || max_len_t < 0) return fail(PA_ERR_INVALID_ARGUMENT, "negative maximum length");
+	if (max_len_s > lim)
+		return fail(PA_ERR_LENGTH, "requested maximum length " + std::to_string(max_len_s) +
+		                               " for s exceeds maximum supported sequence length in this implementation " +
+		                               std::to_string(lim));
+	if (max_len_t > lim)
+		return fail(PA_ERR_LENGTH, "requested maximum length " + std::to_string(max_len_t) +
+		                               " for t exceeds maximum supported sequence length in this implementation " +
+		                               std::to_string(lim));
+	if (o->direction != PA_MINIMIZE && o->direction != PA_MAXIMIZE)
+		return fail(PA_ERR_INVALID_ARGUMENT, "illegal direction");
+	if (o->type != PA_TYPE_ALIGNMENT && o->type != PA_TYPE_DTW)
+		return fail(PA_ERR_INVALID_ARGUMENT, "illegal solver type");
+	if (o->type == PA_TYPE_ALIGNMENT) {
+		if (o->locality < 0 || o->locality > 2) return fail(PA_ERR_INVALID_ARGUMENT, "invalid locality");
+		if (o->count < 0 || o->count > 1) return fail(PA_ERR_INVALID_ARGUMENT, "invalid count");
+		if (o->detail < 0 || o->detail > 2) return fail(PA_ERR_INVALID_ARGUMENT, "invalid detail");
+		if (o->gap_kind < 0 || o->gap_kind > 2) return fail(PA_ERR_INVALID_ARGUMENT, "invalid gap cost kind");
+	}
+	auto s = std::make_unique<pa_solver>();
+	s->opt = *o;
+	s->opt.general_s = nullptr;
+	s->opt.general_t = nullptr;
+	s->cap_s = max_len_s;
+	s->cap_t = max_len_t;
+	s->batch_size = o->batch ? (o->batch_size > 0 ? o->batch_size : 2048) : 1;
+	s->sign = o->direction == PA_MAXIMIZE ? 1.0f : -1.0f;
+	const float sgn = o->direction == PA_MINIMIZE ? 1.0f : -1.0f;  // gap_sgn (solver.h:2807)
+	const size_t ns = size_t(max_len_s) + 1, nt = size_t(max_len_t) + 1;
+	s->left_D.assign(ns, 0.0f);
+	s->left_P.assign(ns, 0.0f);
+	s->top_D.assign(nt, 0.0f);
+	s->top_Q.assign(nt, 0.0f);
+	// normalised value = sign * reference value
+	auto norm = [&](float ref) { return ref * s->sign; };
+	if (o->type == PA_TYPE_DTW) {
+		s->gap = GAP_DTW;
+		s->goal = GOAL_ONE;  // factory.h:1055-1099
+		s->loc = LOC_GLOBAL;
+		const float worst = -INFINITY;  // normalised
+		std::fill(s->left_D.begin(), s->left_D.end(), worst);
+		std::fill(s->top_D.begin(), s->top_D.end(), worst);
+		s->left_D[0] = s->top_D[0] = 0.0f;  // solver.h:3205-3210
+		s->alg[0] = "DTW";
+		s->alg[1] = "n^2";
+		s->alg[2] = "n^2";
+	} else {
+		s->gap = o->gap_kind == PA_GAP_LINEAR ? GAP_LINEAR : o->gap_kind == PA_GAP_AFFINE ? GAP_AFFINE : GAP_GENERAL;
+		s->goal = o->count == PA_COUNT_ALL ? GOAL_ALL : (o->detail == PA_DETAIL_SCORE ? GOAL_SCORE : GOAL_ONE);
+		s->loc = o->locality == PA_LOCAL ? LOC_LOCAL : o->locality == PA_GLOBAL ? LOC_GLOBAL : LOC_SEMI;
+		const bool global = s->loc == LOC_GLOBAL;
+		if (s->gap == GAP_LINEAR) {  // solver.h:2806-2814: arange(0, n) * g * gap_sgn
+			for (size_t k = 0; k < ns; k++) s->left_D[k] = global ? norm((float(int64_t(k)) * o->linear_s) * sgn) : 0.0f;
+			for (size_t k = 0; k < nt; k++) s->top_D[k] = global ? norm((float(int64_t(k)) * o->linear_t) * sgn) : 0.0f;
+			s->alg[0] = global ? "Needleman-Wunsch" : "Smith-Waterman";
+			s->alg[1] = "n^2";
+			s->alg[2] = "n^2";
+		} else if (s->gap == GAP_AFFINE) {  // solver.h:2918-2967
+			const auto ws = affine_vector(o->affine_u_s, o->affine_v_s, ns);
+			const auto wt = affine_vector(o->affine_u_t, o->affine_v_t, nt);
+			for (size_t k = 0; k < ns; k++) s->left_D[k] = s->left_P[k] = global ? norm(ws[k] * sgn) : 0.0f;
+			for (size_t k = 0; k < nt; k++) s->top_D[k] = s->top_Q[k] = global ? norm(wt[k] * sgn) : 0.0f;
+			s->alg[0] = "Gotoh";
+			s->alg[1] = "n^2";
+			s->alg[2] = "n^2";
+		} else {  // solver.h:3095-3126
+			if (!o->general_s || !o->general_t)
+				return fail(PA_ERR_INVALID_ARGUMENT, "general gap cost needs cost vectors");
+			s->gen_s.assign(o->general_s, o->general_s + ns);
+			s->gen_t.assign(o->general_t, o->general_t + nt);
+			for (size_t k = 0; k < ns; k++) s->left_D[k] = global ? norm(s->gen_s[k] * sgn) : 0.0f;
+			for (size_t k = 0; k < nt; k++) s->top_D[k] = global ? norm(s->gen_t[k] * sgn) : 0.0f;
+			s->alg[0] = "Waterman-Smith-Beyer";
+			s->alg[1] = "n^3";
+			s->alg[2] = "n^2";
+		}
+	}
+	*out = s.release();
+	return PA_OK;
+}
+
+void pa_solver_destroy(pa_solver *s) { delete s; }
+
+int32_t pa_solver_batch_size(const pa_solver *s) { return s ? s->batch_size : 0; }
+
+pa_status pa_solver_set_stream(pa_solver *s, void *stream) {
+	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
+	if (pa_status st = ensure_device(s)) return st;
+	s->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : s->own_stream;
+	return PA_OK;
+}
+
+pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel_launches) {
+	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
+	if (ms4)
+		for (int k = 0; k < 4; k++) ms4[k] = s->last_ms[k];
+	if (kernel_launches) *kernel_launches = s->last_launches;
+	return PA_OK;
+}
+
+#define PA_DENSE_INPUT                                                                            \
+	Input in{};                                                                                   \
+	in.form = F_DENSE;                                                                            \
+	in.location = PA_HOST;                                                                        \
+	in.batch = batch;                                                                             \
+	in.n_s = n_s;                                                                                 \
+	in.n_t = n_t;                                                                                 \
+	in.sim = sim;                                                                                 \
+	in.length = length;
+#define PA_INDEXED_INPUT                                                                          \
+	Input in{};                                                                                   \
+	in.form = F_INDEXED;                                                                          \
+	in.location = PA_HOST;                                                                        \
+	in.batch = batch;                                                                             \
+	in.n_s = n_s;                                                                                 \
+	in.n_t = n_t;                                                                                 \
+	in.a = a;                                                                                     \
+	in.b = b;                                                                                     \
+	in.table = table;                                                                             \
+	in.table_rows = table_rows;                                                                   \
+	in.table_cols = table_cols;                                                                   \
+	in.length = length;
+#define PA_BINARY_INPUT                                                                           \
+	Input in{};                                                                                   \
+	in.form = F_BINARY;                                                                           \
+	in.location = PA_HOST;                                                                        \
+	in.batch = batch;                                                                             \
+	in.n_s = n_s;                                                                                 \
+	in.n_t = n_t;                                                                                 \
+	in.a = a;                                                                                     \
+	in.b = b;                                                                                     \
+	in.eq = eq;                                                                                   \
+	in.ne = ne;                                                                                   \
+	in.length = length;
+
+pa_status pa_solve_for_score(pa_solver *s, const float *sim, int64_t n_s, int64_t n_t, int64_t batch,
+                             const int32_t *length, float *scores) {
+	PA_DENSE_INPUT return solve_impl(s, in, M_SCORE, scores, nullptr);
+}
+pa_status pa_solve_indexed_for_score(pa_solver *s, const uint32_t *a, const uint32_t *b, int64_t batch, int64_t n_s,
+                                     int64_t n_t, const float *table, int64_t table_rows, int64_t table_cols,
+                                     const int32_t *length, float *scores) {
+	PA_INDEXED_INPUT return solve_impl(s, in, M_SCORE, scores, nullptr);
+}
+pa_status pa_solve_binary_for_score(pa_solver *s, const uint32_t *a, const uint32_t *b, int64_t batch, int64_t n_s,
+                                    int64_t n_t, float eq, float ne, const int32_t *length, float *scores) {
+	PA_BINARY_INPUT return solve_impl(s, in, M_SCORE, scores, nullptr);
+}
+
+#define PA_METHODS(NAME, M)                                                                               \
+	pa_status pa_solve_for_##NAME(pa_solver *s, const float *sim, int64_t n_s, int64_t n_t, int64_t batch, \
+	                              const int32_t *length, pa_result **out) {                              \
+		PA_DENSE_INPUT return solve_impl(s, in, M, nullptr, out);                                        \
+	}                                                                                                    \
+	pa_status pa_solve_indexed_for_##NAME(pa_solver *s, const uint32_t *a, const uint32_t *b, int64_t batch, \
+	                                      int64_t n_s, int64_t n_t, const float *table, int64_t table_rows,  \
+	                                      int64_t table_cols, const int32_t *length, pa_result **out) {      \
+		PA_INDEXED_INPUT return solve_impl(s, in, M, nullptr, out);                                      \
+	}                                                                                                    \
+	pa_status pa_solve_binary_for_##NAME(pa_solver *s, const uint32_t *a, const uint32_t *b, int64_t batch, \
+	                                     int64_t n_s, int64_t n_t, float eq, float ne, const int32_t *length, \
+	                                     pa_result **out) {                                              \
+		PA_BINARY_INPUT return solve_impl(s, in, M, nullptr, out);                                       \
+	}
+
+PA_METHODS(alignment, M_ALIGNMENT)
+PA_METHODS(alignment_iterator, M_ALIGNMENT_ITER)
+PA_METHODS(solution, M_SOLUTION)
+PA_METHODS(solution_iterator, M_SOLUTION_ITER)
+
+pa_status pa_solve_batch(pa_solver *s, const pa_batch *b, float *scores, int32_t *maps, const int64_t *map_offsets) {
+	if (!s || !b) return fail(PA_ERR_INVALID_ARGUMENT, "null argument");
+	Input in{};
+	in.form = b->form;
+	in.location = b->location;
+	in.batch = b->batch;
+	in.n_s = b->n_s;
+	in.n_t = b->n_t;
+	in.a = b->a;
+	in.b = b->b;
+	in.sim = b->sim;
+	in.table = b->table;
+	in.table_rows = b->table_rows;
+	in.table_cols = b->table_cols;
+	in.eq = b->eq;
+	in.ne = b->ne;
+	in.length = b->length;
+	if (s->goal == GOAL_ALL) return fail(PA_ERR_UNSUPPORTED, "pa_solve_batch returns one alignment per pair");
+	pa_result *r = nullptr;
+	const bool dev = b->location == PA_DEVICE;
+	pa_status st = solve_impl(s, in, maps ? M_ALIGNMENT : M_SCORE, dev ? nullptr : scores, &r, maps, map_offsets);
+	if (st) return st;
+	if (dev && scores) {
+		cudaError_t e = cudaMemcpyAsync(scores, s->d_score.p, size_t(b->batch) * 4, cudaMemcpyDeviceToDevice, s->stream);
+		if (e != cudaSuccess) {
+			pa_result_destroy(r);
+			return fail(PA_ERR_CUDA, cudaGetErrorString(e));
+		}
+	}
+	pa_result_destroy(r);
+	return PA_OK;
+}
+
+void pa_result_destroy(pa_result *r) { delete r; }
+int64_t pa_result_size(const pa_result *r) { return r ? r->d->batch : 0; }
+int64_t pa_result_len_s(const pa_result *r, int64_t lane) { return r->d->ls[size_t(lane)]; }
+int64_t pa_result_len_t(const pa_result *r, int64_t lane) { return r->d->lt[size_t(lane)]; }
+
+int32_t pa_result_has_alignment(const pa_result *r, int64_t lane) {
+	const ResultData &d = *r->d;
+	if (d.goal == GOAL_ALL) {
+		pa_iterator it;
+		it.d = r->d;
+		it.lane = lane;
+		iterator_init(&it);
+		return it.stk.empty() ? 0 : 1;
+	}
+	return d.has[size_t(lane)];
+}
+
+float pa_result_score(const pa_result *r, int64_t lane) {
+	const ResultData &d = *r->d;
+	if (!pa_result_has_alignment(r, lane)) return d.worst;
+	return d.scores[size_t(lane)];
+}
+
+}  // extern "C"
+
+static void map_from_path(const ResultData &d, int64_t lane, const std::vector<std::pair<int, int>> &path,
+                          int32_t *map) {
+	const int ls = d.ls[size_t(lane)], lt = d.lt[size_t(lane)];
+	const int n = std::min(ls, lt);
+	for (int k = 0; k < n; k++) map[k] = -1;
+	std::vector<int32_t> cp;
+	compress(path, cp);
+	for (size_t k = 0; k + 1 < cp.size(); k += 2) {
+		if (ls <= lt) map[cp[k]] = cp[k + 1];
+		else map[cp[k + 1]] = cp[k];
+	}
+}
+
+// The one-path walk of a lane from the device results or (all-optimal goal) the first
+// result of the DFS.
+static bool lane_walk(const pa_result *r, int64_t lane, std::vector<std::pair<int, int>> *path, int32_t *map) {
+	const ResultData &d = *r->d;
+	if (d.goal == GOAL_ALL) {
+		pa_iterator it;
+		it.d = r->d;
+		it.lane = lane;
+		iterator_init(&it);
+		std::vector<std::pair<int, int>> p;
+		if (!iterator_next_all(&it, p)) return false;
+		if (map) map_from_path(d, lane, p, map);
+		if (path) *path = p;
+		return true;
+	}
+	if (!d.has[size_t(lane)]) return false;
+	const int n = std::min(d.ls[size_t(lane)], d.lt[size_t(lane)]);
+	if (map) {
+		if (d.gap == GAP_GENERAL) {
+			std::vector<std::pair<int, int>> p;
+			// WSB one-optimal walk from the device traceback codes
+			int u = d.seeds[size_t(2 * lane)], v = d.seeds[size_t(2 * lane + 1)];
+			p.push_back({u, v});
+			while (u >= 0 && v >= 0) {
+				if (d.loc == LOC_LOCAL && !(d.wsb_val(lane, u, v) > 0.0f)) break;
+				const int32_t c = d.wsb(lane, u, v);
+				const int kind = c & 3, kk = (c >> 2) - 1;
+				if (kind == 0) { u = NO_TB; v = NO_TB; }
+				else if (kind == 1) { u--; v--; }
+				else if (kind == 2) u = kk;
+				else v = kk;
+				p.push_back({u, v});
+			}
+			map_from_path(d, lane, p, map);
+			if (path) *path = p;
+			return true;
+		}
+		if (d.maps.empty()) {
+			for (int k = 0; k < n; k++) map[k] = -1;
+		} else {
+			std::memcpy(map, d.maps.data() + d.map_off[size_t(lane)], size_t(n) * 4);
+		}
+	}
+	if (path && !d.path_len.empty()) {
+		path->clear();
+		const int32_t *pp = d.paths.data() + d.path_off[size_t(lane)];
+		for (int k = 0; k < d.path_len[size_t(lane)]; k++) path->push_back({pp[2 * k], pp[2 * k + 1]});
+	}
+	return true;
+}
+
+extern "C" {
+
+pa_status pa_result_alignment(const pa_result *r, int64_t lane, int32_t *map) {
+	if (!r || lane < 0 || lane >= r->d->batch) return fail(PA_ERR_INVALID_ARGUMENT, "bad lane");
+	const ResultData &d = *r->d;
+	const int n = std::min(d.ls[size_t(lane)], d.lt[size_t(lane)]);
+	if (!lane_walk(r, lane, nullptr, map))
+		for (int k = 0; k < n; k++) map[k] = -1;
+	return PA_OK;
+}
+
+pa_status pa_result_export(const pa_result *r, float *scores, int32_t *maps, const int64_t *map_offsets) {
+	if (!r) return fail(PA_ERR_INVALID_ARGUMENT, "null result");
+	for (int64_t k = 0; k < r->d->batch; k++) {
+		if (scores) scores[k] = pa_result_score(r, k);
+		if (maps) pa_result_alignment(r, k, maps + map_offsets[k]);
+	}
+	return PA_OK;
+}
+
+int32_t pa_result_layers(const pa_result *r, int64_t) {
+	// Solver::solution copies every layer; the iterators detach layer D only
+	// (solver.h:2644-2651, 2680, 2720-2721)
+	const ResultData &d = *r->d;
+	return d.method == M_SOLUTION ? d.layers : 1;
+}
+
+int32_t pa_result_max_degree_1(const pa_result *r) { return r->d->goal != GOAL_ALL ? 1 : 0; }
+
+pa_status pa_result_values(const pa_result *r, int64_t lane, float *values) {
+	const ResultData &d = *r->d;
+	const int ls = d.ls[size_t(lane)], lt = d.lt[size_t(lane)];
+	const size_t n = size_t(ls + 1) * size_t(lt + 1) * size_t(pa_result_layers(r, lane));
+	if (d.gap == GAP_GENERAL) {
+		const float *v = d.wsb_vals.data() + d.wsb_voff[size_t(lane)];
+		for (size_t k = 0; k < n; k++) values[k] = v[k] * d.sign;
+		return PA_OK;
+	}
+	if (d.values.empty()) return fail(PA_ERR_INVALID_ARGUMENT, "no values in this result");
+	std::memcpy(values, d.values.data() + d.val_off[size_t(lane)], n * 4);
+	return PA_OK;
+}
+
+}  // extern "C"
+
+// traceback of one cell and layer as a list (one- or all-optimal), storage indices
+// i, j >= 0 meaning cell (i-1, j-1).
+static void cell_tb(const ResultData &d, int64_t lane, int layer, int i, int j, std::vector<std::pair<int, int>> &out,
+                    std::vector<int32_t> &colP, std::vector<int32_t> &rowQ) {
+	out.clear();
+	if (i == 0 || j == 0) return;  // borders are cleared (solver.h:530-537, 2953-2967)
+	const int u = i - 1, v = j - 1;
+	if (d.goal == GOAL_ALL) {
+		d.tb_list_all(lane, u, v, out, layer);
+		return;
+	}
+	if (d.gap == GAP_GENERAL) {
+		const int32_t c = d.wsb(lane, u, v);
+		const int kind = c & 3, kk = (c >> 2) - 1;
+		if (kind == 1) out.push_back({u - 1, v - 1});
+		else if (kind == 2) out.push_back({kk, v});
+		else if (kind == 3) out.push_back({u, kk});
+		return;
+	}
+	const uint32_t nb = d.nib(lane, u, v);
+	const int lt = d.lt[size_t(lane)];
+	(void)lt;
+	if (layer == 1) {  // P: (u-1, v) or tb_P(u-1, v) -- colP holds tb_P row index per column
+		out.push_back({colP[size_t(v)], v});
+		return;
+	}
+	if (layer == 2) {
+		out.push_back({u, rowQ[size_t(u)]});
+		return;
+	}
+	const uint32_t code = nb & 3u;
+	if (code == 3u && d.loc == LOC_LOCAL) return;  // the zero candidate: traceback_1 of size 0
+	if (code == 2u) out.push_back({u - 1, v - 1});
+	else if (code == 1u) out.push_back({d.gap == GAP_AFFINE ? colP[size_t(v)] : u - 1, v});
+	else out.push_back({u, d.gap == GAP_AFFINE ? rowQ[size_t(u)] : v - 1});
+}
+
+// Iterate the cells in storage order, maintaining tb_P (per column) and tb_Q (per row)
+// gap-open coordinates for one-optimal affine masks.
+template <typename F>
+static void for_each_cell_tb(const ResultData &d, int64_t lane, int layer, F f) {
+	const int ls = d.ls[size_t(lane)], lt = d.lt[size_t(lane)];
+	std::vector<int32_t> colP(size_t(std::max(lt, 1)), 0), rowQ(size_t(std::max(ls, 1)), 0);
+	std::vector<std::pair<int, int>> lst;
+	const bool affine_one = d.gap == GAP_AFFINE && d.goal != GOAL_ALL && d.gap != GAP_GENERAL;
+	for (int i = 0; i <= ls; i++) {
+		for (int j = 0; j <= lt; j++) {
+			if (affine_one && i > 0 && j > 0) {
+				const int u = i - 1, v = j - 1;
+				const uint32_t nb = d.nib(lane, u, v);
+				colP[size_t(v)] = (nb & 4u) ? colP[size_t(v)] : u - 1;  // tb_P(u, v)
+				rowQ[size_t(u)] = (nb & 8u) ? rowQ[size_t(u)] : v - 1;  // tb_Q(u, v)
+			}
+			cell_tb(d, lane, layer, i, j, lst, colP, rowQ);
+			f(i, j, lst);
+		}
+	}
+}
+
+extern "C" {
+
+pa_status pa_result_tb_matrix(const pa_result *r, int64_t lane, int32_t *tb) {
+	const ResultData &d = *r->d;
+	const int ls = d.ls[size_t(lane)], lt = d.lt[size_t(lane)];
+	const int layers = pa_result_layers(r, lane);
+	for (int layer = 0; layer < layers; layer++) {
+		int32_t *t = tb + size_t(layer) * size_t(ls + 1) * size_t(lt + 1) * 2;
+		for_each_cell_tb(d, lane, layer, [&](int i, int j, const std::vector<std::pair<int, int>> &l) {
+			const size_t c = size_t(i) * size_t(lt + 1) + size_t(j);
+			t[2 * c] = l.empty() ? NO_TB : l[0].first;
+			t[2 * c + 1] = l.empty() ? NO_TB : l[0].second;
+		});
+	}
+	return PA_OK;
+}
+
+int64_t pa_result_tb_edges(const pa_result *r, int64_t lane, int32_t layer, int32_t *edges) {
+	const ResultData &d = *r->d;
+	int64_t n = 0;
+	for_each_cell_tb(d, lane, layer, [&](int i, int j, const std::vector<std::pair<int, int>> &l) {
+		for (const auto &pt : l) {
+			if (edges) {
+				edges[4 * n + 0] = i - 1;
+				edges[4 * n + 1] = j - 1;
+				edges[4 * n + 2] = pt.first;
+				edges[4 * n + 3] = pt.second;
+			}
+			n++;
+		}
+	});
+	return n;
+}
+
+int64_t pa_result_path(const pa_result *r, int64_t lane, int32_t *path) {
+	std::vector<std::pair<int, int>> p;
+	if (!lane_walk(r, lane, &p, nullptr)) return -1;
+	if (path)
+		for (size_t k = 0; k < p.size(); k++) {
+			path[2 * k] = p[k].first;
+			path[2 * k + 1] = p[k].second;
+		}
+	return int64_t(p.size());
+}
+
+const char *pa_result_algorithm(const pa_result *r, int32_t field) {
+	if (!r || field < 0 || field > 2) return "";
+	return r->d->alg[field].c_str();
+}
+
+pa_status pa_result_iterator(pa_result *r, int64_t lane, pa_iterator **out) {
+	if (!r || lane < 0 || lane >= r->d->batch) return fail(PA_ERR_INVALID_ARGUMENT, "bad lane");
+	auto *it = new pa_iterator();
+	it->d = r->d;
+	it->lane = lane;
+	iterator_init(it);
+	*out = it;
+	return PA_OK;
+}
+
+int32_t pa_iterator_next(pa_iterator *it, float *score, int32_t *map, int32_t *path, int64_t *path_len) {
+	const ResultData &d = *it->d;
+	const int64_t lane = it->lane;
+	std::vector<std::pair<int, int>> p;
+	if (d.goal != GOAL_ALL) {
+		// TracebackIterators<false>: a single result (solver.h:1497-1536)
+		if (it->one_done) return 0;
+		it->one_done = true;
+		pa_result tmp{it->d};
+		if (!lane_walk(&tmp, lane, &p, map)) return 0;
+		if (score) *score = d.scores[size_t(lane)];
+	} else {
+		if (!iterator_next_all(it, p)) return 0;
+		if (map) map_from_path(d, lane, p, map);
+		if (score) *score = d.scores[size_t(lane)];
+	}
+	if (path)
+		for (size_t k = 0; k < p.size(); k++) {
+			path[2 * k] = p[k].first;
+			path[2 * k + 1] = p[k].second;
+		}
+	if (path_len) *path_len = int64_t(p.size());
+	return 1;
+}
+
+void pa_iterator_destroy(pa_iterator *it) { delete it; }
+
+}  // extern "C"

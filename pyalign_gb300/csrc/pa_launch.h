@@ -1,0 +1,19 @@
+// Launch entry points of the DP kernel families (one translation unit each).
+#pragma once
+#include "pa_dp.cuh"
+
+namespace pa {
+
+#define PA_DECL(V, VT, GAP)                                                                      \
+	cudaError_t launch_dp_##V##_##GAP(int loc, int tb, const DpParams<VT> &p, int grid, size_t smem, \
+	                                  cudaStream_t st);                                          \
+	cudaError_t occupancy_dp_##V##_##GAP(int loc, int tb, size_t smem, int *blocks_per_sm);
+PA_DECL(i, int32_t, linear)
+PA_DECL(i, int32_t, affine)
+PA_DECL(i, int32_t, dtw)
+PA_DECL(f, float, linear)
+PA_DECL(f, float, affine)
+PA_DECL(f, float, dtw)
+#undef PA_DECL
+
+}  // namespace pa
