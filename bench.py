@@ -1,0 +1,436 @@
+"""Benchmark of the batched alignment solve on GB300 (one JSON line on stdout).
+
+Workload (the batched form of pyalign's ProblemBatch solve): local alignment
+(Smith-Waterman) with affine gaps (Gotoh, open 5, extend 2), DNA alphabet {A,C,G,T}
+i.i.d. uniform, match +2 / mismatch -3 (int32 scores), 65,536 pairs whose lengths are drawn
+independently uniform in [100, 1000]; half of the pairs are a seeded query and a copy of it
+with 10% random substitutions/insertions/deletions.  Codomain: score plus one optimal
+traceback per pair (pyalign.solve.LocalSolver(AffineGapCost(5, 2), codomain=Alignment)).
+Data is synthetic and seeded (no dataset involved).
+
+A "step" is one pass of the solve over the whole batch.  `value` is GCUPS (cells = sum of
+|s|*|t|) with the codes already resident in HBM; `e2e` is the same metric through the C ABI
+with pinned host buffers, host<->device copies inside the timed region.  The reference arm
+(--impl reference) times the CPU restatement of the reference's solver (the reference's
+xtensor core cannot be built here) on the host cores.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "GCUPS: batched Gotoh score+traceback, and fwd+bwd, vs plain GPU path, 1 GB300"
+WORKLOAD = "local affine (Gotoh 5/2) DNA +2/-3, 65536 pairs, |s|,|t| ~ U[100,1000], score + one traceback"
+# algorithmic ALU ops per cell: Gotoh 9 + local zero 1 + one-optimal traceback mask 4
+OPS_PER_CELL = 14
+# algorithmic HBM bytes per cell: the 4-bit traceback nibble
+BYTES_PER_CELL = 0.5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--pairs", type=int, default=65536)
+    ap.add_argument("--seed", type=int, default=1002)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------- workload
+
+def mutate(rng, s, rate=0.1, alphabet=4):
+    """Copy of s with `rate` events per position: substitution / insertion / deletion."""
+    n = len(s)
+    ev = rng.random(n) < rate
+    kind = rng.integers(0, 3, n)
+    out = s.copy()
+    sub = ev & (kind == 0)
+    out[sub] = rng.integers(0, alphabet, int(sub.sum()))
+    ins = ev & (kind == 1)
+    keep = ~(ev & (kind == 2))
+    counts = keep.astype(np.int64) + ins.astype(np.int64)
+    idx = np.repeat(np.arange(n), counts)
+    vals = out[idx]
+    first = np.cumsum(counts) - counts
+    vals[first[ins]] = rng.integers(0, alphabet, int(ins.sum()))
+    return vals.astype(np.uint32)
+
+
+def make_workload(pairs, seed, lo=100, hi=1000):
+    rng = np.random.default_rng(seed)
+    ls = rng.integers(lo, hi + 1, size=pairs).astype(np.int32)
+    lt = rng.integers(lo, hi + 1, size=pairs).astype(np.int32)
+    a = rng.integers(0, 4, size=(pairs, hi), dtype=np.uint32)
+    b = rng.integers(0, 4, size=(pairs, hi), dtype=np.uint32)
+    related = rng.random(pairs) < 0.5
+    for k in np.nonzero(related)[0]:
+        t = mutate(rng, a[k, :ls[k]])
+        if len(t) > hi:
+            t = t[:hi]
+        if len(t) < lo:
+            t = np.concatenate([t, rng.integers(0, 4, lo - len(t)).astype(np.uint32)])
+        b[k, :len(t)] = t
+        lt[k] = len(t)
+    for k in range(pairs):  # padding as the reference's forms leave it: zeros
+        a[k, ls[k]:] = 0
+        b[k, lt[k]:] = 0
+    table = np.full((4, 4), -3.0, dtype=np.float32)
+    np.fill_diagonal(table, 2.0)
+    return a, b, ls, lt, table
+
+
+class AffineGap:
+    """pyalign.gaps.AffineGapCost(open, extend) as seen by the native module (gaps.py:164-193)."""
+
+    def __init__(self, open_, extend):
+        self.u, self.v = open_ - extend, extend
+
+    def to_special_case(self):
+        return {"affine": (self.u, self.v)}
+
+
+def options_dict(alg, batch_size):
+    import types
+    return {
+        "solver": alg.Type.ALIGNMENT, "direction": alg.Direction.MAXIMIZE, "batch": True,
+        "batch_size": batch_size, "return_dup": False, "locality": alg.Locality.LOCAL,
+        "codomain": types.SimpleNamespace(detail=alg.Detail.ALIGNMENT, count=alg.Count.ONE),
+        "gap_cost": AffineGap(5.0, 2.0),
+    }
+
+
+# --------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region (read-only)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- CPU baseline
+
+def cpu_baseline(a, b, ls, lt, table, seconds):
+    """The oracle (CPU restatement of the reference's solver) on a bounded sample, all host
+    threads.  Returns (GCUPS, threads, sample description)."""
+    import oracle.algorithm as oalg
+    L = ctypes.CDLL(oalg.build())
+    L.pao_batch_alignments.restype = ctypes.c_int64
+    vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+    L.pao_batch_alignments.argtypes = [vp, i32, vp, vp, vp, i64, vp, i64, vp, i32, i32, vp, vp, vp]
+    threads = os.cpu_count() or 1
+    opts = oalg._Options()
+    opts.type, opts.direction, opts.detail, opts.count, opts.locality = 0, 1, 1, 0, 0
+    opts.remove_dup, opts.gap_kind = 1, 1
+    opts.affine_u_s = opts.affine_u_t = 2.0   # Gotoh u = extend
+    opts.affine_v_s = opts.affine_v_t = 3.0   # Gotoh v = open - extend
+    opts.cap_s = opts.cap_t = 1000
+
+    def run(idx):
+        n = len(idx)
+        sa = np.ascontiguousarray(a[idx])
+        sb = np.ascontiguousarray(b[idx])
+        sls = np.ascontiguousarray(ls[idx])
+        slt = np.ascontiguousarray(lt[idx])
+        sizes = np.minimum(sls, slt).astype(np.int64)
+        offs = np.zeros(n, np.int64)
+        offs[1:] = np.cumsum(sizes)[:-1]
+        maps = np.zeros(int(sizes.sum()) + 1, np.int32)
+        scores = np.zeros(n, np.float32)
+        t0 = time.perf_counter()
+        cells = L.pao_batch_alignments(
+            ctypes.addressof(opts), n, sls.ctypes.data, slt.ctypes.data, sa.ctypes.data, sa.shape[1],
+            sb.ctypes.data, sb.shape[1], table.ctypes.data, 4, threads, scores.ctypes.data,
+            maps.ctypes.data, offs.ctypes.data)
+        return cells, time.perf_counter() - t0
+
+    probe = np.arange(0, min(len(ls), threads * 2))
+    cells, dt = run(probe)
+    rate = cells / max(dt, 1e-6)
+    target = rate * seconds
+    cum = np.cumsum(ls.astype(np.int64) * lt.astype(np.int64))
+    n = int(np.searchsorted(cum, target)) + 1
+    n = max(threads, min(n, len(ls)))
+    cells, dt = run(np.arange(n))
+    return cells / dt / 1e9, threads, f"first {n} pairs of the workload ({cells:.3e} cells, {dt:.1f} s)"
+
+
+# --------------------------------------------------------------------------- arms
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    a, b, ls, lt, table = make_workload(args.pairs, args.seed)
+    per_step = args.cpu_seconds / max(args.steps, 1)
+    vals = []
+    desc = None
+    threads = os.cpu_count() or 1
+    for k in range(args.warmup + args.steps):
+        g, threads, desc = cpu_baseline(a, b, ls, lt, table, per_step if k >= args.warmup else 1.0)
+        if k >= args.warmup:
+            vals.append(g)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "pairs": args.pairs, "sample_per_step": desc},
+        "cpu_baseline": {"value": value, "unit": "GCUPS", "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of pyalign's solver.h (oracle/pa_oracle.cpp): the reference's xtensor "
+                "core has no buildable sources here",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from pyalign_gb300 import algorithm as alg
+    from pyalign_gb300 import build as pbuild
+    pbuild.build()
+    L = alg.lib()
+    L.pa_measure_int32_peak.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+    L.pa_solver_last_bytes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+
+    # each rank solves its own batch (pairs are independent: weak scaling, no collective)
+    a, b, ls, lt, table = make_workload(args.pairs, args.seed + rank)
+    B = args.pairs
+    cells = int((ls.astype(np.int64) * lt.astype(np.int64)).sum())
+    mod = alg.m16
+    solver = mod.create_solver(1000, 1000, mod.create_options(options_dict(alg, B)))
+    stream = torch.cuda.current_stream()
+    alg.check(L.pa_solver_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
+
+    length = np.ascontiguousarray(np.stack([ls, lt]), dtype=np.int32)
+    sizes = np.minimum(ls, lt).astype(np.int64)
+    offs = np.zeros(B, np.int64)
+    offs[1:] = np.cumsum(sizes)[:-1]
+    nmap = int(sizes.sum())
+
+    # device-resident inputs and outputs
+    a_d = torch.from_numpy(a.view(np.int32)).cuda()
+    b_d = torch.from_numpy(b.view(np.int32)).cuda()
+    t_d = torch.from_numpy(table).cuda()
+    sc_d = torch.empty(B, dtype=torch.float32, device="cuda")
+    mp_d = torch.empty(nmap, dtype=torch.int32, device="cuda")
+
+    def batch_struct(loc, aa, bb, tt):
+        P = ctypes.POINTER
+        return alg.Batch(form=1, location=loc, batch=B, n_s=a.shape[1], n_t=b.shape[1],
+                         a=ctypes.cast(aa, P(ctypes.c_uint32)), b=ctypes.cast(bb, P(ctypes.c_uint32)),
+                         table=ctypes.cast(tt, P(ctypes.c_float)), table_rows=4, table_cols=4,
+                         length=length.ctypes.data_as(P(ctypes.c_int32)))
+
+    dev_batch = batch_struct(1, a_d.data_ptr(), b_d.data_ptr(), t_d.data_ptr())
+    offs_p = offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+    def step_device():
+        alg.check(L.pa_solve_batch(solver.handle, ctypes.byref(dev_batch), ctypes.c_void_p(sc_d.data_ptr()),
+                                   ctypes.c_void_p(mp_d.data_ptr()), offs_p))
+
+    # pinned host buffers for the end-to-end form
+    a_h = torch.from_numpy(a.view(np.int32)).pin_memory()
+    b_h = torch.from_numpy(b.view(np.int32)).pin_memory()
+    t_h = torch.from_numpy(table).pin_memory()
+    sc_h = torch.empty(B, dtype=torch.float32).pin_memory()
+    mp_h = torch.empty(nmap, dtype=torch.int32).pin_memory()
+    host_batch = batch_struct(0, a_h.data_ptr(), b_h.data_ptr(), t_h.data_ptr())
+
+    def step_host():
+        alg.check(L.pa_solve_batch(solver.handle, ctypes.byref(host_batch), ctypes.c_void_p(sc_h.data_ptr()),
+                                   ctypes.c_void_p(mp_h.data_ptr()), offs_p))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident timing
+    for _ in range(args.warmup):
+        step_device()
+    barrier()
+    dp_ms, walk_ms, launches = [], [], 0
+    ms4 = (ctypes.c_float * 4)()
+    nl = ctypes.c_int32(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_device()
+            L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
+            dp_ms.append(ms4[1])
+            walk_ms.append(ms4[2])
+            launches += nl.value
+        e1.record(stream)
+        barrier()
+    elapsed = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
+    value = cells * world * args.steps / elapsed / 1e9
+
+    # correctness spot check of the device results against the host path below
+    sc_dev = sc_d.cpu().numpy().copy()
+
+    # ---- end-to-end timing through the C ABI with host buffers
+    for _ in range(max(1, args.warmup)):
+        step_host()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = cells * world * args.steps / e2e_s / 1e9
+    h2d, d2h = ctypes.c_int64(0), ctypes.c_int64(0)
+    L.pa_solver_last_bytes(solver.handle, ctypes.byref(h2d), ctypes.byref(d2h))
+    if not np.array_equal(sc_dev, sc_h.numpy()):
+        raise SystemExit("device-resident and host-buffer runs disagree")
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the DP kernel (int32 ALU bound; traceback stores are the HBM side)
+    peak = ctypes.c_float(0)
+    pms = ctypes.c_float(0)
+    alg.check(L.pa_measure_int32_peak(ctypes.byref(peak), ctypes.byref(pms)))
+    dp_s = statistics.mean(dp_ms) / 1000.0
+    achieved_ops = cells * OPS_PER_CELL / dp_s / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    alg_bytes = cells * BYTES_PER_CELL + float((ls.astype(np.int64) + lt.astype(np.int64)).sum()) * 4
+    traffic = None
+    prof = os.path.join(REPO, "profiles", "dp_affine_local_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            pj = json.load(f)
+        traffic = pj["dram_bytes_per_cell"] * cells
+    roof_alu = {"bound": "alu", "achieved": achieved_ops, "peak": float(peak.value), "unit": "Gop/s",
+                "frac": achieved_ops / float(peak.value), "traffic": traffic,
+                "ops_per_cell": OPS_PER_CELL, "peak_source": "measured in-run (pa_measure_int32_peak)"}
+    roof_hbm = {"bound": "hbm", "achieved": alg_bytes / dp_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": alg_bytes / dp_s / 1e9 / hbm_peak, "traffic": traffic,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"}
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        g, threads, desc = cpu_baseline(a, b, ls, lt, table, args.cpu_seconds)
+        cpu = {"value": g, "unit": "GCUPS", "cores": threads, "kind": "port", "sample": desc}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed * 1000.0 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "pairs": B, "cells_per_step": cells, "form": "indexed (a, b uint32 codes)",
+                   "l2": "inputs larger than L2: 524 MB of codes and ~14 GB of traceback masks per step",
+                   "parallelism": f"dp{world} (independent pairs per GPU)"},
+        "roofline": roof_alu,
+        "roofline_hbm": roof_hbm,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "GCUPS", "h2d_bytes_per_step": int(h2d.value),
+                "d2h_bytes_per_step": int(d2h.value)},
+        "gpu_launches": launches,
+        "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms)},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

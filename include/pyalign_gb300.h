@@ -247,6 +247,15 @@ pa_status pa_solve_batch(pa_solver *s, const pa_batch *batch, float *scores, int
  * kernels launched.  Measured with CUDA events on the solver's stream. */
 pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel_launches);
 
+/* Bytes copied host->device and device->host by the last solve call of this solver
+ * (inputs, per-pair metadata, results). */
+pa_status pa_solver_last_bytes(const pa_solver *s, int64_t *h2d, int64_t *d2h);
+
+/* Diagnostic: measured int32 throughput of this GPU (Gop/s) for the add/add/max mix of the
+ * DP cell update, used as the denominator of the DP kernels' roofline.  No counterpart in
+ * the reference (it has no GPU code). */
+pa_status pa_measure_int32_peak(float *gops, float *ms);
+
 #ifdef __cplusplus
 }
 #endif

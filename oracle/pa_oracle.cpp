@@ -16,8 +16,10 @@
 // (no negation trick), so the oracle independently checks the GPU path's
 // "minimize == -maximize(-x)" rewrite.
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <thread>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -79,7 +81,24 @@ struct Dir {
 // solver.h:280-374) it is a list that can hold {NO_TB, NO_TB} as a real entry (the local
 // zero candidate, solver.h:2006-2011).
 struct TB {
-	std::vector<Pt> pts;
+	int32_t n = 0;
+	Pt p0{NO_TB, NO_TB};
+	std::vector<Pt> rest;  // entries 1..n-1 (all-optimal mode only; never allocated otherwise)
+	void clear() { n = 0; rest.clear(); }
+	void push(Pt p) {
+		if (n == 0) p0 = p;
+		else rest.push_back(p);
+		n++;
+	}
+	Pt at(int32_t k) const { return k == 0 ? p0 : rest[size_t(k - 1)]; }
+	void assign(const TB &o) {
+		n = o.n;
+		p0 = o.p0;
+		if (o.n > 1 || !rest.empty()) rest = o.rest;
+	}
+	void append(const TB &o) {
+		for (int32_t k = 0; k < o.n; k++) push(o.at(k));
+	}
 };
 
 // A layer of values and traceback cells with the reference's (-1)-shifted indexing.
@@ -110,13 +129,13 @@ struct Acc {
 	void init(float v, Pt p) {
 		val = v;
 		if (goal != GOAL_SCORE) {
-			tb.pts.clear();
-			if (goal == GOAL_ALL || p.u != NO_TB) tb.pts.push_back(p);
+			tb.clear();
+			if (goal == GOAL_ALL || p.u != NO_TB) tb.push(p);
 		}
 	}
 	void init(float v, const TB &t) {
 		val = v;
-		if (goal != GOAL_SCORE) tb.pts = t.pts;
+		if (goal != GOAL_SCORE) tb.assign(t);
 	}
 	void push(float v, Pt p) {
 		if (goal == GOAL_SCORE) {
@@ -126,7 +145,7 @@ struct Acc {
 		if (dir.is_opt(v, val)) {
 			init(v, p);
 		} else if (goal == GOAL_ALL && v == val) {
-			tb.pts.push_back(p);
+			tb.push(p);
 		}
 	}
 	void push(float v, const TB &t) {
@@ -137,7 +156,7 @@ struct Acc {
 		if (dir.is_opt(v, val)) {
 			init(v, t);
 		} else if (goal == GOAL_ALL && v == val) {
-			for (const auto &p : t.pts) tb.pts.push_back(p);
+			tb.append(t);
 		}
 	}
 };
@@ -379,8 +398,8 @@ struct Problem {
 		path.push_back(Pt{u, v});
 		while (cont1(u, v) && cont2(D.V(u, v))) {
 			const TB &t = D.T(u, v);
-			const int32_t nu = t.pts.empty() ? NO_TB : t.pts[0].u;
-			const int32_t nv = t.pts.empty() ? NO_TB : t.pts[0].v;
+			const int32_t nu = t.n == 0 ? NO_TB : t.p0.u;
+			const int32_t nv = t.n == 0 ? NO_TB : t.p0.v;
 			u = nu; v = nv;
 			path.push_back(Pt{u, v});
 		}
@@ -428,8 +447,8 @@ struct Problem {
 			if (cont1(u1, v1) && cont2(D.V(u1, v1))) {
 				const TB &t = D.T(u1, v1);
 				const int32_t psize = int32_t(dfs_path.size());
-				if (!t.pts.empty()) {
-					for (const auto &p : t.pts) stk.push(Entry{e.path_val, p, psize});
+				if (t.n > 0) {
+					for (int32_t q = 0; q < t.n; q++) stk.push(Entry{e.path_val, t.at(q), psize});
 				} else {
 					stk.push(Entry{e.path_val, Pt{NO_TB, NO_TB}, psize});
 				}
@@ -525,8 +544,8 @@ void pao_tb_matrix(const pao_result *r, int32_t k, int32_t *out) {
 	const auto &L = r->p.layers[size_t(k)];
 	for (size_t c = 0; c < L.tb.size(); c++) {
 		const auto &t = L.tb[c];
-		out[2 * c] = t.pts.empty() ? NO_TB : t.pts[0].u;
-		out[2 * c + 1] = t.pts.empty() ? NO_TB : t.pts[0].v;
+		out[2 * c] = t.n == 0 ? NO_TB : t.p0.u;
+		out[2 * c + 1] = t.n == 0 ? NO_TB : t.p0.v;
 	}
 }
 
@@ -538,7 +557,8 @@ int64_t pao_tb_edges(const pao_result *r, int32_t k, int32_t *out) {
 	for (int32_t i = 0; i <= L.ls; i++) {
 		for (int32_t j = 0; j <= L.lt; j++) {
 			const auto &t = L.tb[size_t(i) * size_t(L.lt + 1) + size_t(j)];
-			for (const auto &p : t.pts) {
+			for (int32_t q = 0; q < t.n; q++) {
+				const Pt p = t.at(q);
 				if (out) {
 					out[4 * n + 0] = i - 1;
 					out[4 * n + 1] = j - 1;
@@ -550,6 +570,46 @@ int64_t pao_tb_edges(const pao_result *r, int32_t k, int32_t *out) {
 		}
 	}
 	return n;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Timed CPU baseline: solves `npairs` problems of the indexed form (codes a/b, a similarity
+// table A x A) on `nthreads` threads, each pair like one lane of Solver::alignment
+// (solver.h:2610-2630): DP with traceback, seed, walk, alignment map.  Returns the cell
+// count; writes scores and maps (concatenated at map_off).
+int64_t pao_batch_alignments(const pao_options *o, int32_t npairs, const int32_t *ls, const int32_t *lt,
+                             const uint32_t *a, int64_t a_stride, const uint32_t *b, int64_t b_stride,
+                             const float *table, int32_t A, int32_t nthreads, float *scores, int32_t *maps,
+                             const int64_t *map_off) {
+	std::atomic<int32_t> next{0};
+	auto work = [&]() {
+		std::vector<float> sim;
+		for (;;) {
+			const int32_t k = next.fetch_add(1);
+			if (k >= npairs) break;
+			const int32_t s_len = ls[k], t_len = lt[k];
+			sim.assign(size_t(s_len) * size_t(t_len), 0.0f);
+			for (int32_t i = 0; i < s_len; i++) {
+				const uint32_t x = a[int64_t(k) * a_stride + i];
+				for (int32_t j = 0; j < t_len; j++)
+					sim[size_t(i) * size_t(t_len) + size_t(j)] = table[size_t(x) * size_t(A) + b[int64_t(k) * b_stride + j]];
+			}
+			pao_result *r = pao_solve(o, s_len, t_len, sim.data());
+			float sc = 0;
+			if (!pao_next(r, &sc, maps ? maps + map_off[k] : nullptr, nullptr, nullptr)) sc = pao_worst(r);
+			scores[k] = sc;
+			pao_free(r);
+		}
+	};
+	std::vector<std::thread> th;
+	for (int32_t t = 0; t < std::max(1, nthreads); t++) th.emplace_back(work);
+	for (auto &t : th) t.join();
+	int64_t cells = 0;
+	for (int32_t k = 0; k < npairs; k++) cells += int64_t(ls[k]) * lt[k];
+	return cells;
 }
 
 }  // extern "C"

@@ -513,11 +513,17 @@ class Solver:
 
     def _call(self, name, form, args):
         L = lib()
+        def batch_check(given):  # factory.h:387-394, checked before the lengths (526-533)
+            if given != self._batch_size:
+                raise ValueError(f"problem of batch size {given} given to solver that was "
+                                 f"configured to batch size {self._batch_size}")
+
         if form == "dense":
             sim, length = args
             sim = np.ascontiguousarray(sim, dtype=np.float32)
             if sim.ndim != 3:
                 raise ValueError("similarity must be a 3-d array (len_s, len_t, batch)")
+            batch_check(sim.shape[2])
             ln = self._len(length)
             head = [self._h, _fp(sim), sim.shape[0], sim.shape[1], sim.shape[2], _ip(ln)]
             keep = (sim, ln)
@@ -526,10 +532,9 @@ class Solver:
             a, b, sim, length = args
             a, b = self._codes(a), self._codes(b)
             sim = np.ascontiguousarray(sim, dtype=np.float32)
+            batch_check(a.shape[0])
+            batch_check(b.shape[0])
             ln = self._len(length)
-            if a.shape[0] != b.shape[0]:
-                raise ValueError(f"problem of batch size {b.shape[0]} given to solver that was "
-                                 f"configured to batch size {self._batch_size}")
             head = [self._h, _up(a), _up(b), a.shape[0], a.shape[1], b.shape[1], _fp(sim),
                     sim.shape[0], sim.shape[1], _ip(ln)]
             keep = (a, b, sim, ln)
@@ -537,10 +542,9 @@ class Solver:
         else:
             a, b, eq, ne, length = args
             a, b = self._codes(a), self._codes(b)
+            batch_check(a.shape[0])
+            batch_check(b.shape[0])
             ln = self._len(length)
-            if a.shape[0] != b.shape[0]:
-                raise ValueError(f"problem of batch size {b.shape[0]} given to solver that was "
-                                 f"configured to batch size {self._batch_size}")
             head = [self._h, _up(a), _up(b), a.shape[0], a.shape[1], b.shape[1], float(eq), float(ne), _ip(ln)]
             keep = (a, b, ln)
             lens = ln

@@ -288,6 +288,7 @@ struct pa_solver {
 	cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 	float last_ms[4] = {0, 0, 0, 0};
 	int32_t last_launches = 0;
+	int64_t bytes_h2d = 0, bytes_d2h = 0;
 
 	DevBuf d_a, d_b, d_tab, d_dense, d_dense_off, d_ls, d_lt, d_order, d_mask_off, d_score, d_seed, d_has,
 	    d_masks, d_scratch, d_counter, d_status, d_border, d_maps, d_map_off, d_paths, d_path_off,
@@ -304,7 +305,12 @@ struct pa_solver {
 
 namespace {
 
-int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+// every host<->device copy of a solve goes through here, so the solver can report bytes
+cudaError_t pa_copy(pa_solver *s, void *dst, const void *src, size_t n, cudaMemcpyKind kind, cudaStream_t st) {
+	if (kind == cudaMemcpyHostToDevice) s->bytes_h2d += int64_t(n);
+	else if (kind == cudaMemcpyDeviceToHost) s->bytes_d2h += int64_t(n);
+	return cudaMemcpyAsync(dst, src, n, kind, st);
+}
 
 pa_status ensure_device(pa_solver *s) {
 	if (s->device >= 0) return PA_OK;
@@ -413,7 +419,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			bv[2 * ns + nt + k] = cvt<V>(s->top_Q[k], ISINT, scale, 0);
 		}
 		PA_CUDA(s->d_border.ensure(bv.size() * sizeof(V)));
-		PA_CUDA(cudaMemcpyAsync(s->d_border.p, bv.data(), bv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
+		PA_CUDA(pa_copy(s, s->d_border.p, bv.data(), bv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
 		V *b = s->d_border.as<V>();
 		p.left_D = b;
 		p.left_P = b + ns;
@@ -423,7 +429,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			// the table is uploaded as floats; convert on the host here (small)
 			std::vector<float> ht(size_t(in.table_rows * in.table_cols));
 			if (in.location == PA_DEVICE) {
-				PA_CUDA(cudaMemcpyAsync(ht.data(), in.table, ht.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+				PA_CUDA(pa_copy(s, ht.data(), in.table, ht.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
 				PA_CUDA(cudaStreamSynchronize(st));
 			} else {
 				std::memcpy(ht.data(), in.table, ht.size() * sizeof(float));
@@ -431,7 +437,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			tabv.resize(ht.size());
 			for (size_t k = 0; k < ht.size(); k++) tabv[k] = cvt<V>(ht[k] * s->sign, ISINT, scale, diag_tag);
 			PA_CUDA(s->d_tab.ensure(tabv.size() * sizeof(V)));
-			PA_CUDA(cudaMemcpyAsync(s->d_tab.p, tabv.data(), tabv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
+			PA_CUDA(pa_copy(s, s->d_tab.p, tabv.data(), tabv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
 			p.table = s->d_tab.as<V>();
 			PA_CUDA(cudaStreamSynchronize(st));  // tabv/bv are host temporaries
 		} else {
@@ -584,11 +590,11 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	std::copy(s->gen_s.begin(), s->gen_s.end(), host.begin() + ns + nt);
 	std::copy(s->gen_t.begin(), s->gen_t.end(), host.begin() + 2 * ns + nt);
 	PA_CUDA(s->d_gen.ensure(host.size() * 4));
-	PA_CUDA(cudaMemcpyAsync(s->d_gen.p, host.data(), host.size() * 4, cudaMemcpyHostToDevice, st));
+	PA_CUDA(pa_copy(s, s->d_gen.p, host.data(), host.size() * 4, cudaMemcpyHostToDevice, st));
 	PA_CUDA(s->d_wsb_off.ensure(voff.size() * 8));
-	PA_CUDA(cudaMemcpyAsync(s->d_wsb_off.p, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, st));
+	PA_CUDA(pa_copy(s, s->d_wsb_off.p, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, st));
 	PA_CUDA(s->d_wsb_sub_off.ensure(toff.size() * 8));
-	PA_CUDA(cudaMemcpyAsync(s->d_wsb_sub_off.p, toff.data(), toff.size() * 8, cudaMemcpyHostToDevice, st));
+	PA_CUDA(pa_copy(s, s->d_wsb_sub_off.p, toff.data(), toff.size() * 8, cudaMemcpyHostToDevice, st));
 	PA_CUDA(s->d_wsb_vals.ensure(size_t(voff[size_t(B)]) * 4));
 	PA_CUDA(s->d_wsb_tb.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
 	PA_CUDA(s->d_wsb_sub.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
@@ -608,7 +614,7 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	if (in.form == F_INDEXED) {
 		const size_t n = size_t(in.table_rows * in.table_cols) * 4;
 		PA_CUDA(s->d_tab.ensure(n));
-		PA_CUDA(cudaMemcpyAsync(s->d_tab.p, in.table, n, in.location == PA_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+		PA_CUDA(pa_copy(s, s->d_tab.p, in.table, n, in.location == PA_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
 		w.table = s->d_tab.as<float>();
 		w.table_rows = int32_t(in.table_rows);
 		w.table_cols = int32_t(in.table_cols);
@@ -648,10 +654,10 @@ pa_status download_wsb(pa_solver *s, ResultData &res) {
 	res.wsb_tb.resize(size_t(res.wsb_off[size_t(B)]));
 	res.wsb_sub.resize(size_t(res.wsb_off[size_t(B)]));
 	if (!res.wsb_vals.empty())
-		PA_CUDA(cudaMemcpyAsync(res.wsb_vals.data(), s->d_wsb_vals.p, res.wsb_vals.size() * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(pa_copy(s, res.wsb_vals.data(), s->d_wsb_vals.p, res.wsb_vals.size() * 4, cudaMemcpyDeviceToHost, st));
 	if (!res.wsb_tb.empty()) {
-		PA_CUDA(cudaMemcpyAsync(res.wsb_tb.data(), s->d_wsb_tb.p, res.wsb_tb.size() * 4, cudaMemcpyDeviceToHost, st));
-		PA_CUDA(cudaMemcpyAsync(res.wsb_sub.data(), s->d_wsb_sub.p, res.wsb_sub.size() * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(pa_copy(s, res.wsb_tb.data(), s->d_wsb_tb.p, res.wsb_tb.size() * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(pa_copy(s, res.wsb_sub.data(), s->d_wsb_sub.p, res.wsb_sub.size() * 4, cudaMemcpyDeviceToHost, st));
 	}
 	return PA_OK;
 }
@@ -661,6 +667,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	if (pa_status st = ensure_device(s)) return st;
 	if (pa_status st = validate(s, in)) return st;
 	cudaStream_t st = s->stream;
+	s->bytes_h2d = s->bytes_d2h = 0;
 	const int64_t B = in.batch;
 
 	// per-lane lengths, clamped to the batch arrays (stale lanes of a partial batch carry
@@ -711,13 +718,13 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		if (in.form == F_DENSE) {
 			const size_t n = size_t(in.n_s * in.n_t * B) * sizeof(float);
 			PA_CUDA(s->d_dense.ensure(n));
-			if (n) PA_CUDA(cudaMemcpyAsync(s->d_dense.p, in.sim, n, cudaMemcpyHostToDevice, st));
+			if (n) PA_CUDA(pa_copy(s, s->d_dense.p, in.sim, n, cudaMemcpyHostToDevice, st));
 		} else {
 			const size_t na = size_t(B * in.n_s) * sizeof(uint32_t), nb = size_t(B * in.n_t) * sizeof(uint32_t);
 			PA_CUDA(s->d_a.ensure(na));
 			PA_CUDA(s->d_b.ensure(nb));
-			if (na) PA_CUDA(cudaMemcpyAsync(s->d_a.p, in.a, na, cudaMemcpyHostToDevice, st));
-			if (nb) PA_CUDA(cudaMemcpyAsync(s->d_b.p, in.b, nb, cudaMemcpyHostToDevice, st));
+			if (na) PA_CUDA(pa_copy(s, s->d_a.p, in.a, na, cudaMemcpyHostToDevice, st));
+			if (nb) PA_CUDA(pa_copy(s, s->d_b.p, in.b, nb, cudaMemcpyHostToDevice, st));
 		}
 	}
 	// per-pair metadata
@@ -747,7 +754,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	auto up = [&](DevBuf &d, const void *h, size_t n) -> cudaError_t {
 		cudaError_t e = d.ensure(n);
 		if (e != cudaSuccess || n == 0) return e;
-		return cudaMemcpyAsync(d.p, h, n, cudaMemcpyHostToDevice, st);
+		return pa_copy(s, d.p, h, n, cudaMemcpyHostToDevice, st);
 	};
 	// the host vectors above must live until the copies complete: synchronise below
 	PA_CUDA(up(s->d_ls, ls.data(), ls.size() * 4));
@@ -781,7 +788,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			                       : run_dp<float>(s, in, plan, TB_NONE, ls.data(), lt.data(), B, false, nullptr, &launches);
 			if (e2) return e2;
 			PA_CUDA(s->d_best.ensure(size_t(B) * 4));
-			PA_CUDA(cudaMemcpyAsync(s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
+			PA_CUDA(pa_copy(s, s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
 		}
 		pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, tb, ls.data(), lt.data(), B, want_values,
 		                                         s->d_best.as<float>(), &launches)
@@ -832,41 +839,41 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	res.has.resize(size_t(B));
 	res.seeds.resize(size_t(2 * B));
 	int32_t status = 0;
-	PA_CUDA(cudaMemcpyAsync(res.scores.data(), s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
-	PA_CUDA(cudaMemcpyAsync(res.has.data(), s->d_has.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
-	PA_CUDA(cudaMemcpyAsync(res.seeds.data(), s->d_seed.p, size_t(B) * 8, cudaMemcpyDeviceToHost, st));
-	PA_CUDA(cudaMemcpyAsync(&status, s->d_status.p, 4, cudaMemcpyDeviceToHost, st));
+	PA_CUDA(pa_copy(s, res.scores.data(), s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+	PA_CUDA(pa_copy(s, res.has.data(), s->d_has.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+	PA_CUDA(pa_copy(s, res.seeds.data(), s->d_seed.p, size_t(B) * 8, cudaMemcpyDeviceToHost, st));
+	PA_CUDA(pa_copy(s, &status, s->d_status.p, 4, cudaMemcpyDeviceToHost, st));
 	res.map_off = map_off;
 	res.mask_off = mask_off;
 	if (need_walk) {
 		if (maps_out && in.location == PA_DEVICE) {
 			// results stay on the device
 		} else if (maps_out) {
-			PA_CUDA(cudaMemcpyAsync(maps_out, s->d_maps.p, size_t(map_off[size_t(B)]) * 4, cudaMemcpyDeviceToHost, st));
+			PA_CUDA(pa_copy(s, maps_out, s->d_maps.p, size_t(map_off[size_t(B)]) * 4, cudaMemcpyDeviceToHost, st));
 		} else {
 			res.maps.resize(size_t(map_off[size_t(B)]));
-			PA_CUDA(cudaMemcpyAsync(res.maps.data(), s->d_maps.p, res.maps.size() * 4, cudaMemcpyDeviceToHost, st));
+			PA_CUDA(pa_copy(s, res.maps.data(), s->d_maps.p, res.maps.size() * 4, cudaMemcpyDeviceToHost, st));
 		}
 		if (want_paths) {
 			res.path_off = path_off;
 			res.paths.resize(size_t(path_off[size_t(B)]));
 			res.path_len.resize(size_t(B));
-			PA_CUDA(cudaMemcpyAsync(res.paths.data(), s->d_paths.p, res.paths.size() * 4, cudaMemcpyDeviceToHost, st));
-			PA_CUDA(cudaMemcpyAsync(res.path_len.data(), s->d_path_len.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+			PA_CUDA(pa_copy(s, res.paths.data(), s->d_paths.p, res.paths.size() * 4, cudaMemcpyDeviceToHost, st));
+			PA_CUDA(pa_copy(s, res.path_len.data(), s->d_path_len.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
 		}
 	}
 	if (tb == TB_ALL && s->gap != GAP_GENERAL) {
 		res.masks_all.resize(size_t(mask_off[size_t(B)]) * 4);
-		PA_CUDA(cudaMemcpyAsync(res.masks_all.data(), s->d_masks.p, res.masks_all.size() * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(pa_copy(s, res.masks_all.data(), s->d_masks.p, res.masks_all.size() * 4, cudaMemcpyDeviceToHost, st));
 	}
 	if (tb == TB_ONE && want_values && s->gap != GAP_GENERAL) {
 		res.masks_one.resize(size_t(mask_off[size_t(B)]));
-		PA_CUDA(cudaMemcpyAsync(res.masks_one.data(), s->d_masks.p, res.masks_one.size() * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(pa_copy(s, res.masks_one.data(), s->d_masks.p, res.masks_one.size() * 4, cudaMemcpyDeviceToHost, st));
 	}
 	if (want_values) {
 		res.val_off = val_off;
 		res.values.resize(size_t(val_off[size_t(B)]));
-		PA_CUDA(cudaMemcpyAsync(res.values.data(), s->d_vals.p, res.values.size() * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(pa_copy(s, res.values.data(), s->d_vals.p, res.values.size() * 4, cudaMemcpyDeviceToHost, st));
 	}
 	if (s->gap == GAP_GENERAL) {
 		if (pa_status e = download_wsb(s, res)) return e;
@@ -1090,6 +1097,13 @@ pa_status pa_solver_set_stream(pa_solver *s, void *stream) {
 	return PA_OK;
 }
 
+pa_status pa_solver_last_bytes(const pa_solver *s, int64_t *h2d, int64_t *d2h) {
+	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
+	if (h2d) *h2d = s->bytes_h2d;
+	if (d2h) *d2h = s->bytes_d2h;
+	return PA_OK;
+}
+
 pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel_launches) {
 	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
 	if (ms4)
@@ -1191,7 +1205,7 @@ pa_status pa_solve_batch(pa_solver *s, const pa_batch *b, float *scores, int32_t
 	pa_status st = solve_impl(s, in, maps ? M_ALIGNMENT : M_SCORE, dev ? nullptr : scores, &r, maps, map_offsets);
 	if (st) return st;
 	if (dev && scores) {
-		cudaError_t e = cudaMemcpyAsync(scores, s->d_score.p, size_t(b->batch) * 4, cudaMemcpyDeviceToDevice, s->stream);
+		cudaError_t e = pa_copy(s, scores, s->d_score.p, size_t(b->batch) * 4, cudaMemcpyDeviceToDevice, s->stream);
 		if (e != cudaSuccess) {
 			pa_result_destroy(r);
 			return fail(PA_ERR_CUDA, cudaGetErrorString(e));
@@ -1256,26 +1270,26 @@ static bool lane_walk(const pa_result *r, int64_t lane, std::vector<std::pair<in
 	}
 	if (!d.has[size_t(lane)]) return false;
 	const int n = std::min(d.ls[size_t(lane)], d.lt[size_t(lane)]);
-	if (map) {
-		if (d.gap == GAP_GENERAL) {
-			std::vector<std::pair<int, int>> p;
-			// WSB one-optimal walk from the device traceback codes
-			int u = d.seeds[size_t(2 * lane)], v = d.seeds[size_t(2 * lane + 1)];
+	if (d.gap == GAP_GENERAL) {
+		// WSB one-optimal walk over the device traceback codes (solver.h:1497-1536)
+		std::vector<std::pair<int, int>> p;
+		int u = d.seeds[size_t(2 * lane)], v = d.seeds[size_t(2 * lane + 1)];
+		p.push_back({u, v});
+		while (u >= 0 && v >= 0) {
+			if (d.loc == LOC_LOCAL && !(d.wsb_val(lane, u, v) > 0.0f)) break;
+			const int32_t c = d.wsb(lane, u, v);
+			const int kind = c & 3, kk = (c >> 2) - 1;
+			if (kind == 0) { u = NO_TB; v = NO_TB; }
+			else if (kind == 1) { u--; v--; }
+			else if (kind == 2) u = kk;
+			else v = kk;
 			p.push_back({u, v});
-			while (u >= 0 && v >= 0) {
-				if (d.loc == LOC_LOCAL && !(d.wsb_val(lane, u, v) > 0.0f)) break;
-				const int32_t c = d.wsb(lane, u, v);
-				const int kind = c & 3, kk = (c >> 2) - 1;
-				if (kind == 0) { u = NO_TB; v = NO_TB; }
-				else if (kind == 1) { u--; v--; }
-				else if (kind == 2) u = kk;
-				else v = kk;
-				p.push_back({u, v});
-			}
-			map_from_path(d, lane, p, map);
-			if (path) *path = p;
-			return true;
 		}
+		if (map) map_from_path(d, lane, p, map);
+		if (path) *path = p;
+		return true;
+	}
+	if (map) {
 		if (d.maps.empty()) {
 			for (int k = 0; k < n; k++) map[k] = -1;
 		} else {
