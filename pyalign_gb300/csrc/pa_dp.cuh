@@ -37,7 +37,7 @@ namespace pa {
 enum GapKind { GAP_LINEAR = 0, GAP_AFFINE = 1, GAP_DTW = 2, GAP_GENERAL = 3 };
 enum LocKind { LOC_LOCAL = 0, LOC_GLOBAL = 1, LOC_SEMI = 2 };
 enum TbKind { TB_NONE = 0, TB_ONE = 1, TB_ALL = 2 };
-enum SubKind { SUB_TABLE = 0, SUB_BINARY = 1, SUB_DENSE = 2 };
+enum SubKind { SUB_TABLE = 0, SUB_BINARY = 1, SUB_DENSE = 2, SUB_PROFILE = 3 };
 
 constexpr int R = 8;              // rows per lane
 constexpr int BLOCK = 128;        // threads per block
@@ -77,6 +77,7 @@ struct DpParams {
 	const V *top_Q;         // values output only: Q(-1,j)
 	V neg_inf;
 	int32_t G;              // lanes per pair group
+	int32_t key_shift;      // local seeds: key = value * 2^key_shift + j
 	// outputs
 	float *score;           // reference-domain score
 	int32_t *seed;          // (i, j) per pair
@@ -128,16 +129,31 @@ struct SubCtx {
 	V eq, ne;
 };
 
-template <typename V, int GAP, int LOC, int TB>
-__global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
+// prmt.b32 in its default mode: byte k of the result is source byte sel[4k+2:4k] of {b, a},
+// sign-replicated when bit 4k+3 is set.  Used to read an int8 substitution profile.
+__device__ __forceinline__ int32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+	uint32_t d;
+	asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+	return int32_t(d);
+}
+
+// Selector that extracts byte t (0..7) of {hi, lo} sign-extended to 32 bits.
+__device__ __forceinline__ uint32_t sext_selector(uint32_t t) {
+	const uint32_t x = t | 8u;
+	return t | (x << 4) | (x << 8) | (x << 12);
+}
+
+template <typename V, int GAP, int LOC, int TB, bool VALS>
+__global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 	constexpr bool ISINT = std::is_same<V, int32_t>::value;
 	constexpr bool TAG = ISINT && TB != TB_ALL;  // int32 tagged values
+	constexpr bool KEYSEED = TAG && TB == TB_ONE && LOC == LOC_LOCAL;  // packed (value, j) seed keys
 	typedef typename V2T<V>::type V2;
 
 	extern __shared__ unsigned char smem_raw[];
 	V *stab = reinterpret_cast<V *>(smem_raw);
-	const bool table_in_smem = p.sub_kind == SUB_TABLE && p.table_rows <= MAX_SMEM_TABLE &&
-	                           p.table_cols <= MAX_SMEM_TABLE;
+	const bool table_in_smem = (p.sub_kind == SUB_TABLE || p.sub_kind == SUB_PROFILE) &&
+	                           p.table_rows <= MAX_SMEM_TABLE && p.table_cols <= MAX_SMEM_TABLE;
 	if (table_in_smem) {
 		const int n = p.table_rows * p.table_cols;
 		for (int k = threadIdx.x; k < n; k += blockDim.x) stab[k] = p.table[k];
@@ -156,6 +172,7 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 	const int64_t half = p.scratch_stride / 2;
 	const V NEG = p.neg_inf;
 	const int rpp = G * R;  // rows per pass
+	const int sub_kind = p.sub_kind;
 
 	for (;;) {
 		int base = 0;
@@ -178,28 +195,24 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 		const uint32_t *arow = p.a ? p.a + int64_t(pair < 0 ? 0 : pair) * p.a_stride : nullptr;
 		const uint32_t *brow = p.b ? p.b + int64_t(pair < 0 ? 0 : pair) * p.b_stride : nullptr;
 		const float *drow = p.dense ? p.dense + (pair >= 0 ? p.dense_off[pair] : 0) : nullptr;
-		const V best_in = (TB == TB_ALL && LOC == LOC_LOCAL && pair >= 0)
-		                      ? V(p.best_in[pair] * p.out_sign)
-		                      : V(0);
-		float *vals = (p.values && pair >= 0) ? p.values + p.val_off[pair] : nullptr;
+		const V best_in = (TB == TB_ALL && LOC == LOC_LOCAL && pair >= 0) ? V(p.best_in[pair] * p.out_sign) : V(0);
+		float *vals = (VALS && pair >= 0) ? p.values + p.val_off[pair] : nullptr;
 		const int64_t lstride = int64_t(lt + 1);
 		const int64_t layer_sz = int64_t(ls + 1) * lstride;
 
 		// --- solution values: borders (solver.h:2806-2814, 2918-2967, 3116-3125, 3205-3210)
-		if (vals) {
-			const bool tg = TAG;
+		if (VALS && vals) {
 			for (int j = sub - 1; j < lt; j += G) {
-				vals[j + 1] = to_ref(p.top_D[j + 1], tg, p.out_sign);
+				vals[j + 1] = to_ref(p.top_D[j + 1], TAG, p.out_sign);
 				if (GAP == GAP_AFFINE) {
-					vals[layer_sz + (j + 1)] = (j < 0) ? to_ref(p.left_P[0], tg, p.out_sign)
-					                                   : -INFINITY * p.out_sign;
-					vals[2 * layer_sz + (j + 1)] = to_ref(p.top_Q[j + 1], tg, p.out_sign);
+					vals[layer_sz + (j + 1)] = (j < 0) ? to_ref(p.left_P[0], TAG, p.out_sign) : -INFINITY * p.out_sign;
+					vals[2 * layer_sz + (j + 1)] = to_ref(p.top_Q[j + 1], TAG, p.out_sign);
 				}
 			}
 			for (int i = sub; i < ls; i += G) {
-				vals[int64_t(i + 1) * lstride] = to_ref(p.left_D[i + 1], tg, p.out_sign);
+				vals[int64_t(i + 1) * lstride] = to_ref(p.left_D[i + 1], TAG, p.out_sign);
 				if (GAP == GAP_AFFINE) {
-					vals[layer_sz + int64_t(i + 1) * lstride] = to_ref(p.left_P[i + 1], tg, p.out_sign);
+					vals[layer_sz + int64_t(i + 1) * lstride] = to_ref(p.left_P[i + 1], TAG, p.out_sign);
 					vals[2 * layer_sz + int64_t(i + 1) * lstride] = -INFINITY * p.out_sign;
 				}
 			}
@@ -223,17 +236,27 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 			V2 *bout = scr + ((q + 1) & 1) * half;
 			const bool write_boundary = sub == G - 1 && q + 1 < npass;
 
+			// query codes, and the int8 substitution profile of each row (SUB_PROFILE)
 			uint32_t qa[R];
+			uint32_t plo[R], phi[R];
 #pragma unroll
 			for (int r = 0; r < R; r++) {
 				const int i = row0 + r;
-				qa[r] = 0;
-				if (pass_active && i < ls && arow) qa[r] = arow[i];
+				qa[r] = (pass_active && i < ls && arow) ? arow[i] : 0u;
+				plo[r] = phi[r] = 0u;
 			}
-			if (p.sub_kind == SUB_TABLE && pass_active) {
+			if (sub_kind == SUB_PROFILE) {
+				const int cols = p.table_cols;
 #pragma unroll
 				for (int r = 0; r < R; r++) {
-					if (row0 + r < ls && int32_t(qa[r]) >= p.table_rows) atomicOr(p.status, ST_BAD_CODE);
+					uint32_t lo = 0, hi = 0;
+					for (int c = 0; c < cols; c++) {
+						const uint32_t byte = uint32_t(int32_t(tab[qa[r] * cols + c])) & 0xffu;
+						if (c < 4) lo |= byte << (8 * c);
+						else hi |= byte << (8 * (c - 4));
+					}
+					plo[r] = lo;
+					phi[r] = hi;
 				}
 			}
 
@@ -248,21 +271,25 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 			V outD = Dl[R - 1], outP = NEG;
 			V prev_up = (pass_active && row0 <= ls) ? p.left_D[row0] : NEG;  // D(row0-1, -1)
 
-			// traceback state of the best per row (local, one optimal path)
-			V bv[(TB == TB_ONE && LOC == LOC_LOCAL) ? R : 1];
-			int bj[(TB == TB_ONE && LOC == LOC_LOCAL) ? R : 1];
-			if (TB == TB_ONE && LOC == LOC_LOCAL) {
+			// best cell per row for local one-optimal seeds (solver.h:2048-2056)
+			constexpr int NB = (TB == TB_ONE && LOC == LOC_LOCAL) ? R : 1;
+			V bv[NB];
+			int bj[NB];
 #pragma unroll
-				for (int r = 0; r < R; r++) { bv[r] = NEG; bj[r] = -1; }
-			}
+			for (int r = 0; r < NB; r++) { bv[r] = KEYSEED ? V(-1) : NEG; bj[r] = -1; }
+			const int kshift = p.key_shift;
+			const int kmul = 1 << kshift;
 			const bool last_row_lane = pass_active && nvalid >= 1 && nvalid <= R;
 			const int r_last = nvalid - 1;
 
+			uint32_t tnext = (pass_active && brow && sub < lt) ? brow[max(0, -sub)] : 0u;
 			for (int s = 0; s < wsteps; s++) {
 				const int j = s - sub;
 				V upD = __shfl_up_sync(0xffffffffu, outD, 1, G);
 				V upP = __shfl_up_sync(0xffffffffu, outP, 1, G);
 				const bool act = pass_active && j >= 0 && j < lt;
+				const uint32_t tcode = tnext;
+				if (act && brow && j + 1 < lt) tnext = brow[j + 1];
 				if (sub == 0 && act) {
 					if (q == 0) {
 						upD = p.top_D[j + 1];
@@ -276,30 +303,25 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 				if (act) {
 					// substitution values of the R rows at column j
 					V S[R];
-					if (p.sub_kind == SUB_DENSE) {
+					if (sub_kind == SUB_PROFILE) {
+						const uint32_t sel = sext_selector(tcode);
+#pragma unroll
+						for (int r = 0; r < R; r++) S[r] = V(prmt(plo[r], phi[r], sel));
+					} else if (sub_kind == SUB_BINARY) {
+#pragma unroll
+						for (int r = 0; r < R; r++) S[r] = (qa[r] == tcode) ? p.eq : p.ne;
+					} else if (sub_kind == SUB_TABLE) {
+#pragma unroll
+						for (int r = 0; r < R; r++) S[r] = tab[qa[r] * p.table_cols + tcode];
+					} else {
 #pragma unroll
 						for (int r = 0; r < R; r++) {
 							const int i = min(row0 + r, ls - 1);
-							const float x = drow[int64_t(i) * p.dense_si + int64_t(j) * p.dense_sj] * p.dense_sign;
-							S[r] = V(x);
-						}
-					} else {
-						const uint32_t tb = brow[j];
-						if (p.sub_kind == SUB_BINARY) {
-#pragma unroll
-							for (int r = 0; r < R; r++) S[r] = (qa[r] == tb) ? p.eq : p.ne;
-						} else {
-							const int tcol = int(tb) < p.table_cols ? int(tb) : 0;
-							if (int(tb) >= p.table_cols) atomicOr(p.status, ST_BAD_CODE);
-#pragma unroll
-							for (int r = 0; r < R; r++) {
-								const int rr = int(qa[r]) < p.table_rows ? int(qa[r]) : 0;
-								S[r] = tab[rr * p.table_cols + tcol];
-							}
+							S[r] = V(drow[int64_t(i) * p.dense_si + int64_t(j) * p.dense_sj] * p.dense_sign);
 						}
 					}
 
-					uint32_t mword = 0;
+					uint32_t codes = 0, extp = 0, extq = 0;
 					uint32_t mall[4] = {0, 0, 0, 0};
 					V dsave = prev_up;  // D(i-1, j-1) for the first row
 					V uD = upD, uP = upP;
@@ -318,17 +340,20 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 								key = vmax(vmax(dsave + S[r], P), Q);
 								if (LOC == LOC_LOCAL) key = vmax(key, 3);
 								D = key & ~3;
-								if (TB == TB_ONE)
-									mword |= (uint32_t(key & 3) | (uint32_t(eP > oP) << 2) | (uint32_t(eQ > oQ) << 3)) << (4 * r);
+								if (TB == TB_ONE) {
+									codes |= uint32_t(key & 3) << (2 * r);
+									extp |= (eP > oP) ? (1u << r) : 0u;
+									extq |= (eQ > oQ) ? (1u << r) : 0u;
+								}
 							} else if (GAP == GAP_LINEAR) {
 								key = vmax(vmax(dsave + S[r], uD + p.c_up), old + p.c_left);
 								if (LOC == LOC_LOCAL) key = vmax(key, 3);
 								D = key & ~3;
-								if (TB == TB_ONE) mword |= uint32_t(key & 3) << (4 * r);
+								if (TB == TB_ONE) codes |= uint32_t(key & 3) << (2 * r);
 							} else {  // DTW
 								key = vmax(vmax(dsave + 2, uD + 1), old);
 								D = (key & ~3) + S[r];
-								if (TB == TB_ONE) mword |= uint32_t(key & 3) << (4 * r);
+								if (TB == TB_ONE) codes |= uint32_t(key & 3) << (2 * r);
 							}
 						} else {
 							// ---- explicit compares (float, or int32 for all-optimal masks)
@@ -353,7 +378,9 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 								if (Q > best) { best = Q; code = 0; }
 								D = best;
 								if (TB == TB_ONE) {
-									cell = uint32_t(code) | (uint32_t(bP) << 2) | (uint32_t(bQ) << 3);
+									codes |= uint32_t(code) << (2 * r);
+									extp |= bP ? (1u << r) : 0u;
+									extq |= bQ ? (1u << r) : 0u;
 								} else if (TB == TB_ALL) {
 									cell = (LOC == LOC_LOCAL && best == V(0) ? 1u : 0u) | (dg == best ? 2u : 0u) |
 									       (P == best ? 4u : 0u) | (Q == best ? 8u : 0u) |
@@ -374,7 +401,7 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 								if (lf > best) { best = lf; code = 0; }
 								D = best;
 								if (TB == TB_ONE) {
-									cell = uint32_t(code);
+									codes |= uint32_t(code) << (2 * r);
 								} else if (TB == TB_ALL) {
 									cell = (LOC == LOC_LOCAL && best == V(0) ? 1u : 0u) | (dg == best ? 2u : 0u) |
 									       (up == best ? 4u : 0u) | (lf == best ? 8u : 0u);
@@ -387,9 +414,8 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 									cell = (dsave == best ? 2u : 0u) | (uD == best ? 4u : 0u) | (old == best ? 8u : 0u);
 								}
 								D = best + S[r];
-								if (TB == TB_ONE) cell = uint32_t(code);
+								if (TB == TB_ONE) codes |= uint32_t(code) << (2 * r);
 							}
-							if (TB == TB_ONE) mword |= cell << (4 * r);
 							if (TB == TB_ALL) {
 								if (LOC == LOC_LOCAL && r < nvalid && best_in > V(0) && D == best_in) cell |= 256u;
 								mall[r >> 1] |= cell << (16 * (r & 1));
@@ -398,13 +424,16 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 
 						// seeds
 						if (LOC == LOC_LOCAL) {
-							if (TB == TB_ONE) {
+							if constexpr (KEYSEED) {
+								// D >= 0 here; key = D * 2^kshift + j orders by value, then j
+								bv[r] = vmax(bv[r], V(D * kmul + j));
+							} else if (TB == TB_ONE) {
 								if (r < nvalid && D >= bv[r]) { bv[r] = D; bj[r] = j; }
 							} else if (TB == TB_NONE) {
 								if (r < nvalid) l_best = vmax(l_best, D);
 							}
 						}
-						if (vals && r < nvalid) {
+						if (VALS && vals && r < nvalid) {
 							const int64_t c = int64_t(row0 + r + 1) * lstride + (j + 1);
 							vals[c] = to_ref(D, TAG, p.out_sign);
 							if (GAP == GAP_AFFINE) {
@@ -424,7 +453,7 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 
 					if (TB == TB_ONE) {
 						uint32_t *m = reinterpret_cast<uint32_t *>(p.masks) + p.mask_off[pair];
-						m[(int64_t(q) * nsteps_pair + s) * G + sub] = mword;
+						m[(int64_t(q) * nsteps_pair + s) * G + sub] = codes | (extp << 16) | (extq << 24);
 					} else if (TB == TB_ALL) {
 						uint4 *m = reinterpret_cast<uint4 *>(p.masks) + p.mask_off[pair];
 						m[(int64_t(q) * nsteps_pair + s) * G + sub] = make_uint4(mall[0], mall[1], mall[2], mall[3]);
@@ -453,11 +482,24 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 				prev_up = upD;
 			}
 			if (TB == TB_ONE && LOC == LOC_LOCAL) {
-				// fold the per-row bests: larger value, then larger i (rows ascend), then the
-				// row's own largest j (solver.h:2048-2056 scans i, j descending, strict)
+				// fold the per-row bests of valid rows: larger value, then larger i (rows
+				// ascend), then the row's own largest j (solver.h:2048-2056 scans i, j
+				// descending with strict replacement)
 #pragma unroll
-				for (int r = 0; r < R; r++) {
-					if (bj[r] >= 0 && bv[r] >= l_best) { l_best = bv[r]; l_bi = row0 + r; l_bj = bj[r]; }
+				for (int r = 0; r < NB; r++) {
+					if (r >= nvalid) continue;
+					V v;
+					int jj;
+					if constexpr (KEYSEED) {
+						if (bv[r] < 0) continue;
+						v = bv[r] >> kshift;
+						jj = bv[r] & (kmul - 1);
+					} else {
+						if (bj[r] < 0) continue;
+						v = bv[r];
+						jj = bj[r];
+					}
+					if (v >= l_best) { l_best = v; l_bi = row0 + r; l_bj = jj; }
 				}
 			}
 			__syncwarp();
@@ -541,6 +583,10 @@ __global__ void __launch_bounds__(BLOCK) dp_kernel(DpParams<V> p) {
 		}
 	}
 }
+
+// Largest code in a batch of sequences (host validation of the indexed form,
+// factory.h:602-614, done on the device for device-resident inputs).
+__global__ void codes_max_kernel(const uint32_t *x, int64_t n, uint32_t *out);
 
 // ---------------------------------------------------------------------------------------
 // Traceback walk for one optimal path (TracebackIterators<false>::Iterator::next,

@@ -4,11 +4,12 @@
 
 namespace pa {
 
-cudaError_t launch_dp_f_dtw(int loc, int tb, const DpParams<float> &p, int grid, size_t smem,
+cudaError_t launch_dp_f_dtw(int loc, int tb, bool vals, const DpParams<float> &p, int grid, size_t smem,
                                   cudaStream_t st) {
-#define PA_CASE(L, T)                                                                       \
-	if (loc == L && tb == T) {                                                          \
-		auto k = dp_kernel<float, GAP_DTW, L, T>;                                         \
+#define PA_CASE(L, T) PA_CASE2(L, T, false) PA_CASE2(L, T, true)
+#define PA_CASE2(L, T, VA)                                                                   \
+	if (loc == L && tb == T && vals == VA) {                                            \
+		auto k = dp_kernel<float, GAP_DTW, L, T, VA>;                                         \
 		if (smem > 48 * 1024)                                                           \
 			cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
 		k<<<grid, BLOCK, smem, st>>>(p);                                                \
@@ -17,15 +18,18 @@ cudaError_t launch_dp_f_dtw(int loc, int tb, const DpParams<float> &p, int grid,
 	PA_CASE(LOC_GLOBAL, TB_NONE)
 	PA_CASE(LOC_GLOBAL, TB_ONE)
 #undef PA_CASE
+#undef PA_CASE2
 	return cudaErrorInvalidValue;
 }
 
-cudaError_t occupancy_dp_f_dtw(int loc, int tb, size_t smem, int *blocks_per_sm) {
+cudaError_t occupancy_dp_f_dtw(int loc, int tb, bool vals, size_t smem, int *blocks_per_sm) {
 	cudaError_t e = cudaErrorInvalidValue;
-#define PA_OCC(L, T) \
-	if (loc == L && tb == T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, dp_kernel<float, GAP_DTW, L, T>, BLOCK, smem);
+#define PA_OCC(L, T) PA_OCC2(L, T, false) PA_OCC2(L, T, true)
+#define PA_OCC2(L, T, VA) \
+	if (loc == L && tb == T && vals == VA) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, dp_kernel<float, GAP_DTW, L, T, VA>, BLOCK, smem);
 	PA_OCC(LOC_GLOBAL, TB_NONE) PA_OCC(LOC_GLOBAL, TB_ONE)
 #undef PA_OCC
+#undef PA_OCC2
 	return e;
 }
 

@@ -157,7 +157,8 @@ struct ResultData {
 		const int q = i / rpp, rem = i - q * rpp, sb = rem / R, r = rem - sb * R;
 		const int64_t S = lt[lane] + G - 1;
 		const uint32_t w = masks_one[size_t(mask_off[lane] + (int64_t(q) * S + (j + sb)) * G + sb)];
-		return (w >> (4 * r)) & 15u;
+		// D source code | P-extend << 2 | Q-extend << 3 (layout written by dp_kernel)
+		return ((w >> (2 * r)) & 3u) | (((w >> (16 + r)) & 1u) << 2) | (((w >> (24 + r)) & 1u) << 3);
 	}
 	uint32_t cell(int64_t lane, int i, int j) const {
 		const int rpp = G * R;
@@ -293,7 +294,7 @@ struct pa_solver {
 	DevBuf d_a, d_b, d_tab, d_dense, d_dense_off, d_ls, d_lt, d_order, d_mask_off, d_score, d_seed, d_has,
 	    d_masks, d_scratch, d_counter, d_status, d_border, d_maps, d_map_off, d_paths, d_path_off,
 	    d_path_len, d_vals, d_val_off, d_best, d_gen, d_wsb_off, d_wsb_tb, d_wsb_vals, d_wsb_sub,
-	    d_wsb_sub_off;
+	    d_wsb_sub_off, d_codes_max;
 	PinBuf h_stage, h_out;
 
 	~pa_solver() {
@@ -332,6 +333,7 @@ struct Plan {
 	bool use_int = false;
 	int tb = TB_ONE;
 	int G = 32;
+	int key_shift = 0;
 	int64_t max_ls = 0, max_lt = 0;
 };
 
@@ -353,9 +355,8 @@ V cvt(float x, bool use_int, int scale, int tag) {
 }
 
 template <typename V>
-pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const int32_t *h_ls,
-                 const int32_t *h_lt, int64_t npairs, bool want_values, const float *best_in_dev,
-                 int *launches) {
+pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const float *host_table,
+                 int64_t npairs, bool want_values, const float *best_in_dev, int *launches) {
 	const bool ISINT = std::is_same<V, int32_t>::value;
 	const bool tag = ISINT && tb != TB_ALL;
 	const int scale = tag ? 4 : 1;
@@ -368,6 +369,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.sub_kind = in.form == F_DENSE ? SUB_DENSE : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
 	p.neg_inf = ISINT ? V(-(1 << 29)) : V(-INFINITY);
 	p.G = plan.G;
+	p.key_shift = plan.key_shift;
 	p.out_sign = s->sign;
 	const int gk = s->gap;  // GAP_LINEAR / GAP_AFFINE / GAP_DTW
 	const int diag_tag = (tag && gk != GAP_DTW) ? 2 : 0;
@@ -426,16 +428,16 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 		p.top_D = b + 2 * ns;
 		p.top_Q = b + 2 * ns + nt;
 		if (in.form == F_INDEXED) {
-			// the table is uploaded as floats; convert on the host here (small)
-			std::vector<float> ht(size_t(in.table_rows * in.table_cols));
-			if (in.location == PA_DEVICE) {
-				PA_CUDA(pa_copy(s, ht.data(), in.table, ht.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
-				PA_CUDA(cudaStreamSynchronize(st));
-			} else {
-				std::memcpy(ht.data(), in.table, ht.size() * sizeof(float));
+			// the table (small) is converted on the host: scaled, tagged, direction-normalised
+			const size_t nt_ = size_t(in.table_rows * in.table_cols);
+			tabv.resize(nt_);
+			bool fits_int8 = ISINT && tag && in.table_cols <= 8 && in.table_rows <= MAX_SMEM_TABLE;
+			for (size_t k = 0; k < nt_; k++) {
+				tabv[k] = cvt<V>(host_table[k] * s->sign, ISINT, scale, diag_tag);
+				if (ISINT && (int64_t(tabv[k]) < -128 || int64_t(tabv[k]) > 127)) fits_int8 = false;
 			}
-			tabv.resize(ht.size());
-			for (size_t k = 0; k < ht.size(); k++) tabv[k] = cvt<V>(ht[k] * s->sign, ISINT, scale, diag_tag);
+			// an int8 query profile read with one prmt per cell (alphabets of <= 8 letters)
+			if (fits_int8) p.sub_kind = SUB_PROFILE;
 			PA_CUDA(s->d_tab.ensure(tabv.size() * sizeof(V)));
 			PA_CUDA(pa_copy(s, s->d_tab.p, tabv.data(), tabv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
 			p.table = s->d_tab.as<V>();
@@ -464,13 +466,13 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	cudaError_t e;
 	const int loc = s->loc;
 	if (ISINT) {
-		e = gk == GAP_LINEAR ? occupancy_dp_i_linear(loc, tb, smem, &bps)
-		    : gk == GAP_AFFINE ? occupancy_dp_i_affine(loc, tb, smem, &bps)
-		                       : occupancy_dp_i_dtw(loc, tb, smem, &bps);
+		e = gk == GAP_LINEAR ? occupancy_dp_i_linear(loc, tb, want_values, smem, &bps)
+		    : gk == GAP_AFFINE ? occupancy_dp_i_affine(loc, tb, want_values, smem, &bps)
+		                       : occupancy_dp_i_dtw(loc, tb, want_values, smem, &bps);
 	} else {
-		e = gk == GAP_LINEAR ? occupancy_dp_f_linear(loc, tb, smem, &bps)
-		    : gk == GAP_AFFINE ? occupancy_dp_f_affine(loc, tb, smem, &bps)
-		                       : occupancy_dp_f_dtw(loc, tb, smem, &bps);
+		e = gk == GAP_LINEAR ? occupancy_dp_f_linear(loc, tb, want_values, smem, &bps)
+		    : gk == GAP_AFFINE ? occupancy_dp_f_affine(loc, tb, want_values, smem, &bps)
+		                       : occupancy_dp_f_dtw(loc, tb, want_values, smem, &bps);
 	}
 	PA_CUDA(e);
 	bps = std::max(bps, 1);
@@ -486,18 +488,16 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 
 	PA_CUDA(cudaMemsetAsync(s->d_counter.p, 0, sizeof(int32_t), st));
 	if (ISINT) {
-		e = gk == GAP_LINEAR ? launch_dp_i_linear(loc, tb, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
-		    : gk == GAP_AFFINE ? launch_dp_i_affine(loc, tb, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
-		                       : launch_dp_i_dtw(loc, tb, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st);
+		e = gk == GAP_LINEAR ? launch_dp_i_linear(loc, tb, want_values, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
+		    : gk == GAP_AFFINE ? launch_dp_i_affine(loc, tb, want_values, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
+		                       : launch_dp_i_dtw(loc, tb, want_values, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st);
 	} else {
-		e = gk == GAP_LINEAR ? launch_dp_f_linear(loc, tb, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
-		    : gk == GAP_AFFINE ? launch_dp_f_affine(loc, tb, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
-		                       : launch_dp_f_dtw(loc, tb, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st);
+		e = gk == GAP_LINEAR ? launch_dp_f_linear(loc, tb, want_values, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
+		    : gk == GAP_AFFINE ? launch_dp_f_affine(loc, tb, want_values, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
+		                       : launch_dp_f_dtw(loc, tb, want_values, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st);
 	}
 	PA_CUDA(e);
 	(*launches)++;
-	(void)h_ls;
-	(void)h_lt;
 	return PA_OK;
 }
 
@@ -515,22 +515,14 @@ pa_status validate(pa_solver *s, const Input &in) {
 		return fail(PA_ERR_LENGTH, "sequence t of length " + std::to_string(in.n_t) +
 		                               " exceeds configured maximum length " + std::to_string(s->cap_t));
 	if (!in.length) return fail(PA_ERR_INVALID_ARGUMENT, "length array missing");
-	if (in.form == F_INDEXED && in.location == PA_HOST) {
-		uint32_t ma = 0, mb = 0;
-		for (int64_t k = 0; k < in.batch * in.n_s; k++) ma = std::max(ma, in.a[k]);
-		for (int64_t k = 0; k < in.batch * in.n_t; k++) mb = std::max(mb, in.b[k]);
-		if (in.batch * in.n_s > 0 && int64_t(ma) >= in.table_rows)
-			return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a");
-		if (in.batch * in.n_t > 0 && int64_t(mb) >= in.table_cols)
-			return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in b");
-	}
 	return PA_OK;
 }
 
 // Decide int32 (exact, faster) vs float32 arithmetic.  Integer mode is used when every
 // similarity, gap cost and border is an integer and every reachable value stays below
 // 2^23 in magnitude, which also means the reference's float32 arithmetic is exact.
-bool int_mode_ok(const pa_solver *s, const Input &in, int64_t max_ls, int64_t max_lt) {
+bool int_mode_ok(const pa_solver *s, const Input &in, const float *host_table, int64_t max_ls, int64_t max_lt,
+                 double *bound_out) {
 	if (in.form == F_DENSE) return false;
 	if (s->gap == GAP_GENERAL) return false;
 	double m = 0;
@@ -548,9 +540,8 @@ bool int_mode_ok(const pa_solver *s, const Input &in, int64_t max_ls, int64_t ma
 	if (in.form == F_BINARY) {
 		if (!(chk(in.eq) && chk(in.ne))) return false;
 	} else {
-		if (in.location == PA_DEVICE) return false;  // table not inspected on the host
 		for (int64_t k = 0; k < in.table_rows * in.table_cols; k++)
-			if (!chk(in.table[k])) return false;
+			if (!chk(host_table[k])) return false;
 	}
 	double mb = 0;
 	for (size_t k = 0; k <= size_t(std::min<int64_t>(max_ls, int64_t(s->left_D.size()) - 1)); k++) {
@@ -566,6 +557,7 @@ bool int_mode_ok(const pa_solver *s, const Input &in, int64_t max_ls, int64_t ma
 		}
 	}
 	const double bound = double(max_ls + max_lt + 2) * m + mb;
+	*bound_out = bound;
 	return bound < double(1 << 23);
 }
 
@@ -727,6 +719,31 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			if (nb) PA_CUDA(pa_copy(s, s->d_b.p, in.b, nb, cudaMemcpyHostToDevice, st));
 		}
 	}
+	// the similarity table is small: keep a host copy (device-resident tables are read back)
+	std::vector<float> host_table;
+	if (in.form == F_INDEXED) {
+		host_table.resize(size_t(in.table_rows * in.table_cols));
+		if (in.location == PA_DEVICE) {
+			PA_CUDA(pa_copy(s, host_table.data(), in.table, host_table.size() * 4, cudaMemcpyDeviceToHost, st));
+		} else if (!host_table.empty()) {
+			std::memcpy(host_table.data(), in.table, host_table.size() * 4);
+		}
+		// codes must index the table (factory.h:602-614); checked on the device
+		PA_CUDA(s->d_codes_max.ensure(8));
+		PA_CUDA(cudaMemsetAsync(s->d_codes_max.p, 0, 8, st));
+		const uint32_t *da = in.location == PA_DEVICE ? in.a : s->d_a.as<uint32_t>();
+		const uint32_t *db = in.location == PA_DEVICE ? in.b : s->d_b.as<uint32_t>();
+		const int grid = std::max(1, std::min(s->sm_count * 4, int((B * std::max(in.n_s, in.n_t) + 255) / 256)));
+		if (B * in.n_s > 0) codes_max_kernel<<<grid, 256, 0, st>>>(da, B * in.n_s, s->d_codes_max.as<uint32_t>());
+		if (B * in.n_t > 0) codes_max_kernel<<<grid, 256, 0, st>>>(db, B * in.n_t, s->d_codes_max.as<uint32_t>() + 1);
+		PA_CUDA(cudaGetLastError());
+		uint32_t mx[2] = {0, 0};
+		PA_CUDA(pa_copy(s, mx, s->d_codes_max.p, 8, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(cudaStreamSynchronize(st));
+		if (B * in.n_s > 0 && int64_t(mx[0]) >= in.table_rows) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a");
+		if (B * in.n_t > 0 && int64_t(mx[1]) >= in.table_cols) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in b");
+	}
+
 	// per-pair metadata
 	Plan plan;
 	plan.max_ls = max_ls;
@@ -780,19 +797,27 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	if (s->gap == GAP_GENERAL) {
 		if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
 	} else {
-		const bool use_int = int_mode_ok(s, in, max_ls, max_lt);
+		double bound = 0;
+		bool use_int = int_mode_ok(s, in, host_table.data(), max_ls, max_lt, &bound);
+		if (use_int && s->loc == LOC_LOCAL && tb == TB_ONE) {
+			// local seeds are packed as value * 2^shift + j in an int32
+			int shift = 1;
+			while ((int64_t(1) << shift) <= max_lt) shift++;
+			plan.key_shift = shift;
+			if ((bound * 4.0 + 4.0) * double(int64_t(1) << shift) >= 2147483647.0) use_int = false;
+		}
 		plan.use_int = use_int;
 		if (tb == TB_ALL && s->loc == LOC_LOCAL) {
 			// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
-			pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, TB_NONE, ls.data(), lt.data(), B, false, nullptr, &launches)
-			                       : run_dp<float>(s, in, plan, TB_NONE, ls.data(), lt.data(), B, false, nullptr, &launches);
+			pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, TB_NONE, host_table.data(), B, false, nullptr, &launches)
+			                       : run_dp<float>(s, in, plan, TB_NONE, host_table.data(), B, false, nullptr, &launches);
 			if (e2) return e2;
 			PA_CUDA(s->d_best.ensure(size_t(B) * 4));
 			PA_CUDA(pa_copy(s, s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
 		}
-		pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, tb, ls.data(), lt.data(), B, want_values,
+		pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, tb, host_table.data(), B, want_values,
 		                                         s->d_best.as<float>(), &launches)
-		                       : run_dp<float>(s, in, plan, tb, ls.data(), lt.data(), B, want_values,
+		                       : run_dp<float>(s, in, plan, tb, host_table.data(), B, want_values,
 		                                       s->d_best.as<float>(), &launches);
 		if (e2) return e2;
 	}

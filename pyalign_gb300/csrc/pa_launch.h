@@ -5,9 +5,9 @@
 namespace pa {
 
 #define PA_DECL(V, VT, GAP)                                                                      \
-	cudaError_t launch_dp_##V##_##GAP(int loc, int tb, const DpParams<VT> &p, int grid, size_t smem, \
+	cudaError_t launch_dp_##V##_##GAP(int loc, int tb, bool vals, const DpParams<VT> &p, int grid, size_t smem, \
 	                                  cudaStream_t st);                                          \
-	cudaError_t occupancy_dp_##V##_##GAP(int loc, int tb, size_t smem, int *blocks_per_sm);
+	cudaError_t occupancy_dp_##V##_##GAP(int loc, int tb, bool vals, size_t smem, int *blocks_per_sm);
 PA_DECL(i, int32_t, linear)
 PA_DECL(i, int32_t, affine)
 PA_DECL(i, int32_t, dtw)

@@ -10,7 +10,8 @@ __device__ __forceinline__ uint32_t nibble_at(const uint32_t *W, int i, int j, i
 	const int sb = rem / R;
 	const int r = rem - sb * R;
 	const uint32_t w = W[(int64_t(q) * S + (j + sb)) * G + sb];
-	return (w >> (4 * r)) & 15u;
+	// word layout: D source codes in bits [2r, 2r+2), P-extend bits at 16 + r, Q-extend at 24 + r
+	return ((w >> (2 * r)) & 3u) | (((w >> (16 + r)) & 1u) << 2) | (((w >> (24 + r)) & 1u) << 3);
 }
 
 // One thread per pair.  Steps follow TracebackIterators<false>::Iterator::next
@@ -75,6 +76,14 @@ __global__ void walk_kernel(WalkParams p) {
 		np++;
 	}
 	if (p.path_len) p.path_len[pair] = np;
+}
+
+__global__ void codes_max_kernel(const uint32_t *x, int64_t n, uint32_t *out) {
+	uint32_t m = 0;
+	const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+	for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) m = max(m, x[k]);
+	for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 }  // namespace pa
