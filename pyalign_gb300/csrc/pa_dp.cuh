@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			const bool last_row_lane = pass_active && nvalid >= 1 && nvalid <= R;
 			const int r_last = nvalid - 1;
 
-			uint32_t tnext = (pass_active && brow && sub < lt) ? brow[max(0, -sub)] : 0u;
+			uint32_t tnext = (pass_active && brow) ? brow[0] : 0u;  // code of column 0 (lt >= 1 here)
 			for (int s = 0; s < wsteps; s++) {
 				const int j = s - sub;
 				V upD = __shfl_up_sync(0xffffffffu, outD, 1, G);
