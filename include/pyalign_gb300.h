@@ -256,6 +256,31 @@ pa_status pa_solver_last_bytes(const pa_solver *s, int64_t *h2d, int64_t *d2h);
  * the reference (it has no GPU code). */
 pa_status pa_measure_int32_peak(float *gops, float *ms);
 
+/* ---- allocation-free score solve ----
+ * No counterpart in the reference (its solver allocates its matrices on the host).
+ * For callers that cannot allocate device memory while they run -- a process that owns
+ * all of its HBM through a preallocated pool, or code where a cudaMalloc would stall or
+ * fail mid-request.  Scores only (Solver::score, solver.h:2593-2608) of `batch` pairs in
+ * the indexed form with linear or affine gap costs (o: type ALIGNMENT, direction,
+ * locality, gap_kind and its costs; other fields ignored; the gap border vectors use the
+ * capacity n_s x n_t).  Inputs a (batch x n_s), b (batch x n_t), table, len_s, len_t
+ * (batch int32 each) and the output scores (batch float32) are device memory of the
+ * caller; the work runs on `stream` (a cudaStream_t, NULL = default stream) and is
+ * complete when the stream is.
+ * All scratch lives in one static device array of PA_NOALLOC_SCRATCH_BYTES per device
+ * (held until the process exits): batch <= PA_NOALLOC_MAX_BATCH, n_s, n_t <=
+ * PA_NOALLOC_MAX_LEN and a table of at most 64 x 64; larger sizes are rejected with
+ * PA_ERR_LENGTH.  Every call shares that array: calls whose GPU work overlaps race and
+ * give wrong results.  The first call on a device looks up the array's address (once per
+ * device, that device current) and so should come before any stream capture. */
+#define PA_NOALLOC_SCRATCH_BYTES (32 * 1024 * 1024)
+#define PA_NOALLOC_MAX_BATCH 65536
+#define PA_NOALLOC_MAX_LEN 4096
+pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, const uint32_t *a, const uint32_t *b,
+                                             int64_t batch, int64_t n_s, int64_t n_t, const float *table,
+                                             int64_t table_rows, int64_t table_cols, const int32_t *len_s,
+                                             const int32_t *len_t, float *scores, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
