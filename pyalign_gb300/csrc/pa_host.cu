@@ -296,6 +296,9 @@ struct pa_solver {
 	    d_path_len, d_vals, d_val_off, d_best, d_gen, d_wsb_off, d_wsb_tb, d_wsb_vals, d_wsb_sub,
 	    d_wsb_sub_off, d_codes_max;
 	PinBuf h_stage, h_out;
+	DevBuf d_border_mode[3];          // borders per arithmetic mode: float, int tagged, int plain
+	bool border_ready[3] = {false, false, false};
+	std::vector<unsigned char> h_tab;  // staging of the converted similarity table
 
 	~pa_solver() {
 		for (auto &e : ev)
@@ -337,12 +340,31 @@ struct Plan {
 	int64_t max_ls = 0, max_lt = 0;
 };
 
-int choose_G(int64_t max_ls) {
-	// rows per lane R = 8: the group height G*R covers the typical length in few passes
-	if (max_ls <= 32) return 4;
-	if (max_ls <= 64) return 8;
-	if (max_ls <= 128) return 16;
-	return 32;
+// Group width G (lanes per pair, R = 8 rows each) that minimises the cells a launch
+// computes: the real cells plus the padding rows of each pair's last stripe and the G-1
+// skew steps of every stripe.  Narrower groups share a warp with other pairs, which costs
+// a little divergence at pair boundaries: a 2% penalty per halving keeps G from shrinking
+// for no gain.
+int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt) {
+	static const int cand[4] = {32, 16, 8, 4};
+	double best = 0;
+	int bestG = 32;
+	for (int c = 0; c < 4; c++) {
+		const int G = cand[c];
+		const int64_t rpp = int64_t(G) * R;
+		double cells = 0;
+		for (size_t k = 0; k < ls.size(); k++) {
+			if (ls[k] == 0 || lt[k] == 0) continue;
+			const int64_t npass = (ls[k] + rpp - 1) / rpp;
+			cells += double(npass * rpp) * double(lt[k] + G - 1);
+		}
+		cells *= 1.0 + 0.02 * c;
+		if (c == 0 || cells < best) {
+			best = cells;
+			bestG = G;
+		}
+	}
+	return bestG;
 }
 
 template <typename V>
@@ -381,7 +403,6 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 		p.a_stride = in.n_s;
 		p.b_stride = in.n_t;
 	}
-	std::vector<V> tabv;
 	if (in.form == F_INDEXED) {
 		p.table_rows = int32_t(in.table_rows);
 		p.table_cols = int32_t(in.table_cols);
@@ -408,29 +429,35 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 		p.c_open_t = cvt<V>(-w1t, ISINT, scale, 0);
 		p.c_ext_t = cvt<V>(-o.affine_u_t, ISINT, scale, 0);
 	}
-	// ---- borders
+	// ---- borders: converted once per solver and arithmetic mode, then kept on the device
 	{
 		const size_t ns = s->left_D.size(), nt = s->top_D.size();
-		std::vector<V> bv(2 * ns + 2 * nt);
-		for (size_t k = 0; k < ns; k++) {
-			bv[k] = cvt<V>(s->left_D[k], ISINT, scale, 0);
-			bv[ns + k] = cvt<V>(s->left_P[k], ISINT, scale, tag ? 1 : 0);
+		const int mode = ISINT ? (tag ? 1 : 2) : 0;
+		if (!s->border_ready[mode]) {
+			std::vector<V> bv(2 * ns + 2 * nt);
+			for (size_t k = 0; k < ns; k++) {
+				bv[k] = cvt<V>(s->left_D[k], ISINT, scale, 0);
+				bv[ns + k] = cvt<V>(s->left_P[k], ISINT, scale, tag ? 1 : 0);
+			}
+			for (size_t k = 0; k < nt; k++) {
+				bv[2 * ns + k] = cvt<V>(s->top_D[k], ISINT, scale, 0);
+				bv[2 * ns + nt + k] = cvt<V>(s->top_Q[k], ISINT, scale, 0);
+			}
+			PA_CUDA(s->d_border_mode[mode].ensure(bv.size() * sizeof(V)));
+			PA_CUDA(cudaMemcpy(s->d_border_mode[mode].p, bv.data(), bv.size() * sizeof(V), cudaMemcpyHostToDevice));
+			s->border_ready[mode] = true;
 		}
-		for (size_t k = 0; k < nt; k++) {
-			bv[2 * ns + k] = cvt<V>(s->top_D[k], ISINT, scale, 0);
-			bv[2 * ns + nt + k] = cvt<V>(s->top_Q[k], ISINT, scale, 0);
-		}
-		PA_CUDA(s->d_border.ensure(bv.size() * sizeof(V)));
-		PA_CUDA(pa_copy(s, s->d_border.p, bv.data(), bv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
-		V *b = s->d_border.as<V>();
+		V *b = s->d_border_mode[mode].as<V>();
 		p.left_D = b;
 		p.left_P = b + ns;
 		p.top_D = b + 2 * ns;
 		p.top_Q = b + 2 * ns + nt;
 		if (in.form == F_INDEXED) {
-			// the table (small) is converted on the host: scaled, tagged, direction-normalised
+			// the table (small) is converted on the host: scaled, tagged, direction-normalised;
+			// the staging buffer belongs to the solver, so the copy needs no synchronisation
 			const size_t nt_ = size_t(in.table_rows * in.table_cols);
-			tabv.resize(nt_);
+			s->h_tab.resize(nt_ * sizeof(V));
+			V *tabv = reinterpret_cast<V *>(s->h_tab.data());
 			bool fits_int8 = ISINT && tag && in.table_cols <= 8 && in.table_rows <= MAX_SMEM_TABLE;
 			for (size_t k = 0; k < nt_; k++) {
 				tabv[k] = cvt<V>(host_table[k] * s->sign, ISINT, scale, diag_tag);
@@ -438,12 +465,9 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			}
 			// an int8 query profile read with one prmt per cell (alphabets of <= 8 letters)
 			if (fits_int8) p.sub_kind = SUB_PROFILE;
-			PA_CUDA(s->d_tab.ensure(tabv.size() * sizeof(V)));
-			PA_CUDA(pa_copy(s, s->d_tab.p, tabv.data(), tabv.size() * sizeof(V), cudaMemcpyHostToDevice, st));
+			PA_CUDA(s->d_tab.ensure(nt_ * sizeof(V)));
+			PA_CUDA(pa_copy(s, s->d_tab.p, tabv, nt_ * sizeof(V), cudaMemcpyHostToDevice, st));
 			p.table = s->d_tab.as<V>();
-			PA_CUDA(cudaStreamSynchronize(st));  // tabv/bv are host temporaries
-		} else {
-			PA_CUDA(cudaStreamSynchronize(st));
 		}
 	}
 	// ---- outputs
@@ -748,14 +772,25 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	Plan plan;
 	plan.max_ls = max_ls;
 	plan.max_lt = max_lt;
-	plan.G = choose_G(max_ls);
+	plan.G = choose_G(ls, lt);
 	plan.tb = tb;
 	res.G = plan.G;
+	// processing order: by number of stripes, then |t|, largest first (a counting sort), so
+	// the groups that share a warp get pairs of the same shape and long pairs start early
 	std::vector<int32_t> order(static_cast<size_t>(B));
-	std::iota(order.begin(), order.end(), 0);
-	std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-		return int64_t(ls[size_t(x)]) * lt[size_t(x)] > int64_t(ls[size_t(y)]) * lt[size_t(y)];
-	});
+	{
+		const int64_t rpp = int64_t(plan.G) * R;
+		const int64_t kt = max_lt + 1;
+		const int64_t nkeys = ((max_ls + rpp - 1) / rpp + 1) * kt;
+		std::vector<int32_t> count(size_t(nkeys) + 1, 0);
+		auto key = [&](int64_t k) {
+			const int64_t np = (ls[size_t(k)] + rpp - 1) / rpp;
+			return nkeys - 1 - (np * kt + lt[size_t(k)]);  // descending
+		};
+		for (int64_t k = 0; k < B; k++) count[size_t(key(k)) + 1]++;
+		for (int64_t c = 0; c < nkeys; c++) count[size_t(c) + 1] += count[size_t(c)];
+		for (int64_t k = 0; k < B; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
+	}
 	std::vector<int64_t> mask_off(size_t(B) + 1, 0), map_off(size_t(B) + 1, 0), path_off(size_t(B) + 1, 0),
 	    val_off(size_t(B) + 1, 0), dense_off(size_t(B), 0);
 	const int rpp = plan.G * R;
