@@ -137,10 +137,18 @@ __device__ __forceinline__ int32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
 	return int32_t(d);
 }
 
-// Selector that extracts byte t (0..7) of {hi, lo} sign-extended to 32 bits.
-__device__ __forceinline__ uint32_t sext_selector(uint32_t t) {
-	const uint32_t x = t | 8u;
-	return t | (x << 4) | (x << 8) | (x << 12);
+// Selector that extracts byte t (0..7) of {hi, lo} sign-extended to 32 bits:
+// nibbles t, t|8, t|8, t|8, i.e. t * 0x1111 + 0x8880 for t < 8.
+__device__ __forceinline__ uint32_t sext_selector(uint32_t t) { return t * 0x1111u + 0x8880u; }
+
+// max(a + b, c) in one DPX instruction.
+__device__ __forceinline__ int32_t addmax(int32_t a, int32_t b, int32_t c) { return __viaddmax_s32(a, b, c); }
+
+// 0xffffffff when a > b, else 0.
+__device__ __forceinline__ uint32_t gt_mask(int32_t a, int32_t b) {
+	uint32_t d;
+	asm("set.gt.u32.s32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+	return d;
 }
 
 template <typename V, int GAP, int LOC, int TB, bool VALS>
@@ -333,25 +341,26 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 							// ---- int32 tagged: one max chain gives value and tie winner
 							int32_t key;
 							if (GAP == GAP_AFFINE) {
-								const V oP = uD + p.c_open_s, eP = uP + p.c_ext_s;
-								P = vmax(oP, eP);
-								const V oQ = old + p.c_open_t, eQ = Ql[r] + p.c_ext_t;
-								Q = vmax(oQ, eQ);
-								key = vmax(vmax(dsave + S[r], P), Q);
+								// P = max(D(i-1,j) - open, P(i-1,j) - extend); extend only when strictly better
+								const V oP = uD + p.c_open_s;
+								P = addmax(uP, p.c_ext_s, oP);
+								const V oQ = old + p.c_open_t;
+								Q = addmax(Ql[r], p.c_ext_t, oQ);
+								key = addmax(dsave, S[r], vmax(P, Q));
 								if (LOC == LOC_LOCAL) key = vmax(key, 3);
 								D = key & ~3;
 								if (TB == TB_ONE) {
 									codes |= uint32_t(key & 3) << (2 * r);
-									extp |= (eP > oP) ? (1u << r) : 0u;
-									extq |= (eQ > oQ) ? (1u << r) : 0u;
+									extp |= gt_mask(P, oP) & (1u << r);
+									extq |= gt_mask(Q, oQ) & (1u << r);
 								}
 							} else if (GAP == GAP_LINEAR) {
-								key = vmax(vmax(dsave + S[r], uD + p.c_up), old + p.c_left);
+								key = addmax(dsave, S[r], addmax(uD, p.c_up, old + p.c_left));
 								if (LOC == LOC_LOCAL) key = vmax(key, 3);
 								D = key & ~3;
 								if (TB == TB_ONE) codes |= uint32_t(key & 3) << (2 * r);
 							} else {  // DTW
-								key = vmax(vmax(dsave + 2, uD + 1), old);
+								key = addmax(dsave, 2, addmax(uD, 1, old));
 								D = (key & ~3) + S[r];
 								if (TB == TB_ONE) codes |= uint32_t(key & 3) << (2 * r);
 							}

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -345,8 +346,14 @@ struct Plan {
 // skew steps of every stripe.  Narrower groups share a warp with other pairs, which costs
 // a little divergence at pair boundaries: a 2% penalty per halving keeps G from shrinking
 // for no gain.
-int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt) {
+int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, int sm_count) {
+	if (const char *e = std::getenv("PA_GROUP_WIDTH")) {  // experiments and tuning
+		const int g = std::atoi(e);
+		if (g == 4 || g == 8 || g == 16 || g == 32) return g;
+	}
 	static const int cand[4] = {32, 16, 8, 4};
+	int64_t pairs = 0;
+	for (size_t k = 0; k < ls.size(); k++) pairs += (ls[k] > 0 && lt[k] > 0);
 	double best = 0;
 	int bestG = 32;
 	for (int c = 0; c < 4; c++) {
@@ -359,6 +366,9 @@ int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt) {
 			cells += double(npass * rpp) * double(lt[k] + G - 1);
 		}
 		cells *= 1.0 + 0.02 * c;
+		// keep at least 16 warps per SM busy: narrower groups pack more pairs per warp
+		const int64_t warps = (pairs + 32 / G - 1) / (32 / G);
+		if (c > 0 && warps < int64_t(sm_count) * 16) break;
 		if (c == 0 || cells < best) {
 			best = cells;
 			bestG = G;
@@ -772,7 +782,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	Plan plan;
 	plan.max_ls = max_ls;
 	plan.max_lt = max_lt;
-	plan.G = choose_G(ls, lt);
+	plan.G = choose_G(ls, lt, s->sm_count);
 	plan.tb = tb;
 	res.G = plan.G;
 	// processing order: by number of stripes, then |t|, largest first (a counting sort), so
