@@ -78,6 +78,7 @@ struct DpParams {
 	V neg_inf;
 	int32_t G;              // lanes per pair group
 	int32_t key_shift;      // local seeds: key = value * 2^key_shift + j
+	int32_t one, minus_one, minus_four, minus_eight, sixteen;  // IMAD multipliers (see imad)
 	// outputs
 	float *score;           // reference-domain score
 	int32_t *seed;          // (i, j) per pair
@@ -143,6 +144,15 @@ __device__ __forceinline__ uint32_t sext_selector(uint32_t t) { return t * 0x111
 
 // max(a + b, c) in one DPX instruction.
 __device__ __forceinline__ int32_t addmax(int32_t a, int32_t b, int32_t c) { return __viaddmax_s32(a, b, c); }
+
+// a * b + c on the FMA pipe.  Callers pass multipliers that come from kernel parameters, so
+// the compiler keeps the IMAD instead of turning it into an ALU add/shift: the DP cell
+// update is ALU-pipe bound and this moves part of it to the otherwise idle FMA pipe.
+__device__ __forceinline__ int32_t imad(int32_t a, int32_t b, int32_t c) {
+	int32_t d;
+	asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+	return d;
+}
 
 // 0xffffffff when a > b, else 0.
 __device__ __forceinline__ uint32_t gt_mask(int32_t a, int32_t b) {
@@ -329,7 +339,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 						}
 					}
 
-					uint32_t codes = 0, extp = 0, extq = 0;
+					uint32_t mword = 0;  // one-optimal traceback nibbles of the R rows
 					uint32_t mall[4] = {0, 0, 0, 0};
 					V dsave = prev_up;  // D(i-1, j-1) for the first row
 					V uD = upD, uP = upP;
@@ -342,27 +352,31 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 							int32_t key;
 							if (GAP == GAP_AFFINE) {
 								// P = max(D(i-1,j) - open, P(i-1,j) - extend); extend only when strictly better
-								const V oP = uD + p.c_open_s;
+								const V oP = imad(uD, p.one, p.c_open_s);
 								P = addmax(uP, p.c_ext_s, oP);
-								const V oQ = old + p.c_open_t;
+								const V oQ = imad(old, p.one, p.c_open_t);
 								Q = addmax(Ql[r], p.c_ext_t, oQ);
 								key = addmax(dsave, S[r], vmax(P, Q));
 								if (LOC == LOC_LOCAL) key = vmax(key, 3);
-								D = key & ~3;
+								const int32_t code = key & 3;
+								D = imad(code, p.minus_one, key);
 								if (TB == TB_ONE) {
-									codes |= uint32_t(key & 3) << (2 * r);
-									extp |= gt_mask(P, oP) & (1u << r);
-									extq |= gt_mask(Q, oQ) & (1u << r);
+									// nibble code | P-extend << 2 | Q-extend << 3, row r at bits 4(R-1-r)
+									int32_t nb = imad(int32_t(gt_mask(P, oP)), p.minus_four, code);
+									nb = imad(int32_t(gt_mask(Q, oQ)), p.minus_eight, nb);
+									mword = uint32_t(imad(int32_t(mword), p.sixteen, nb));
 								}
 							} else if (GAP == GAP_LINEAR) {
-								key = addmax(dsave, S[r], addmax(uD, p.c_up, old + p.c_left));
+								key = addmax(dsave, S[r], addmax(uD, p.c_up, imad(old, p.one, p.c_left)));
 								if (LOC == LOC_LOCAL) key = vmax(key, 3);
-								D = key & ~3;
-								if (TB == TB_ONE) codes |= uint32_t(key & 3) << (2 * r);
+								const int32_t code = key & 3;
+								D = imad(code, p.minus_one, key);
+								if (TB == TB_ONE) mword = uint32_t(imad(int32_t(mword), p.sixteen, code));
 							} else {  // DTW
 								key = addmax(dsave, 2, addmax(uD, 1, old));
-								D = (key & ~3) + S[r];
-								if (TB == TB_ONE) codes |= uint32_t(key & 3) << (2 * r);
+								const int32_t code = key & 3;
+								D = imad(code, p.minus_one, key) + S[r];
+								if (TB == TB_ONE) mword = uint32_t(imad(int32_t(mword), p.sixteen, code));
 							}
 						} else {
 							// ---- explicit compares (float, or int32 for all-optimal masks)
@@ -387,9 +401,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 								if (Q > best) { best = Q; code = 0; }
 								D = best;
 								if (TB == TB_ONE) {
-									codes |= uint32_t(code) << (2 * r);
-									extp |= bP ? (1u << r) : 0u;
-									extq |= bQ ? (1u << r) : 0u;
+									mword = (mword << 4) | uint32_t(code) | (bP ? 4u : 0u) | (bQ ? 8u : 0u);
 								} else if (TB == TB_ALL) {
 									cell = (LOC == LOC_LOCAL && best == V(0) ? 1u : 0u) | (dg == best ? 2u : 0u) |
 									       (P == best ? 4u : 0u) | (Q == best ? 8u : 0u) |
@@ -410,7 +422,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 								if (lf > best) { best = lf; code = 0; }
 								D = best;
 								if (TB == TB_ONE) {
-									codes |= uint32_t(code) << (2 * r);
+									mword = (mword << 4) | uint32_t(code);
 								} else if (TB == TB_ALL) {
 									cell = (LOC == LOC_LOCAL && best == V(0) ? 1u : 0u) | (dg == best ? 2u : 0u) |
 									       (up == best ? 4u : 0u) | (lf == best ? 8u : 0u);
@@ -423,7 +435,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 									cell = (dsave == best ? 2u : 0u) | (uD == best ? 4u : 0u) | (old == best ? 8u : 0u);
 								}
 								D = best + S[r];
-								if (TB == TB_ONE) codes |= uint32_t(code) << (2 * r);
+								if (TB == TB_ONE) mword = (mword << 4) | uint32_t(code);
 							}
 							if (TB == TB_ALL) {
 								if (LOC == LOC_LOCAL && r < nvalid && best_in > V(0) && D == best_in) cell |= 256u;
@@ -462,7 +474,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 
 					if (TB == TB_ONE) {
 						uint32_t *m = reinterpret_cast<uint32_t *>(p.masks) + p.mask_off[pair];
-						m[(int64_t(q) * nsteps_pair + s) * G + sub] = codes | (extp << 16) | (extq << 24);
+						m[(int64_t(q) * nsteps_pair + s) * G + sub] = mword;
 					} else if (TB == TB_ALL) {
 						uint4 *m = reinterpret_cast<uint4 *>(p.masks) + p.mask_off[pair];
 						m[(int64_t(q) * nsteps_pair + s) * G + sub] = make_uint4(mall[0], mall[1], mall[2], mall[3]);

@@ -158,8 +158,8 @@ struct ResultData {
 		const int q = i / rpp, rem = i - q * rpp, sb = rem / R, r = rem - sb * R;
 		const int64_t S = lt[lane] + G - 1;
 		const uint32_t w = masks_one[size_t(mask_off[lane] + (int64_t(q) * S + (j + sb)) * G + sb)];
-		// D source code | P-extend << 2 | Q-extend << 3 (layout written by dp_kernel)
-		return ((w >> (2 * r)) & 3u) | (((w >> (16 + r)) & 1u) << 2) | (((w >> (24 + r)) & 1u) << 3);
+		// row r's nibble: D source code | P-extend << 2 | Q-extend << 3, at bits 4(R-1-r)
+		return (w >> (4 * (R - 1 - r))) & 15u;
 	}
 	uint32_t cell(int64_t lane, int i, int j) const {
 		const int rpp = G * R;
@@ -402,6 +402,11 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.neg_inf = ISINT ? V(-(1 << 29)) : V(-INFINITY);
 	p.G = plan.G;
 	p.key_shift = plan.key_shift;
+	p.one = 1;
+	p.minus_one = -1;
+	p.minus_four = -4;
+	p.minus_eight = -8;
+	p.sixteen = 16;
 	p.out_sign = s->sign;
 	const int gk = s->gap;  // GAP_LINEAR / GAP_AFFINE / GAP_DTW
 	const int diag_tag = (tag && gk != GAP_DTW) ? 2 : 0;

@@ -251,6 +251,11 @@ extern "C" pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, con
 	p.top_Q = top_D;
 	p.neg_inf = -INFINITY;
 	p.G = G;
+	p.one = 1;
+	p.minus_one = -1;
+	p.minus_four = -4;
+	p.minus_eight = -8;
+	p.sixteen = 16;
 	p.score = scores;
 	p.seed = seeds;
 	p.has_seed = has;

@@ -10,8 +10,8 @@ __device__ __forceinline__ uint32_t nibble_at(const uint32_t *W, int i, int j, i
 	const int sb = rem / R;
 	const int r = rem - sb * R;
 	const uint32_t w = W[(int64_t(q) * S + (j + sb)) * G + sb];
-	// word layout: D source codes in bits [2r, 2r+2), P-extend bits at 16 + r, Q-extend at 24 + r
-	return ((w >> (2 * r)) & 3u) | (((w >> (16 + r)) & 1u) << 2) | (((w >> (24 + r)) & 1u) << 3);
+	// row r's nibble (D source code | P-extend << 2 | Q-extend << 3) at bits 4(R-1-r)
+	return (w >> (4 * (R - 1 - r))) & 15u;
 }
 
 // One thread per pair.  Steps follow TracebackIterators<false>::Iterator::next
