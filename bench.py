@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1002)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fwd-bwd-pairs", type=int, default=4096, help="pairs of the fwd+bwd measurement (0: skip)")
+    ap.add_argument("--plain-pairs", type=int, default=2048,
+                    help="pairs timed on the plain path (one launch per 4-pair batch)")
     return ap.parse_args()
 
 
@@ -221,6 +224,80 @@ def cpu_baseline(a, b, ls, lt, table, seconds):
     return cells / dt / 1e9, threads, f"first {n} pairs of the workload ({cells:.3e} cells, {dt:.1f} s)"
 
 
+# --------------------------------------------------------------------------- fwd + bwd
+
+def fwd_bwd(torch, pairs, seed, steps=3):
+    """The differentiation form: global Gotoh (open 0.5, extend 0.1) on cosine similarities
+    of per-token embeddings (d = 128, lengths U[64, 256], BF16 product with FP32
+    accumulation), forward vs forward + backward (path subgradient, embedding gradients
+    through the product), and DTW (minimize, |x - y|) on Gaussian random walks (lengths
+    U[128, 1024]) with gradients w.r.t. the series.  GCUPS over real cells."""
+    from pyalign_gb300 import autograd as ag
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    ls = rng.integers(64, 257, pairs)
+    lt = rng.integers(64, 257, pairs)
+    lengths = np.stack([ls, lt], axis=1)
+    cells = float((ls.astype(np.int64) * lt).sum())
+    Es = torch.randn(pairs, 256, 128, device="cuda", generator=g)
+    Et = torch.randn(pairs, 256, 128, device="cuda", generator=g)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def run(backward):
+        a = Es.clone().requires_grad_(backward)
+        b = Et.clone().requires_grad_(backward)
+        S = ag.cosine_similarity_batch(a, b)
+        sc = ag.alignment_score(S, lengths, 0.5, 0.1, "global", "maximize")
+        if backward:
+            sc.sum().backward()
+        return sc
+
+    for _ in range(2):
+        run(True)
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(steps):
+        run(False)
+    ev[1].record()
+    for _ in range(steps):
+        run(True)
+    ev[2].record()
+    torch.cuda.synchronize()
+    fwd = cells * steps / (ev[0].elapsed_time(ev[1]) / 1000) / 1e9
+    fb = cells * steps / (ev[1].elapsed_time(ev[2]) / 1000) / 1e9
+
+    # DTW on random walks
+    nd = max(1, pairs // 4)
+    dl = rng.integers(128, 1025, size=(nd, 2))
+    dcells = float((dl[:, 0].astype(np.int64) * dl[:, 1]).sum())
+    x0 = torch.cumsum(torch.randn(nd, 1024, device="cuda", generator=g), dim=1)
+    y0 = torch.cumsum(torch.randn(nd, 1024, device="cuda", generator=g), dim=1)
+
+    def run_dtw(backward):
+        x = x0.clone().requires_grad_(backward)
+        y = y0.clone().requires_grad_(backward)
+        D = (x[:, :, None] - y[:, None, :]).abs()
+        sc = ag.alignment_score(D, dl, locality="global", direction="minimize", dtw=True)
+        if backward:
+            sc.sum().backward()
+        return sc
+
+    run_dtw(True)
+    torch.cuda.synchronize()
+    ev[0].record()
+    run_dtw(False)
+    ev[1].record()
+    run_dtw(True)
+    ev[2].record()
+    torch.cuda.synchronize()
+    dfwd = dcells / (ev[0].elapsed_time(ev[1]) / 1000) / 1e9
+    dfb = dcells / (ev[1].elapsed_time(ev[2]) / 1000) / 1e9
+    return {"value": fb, "unit": "GCUPS", "fwd_only": fwd, "fwd_bwd_over_fwd": fb / fwd,
+            "workload": f"{pairs} pairs, global Gotoh 0.5/0.1 on cosine(E_s, E_t), d=128, L~U[64,256]",
+            "dtw": {"fwd_bwd": dfb, "fwd_only": dfwd, "fwd_bwd_over_fwd": dfb / dfwd,
+                    "workload": f"{nd} pairs, DTW |x-y| on Gaussian random walks, L~U[128,1024]"}}
+
+
 # --------------------------------------------------------------------------- arms
 
 def run_reference(args):
@@ -351,6 +428,51 @@ def run_ours(args):
     # correctness spot check of the device results against the host path below
     sc_dev = sc_d.cpu().numpy().copy()
 
+    # ---- the plain GPU path: pyalign's ProblemBatch shape, one native call (one DP launch)
+    # per batch of 4 pairs -- the SIMD width of the reference on the aarch64 host -- with the
+    # batch padded to its master shape, on a sample of the workload (device-resident codes)
+    plain = None
+    if args.plain_pairs > 0:
+        lanes = 4
+        npl = min(args.plain_pairs, B) // lanes * lanes
+        psolver = mod.create_solver(1000, 1000, mod.create_options(options_dict(alg, lanes)))
+        alg.check(L.pa_solver_set_stream(psolver.handle, ctypes.c_void_p(stream.cuda_stream)))
+        order = np.argsort(ls[:npl].astype(np.int64) * lt[:npl], kind="stable")
+        batches = []
+        for k0 in range(0, npl, lanes):
+            idx = order[k0:k0 + lanes]
+            n_s, n_t = int(ls[idx].max()), int(lt[idx].max())
+            pa_ = torch.from_numpy(np.ascontiguousarray(a[idx, :n_s]).view(np.int32)).cuda()
+            pb_ = torch.from_numpy(np.ascontiguousarray(b[idx, :n_t]).view(np.int32)).cuda()
+            plen = np.ascontiguousarray(np.stack([ls[idx], lt[idx]]), dtype=np.int32)
+            psz = np.minimum(ls[idx], lt[idx]).astype(np.int64)
+            poff = np.zeros(lanes, np.int64)
+            poff[1:] = np.cumsum(psz)[:-1]
+            pmaps = torch.empty(int(psz.sum()), dtype=torch.int32, device="cuda")
+            psc = torch.empty(lanes, dtype=torch.float32, device="cuda")
+            P = ctypes.POINTER
+            bt = alg.Batch(form=1, location=1, batch=lanes, n_s=n_s, n_t=n_t,
+                           a=ctypes.cast(pa_.data_ptr(), P(ctypes.c_uint32)),
+                           b=ctypes.cast(pb_.data_ptr(), P(ctypes.c_uint32)),
+                           table=ctypes.cast(t_d.data_ptr(), P(ctypes.c_float)), table_rows=4, table_cols=4,
+                           length=plen.ctypes.data_as(P(ctypes.c_int32)))
+            batches.append((bt, psc, pmaps, poff, plen, pa_, pb_))
+        pcells = int((ls[:npl].astype(np.int64) * lt[:npl]).sum())
+
+        def plain_pass():
+            for bt, psc, pmaps, poff, _, _, _ in batches:
+                alg.check(L.pa_solve_batch(psolver.handle, ctypes.byref(bt), ctypes.c_void_p(psc.data_ptr()),
+                                           ctypes.c_void_p(pmaps.data_ptr()),
+                                           poff.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        plain_pass()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plain_pass()
+        torch.cuda.synchronize()
+        pt = time.perf_counter() - t0
+        plain = {"value": pcells / pt / 1e9, "unit": "GCUPS", "pairs": npl, "pairs_per_launch": lanes,
+                 "batched_over_plain": None}
+
     # ---- end-to-end timing through the C ABI with host buffers
     for _ in range(max(1, args.warmup)):
         step_host()
@@ -398,11 +520,15 @@ def run_ours(args):
                 "frac": alg_bytes / dp_s / 1e9 / hbm_peak, "traffic": traffic,
                 "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"}
 
+    fb = fwd_bwd(torch, args.fwd_bwd_pairs, args.seed + 5) if args.fwd_bwd_pairs > 0 else None
+
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         g, threads, desc = cpu_baseline(a, b, ls, lt, table, args.cpu_seconds)
         cpu = {"value": g, "unit": "GCUPS", "cores": threads, "kind": "port", "sample": desc}
 
+    if plain is not None:
+        plain["batched_over_plain"] = value / plain["value"]
     line = {
         "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed * 1000.0 / args.steps, "higher_is_better": True,
@@ -416,6 +542,8 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": "GCUPS", "h2d_bytes_per_step": int(h2d.value),
                 "d2h_bytes_per_step": int(d2h.value)},
         "gpu_launches": launches,
+        "plain_gpu": plain,
+        "fwd_bwd": fb,
         "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms)},
         "clocks": clocks.summary(),
     }

@@ -242,6 +242,30 @@ typedef struct pa_batch {
 pa_status pa_solve_batch(pa_solver *s, const pa_batch *batch, float *scores, int32_t *maps,
                          const int64_t *map_offsets);
 
+/* ---- differentiation (the fwd+bwd form) ----
+ * Forward: score plus one optimal path per pair for a dense similarity held in device
+ * memory with an explicit layout, S(k, i, j) = sim[offsets[k] + i*stride_s + j*stride_t]
+ * (offsets: host array).  Writes scores (device, batch), the traceback walk of each pair
+ * (device, 2 ints per point, |s| + |t| + 2 points at path_offsets[k] ints; host array of
+ * offsets) and path_len (device).  The solver must be a one-optimal-path solver
+ * (linear, affine or DTW).  No counterpart in the reference, which has no gradients; the
+ * path is the one Solver::solution reports (solver.h:2665-2705). */
+pa_status pa_solve_dense_paths(pa_solver *s, const float *sim, const int64_t *offsets, int64_t stride_s,
+                               int64_t stride_t, int64_t batch, int64_t n_s, int64_t n_t, const int32_t *length,
+                               float *scores, int32_t *paths, const int64_t *path_offsets, int32_t *path_len);
+
+/* Backward: the max-plus subgradient of the optimal score.  Adds grad_scores[k] to dS at
+ * every aligned (diagonal-step) cell of pair k's path -- every visited cell for DTW -- and
+ * writes dgap[4k..4k+3] = d score / d (open_s, extend_s, open_t, extend_t) times
+ * grad_scores[k], for w(len) = open + extend * (len - 1), border gaps of global paths
+ * included.  paths/path_offsets/path_len as produced by pa_solve_dense_paths but ALL in
+ * device memory, as are grad_scores, dS, ds_offsets and dgap (may be NULL).  Allocates
+ * nothing; runs on `stream`. */
+pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t direction, int64_t batch,
+                            const int32_t *paths, const int64_t *path_offsets, const int32_t *path_len,
+                            const float *grad_scores, float *dS, const int64_t *ds_offsets, int64_t stride_s,
+                            int64_t stride_t, float *dgap, void *stream);
+
 /* Device time of the phases of the last solve on this solver, in milliseconds
  * (0: upload, 1: DP kernels, 2: traceback kernels, 3: download), and the number of
  * kernels launched.  Measured with CUDA events on the solver's stream. */

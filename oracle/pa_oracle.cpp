@@ -66,14 +66,17 @@ typedef struct {
 
 namespace {
 
+// T is float (the reference's Value, module.cpp:11-14) or double (the FP64 twin used to
+// check float results and gradients).
+template <typename T>
 struct Dir {
 	bool maximize;
-	float worst() const {  // solver.h:62-65, 88-91
-		return maximize ? -std::numeric_limits<float>::infinity() : std::numeric_limits<float>::infinity();
+	T worst() const {  // solver.h:62-65, 88-91
+		return maximize ? -std::numeric_limits<T>::infinity() : std::numeric_limits<T>::infinity();
 	}
-	bool is_opt(float a, float b) const { return maximize ? (a > b) : (a < b); }  // solver.h:53-56, 79-82
-	float opt(float a, float b) const { return is_opt(a, b) ? a : b; }
-	float sgn() const { return maximize ? -1.0f : 1.0f; }  // gap_sgn, solver.h:2807
+	bool is_opt(T a, T b) const { return maximize ? (a > b) : (a < b); }  // solver.h:53-56, 79-82
+	T opt(T a, T b) const { return is_opt(a, b) ? a : b; }
+	T sgn() const { return maximize ? T(-1) : T(1); }  // gap_sgn, solver.h:2807
 };
 
 // One traceback cell.  In "one" mode (traceback_1, solver.h:196-278) the list holds at most
@@ -102,42 +105,44 @@ struct TB {
 };
 
 // A layer of values and traceback cells with the reference's (-1)-shifted indexing.
+template <typename T>
 struct Layer {
 	int32_t ls = 0, lt = 0;
-	std::vector<float> val;
+	std::vector<T> val;
 	std::vector<TB> tb;
-	void init(int32_t s, int32_t t, float fill) {
+	void init(int32_t s, int32_t t, T fill) {
 		ls = s; lt = t;
 		val.assign(size_t(s + 1) * size_t(t + 1), fill);
 		tb.assign(size_t(s + 1) * size_t(t + 1), TB());
 	}
 	size_t idx(int32_t i, int32_t j) const { return size_t(i + 1) * size_t(lt + 1) + size_t(j + 1); }
-	float &V(int32_t i, int32_t j) { return val[idx(i, j)]; }
-	float V(int32_t i, int32_t j) const { return val[idx(i, j)]; }
-	TB &T(int32_t i, int32_t j) { return tb[idx(i, j)]; }
-	const TB &T(int32_t i, int32_t j) const { return tb[idx(i, j)]; }
+	T &V(int32_t i, int32_t j) { return val[idx(i, j)]; }
+	T V(int32_t i, int32_t j) const { return val[idx(i, j)]; }
+	TB &Tb(int32_t i, int32_t j) { return tb[idx(i, j)]; }
+	const TB &Tb(int32_t i, int32_t j) const { return tb[idx(i, j)]; }
 };
 
 // The accumulators of solver.h:1226-1427: the first push initialises, later pushes replace
 // only when strictly better (direction::opt_q); in "all" mode, equal values append.
+template <typename T>
 struct Acc {
-	const Dir &dir;
+	const Dir<T> &dir;
 	int goal;
-	float &val;
+	T &val;
 	TB &tb;
 
-	void init(float v, Pt p) {
+	void init(T v, Pt p) {
 		val = v;
 		if (goal != GOAL_SCORE) {
 			tb.clear();
 			if (goal == GOAL_ALL || p.u != NO_TB) tb.push(p);
 		}
 	}
-	void init(float v, const TB &t) {
+	void init(T v, const TB &t) {
 		val = v;
 		if (goal != GOAL_SCORE) tb.assign(t);
 	}
-	void push(float v, Pt p) {
+	void push(T v, Pt p) {
 		if (goal == GOAL_SCORE) {
 			val = dir.opt(v, val);
 			return;
@@ -148,7 +153,7 @@ struct Acc {
 			tb.push(p);
 		}
 	}
-	void push(float v, const TB &t) {
+	void push(T v, const TB &t) {
 		if (goal == GOAL_SCORE) {
 			val = dir.opt(v, val);
 			return;
@@ -164,11 +169,12 @@ struct Acc {
 // xt::linspace<float>(start, stop, n): start + step * i, step = (stop - start) / (n - 1).
 // This is the assumed semantics of the xtensor generator used by AffineCost::vector
 // (solver.h:2876-2880); it is exact for integer costs.
-std::vector<float> affine_vector(float u, float v, size_t n) {
-	std::vector<float> w(n);
-	const float stop = float(n - 1) * u;
-	const float step = n > 1 ? (stop - 0.0f) / float(n - 1) : 0.0f;
-	for (size_t i = 0; i < n; i++) w[i] = (0.0f + step * float(i)) + v;
+template <typename T>
+std::vector<T> affine_vector(T u, T v, size_t n) {
+	std::vector<T> w(n);
+	const T stop = T(n - 1) * u;
+	const T step = n > 1 ? (stop - T(0)) / T(n - 1) : T(0);
+	for (size_t i = 0; i < n; i++) w[i] = (T(0) + step * T(i)) + v;
 	if (n > 0) w[0] = 0;
 	return w;
 }
@@ -226,46 +232,48 @@ struct PathHash {
 	}
 };
 
+template <typename T>
 struct Problem {
 	pao_options o;
-	Dir dir;
+	Dir<T> dir;
 	int goal;
 	int32_t ls, lt;
-	std::vector<float> sim;  // ls x lt row-major
-	std::vector<float> gen_s, gen_t;
-	std::vector<Layer> layers;  // D (, P, Q)
+	std::vector<T> sim;  // ls x lt row-major
+	std::vector<T> gen_s, gen_t;
+	T lin_s = 0, lin_t = 0, au_s = 0, av_s = 0, au_t = 0, av_t = 0;  // gap costs
+	std::vector<Layer<T>> layers;  // D (, P, Q)
 
 	// traceback strategy (solver.h:2094-2124, 2190-2220, 2296-2326)
 	bool cont1(int32_t u, int32_t v) const { return u >= 0 && v >= 0; }
-	bool cont2(float val) const {
-		if (o.type == TYPE_ALIGNMENT && o.locality == LOC_LOCAL) return dir.is_opt(val, 0.0f);
+	bool cont2(T val) const {
+		if (o.type == TYPE_ALIGNMENT && o.locality == LOC_LOCAL) return dir.is_opt(val, T(0));
 		return true;
 	}
 	bool has_trace() const { return goal != GOAL_SCORE; }
-	float s(int32_t i, int32_t j) const { return sim[size_t(i) * size_t(lt) + size_t(j)]; }
+	T s(int32_t i, int32_t j) const { return sim[size_t(i) * size_t(lt) + size_t(j)]; }
 
 	// seeds pushed onto a LIFO stack (solver.h:1937-2092, 2174-2188, 2266-2294)
 	std::vector<Pt> seeds() const {
 		std::vector<Pt> out;
-		const Layer &D = layers[0];
+		const Layer<T> &D = layers[0];
 		const int loc = o.type == TYPE_DTW ? LOC_GLOBAL : o.locality;
 		if (loc == LOC_GLOBAL) {
 			out.push_back(Pt{ls - 1, lt - 1});
 		} else if (loc == LOC_LOCAL && goal == GOAL_ALL) {
-			float best = 0.0f;
+			T best = T(0);
 			for (int32_t i = ls - 1; i >= 0; i--)
 				for (int32_t j = lt - 1; j >= 0; j--) best = dir.opt(D.V(i, j), best);
 			for (int32_t i = ls - 1; i >= 0; i--)
 				for (int32_t j = lt - 1; j >= 0; j--) {
-					const float x = D.V(i, j);
-					if (x == best && dir.is_opt(x, 0.0f)) out.push_back(Pt{i, j});
+					const T x = D.V(i, j);
+					if (x == best && dir.is_opt(x, T(0))) out.push_back(Pt{i, j});
 				}
 		} else {
 			// Optima: strict replacement in scan order
-			float best = dir.worst();
+			T best = dir.worst();
 			Pt bp{0, 0};
 			auto add = [&](int32_t i, int32_t j) {
-				const float x = D.V(i, j);
+				const T x = D.V(i, j);
 				if (dir.is_opt(x, best)) { best = x; bp = Pt{i, j}; }
 			};
 			if (loc == LOC_LOCAL) {
@@ -283,42 +291,42 @@ struct Problem {
 	void build_layers() {
 		const bool dtw = o.type == TYPE_DTW;
 		const int loc = dtw ? LOC_GLOBAL : o.locality;
-		const float sgn = dir.sgn();
-		const float worst = dir.worst();
+		const T sgn = dir.sgn();
+		const T worst = dir.worst();
 		const int nlayers = (!dtw && o.gap_kind == GAP_AFFINE) ? 3 : 1;
-		layers.assign(size_t(nlayers), Layer());
-		for (auto &L : layers) L.init(ls, lt, 0.0f);
-		Layer &D = layers[0];
+		layers.assign(size_t(nlayers), Layer<T>());
+		for (auto &L : layers) L.init(ls, lt, T(0));
+		Layer<T> &D = layers[0];
 
 		if (dtw) {  // solver.h:3205-3210
 			for (auto &x : D.val) x = worst;
-			D.V(-1, -1) = 0.0f;
+			D.V(-1, -1) = T(0);
 		} else if (o.gap_kind == GAP_LINEAR) {  // solver.h:2806-2814
 			for (int32_t i = -1; i < ls; i++)
-				D.V(i, -1) = loc == LOC_GLOBAL ? (float(i + 1) * o.linear_s) * sgn : 0.0f;
+				D.V(i, -1) = loc == LOC_GLOBAL ? (T(i + 1) * lin_s) * sgn : T(0);
 			for (int32_t j = -1; j < lt; j++)
-				D.V(-1, j) = loc == LOC_GLOBAL ? (float(j + 1) * o.linear_t) * sgn : 0.0f;
+				D.V(-1, j) = loc == LOC_GLOBAL ? (T(j + 1) * lin_t) * sgn : T(0);
 		} else if (o.gap_kind == GAP_AFFINE) {  // solver.h:2918-2967
-			Layer &P = layers[1], &Q = layers[2];
-			const auto ws = affine_vector(o.affine_u_s, o.affine_v_s, size_t(o.cap_s) + 1);
-			const auto wt = affine_vector(o.affine_u_t, o.affine_v_t, size_t(o.cap_t) + 1);
+			Layer<T> &P = layers[1], &Q = layers[2];
+			const auto ws = affine_vector<T>(au_s, av_s, size_t(o.cap_s) + 1);
+			const auto wt = affine_vector<T>(au_t, av_t, size_t(o.cap_t) + 1);
 			for (int32_t i = -1; i < ls; i++) Q.V(i, -1) = worst;
 			for (int32_t j = -1; j < lt; j++) P.V(-1, j) = worst;
 			for (int32_t i = -1; i < ls; i++) {
-				const float x = loc == LOC_GLOBAL ? ws[size_t(i + 1)] * sgn : 0.0f;
+				const T x = loc == LOC_GLOBAL ? ws[size_t(i + 1)] * sgn : T(0);
 				D.V(i, -1) = x;
 				P.V(i, -1) = x;
 			}
 			for (int32_t j = -1; j < lt; j++) {
-				const float x = loc == LOC_GLOBAL ? wt[size_t(j + 1)] * sgn : 0.0f;
+				const T x = loc == LOC_GLOBAL ? wt[size_t(j + 1)] * sgn : T(0);
 				D.V(-1, j) = x;
 				Q.V(-1, j) = x;
 			}
 		} else {  // solver.h:3116-3125
 			for (int32_t i = -1; i < ls; i++)
-				D.V(i, -1) = loc == LOC_GLOBAL ? gen_s[size_t(i + 1)] * sgn : 0.0f;
+				D.V(i, -1) = loc == LOC_GLOBAL ? gen_s[size_t(i + 1)] * sgn : T(0);
 			for (int32_t j = -1; j < lt; j++)
-				D.V(-1, j) = loc == LOC_GLOBAL ? gen_t[size_t(j + 1)] * sgn : 0.0f;
+				D.V(-1, j) = loc == LOC_GLOBAL ? gen_t[size_t(j + 1)] * sgn : T(0);
 		}
 	}
 
@@ -326,58 +334,58 @@ struct Problem {
 		build_layers();
 		const bool dtw = o.type == TYPE_DTW;
 		const bool local = !dtw && o.locality == LOC_LOCAL;
-		const float sgn = dir.sgn();
-		Layer &D = layers[0];
+		const T sgn = dir.sgn();
+		Layer<T> &D = layers[0];
 
-		auto start = [&](float &val, TB &tb) {
-			Acc a{dir, goal, val, tb};
+		auto start = [&](T &val, TB &tb) {
+			Acc<T> a{dir, goal, val, tb};
 			return a;
 		};
 
 		for (int32_t u = 0; u < ls; u++) {
 			for (int32_t v = 0; v < lt; v++) {
 				if (dtw) {  // solver.h:3233-3250
-					Acc a = start(D.V(u, v), D.T(u, v));
+					Acc<T> a = start(D.V(u, v), D.Tb(u, v));
 					a.init(D.V(u - 1, v - 1), Pt{u - 1, v - 1});
 					a.push(D.V(u - 1, v), Pt{u - 1, v});
 					a.push(D.V(u, v - 1), Pt{u, v - 1});
 					D.V(u, v) += s(u, v);
 				} else if (o.gap_kind == GAP_LINEAR) {  // solver.h:2837-2854
-					Acc a = start(D.V(u, v), D.T(u, v));
+					Acc<T> a = start(D.V(u, v), D.Tb(u, v));
 					bool first = true;
-					if (local) { a.init(0.0f, Pt{NO_TB, NO_TB}); first = false; }
-					const float dg = D.V(u - 1, v - 1) + s(u, v);
+					if (local) { a.init(T(0), Pt{NO_TB, NO_TB}); first = false; }
+					const T dg = D.V(u - 1, v - 1) + s(u, v);
 					if (first) a.init(dg, Pt{u - 1, v - 1}); else a.push(dg, Pt{u - 1, v - 1});
-					a.push(D.V(u - 1, v) + o.linear_s * sgn, Pt{u - 1, v});
-					a.push(D.V(u, v - 1) + o.linear_t * sgn, Pt{u, v - 1});
+					a.push(D.V(u - 1, v) + lin_s * sgn, Pt{u - 1, v});
+					a.push(D.V(u, v - 1) + lin_t * sgn, Pt{u, v - 1});
 				} else if (o.gap_kind == GAP_AFFINE) {  // solver.h:2989-3035
-					Layer &P = layers[1], &Q = layers[2];
-					const float w1s = o.affine_u_s + o.affine_v_s;
-					const float w1t = o.affine_u_t + o.affine_v_t;
+					Layer<T> &P = layers[1], &Q = layers[2];
+					const T w1s = au_s + av_s;
+					const T w1t = au_t + av_t;
 					{
-						Acc a = start(P.V(u, v), P.T(u, v));
+						Acc<T> a = start(P.V(u, v), P.Tb(u, v));
 						a.init(D.V(u - 1, v) + w1s * sgn, Pt{u - 1, v});
-						a.push(P.V(u - 1, v) + o.affine_u_s * sgn, P.T(u - 1, v));
+						a.push(P.V(u - 1, v) + au_s * sgn, P.Tb(u - 1, v));
 					}
 					{
-						Acc a = start(Q.V(u, v), Q.T(u, v));
+						Acc<T> a = start(Q.V(u, v), Q.Tb(u, v));
 						a.init(D.V(u, v - 1) + w1t * sgn, Pt{u, v - 1});
-						a.push(Q.V(u, v - 1) + o.affine_u_t * sgn, Q.T(u, v - 1));
+						a.push(Q.V(u, v - 1) + au_t * sgn, Q.Tb(u, v - 1));
 					}
 					{
-						Acc a = start(D.V(u, v), D.T(u, v));
+						Acc<T> a = start(D.V(u, v), D.Tb(u, v));
 						bool first = true;
-						if (local) { a.init(0.0f, Pt{NO_TB, NO_TB}); first = false; }
-						const float dg = D.V(u - 1, v - 1) + s(u, v);
+						if (local) { a.init(T(0), Pt{NO_TB, NO_TB}); first = false; }
+						const T dg = D.V(u - 1, v - 1) + s(u, v);
 						if (first) a.init(dg, Pt{u - 1, v - 1}); else a.push(dg, Pt{u - 1, v - 1});
-						a.push(P.V(u, v), P.T(u, v));
-						a.push(Q.V(u, v), Q.T(u, v));
+						a.push(P.V(u, v), P.Tb(u, v));
+						a.push(Q.V(u, v), Q.Tb(u, v));
 					}
 				} else {  // solver.h:3153-3182
-					Acc a = start(D.V(u, v), D.T(u, v));
+					Acc<T> a = start(D.V(u, v), D.Tb(u, v));
 					bool first = true;
-					if (local) { a.init(0.0f, Pt{NO_TB, NO_TB}); first = false; }
-					const float dg = D.V(u - 1, v - 1) + s(u, v);
+					if (local) { a.init(T(0), Pt{NO_TB, NO_TB}); first = false; }
+					const T dg = D.V(u - 1, v - 1) + s(u, v);
 					if (first) a.init(dg, Pt{u - 1, v - 1}); else a.push(dg, Pt{u - 1, v - 1});
 					for (int32_t k = -1; k < u; k++)
 						a.push(D.V(k, v) + gen_s[size_t(u - k)] * sgn, Pt{k, v});
@@ -389,15 +397,15 @@ struct Problem {
 	}
 
 	// TracebackIterators<false>::Iterator::next (solver.h:1497-1536) for one seed.
-	bool walk_one(Pt seed, float &score, std::vector<Pt> &path) const {
-		const Layer &D = layers[0];
+	bool walk_one(Pt seed, T &score, std::vector<Pt> &path) const {
+		const Layer<T> &D = layers[0];
 		int32_t u = seed.u, v = seed.v;
 		score = D.V(u, v);
 		path.clear();
 		if (!has_trace()) return true;
 		path.push_back(Pt{u, v});
 		while (cont1(u, v) && cont2(D.V(u, v))) {
-			const TB &t = D.T(u, v);
+			const TB &t = D.Tb(u, v);
 			const int32_t nu = t.n == 0 ? NO_TB : t.p0.u;
 			const int32_t nv = t.n == 0 ? NO_TB : t.p0.v;
 			u = nu; v = nv;
@@ -408,7 +416,7 @@ struct Problem {
 
 	// --- all-optimal DFS state (solver.h:1582-1716) ---
 	struct Entry {
-		float path_val;
+		T path_val;
 		Pt cur;
 		int32_t path_len;
 	};
@@ -428,7 +436,7 @@ struct Problem {
 		}
 	}
 
-	bool next(float &score, std::vector<Pt> &path) {
+	bool next(T &score, std::vector<Pt> &path) {
 		if (goal != GOAL_ALL) {
 			if (one_seeds.empty()) return false;
 			const Pt sd = one_seeds.back();
@@ -436,7 +444,7 @@ struct Problem {
 			walk_one(sd, score, path);
 			return true;
 		}
-		const Layer &D = layers[0];
+		const Layer<T> &D = layers[0];
 		while (!stk.empty()) {
 			const Entry e = stk.top();
 			stk.pop();
@@ -445,7 +453,7 @@ struct Problem {
 			dfs_path.push_back(e.cur);
 			const int32_t u1 = e.cur.u, v1 = e.cur.v;
 			if (cont1(u1, v1) && cont2(D.V(u1, v1))) {
-				const TB &t = D.T(u1, v1);
+				const TB &t = D.Tb(u1, v1);
 				const int32_t psize = int32_t(dfs_path.size());
 				if (t.n > 0) {
 					for (int32_t q = 0; q < t.n; q++) stk.push(Entry{e.path_val, t.at(q), psize});
@@ -472,7 +480,7 @@ struct Problem {
 extern "C" {
 
 struct pao_result {
-	Problem p;
+	Problem<float> p;
 	// result of the one-shot codomains
 	Alignment one;
 	float score = 0;
@@ -486,9 +494,15 @@ struct pao_result {
 // Solve one pair.  `sim` is the ls x lt similarity (or distance) matrix, row-major.
 pao_result *pao_solve(const pao_options *o, int32_t ls, int32_t lt, const float *sim) {
 	auto *r = new pao_result();
-	Problem &p = r->p;
+	Problem<float> &p = r->p;
 	p.o = *o;
-	p.dir = Dir{o->direction == DIR_MAX};
+	p.dir = Dir<float>{o->direction == DIR_MAX};
+	p.lin_s = o->linear_s;
+	p.lin_t = o->linear_t;
+	p.au_s = o->affine_u_s;
+	p.av_s = o->affine_v_s;
+	p.au_t = o->affine_u_t;
+	p.av_t = o->affine_v_t;
 	if (o->type == TYPE_DTW) p.goal = GOAL_ONE;  // factory.h:1055-1099
 	else if (o->count == 1) p.goal = GOAL_ALL;   // factory.h:1219-1233
 	else p.goal = o->detail == 0 ? GOAL_SCORE : GOAL_ONE;  // factory.h:1198-1216
@@ -610,6 +624,47 @@ int64_t pao_batch_alignments(const pao_options *o, int32_t npairs, const int32_t
 	int64_t cells = 0;
 	for (int32_t k = 0; k < npairs; k++) cells += int64_t(ls[k]) * lt[k];
 	return cells;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// FP64 twin of pao_solve + pao_next for one pair (the same recurrences with every value a
+// double): gaps = {linear_s, linear_t, affine_u_s, affine_v_s, affine_u_t, affine_v_t} in
+// double, general costs (cap + 1 entries) in double when o->gap_kind is general.  Returns
+// 1 and fills the score and the one-optimal path (path_len points) when a result exists.
+int32_t pao_solve_f64(const pao_options *o, const double *gaps, const double *gen_s, const double *gen_t,
+                      int32_t ls, int32_t lt, const double *sim, double *score, int32_t *path, int32_t *path_len) {
+	Problem<double> p;
+	p.o = *o;
+	p.dir = Dir<double>{o->direction == DIR_MAX};
+	if (o->type == TYPE_DTW) p.goal = GOAL_ONE;
+	else if (o->count == 1) p.goal = GOAL_ALL;
+	else p.goal = o->detail == 0 ? GOAL_SCORE : GOAL_ONE;
+	p.ls = ls;
+	p.lt = lt;
+	p.lin_s = gaps[0];
+	p.lin_t = gaps[1];
+	p.au_s = gaps[2];
+	p.av_s = gaps[3];
+	p.au_t = gaps[4];
+	p.av_t = gaps[5];
+	p.sim.assign(sim, sim + size_t(ls) * size_t(lt));
+	if (o->type == TYPE_ALIGNMENT && o->gap_kind == GAP_GENERAL) {
+		p.gen_s.assign(gen_s, gen_s + o->cap_s + 1);
+		p.gen_t.assign(gen_t, gen_t + o->cap_t + 1);
+	}
+	p.solve();
+	p.init_iterator();
+	double sc = 0;
+	std::vector<Pt> pth;
+	if (!p.next(sc, pth)) return 0;
+	*score = sc;
+	if (path)
+		for (size_t k = 0; k < pth.size(); k++) { path[2 * k] = pth[k].u; path[2 * k + 1] = pth[k].v; }
+	if (path_len) *path_len = int32_t(pth.size());
+	return 1;
 }
 
 }  // extern "C"

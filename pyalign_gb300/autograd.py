@@ -1,0 +1,152 @@
+"""Differentiable optimal alignment scores (torch.autograd) on the GB300 kernels.
+
+The reference has no gradients; this is the "differentiation" form of the batched solve.
+The forward pass is the same sm_103a DP as the drop-in module (one optimal path per pair,
+solver.h:2665-2705); the backward pass is the max-plus subgradient of the optimal score:
+the indicator of the aligned cells of the optimal path for dScore/dS (every visited cell
+for DTW) and the gap counts along the path for dScore/d(open, extend), computed by
+`pa_path_gradients` from the paths the forward pass keeps on the device.  Gradients with
+respect to embeddings flow through the similarity product by torch's autograd.
+
+Tie-breaking follows the reference, so on inputs with ties the subgradient is the one of
+the reference's optimal path.
+"""
+
+import ctypes
+import types
+
+import numpy as np
+import torch
+
+from . import algorithm as _alg
+
+_SOLVERS = {}
+
+
+class _Gap:
+    def __init__(self, open_, extend):
+        self.open, self.extend = float(open_), float(extend)
+
+    def to_special_case(self):
+        return {"affine": (self.open - self.extend, self.extend)}
+
+
+class _Linear:
+    def __init__(self, g):
+        self.g = float(g)
+
+    def to_special_case(self):
+        return {"linear": self.g}
+
+
+def _solver(batch, n_s, n_t, locality, direction, dtw, gap):
+    key = (batch, n_s, n_t, locality, direction, dtw, gap)
+    s = _SOLVERS.get(key)
+    if s is None:
+        A = _alg
+        d = {
+            "solver": A.Type.DTW if dtw else A.Type.ALIGNMENT,
+            "direction": A.Direction.__members__[direction.upper()],
+            "batch": True, "batch_size": batch, "return_dup": False,
+            "locality": A.Locality.__members__[locality.upper()],
+            "codomain": types.SimpleNamespace(detail=A.Detail.ALIGNMENT, count=A.Count.ONE),
+            "gap_cost": None if dtw else (_Linear(gap[0]) if gap[1] is None else _Gap(*gap)),
+        }
+        mod = A.m32 if max(n_s, n_t) >= 16000 else A.m16
+        s = mod.create_solver(n_s, n_t, mod.create_options(d))
+        if len(_SOLVERS) > 32:
+            _SOLVERS.clear()
+        _SOLVERS[key] = s
+    return s
+
+
+def _lib():
+    L = _alg.lib()
+    if not getattr(L, "_pa_grad_bound", False):
+        vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+        L.pa_solve_dense_paths.restype = i32
+        L.pa_solve_dense_paths.argtypes = [vp, vp, vp, i64, i64, i64, i64, i64, vp, vp, vp, vp, vp]
+        L.pa_path_gradients.restype = i32
+        L.pa_path_gradients.argtypes = [i32, i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp]
+        L._pa_grad_bound = True
+    return L
+
+
+class AlignmentScore(torch.autograd.Function):
+    """Optimal alignment score of each pair; backward = path indicator and gap counts."""
+
+    @staticmethod
+    def forward(ctx, S, lengths, gap_open, gap_extend, locality, direction, dtw, linear):
+        if not S.is_cuda or S.dtype != torch.float32 or S.dim() != 3:
+            raise ValueError("S must be a (batch, len_s, len_t) float32 CUDA tensor")
+        S = S.contiguous()
+        B, n_s, n_t = S.shape
+        ln = np.ascontiguousarray(np.asarray(lengths).reshape(B, 2).T, dtype=np.int32)
+        if (ln[0] > n_s).any() or (ln[1] > n_t).any() or (ln < 0).any():
+            raise ValueError("lengths exceed the similarity tensor")
+        gap = None if dtw else ((float(gap_open), None) if linear else (float(gap_open), float(gap_extend)))
+        solver = _solver(B, n_s, n_t, locality, direction, dtw, gap)
+        L = _lib()
+        stream = torch.cuda.current_stream()
+        _alg.check(L.pa_solver_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
+        offsets = np.arange(B, dtype=np.int64) * (n_s * n_t)
+        sizes = 2 * (ln[0].astype(np.int64) + ln[1] + 2)
+        poff = np.zeros(B, np.int64)
+        poff[1:] = np.cumsum(sizes)[:-1]
+        paths = torch.empty(int(sizes.sum()), dtype=torch.int32, device=S.device)
+        plen = torch.zeros(B, dtype=torch.int32, device=S.device)
+        scores = torch.empty(B, dtype=torch.float32, device=S.device)
+        _alg.check(L.pa_solve_dense_paths(
+            solver.handle, S.data_ptr(), offsets.ctypes.data, n_t, 1, B, n_s, n_t, ln.ctypes.data,
+            scores.data_ptr(), paths.data_ptr(), poff.ctypes.data, plen.data_ptr()))
+        ctx.save_for_backward(paths, plen, torch.from_numpy(poff).to(S.device),
+                              torch.from_numpy(offsets).to(S.device))
+        ctx.meta = (B, n_s, n_t, locality, direction, dtw, linear)
+        return scores
+
+    @staticmethod
+    def backward(ctx, grad):
+        paths, plen, poff, offsets = ctx.saved_tensors
+        B, n_s, n_t, locality, direction, dtw, linear = ctx.meta
+        A = _alg
+        grad = grad.contiguous().float()
+        dS = torch.zeros((B, n_s, n_t), dtype=torch.float32, device=grad.device)
+        dgap = torch.zeros((B, 4), dtype=torch.float32, device=grad.device)
+        L = _lib()
+        st = L.pa_path_gradients(
+            int(A.Type.DTW if dtw else A.Type.ALIGNMENT), int(A.Locality.__members__[locality.upper()]),
+            int(A.Direction.__members__[direction.upper()]), B, paths.data_ptr(), poff.data_ptr(),
+            plen.data_ptr(), grad.data_ptr(), dS.data_ptr(), offsets.data_ptr(), n_t, 1, dgap.data_ptr(),
+            torch.cuda.current_stream().cuda_stream)
+        _alg.check(st)
+        tot = dgap.sum(dim=0)
+        if dtw:
+            d_open = d_ext = None
+        elif linear:
+            d_open, d_ext = tot[0] + tot[1] + tot[2] + tot[3], None
+        else:
+            d_open, d_ext = tot[0] + tot[2], tot[1] + tot[3]
+        return dS, None, d_open, d_ext, None, None, None, None
+
+
+def alignment_score(S, lengths, gap_open=None, gap_extend=None, locality="global", direction="maximize",
+                    dtw=False):
+    """Differentiable optimal scores of `batch` pairs.
+
+    S: (batch, len_s, len_t) float32 CUDA tensor of similarities (distances when
+    minimizing), padded; lengths: (batch, 2) of |s|, |t|.  Affine gaps w(k) = open +
+    extend (k - 1) when both are given, linear w(k) = open * k when gap_extend is None;
+    DTW ignores gaps.  gap_open/gap_extend may be tensors that require grad.
+    """
+    linear = gap_extend is None
+    go = gap_open if isinstance(gap_open, torch.Tensor) else torch.tensor(float(gap_open or 0.0))
+    ge = gap_extend if isinstance(gap_extend, torch.Tensor) else torch.tensor(float(gap_extend or 0.0))
+    return AlignmentScore.apply(S, lengths, go, ge, locality, direction, dtw, linear)
+
+
+def cosine_similarity_batch(Es, Et):
+    """S = cos(E_s, E_t) per pair: L2-normalised embeddings multiplied in BF16 with FP32
+    accumulation.  Es: (batch, len_s, d), Et: (batch, len_t, d)."""
+    Es = torch.nn.functional.normalize(Es, dim=-1)
+    Et = torch.nn.functional.normalize(Et, dim=-1)
+    return torch.bmm(Es.to(torch.bfloat16), Et.to(torch.bfloat16).transpose(1, 2)).float()

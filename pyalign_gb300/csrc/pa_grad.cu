@@ -1,0 +1,97 @@
+// Backward of the optimal alignment score: the max-plus subgradient along the optimal path.
+//
+// The score of an alignment is the sum of the similarities of its aligned cells minus the
+// costs of its gaps (maximize; plus for minimize), so its derivative is 1 for every
+// aligned (diagonal-step) cell of the optimal path, 0 elsewhere, and -(number of gaps) /
+// -(sum of gap lengths - 1) for the open / extend costs, w(k) = open + extend (k - 1)
+// (pyalign/gaps.py:164-193 with solver.h:2858-2881).  For DTW the score is the sum of the
+// distances of every visited cell (solver.h:3233-3250).  Global alignments also pay the
+// border gap their path ends in (solver.h:2918-2951).
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "../../include/pyalign_gb300.h"
+
+namespace {
+
+struct GradParams {
+	int64_t batch;
+	int32_t dtw, global;
+	float gap_sign;  // -1 maximize, +1 minimize (gap_sgn of solver.h:2807)
+	const int32_t *paths;
+	const int64_t *path_off;
+	const int32_t *path_len;
+	const float *grad;
+	float *dS;
+	const int64_t *ds_off;
+	int64_t ss, st;
+	float *dgap;  // 4 per pair: open_s, extend_s, open_t, extend_t
+};
+
+__global__ void path_grad_kernel(GradParams p) {
+	const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (k >= p.batch) return;
+	const float g = p.grad[k];
+	const int n = p.path_len[k];
+	const int32_t *P = p.paths + p.path_off[k];
+	float *d = p.dS + p.ds_off[k];
+	int open_s = 0, ext_s = 0, open_t = 0, ext_t = 0;
+	for (int q = 0; q + 1 < n; q++) {
+		const int u0 = P[2 * q], v0 = P[2 * q + 1], u1 = P[2 * q + 2], v1 = P[2 * q + 3];
+		if (u0 < 0 || v0 < 0) break;
+		if (p.dtw) {
+			d[int64_t(u0) * p.ss + int64_t(v0) * p.st] += g;
+		} else if (u1 == u0 - 1 && v1 == v0 - 1) {
+			d[int64_t(u0) * p.ss + int64_t(v0) * p.st] += g;
+		} else if (v1 == v0 && u1 < u0) {
+			open_s += 1;
+			ext_s += u0 - u1 - 1;
+		} else if (u1 == u0 && v1 < v0) {
+			open_t += 1;
+			ext_t += v0 - v1 - 1;
+		}
+	}
+	if (n > 0 && p.global && !p.dtw) {
+		const int ul = P[2 * (n - 1)], vl = P[2 * (n - 1) + 1];
+		if (ul < 0 && vl >= 0) {  // D(-1, vl) = w_t(vl + 1)
+			open_t += 1;
+			ext_t += vl;
+		} else if (vl < 0 && ul >= 0) {  // D(ul, -1) = w_s(ul + 1)
+			open_s += 1;
+			ext_s += ul;
+		}
+	}
+	if (p.dgap) {
+		const float c = p.gap_sign * g;
+		p.dgap[4 * k + 0] = c * float(open_s);
+		p.dgap[4 * k + 1] = c * float(ext_s);
+		p.dgap[4 * k + 2] = c * float(open_t);
+		p.dgap[4 * k + 3] = c * float(ext_t);
+	}
+}
+
+}  // namespace
+
+extern "C" pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t direction, int64_t batch,
+                                       const int32_t *paths, const int64_t *path_offsets, const int32_t *path_len,
+                                       const float *grad_scores, float *dS, const int64_t *ds_offsets,
+                                       int64_t stride_s, int64_t stride_t, float *dgap, void *stream) {
+	if (batch < 0 || !paths || !path_offsets || !path_len || !grad_scores || !dS || !ds_offsets)
+		return PA_ERR_INVALID_ARGUMENT;
+	if (batch == 0) return PA_OK;
+	GradParams p{};
+	p.batch = batch;
+	p.dtw = type == PA_TYPE_DTW;
+	p.global = type == PA_TYPE_DTW || locality == PA_GLOBAL;
+	p.gap_sign = direction == PA_MINIMIZE ? 1.0f : -1.0f;
+	p.paths = paths;
+	p.path_off = path_offsets;
+	p.path_len = path_len;
+	p.grad = grad_scores;
+	p.dS = dS;
+	p.ds_off = ds_offsets;
+	p.ss = stride_s;
+	p.st = stride_t;
+	p.dgap = dgap;
+	path_grad_kernel<<<int((batch + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}

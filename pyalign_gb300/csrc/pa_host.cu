@@ -89,7 +89,7 @@ struct PinBuf {
 // Goals of solver.h:13-39 as selected by FactoryCreator (factory.h:1195-1240).
 enum Goal { GOAL_SCORE = 0, GOAL_ONE = 1, GOAL_ALL = 2 };
 // Output shapes of the 15 solve methods (factory.h:699-808).
-enum Method { M_SCORE = 0, M_ALIGNMENT = 1, M_ALIGNMENT_ITER = 2, M_SOLUTION = 3, M_SOLUTION_ITER = 4 };
+enum Method { M_SCORE = 0, M_ALIGNMENT = 1, M_ALIGNMENT_ITER = 2, M_SOLUTION = 3, M_SOLUTION_ITER = 4, M_PATHS = 5 };
 enum Form { F_DENSE = 0, F_INDEXED = 1, F_BINARY = 2 };
 
 struct Input {
@@ -102,6 +102,17 @@ struct Input {
 	int64_t table_rows, table_cols;
 	float eq, ne;
 	const int32_t *length;  // host (2, batch)
+	// dense form with explicit layout: S(k, i, j) = sim[dense_off[k] + i * dense_si + j * dense_sj]
+	const int64_t *dense_off_host = nullptr;
+	int64_t dense_si = 0, dense_sj = 0;
+};
+
+// Device buffers of the caller that receive the one-optimal paths (M_PATHS).
+struct UserPaths {
+	int32_t *paths = nullptr;          // 2 ints per point, |s| + |t| + 2 points per pair
+	const int64_t *path_off = nullptr;  // host, in ints
+	int32_t *path_len = nullptr;
+	float *scores = nullptr;
 };
 
 // xt::linspace<float>(0, (n-1)*u, n) + v with w[0] = 0 -- AffineCost::vector
@@ -343,9 +354,10 @@ struct Plan {
 
 // Group width G (lanes per pair, R = 8 rows each) that minimises the cells a launch
 // computes: the real cells plus the padding rows of each pair's last stripe and the G-1
-// skew steps of every stripe.  Narrower groups share a warp with other pairs, which costs
-// a little divergence at pair boundaries: a 2% penalty per halving keeps G from shrinking
-// for no gain.
+// skew steps of every stripe.  Narrower groups share a warp with other pairs and pay more
+// per-stripe overhead: a 6% penalty per halving (measured: G = 8 beats G = 4 on uniform
+// lengths in [100, 1000] although it computes 3% more cells) keeps G from shrinking for no
+// gain.
 int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, int sm_count) {
 	if (const char *e = std::getenv("PA_GROUP_WIDTH")) {  // experiments and tuning
 		const int g = std::atoi(e);
@@ -365,7 +377,7 @@ int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, int
 			const int64_t npass = (ls[k] + rpp - 1) / rpp;
 			cells += double(npass * rpp) * double(lt[k] + G - 1);
 		}
-		cells *= 1.0 + 0.02 * c;
+		cells *= 1.0 + 0.06 * c;
 		// keep at least 16 warps per SM busy: narrower groups pack more pairs per warp
 		const int64_t warps = (pairs + 32 / G - 1) / (32 / G);
 		if (c > 0 && warps < int64_t(sm_count) * 16) break;
@@ -428,8 +440,8 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	} else {
 		p.dense = in.location == PA_DEVICE ? in.sim : s->d_dense.as<float>();
 		p.dense_off = s->d_dense_off.as<int64_t>();
-		p.dense_si = in.n_t * in.batch;
-		p.dense_sj = in.batch;
+		p.dense_si = in.dense_si ? in.dense_si : in.n_t * in.batch;
+		p.dense_sj = in.dense_si ? in.dense_sj : in.batch;
 		p.dense_sign = s->sign;
 	}
 	// ---- gaps (negative addends, maximize form)
@@ -694,7 +706,8 @@ pa_status download_wsb(pa_solver *s, ResultData &res) {
 }
 
 pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_out, pa_result **out,
-                     int32_t *maps_out = nullptr, const int64_t *map_offsets = nullptr) {
+                     int32_t *maps_out = nullptr, const int64_t *map_offsets = nullptr,
+                     const UserPaths *user_paths = nullptr) {
 	if (pa_status st = ensure_device(s)) return st;
 	if (pa_status st = validate(s, in)) return st;
 	cudaStream_t st = s->stream;
@@ -735,11 +748,13 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	const int goal = s->goal;
 	int tb;
 	if (goal == GOAL_SCORE) tb = TB_NONE;
-	else if (goal == GOAL_ONE) tb = (method == M_SCORE) ? TB_NONE : TB_ONE;
+	else if (goal == GOAL_ONE || method == M_PATHS) tb = (method == M_SCORE) ? TB_NONE : TB_ONE;
 	else tb = method == M_SCORE ? TB_NONE : TB_ALL;
 	const bool want_values = (method == M_SOLUTION || method == M_SOLUTION_ITER) && s->gap != GAP_GENERAL;
 	const bool want_paths = method == M_SOLUTION || (goal == GOAL_ONE && method == M_SOLUTION_ITER) ||
-	                        (goal == GOAL_ONE && method == M_ALIGNMENT_ITER);
+	                        (goal == GOAL_ONE && method == M_ALIGNMENT_ITER) || method == M_PATHS;
+	if (method == M_PATHS && s->gap == GAP_GENERAL)
+		return fail(PA_ERR_UNSUPPORTED, "paths of general (WSB) gap costs are not produced on the device");
 
 	cudaEventRecord(s->ev[0], st);
 	int launches = 0;
@@ -816,7 +831,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		map_off[size_t(k) + 1] = map_off[size_t(k)] + std::min(a, b);
 		path_off[size_t(k) + 1] = path_off[size_t(k)] + 2 * (a + b + 2);
 		val_off[size_t(k) + 1] = val_off[size_t(k)] + int64_t(res.layers) * (a + 1) * (b + 1);
-		dense_off[size_t(k)] = k;
+		dense_off[size_t(k)] = in.dense_off_host ? in.dense_off_host[k] : k;
 	}
 	auto up = [&](DevBuf &d, const void *h, size_t n) -> cudaError_t {
 		cudaError_t e = d.ensure(n);
@@ -876,7 +891,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	// ---- traceback walk (one optimal path)
 	const bool need_walk = tb == TB_ONE && s->gap != GAP_GENERAL &&
 	                       (method == M_ALIGNMENT || method == M_ALIGNMENT_ITER || method == M_SOLUTION ||
-	                        method == M_SOLUTION_ITER);
+	                        method == M_SOLUTION_ITER || method == M_PATHS);
+	const bool paths_to_user = method == M_PATHS && user_paths;
 	if (need_walk) {
 		const bool to_user = maps_out && in.location == PA_DEVICE;
 		PA_CUDA(s->d_maps.ensure(size_t(map_off[size_t(B)]) * 4));
@@ -903,6 +919,12 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		w.paths = want_paths ? s->d_paths.as<int32_t>() : nullptr;
 		w.path_off = s->d_path_off.as<int64_t>();
 		w.path_len = want_paths ? s->d_path_len.as<int32_t>() : nullptr;
+		if (paths_to_user) {
+			w.maps = nullptr;
+			w.paths = user_paths->paths;
+			w.path_len = user_paths->path_len;
+			PA_CUDA(up(s->d_path_off, user_paths->path_off, size_t(B) * 8));
+		}
 		walk_kernel<<<int((B + 127) / 128), 128, 0, st>>>(w);
 		PA_CUDA(cudaGetLastError());
 		launches++;
@@ -921,7 +943,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	res.map_off = map_off;
 	res.mask_off = mask_off;
 	if (need_walk) {
-		if (maps_out && in.location == PA_DEVICE) {
+		if ((maps_out && in.location == PA_DEVICE) || paths_to_user) {
 			// results stay on the device
 		} else if (maps_out) {
 			PA_CUDA(pa_copy(s, maps_out, s->d_maps.p, size_t(map_off[size_t(B)]) * 4, cudaMemcpyDeviceToHost, st));
@@ -929,7 +951,10 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			res.maps.resize(size_t(map_off[size_t(B)]));
 			PA_CUDA(pa_copy(s, res.maps.data(), s->d_maps.p, res.maps.size() * 4, cudaMemcpyDeviceToHost, st));
 		}
-		if (want_paths) {
+		if (paths_to_user) {
+			if (user_paths->scores)
+				PA_CUDA(cudaMemcpyAsync(user_paths->scores, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
+		} else if (want_paths) {
 			res.path_off = path_off;
 			res.paths.resize(size_t(path_off[size_t(B)]));
 			res.path_len.resize(size_t(B));
@@ -1288,6 +1313,33 @@ pa_status pa_solve_batch(pa_solver *s, const pa_batch *b, float *scores, int32_t
 	}
 	pa_result_destroy(r);
 	return PA_OK;
+}
+
+pa_status pa_solve_dense_paths(pa_solver *s, const float *sim, const int64_t *offsets, int64_t stride_s,
+                               int64_t stride_t, int64_t batch, int64_t n_s, int64_t n_t, const int32_t *length,
+                               float *scores, int32_t *paths, const int64_t *path_offsets, int32_t *path_len) {
+	if (!s || !sim || !offsets || !length || !paths || !path_offsets || !path_len)
+		return fail(PA_ERR_INVALID_ARGUMENT, "null argument");
+	Input in{};
+	in.form = F_DENSE;
+	in.location = PA_DEVICE;
+	in.batch = batch;
+	in.n_s = n_s;
+	in.n_t = n_t;
+	in.sim = sim;
+	in.length = length;
+	in.dense_off_host = offsets;
+	in.dense_si = stride_s;
+	in.dense_sj = stride_t;
+	UserPaths up_{};
+	up_.paths = paths;
+	up_.path_off = path_offsets;
+	up_.path_len = path_len;
+	up_.scores = scores;
+	pa_result *r = nullptr;
+	pa_status st = solve_impl(s, in, M_PATHS, nullptr, &r, nullptr, nullptr, &up_);
+	if (r) pa_result_destroy(r);
+	return st;
 }
 
 void pa_result_destroy(pa_result *r) { delete r; }

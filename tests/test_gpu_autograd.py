@@ -1,0 +1,168 @@
+"""Gradients of the optimal alignment score (the differentiation form; needs a GPU).
+
+1. dScore/dS from pa_path_gradients equals the indicator of the aligned cells of the
+   oracle's optimal path (every visited cell for DTW) -- exactly.
+2. Central finite differences in FP64 (eps = 1e-3, the oracle's FP64 twin) on tie-free
+   continuous inputs agree with dScore/dS and dScore/d(open, extend) to 1e-6.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_ag():
+    torch = pytest.importorskip("torch")
+    from pyalign_gb300 import build
+    build.build()
+    if not torch.cuda.is_available():
+        pytest.fail("no CUDA device visible")
+    from pyalign_gb300 import autograd
+    return torch, autograd
+
+
+@pytest.fixture(scope="module")
+def f64():
+    import oracle.algorithm as oalg
+    L = ctypes.CDLL(oalg.build())
+    vp, i32 = ctypes.c_void_p, ctypes.c_int32
+    L.pao_solve_f64.restype = i32
+    L.pao_solve_f64.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp, vp, vp]
+    return oalg, L
+
+
+def _oracle_f64(f64, S, ls, lt, locality, direction, dtw, gap):
+    """FP64 score and path of one pair (S: ls x lt float64)."""
+    oalg, L = f64
+    o = oalg._Options()
+    o.type = 1 if dtw else 0
+    o.direction = 1 if direction == "maximize" else 0
+    o.detail, o.count = 1, 0
+    o.locality = {"local": 0, "global": 1, "semiglobal": 2}[locality]
+    o.remove_dup = 1
+    o.cap_s, o.cap_t = ls, lt
+    gaps = np.zeros(6, np.float64)
+    if not dtw:
+        if gap[1] is None:
+            o.gap_kind = 0
+            gaps[0] = gaps[1] = gap[0]
+        else:
+            o.gap_kind = 1
+            op, ex = gap
+            gaps[2] = gaps[4] = ex            # Gotoh u = extend
+            gaps[3] = gaps[5] = op - ex       # Gotoh v = open - extend
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    sc = ctypes.c_double(0)
+    path = np.zeros((ls + lt + 4, 2), np.int32)
+    n = ctypes.c_int32(0)
+    ok = L.pao_solve_f64(ctypes.addressof(o), gaps.ctypes.data, None, None, ls, lt, S.ctypes.data,
+                         ctypes.addressof(sc), path.ctypes.data, ctypes.addressof(n))
+    assert ok
+    return sc.value, path[:n.value]
+
+
+def _indicator(path, ls, lt, dtw):
+    ind = np.zeros((ls, lt), np.float64)
+    for q in range(len(path) - 1):
+        u0, v0 = path[q]
+        u1, v1 = path[q + 1]
+        if u0 < 0 or v0 < 0:
+            break
+        if dtw or (u1 == u0 - 1 and v1 == v0 - 1):
+            ind[u0, v0] += 1
+    return ind
+
+
+CASES = [("global", "maximize", False, (0.5, 0.1)), ("local", "maximize", False, (1.0, 0.25)),
+         ("semiglobal", "maximize", False, (0.75, 0.2)), ("global", "minimize", False, (0.5, 0.1)),
+         ("global", "maximize", False, (0.4, None)), ("global", "minimize", True, None)]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[1]}-{'dtw' if c[2] else 'gap'}")
+def test_path_indicator_matches_oracle_path(torch_ag, f64, case):
+    torch, ag = torch_ag
+    locality, direction, dtw, gap = case
+    rng = np.random.default_rng(17)
+    B, n = 24, 48
+    lengths = np.stack([rng.integers(1, n + 1, B), rng.integers(1, n + 1, B)], axis=1)
+    if dtw:
+        x = np.cumsum(rng.normal(size=(B, n)), axis=1)
+        y = np.cumsum(rng.normal(size=(B, n)), axis=1)
+        S = np.abs(x[:, :, None] - y[:, None, :]).astype(np.float32)
+    else:
+        S = rng.normal(size=(B, n, n)).astype(np.float32)
+    St = torch.from_numpy(S).cuda().requires_grad_(True)
+    go = torch.tensor(gap[0] if gap else 0.0, requires_grad=not dtw)
+    ge = torch.tensor(gap[1], requires_grad=True) if gap and gap[1] is not None else None
+    scores = ag.alignment_score(St, lengths, go, ge, locality, direction, dtw)
+    scores.sum().backward()
+    dS = St.grad.cpu().numpy()
+    for k in range(B):
+        ls, lt = lengths[k]
+        sc, path = _oracle_f64(f64, S[k, :ls, :lt], ls, lt, locality, direction, dtw, gap)
+        ind = _indicator(path, ls, lt, dtw)
+        assert np.array_equal(dS[k, :ls, :lt], ind), k
+        assert not dS[k, ls:, :].any() and not dS[k, :, lt:].any()
+        assert abs(scores[k].item() - sc) <= 1e-4 * max(1.0, abs(sc))
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[1]}-{'dtw' if c[2] else 'gap'}")
+def test_central_finite_differences_fp64(torch_ag, f64, case):
+    torch, ag = torch_ag
+    locality, direction, dtw, gap = case
+    rng = np.random.default_rng(91)
+    B, n, eps = 8, 24, 1e-3
+    lengths = np.stack([rng.integers(8, n + 1, B), rng.integers(8, n + 1, B)], axis=1)
+    S = rng.normal(size=(B, n, n)).astype(np.float32)
+    if dtw:
+        S = np.abs(S)
+    St = torch.from_numpy(S).cuda().requires_grad_(True)
+    go = torch.tensor(gap[0] if gap else 0.0, requires_grad=not dtw)
+    ge = torch.tensor(gap[1], requires_grad=True) if gap and gap[1] is not None else None
+    ag.alignment_score(St, lengths, go, ge, locality, direction, dtw).sum().backward()
+    dS = St.grad.cpu().numpy()
+    d_open_fd = d_ext_fd = 0.0
+    for k in range(B):
+        ls, lt = lengths[k]
+        base = S[k, :ls, :lt].astype(np.float64)
+        cells = [(int(rng.integers(0, ls)), int(rng.integers(0, lt))) for _ in range(12)]
+        _, path = _oracle_f64(f64, base, ls, lt, locality, direction, dtw, gap)
+        cells += [tuple(p) for p in path if p[0] >= 0 and p[1] >= 0][:12]
+        for (i, j) in cells:
+            hi, lo = base.copy(), base.copy()
+            hi[i, j] += eps
+            lo[i, j] -= eps
+            fd = (_oracle_f64(f64, hi, ls, lt, locality, direction, dtw, gap)[0] -
+                  _oracle_f64(f64, lo, ls, lt, locality, direction, dtw, gap)[0]) / (2 * eps)
+            assert abs(fd - dS[k, i, j]) < 1e-6, (k, i, j, fd, dS[k, i, j])
+        if not dtw:
+            g2 = (gap[0] + eps, gap[1]) if gap[1] is not None else (gap[0] + eps, None)
+            g1 = (gap[0] - eps, gap[1]) if gap[1] is not None else (gap[0] - eps, None)
+            d_open_fd += (_oracle_f64(f64, base, ls, lt, locality, direction, dtw, g2)[0] -
+                          _oracle_f64(f64, base, ls, lt, locality, direction, dtw, g1)[0]) / (2 * eps)
+            if gap[1] is not None:
+                e2 = (gap[0], gap[1] + eps)
+                e1 = (gap[0], gap[1] - eps)
+                d_ext_fd += (_oracle_f64(f64, base, ls, lt, locality, direction, dtw, e2)[0] -
+                             _oracle_f64(f64, base, ls, lt, locality, direction, dtw, e1)[0]) / (2 * eps)
+    if not dtw:
+        assert abs(go.grad.item() - d_open_fd) < 1e-5, (go.grad.item(), d_open_fd)
+        if ge is not None:
+            assert abs(ge.grad.item() - d_ext_fd) < 1e-5, (ge.grad.item(), d_ext_fd)
+
+
+def test_embedding_gradients_flow(torch_ag):
+    """S = cos(E_s, E_t) in BF16 with FP32 accumulation; gradients reach the embeddings."""
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(5)
+    Es = torch.randn(16, 40, 64, device="cuda", generator=g, requires_grad=True)
+    Et = torch.randn(16, 36, 64, device="cuda", generator=g, requires_grad=True)
+    lengths = np.full((16, 2), (40, 36))
+    S = ag.cosine_similarity_batch(Es, Et)
+    ag.alignment_score(S, lengths, 0.5, 0.1).sum().backward()
+    assert torch.isfinite(Es.grad).all() and Es.grad.abs().sum() > 0
+    assert torch.isfinite(Et.grad).all() and Et.grad.abs().sum() > 0
