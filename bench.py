@@ -276,7 +276,7 @@ def fwd_bwd(torch, pairs, seed, steps=3):
     def run_dtw(backward):
         x = x0.clone().requires_grad_(backward)
         y = y0.clone().requires_grad_(backward)
-        D = (x[:, :, None] - y[:, None, :]).abs()
+        D = (y[:, :, None] - x[:, None, :]).abs().transpose(1, 2)  # |x_u - y_v|, stride 1 along u
         sc = ag.alignment_score(D, dl, locality="global", direction="minimize", dtw=True)
         if backward:
             sc.sum().backward()

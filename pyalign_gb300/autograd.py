@@ -79,8 +79,12 @@ class AlignmentScore(torch.autograd.Function):
     def forward(ctx, S, lengths, gap_open, gap_extend, locality, direction, dtw, linear):
         if not S.is_cuda or S.dtype != torch.float32 or S.dim() != 3:
             raise ValueError("S must be a (batch, len_s, len_t) float32 CUDA tensor")
-        S = S.contiguous()
+        # any layout with unit stride along s or t is read in place; a transposed view
+        # (stride 1 along s) is the fastest: each lane reads its 8 rows as one 32-byte sector
+        if S.stride(1) != 1 and S.stride(2) != 1:
+            S = S.contiguous()
         B, n_s, n_t = S.shape
+        ss, st_ = S.stride(1), S.stride(2)
         ln = np.ascontiguousarray(np.asarray(lengths).reshape(B, 2).T, dtype=np.int32)
         if (ln[0] > n_s).any() or (ln[1] > n_t).any() or (ln < 0).any():
             raise ValueError("lengths exceed the similarity tensor")
@@ -89,35 +93,40 @@ class AlignmentScore(torch.autograd.Function):
         L = _lib()
         stream = torch.cuda.current_stream()
         _alg.check(L.pa_solver_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
-        offsets = np.arange(B, dtype=np.int64) * (n_s * n_t)
+        offsets = S.storage_offset() + np.arange(B, dtype=np.int64) * S.stride(0)
         sizes = 2 * (ln[0].astype(np.int64) + ln[1] + 2)
         poff = np.zeros(B, np.int64)
         poff[1:] = np.cumsum(sizes)[:-1]
         paths = torch.empty(int(sizes.sum()), dtype=torch.int32, device=S.device)
         plen = torch.zeros(B, dtype=torch.int32, device=S.device)
         scores = torch.empty(B, dtype=torch.float32, device=S.device)
+        base = S.data_ptr() - S.storage_offset() * S.element_size()
         _alg.check(L.pa_solve_dense_paths(
-            solver.handle, S.data_ptr(), offsets.ctypes.data, n_t, 1, B, n_s, n_t, ln.ctypes.data,
+            solver.handle, base, offsets.ctypes.data, ss, st_, B, n_s, n_t, ln.ctypes.data,
             scores.data_ptr(), paths.data_ptr(), poff.ctypes.data, plen.data_ptr()))
-        ctx.save_for_backward(paths, plen, torch.from_numpy(poff).to(S.device),
-                              torch.from_numpy(offsets).to(S.device))
-        ctx.meta = (B, n_s, n_t, locality, direction, dtw, linear)
+        ctx.save_for_backward(paths, plen, torch.from_numpy(poff).to(S.device))
+        ctx.meta = (B, n_s, n_t, locality, direction, dtw, linear, ss == 1)
         return scores
 
     @staticmethod
     def backward(ctx, grad):
-        paths, plen, poff, offsets = ctx.saved_tensors
-        B, n_s, n_t, locality, direction, dtw, linear = ctx.meta
+        paths, plen, poff = ctx.saved_tensors
+        B, n_s, n_t, locality, direction, dtw, linear, transposed = ctx.meta
         A = _alg
         grad = grad.contiguous().float()
-        dS = torch.zeros((B, n_s, n_t), dtype=torch.float32, device=grad.device)
+        # dS in the layout S came in: a transposed view when S was one
+        if transposed:
+            dS = torch.zeros((B, n_t, n_s), dtype=torch.float32, device=grad.device).transpose(1, 2)
+        else:
+            dS = torch.zeros((B, n_s, n_t), dtype=torch.float32, device=grad.device)
         dgap = torch.zeros((B, 4), dtype=torch.float32, device=grad.device)
+        offsets = torch.arange(B, dtype=torch.int64, device=grad.device) * (n_s * n_t)
         L = _lib()
         st = L.pa_path_gradients(
             int(A.Type.DTW if dtw else A.Type.ALIGNMENT), int(A.Locality.__members__[locality.upper()]),
             int(A.Direction.__members__[direction.upper()]), B, paths.data_ptr(), poff.data_ptr(),
-            plen.data_ptr(), grad.data_ptr(), dS.data_ptr(), offsets.data_ptr(), n_t, 1, dgap.data_ptr(),
-            torch.cuda.current_stream().cuda_stream)
+            plen.data_ptr(), grad.data_ptr(), dS.data_ptr(), offsets.data_ptr(), dS.stride(1), dS.stride(2),
+            dgap.data_ptr(), torch.cuda.current_stream().cuda_stream)
         _alg.check(st)
         tot = dgap.sum(dim=0)
         if dtw:
@@ -146,7 +155,9 @@ def alignment_score(S, lengths, gap_open=None, gap_extend=None, locality="global
 
 def cosine_similarity_batch(Es, Et):
     """S = cos(E_s, E_t) per pair: L2-normalised embeddings multiplied in BF16 with FP32
-    accumulation.  Es: (batch, len_s, d), Et: (batch, len_t, d)."""
+    accumulation.  Es: (batch, len_s, d), Et: (batch, len_t, d).  Returned as a transposed
+    view of S^T (stride 1 along s), the layout the DP reads fastest."""
     Es = torch.nn.functional.normalize(Es, dim=-1)
     Et = torch.nn.functional.normalize(Et, dim=-1)
-    return torch.bmm(Es.to(torch.bfloat16), Et.to(torch.bfloat16).transpose(1, 2)).float()
+    St = torch.bmm(Et.to(torch.bfloat16), Es.to(torch.bfloat16).transpose(1, 2)).float()
+    return St.transpose(1, 2)

@@ -1,7 +1,8 @@
 """Gradients of the optimal alignment score (the differentiation form; needs a GPU).
 
 1. dScore/dS from pa_path_gradients equals the indicator of the aligned cells of the
-   oracle's optimal path (every visited cell for DTW) -- exactly.
+   float32 oracle's optimal path (every visited cell for DTW) -- exactly, and the scores
+   are bit-identical.
 2. Central finite differences in FP64 (eps = 1e-3, the oracle's FP64 twin) on tie-free
    continuous inputs agree with dScore/dS and dScore/d(open, extend) to 1e-6.
 """
@@ -65,6 +66,29 @@ def _oracle_f64(f64, S, ls, lt, locality, direction, dtw, gap):
     return sc.value, path[:n.value]
 
 
+def _oracle_f32(S, ls, lt, locality, direction, dtw, gap, cap):
+    """Float32 score and path of one pair from the oracle (the reference's arithmetic).
+
+    `cap` is the solver capacity: for non-integer gap costs the affine border vector
+    depends on it through its linspace (solver.h:2876-2880), so it must match the GPU
+    solver's (the padded shape of S)."""
+    import types
+    import oracle.algorithm as oalg
+    gc = None
+    if not dtw:
+        from _cases import Gap
+        gc = Gap("linear", gap[0]) if gap[1] is None else Gap("affine", gap[0], gap[1])
+    d = {"solver": oalg.Type.DTW if dtw else oalg.Type.ALIGNMENT,
+         "direction": oalg.Direction.__members__[direction.upper()], "batch": False, "return_dup": False,
+         "locality": oalg.Locality.__members__[locality.upper()],
+         "codomain": types.SimpleNamespace(detail=oalg.Detail.SOLUTION, count=oalg.Count.ONE),
+         "gap_cost": gc}
+    solver = oalg.m16.create_solver(cap[0], cap[1], oalg.m16.create_options(d))
+    sol = solver.solve_for_solution(np.ascontiguousarray(S, dtype=np.float32)[:, :, None],
+                                    np.array([[ls], [lt]], np.uint16))[0]
+    return sol.score, np.asarray(sol.path, dtype=np.int64)
+
+
 def _indicator(path, ls, lt, dtw):
     ind = np.zeros((ls, lt), np.float64)
     for q in range(len(path) - 1):
@@ -103,11 +127,13 @@ def test_path_indicator_matches_oracle_path(torch_ag, f64, case):
     dS = St.grad.cpu().numpy()
     for k in range(B):
         ls, lt = lengths[k]
-        sc, path = _oracle_f64(f64, S[k, :ls, :lt], ls, lt, locality, direction, dtw, gap)
+        sc, path = _oracle_f32(S[k, :ls, :lt], ls, lt, locality, direction, dtw, gap, (n, n))
         ind = _indicator(path, ls, lt, dtw)
         assert np.array_equal(dS[k, :ls, :lt], ind), k
         assert not dS[k, ls:, :].any() and not dS[k, :, lt:].any()
-        assert abs(scores[k].item() - sc) <= 1e-4 * max(1.0, abs(sc))
+        assert scores[k].item() == sc, (k, scores[k].item(), sc)
+        sc64, _ = _oracle_f64(f64, S[k, :ls, :lt], ls, lt, locality, direction, dtw, gap)
+        assert abs(sc - sc64) <= 1e-5 * max(1.0, abs(sc64)), (sc, sc64)
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[1]}-{'dtw' if c[2] else 'gap'}")
