@@ -243,13 +243,15 @@ def fwd_bwd(torch, pairs, seed, steps=3):
     Et = torch.randn(pairs, 256, 128, device="cuda", generator=g)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
 
+    a = Es.clone().requires_grad_(True)
+    b = Et.clone().requires_grad_(True)
+
     def run(backward):
-        a = Es.clone().requires_grad_(backward)
-        b = Et.clone().requires_grad_(backward)
-        S = ag.cosine_similarity_batch(a, b)
-        sc = ag.alignment_score(S, lengths, 0.5, 0.1, "global", "maximize")
+        with torch.set_grad_enabled(backward):
+            sc = ag.embedding_alignment_score(a, b, lengths, 0.5, 0.1, "global", "maximize")
         if backward:
             sc.sum().backward()
+            a.grad = b.grad = None
         return sc
 
     for _ in range(2):
@@ -273,13 +275,15 @@ def fwd_bwd(torch, pairs, seed, steps=3):
     x0 = torch.cumsum(torch.randn(nd, 1024, device="cuda", generator=g), dim=1)
     y0 = torch.cumsum(torch.randn(nd, 1024, device="cuda", generator=g), dim=1)
 
+    x = x0.clone().requires_grad_(True)
+    y = y0.clone().requires_grad_(True)
+
     def run_dtw(backward):
-        x = x0.clone().requires_grad_(backward)
-        y = y0.clone().requires_grad_(backward)
-        D = (y[:, :, None] - x[:, None, :]).abs().transpose(1, 2)  # |x_u - y_v|, stride 1 along u
-        sc = ag.alignment_score(D, dl, locality="global", direction="minimize", dtw=True)
+        with torch.set_grad_enabled(backward):
+            sc = ag.dtw_series_score(x, y, dl)
         if backward:
             sc.sum().backward()
+            x.grad = y.grad = None
         return sc
 
     run_dtw(True)

@@ -259,12 +259,28 @@ pa_status pa_solve_dense_paths(pa_solver *s, const float *sim, const int64_t *of
  * writes dgap[4k..4k+3] = d score / d (open_s, extend_s, open_t, extend_t) times
  * grad_scores[k], for w(len) = open + extend * (len - 1), border gaps of global paths
  * included.  paths/path_offsets/path_len as produced by pa_solve_dense_paths but ALL in
- * device memory, as are grad_scores, dS, ds_offsets and dgap (may be NULL).  Allocates
- * nothing; runs on `stream`. */
+ * device memory, as are grad_scores, dS, ds_offsets and dgap (dS and dgap may be NULL).
+ * Allocates nothing; runs on `stream`. */
 pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t direction, int64_t batch,
                             const int32_t *paths, const int64_t *path_offsets, const int32_t *path_len,
                             const float *grad_scores, float *dS, const int64_t *ds_offsets, int64_t stride_s,
                             int64_t stride_t, float *dgap, void *stream);
+
+/* Fused backward for S(i, j) = <Es[i], Et[j]> (per-token embeddings, contiguous
+ * (batch, n_s, dim) and (batch, n_t, dim) float32): adds grad_scores[k] * Et[j] to dEs[i]
+ * and grad_scores[k] * Es[i] to dEt[j] for every aligned cell (i, j) of pair k's path,
+ * without materialising dS.  Device memory; allocates nothing. */
+pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, const int32_t *paths,
+                                      const int64_t *path_offsets, const int32_t *path_len,
+                                      const float *grad_scores, const float *Es, const float *Et, int64_t n_s,
+                                      int64_t n_t, float *dEs, float *dEt, void *stream);
+
+/* Fused backward of DTW on two series with d(u, v) = |x_u - y_v| (x: (batch, n_s),
+ * y: (batch, n_t) float32): every visited cell adds grad * sign(x_u - y_v) to dx_u and
+ * subtracts it from dy_v.  Device memory; allocates nothing. */
+pa_status pa_path_series_gradients(int64_t batch, const int32_t *paths, const int64_t *path_offsets,
+                                   const int32_t *path_len, const float *grad_scores, const float *x,
+                                   const float *y, int64_t n_s, int64_t n_t, float *dx, float *dy, void *stream);
 
 /* Device time of the phases of the last solve on this solver, in milliseconds
  * (0: upload, 1: DP kernels, 2: traceback kernels, 3: download), and the number of

@@ -68,8 +68,61 @@ def _lib():
         L.pa_solve_dense_paths.argtypes = [vp, vp, vp, i64, i64, i64, i64, i64, vp, vp, vp, vp, vp]
         L.pa_path_gradients.restype = i32
         L.pa_path_gradients.argtypes = [i32, i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp]
+        L.pa_path_embedding_gradients.restype = i32
+        L.pa_path_embedding_gradients.argtypes = [i64, i32, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp]
+        L.pa_path_series_gradients.restype = i32
+        L.pa_path_series_gradients.argtypes = [i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp]
         L._pa_grad_bound = True
     return L
+
+
+def _forward_paths(S, lengths, gap, locality, direction, dtw):
+    """Scores and optimal paths of the pairs of S (device); returns (scores, paths, path
+    lengths, device path offsets, layout flag)."""
+    if not S.is_cuda or S.dtype != torch.float32 or S.dim() != 3:
+        raise ValueError("S must be a (batch, len_s, len_t) float32 CUDA tensor")
+    # any layout with unit stride along s or t is read in place; a transposed view
+    # (stride 1 along s) is the fastest: each lane reads its 8 rows as one 32-byte sector
+    if S.stride(1) != 1 and S.stride(2) != 1:
+        S = S.contiguous()
+    B, n_s, n_t = S.shape
+    ss, st_ = S.stride(1), S.stride(2)
+    ln = np.ascontiguousarray(np.asarray(lengths).reshape(B, 2).T, dtype=np.int32)
+    if (ln[0] > n_s).any() or (ln[1] > n_t).any() or (ln < 0).any():
+        raise ValueError("lengths exceed the similarity tensor")
+    solver = _solver(B, n_s, n_t, locality, direction, dtw, gap)
+    L = _lib()
+    stream = torch.cuda.current_stream()
+    _alg.check(L.pa_solver_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
+    offsets = S.storage_offset() + np.arange(B, dtype=np.int64) * S.stride(0)
+    sizes = 2 * (ln[0].astype(np.int64) + ln[1] + 2)
+    poff = np.zeros(B, np.int64)
+    poff[1:] = np.cumsum(sizes)[:-1]
+    paths = torch.empty(int(sizes.sum()), dtype=torch.int32, device=S.device)
+    plen = torch.zeros(B, dtype=torch.int32, device=S.device)
+    scores = torch.empty(B, dtype=torch.float32, device=S.device)
+    base = S.data_ptr() - S.storage_offset() * S.element_size()
+    _alg.check(L.pa_solve_dense_paths(
+        solver.handle, base, offsets.ctypes.data, ss, st_, B, n_s, n_t, ln.ctypes.data,
+        scores.data_ptr(), paths.data_ptr(), poff.ctypes.data, plen.data_ptr()))
+    return scores, paths, plen, torch.from_numpy(poff).to(S.device, non_blocking=False), ss == 1
+
+
+def _gap_grads(dtw, linear, locality, direction, B, paths, plen, poff, grad):
+    """d score / d (open, extend) summed over pairs (pa_path_gradients without dS)."""
+    if dtw:
+        return None, None
+    A = _alg
+    dgap = torch.zeros((B, 4), dtype=torch.float32, device=grad.device)
+    _alg.check(_lib().pa_path_gradients(
+        int(A.Type.ALIGNMENT), int(A.Locality.__members__[locality.upper()]),
+        int(A.Direction.__members__[direction.upper()]), B, paths.data_ptr(), poff.data_ptr(),
+        plen.data_ptr(), grad.data_ptr(), None, None, 0, 0, dgap.data_ptr(),
+        torch.cuda.current_stream().cuda_stream))
+    tot = dgap.sum(dim=0)
+    if linear:
+        return tot[0] + tot[1] + tot[2] + tot[3], None
+    return tot[0] + tot[2], tot[1] + tot[3]
 
 
 class AlignmentScore(torch.autograd.Function):
@@ -77,41 +130,16 @@ class AlignmentScore(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, S, lengths, gap_open, gap_extend, locality, direction, dtw, linear):
-        if not S.is_cuda or S.dtype != torch.float32 or S.dim() != 3:
-            raise ValueError("S must be a (batch, len_s, len_t) float32 CUDA tensor")
-        # any layout with unit stride along s or t is read in place; a transposed view
-        # (stride 1 along s) is the fastest: each lane reads its 8 rows as one 32-byte sector
-        if S.stride(1) != 1 and S.stride(2) != 1:
-            S = S.contiguous()
-        B, n_s, n_t = S.shape
-        ss, st_ = S.stride(1), S.stride(2)
-        ln = np.ascontiguousarray(np.asarray(lengths).reshape(B, 2).T, dtype=np.int32)
-        if (ln[0] > n_s).any() or (ln[1] > n_t).any() or (ln < 0).any():
-            raise ValueError("lengths exceed the similarity tensor")
         gap = None if dtw else ((float(gap_open), None) if linear else (float(gap_open), float(gap_extend)))
-        solver = _solver(B, n_s, n_t, locality, direction, dtw, gap)
-        L = _lib()
-        stream = torch.cuda.current_stream()
-        _alg.check(L.pa_solver_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
-        offsets = S.storage_offset() + np.arange(B, dtype=np.int64) * S.stride(0)
-        sizes = 2 * (ln[0].astype(np.int64) + ln[1] + 2)
-        poff = np.zeros(B, np.int64)
-        poff[1:] = np.cumsum(sizes)[:-1]
-        paths = torch.empty(int(sizes.sum()), dtype=torch.int32, device=S.device)
-        plen = torch.zeros(B, dtype=torch.int32, device=S.device)
-        scores = torch.empty(B, dtype=torch.float32, device=S.device)
-        base = S.data_ptr() - S.storage_offset() * S.element_size()
-        _alg.check(L.pa_solve_dense_paths(
-            solver.handle, base, offsets.ctypes.data, ss, st_, B, n_s, n_t, ln.ctypes.data,
-            scores.data_ptr(), paths.data_ptr(), poff.ctypes.data, plen.data_ptr()))
-        ctx.save_for_backward(paths, plen, torch.from_numpy(poff).to(S.device))
-        ctx.meta = (B, n_s, n_t, locality, direction, dtw, linear, ss == 1)
+        scores, paths, plen, poff, transposed = _forward_paths(S, lengths, gap, locality, direction, dtw)
+        ctx.save_for_backward(paths, plen, poff)
+        ctx.meta = (S.shape, locality, direction, dtw, linear, transposed)
         return scores
 
     @staticmethod
     def backward(ctx, grad):
         paths, plen, poff = ctx.saved_tensors
-        B, n_s, n_t, locality, direction, dtw, linear, transposed = ctx.meta
+        (B, n_s, n_t), locality, direction, dtw, linear, transposed = ctx.meta
         A = _alg
         grad = grad.contiguous().float()
         # dS in the layout S came in: a transposed view when S was one
@@ -121,13 +149,11 @@ class AlignmentScore(torch.autograd.Function):
             dS = torch.zeros((B, n_s, n_t), dtype=torch.float32, device=grad.device)
         dgap = torch.zeros((B, 4), dtype=torch.float32, device=grad.device)
         offsets = torch.arange(B, dtype=torch.int64, device=grad.device) * (n_s * n_t)
-        L = _lib()
-        st = L.pa_path_gradients(
+        _alg.check(_lib().pa_path_gradients(
             int(A.Type.DTW if dtw else A.Type.ALIGNMENT), int(A.Locality.__members__[locality.upper()]),
             int(A.Direction.__members__[direction.upper()]), B, paths.data_ptr(), poff.data_ptr(),
             plen.data_ptr(), grad.data_ptr(), dS.data_ptr(), offsets.data_ptr(), dS.stride(1), dS.stride(2),
-            dgap.data_ptr(), torch.cuda.current_stream().cuda_stream)
-        _alg.check(st)
+            dgap.data_ptr(), torch.cuda.current_stream().cuda_stream))
         tot = dgap.sum(dim=0)
         if dtw:
             d_open = d_ext = None
@@ -161,3 +187,83 @@ def cosine_similarity_batch(Es, Et):
     Et = torch.nn.functional.normalize(Et, dim=-1)
     St = torch.bmm(Et.to(torch.bfloat16), Es.to(torch.bfloat16).transpose(1, 2)).float()
     return St.transpose(1, 2)
+
+
+class EmbeddingAlignmentScore(torch.autograd.Function):
+    """Alignment score of S = <Es, Et^T> (per-token embeddings); the backward walks the
+    optimal paths and writes dEs, dEt directly (pa_path_embedding_gradients): O(path * d)
+    instead of a dense dS and two batched products."""
+
+    @staticmethod
+    def forward(ctx, Es, Et, lengths, gap_open, gap_extend, locality, direction, linear):
+        Es = Es.contiguous().float()
+        Et = Et.contiguous().float()
+        # S^T = Et Es^T in BF16 with FP32 accumulation; the transposed view is S
+        S = torch.bmm(Et.to(torch.bfloat16), Es.to(torch.bfloat16).transpose(1, 2)).float().transpose(1, 2)
+        gap = (float(gap_open), None) if linear else (float(gap_open), float(gap_extend))
+        scores, paths, plen, poff, _ = _forward_paths(S, lengths, gap, locality, direction, False)
+        ctx.save_for_backward(Es, Et, paths, plen, poff)
+        ctx.meta = (locality, direction, linear)
+        return scores
+
+    @staticmethod
+    def backward(ctx, grad):
+        Es, Et, paths, plen, poff = ctx.saved_tensors
+        locality, direction, linear = ctx.meta
+        grad = grad.contiguous().float()
+        B, n_s, dim = Es.shape
+        n_t = Et.shape[1]
+        # the product was taken in BF16: its gradient uses the same rounded factors
+        Esb = Es.to(torch.bfloat16).float()
+        Etb = Et.to(torch.bfloat16).float()
+        dEs = torch.zeros_like(Es)
+        dEt = torch.zeros_like(Et)
+        _alg.check(_lib().pa_path_embedding_gradients(
+            B, dim, paths.data_ptr(), poff.data_ptr(), plen.data_ptr(), grad.data_ptr(), Esb.data_ptr(),
+            Etb.data_ptr(), n_s, n_t, dEs.data_ptr(), dEt.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        d_open, d_ext = _gap_grads(False, linear, locality, direction, B, paths, plen, poff, grad)
+        return dEs, dEt, None, d_open, d_ext, None, None, None
+
+
+def embedding_alignment_score(Es, Et, lengths, gap_open, gap_extend=None, locality="global",
+                              direction="maximize", normalize=True):
+    """Differentiable alignment scores on the cosine (normalize=True) or dot similarity of
+    per-token embeddings Es (batch, len_s, d) and Et (batch, len_t, d), padded."""
+    if normalize:
+        Es = torch.nn.functional.normalize(Es, dim=-1)
+        Et = torch.nn.functional.normalize(Et, dim=-1)
+    linear = gap_extend is None
+    go = gap_open if isinstance(gap_open, torch.Tensor) else torch.tensor(float(gap_open))
+    ge = gap_extend if isinstance(gap_extend, torch.Tensor) else torch.tensor(float(gap_extend or 0.0))
+    return EmbeddingAlignmentScore.apply(Es, Et, lengths, go, ge, locality, direction, linear)
+
+
+class SeriesDTW(torch.autograd.Function):
+    """DTW score (minimize) of series pairs with d(u, v) = |x_u - y_v|; the backward walks
+    the optimal paths (pa_path_series_gradients)."""
+
+    @staticmethod
+    def forward(ctx, x, y, lengths):
+        x = x.contiguous().float()
+        y = y.contiguous().float()
+        D = (y[:, :, None] - x[:, None, :]).abs().transpose(1, 2)  # stride 1 along u
+        scores, paths, plen, poff, _ = _forward_paths(D, lengths, None, "global", "minimize", True)
+        ctx.save_for_backward(x, y, paths, plen, poff)
+        return scores
+
+    @staticmethod
+    def backward(ctx, grad):
+        x, y, paths, plen, poff = ctx.saved_tensors
+        grad = grad.contiguous().float()
+        dx = torch.zeros_like(x)
+        dy = torch.zeros_like(y)
+        _alg.check(_lib().pa_path_series_gradients(
+            x.shape[0], paths.data_ptr(), poff.data_ptr(), plen.data_ptr(), grad.data_ptr(), x.data_ptr(),
+            y.data_ptr(), x.shape[1], y.shape[1], dx.data_ptr(), dy.data_ptr(),
+            torch.cuda.current_stream().cuda_stream))
+        return dx, dy, None
+
+
+def dtw_series_score(x, y, lengths):
+    """Differentiable DTW (minimize, |x_u - y_v|) of series x (batch, len_s), y (batch, len_t)."""
+    return SeriesDTW.apply(x, y, lengths)

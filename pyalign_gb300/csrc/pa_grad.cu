@@ -33,15 +33,15 @@ __global__ void path_grad_kernel(GradParams p) {
 	const float g = p.grad[k];
 	const int n = p.path_len[k];
 	const int32_t *P = p.paths + p.path_off[k];
-	float *d = p.dS + p.ds_off[k];
+	float *d = p.dS ? p.dS + p.ds_off[k] : nullptr;
 	int open_s = 0, ext_s = 0, open_t = 0, ext_t = 0;
 	for (int q = 0; q + 1 < n; q++) {
 		const int u0 = P[2 * q], v0 = P[2 * q + 1], u1 = P[2 * q + 2], v1 = P[2 * q + 3];
 		if (u0 < 0 || v0 < 0) break;
 		if (p.dtw) {
-			d[int64_t(u0) * p.ss + int64_t(v0) * p.st] += g;
+			if (d) d[int64_t(u0) * p.ss + int64_t(v0) * p.st] += g;
 		} else if (u1 == u0 - 1 && v1 == v0 - 1) {
-			d[int64_t(u0) * p.ss + int64_t(v0) * p.st] += g;
+			if (d) d[int64_t(u0) * p.ss + int64_t(v0) * p.st] += g;
 		} else if (v1 == v0 && u1 < u0) {
 			open_s += 1;
 			ext_s += u0 - u1 - 1;
@@ -75,7 +75,7 @@ extern "C" pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t d
                                        const int32_t *paths, const int64_t *path_offsets, const int32_t *path_len,
                                        const float *grad_scores, float *dS, const int64_t *ds_offsets,
                                        int64_t stride_s, int64_t stride_t, float *dgap, void *stream) {
-	if (batch < 0 || !paths || !path_offsets || !path_len || !grad_scores || !dS || !ds_offsets)
+	if (batch < 0 || !paths || !path_offsets || !path_len || !grad_scores || (dS && !ds_offsets))
 		return PA_ERR_INVALID_ARGUMENT;
 	if (batch == 0) return PA_OK;
 	GradParams p{};
@@ -93,5 +93,109 @@ extern "C" pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t d
 	p.st = stride_t;
 	p.dgap = dgap;
 	path_grad_kernel<<<int((batch + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------------------
+// Fused backward for similarity-matrix problems built from per-token embeddings,
+// S(i, j) = <Es[i], Et[j]>: dScore/dEs[i] = sum over the aligned cells (i, j) of the
+// path of g * Et[j] (and symmetrically for Et), without materialising dS.  In one path the
+// aligned cells have distinct i and distinct j, so a warp per pair writes without atomics;
+// lanes run over the embedding dimension.
+
+namespace {
+
+struct EmbGradParams {
+	int64_t batch;
+	int32_t dim;
+	const int32_t *paths;
+	const int64_t *path_off;
+	const int32_t *path_len;
+	const float *grad;
+	const float *Es, *Et;  // (batch, n_s, dim), (batch, n_t, dim) contiguous
+	float *dEs, *dEt;
+	int64_t n_s, n_t;
+};
+
+__global__ void path_embedding_grad_kernel(EmbGradParams p) {
+	const int64_t k = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (k >= p.batch) return;
+	const float g = p.grad[k];
+	const int n = p.path_len[k];
+	const int32_t *P = p.paths + p.path_off[k];
+	const float *es = p.Es + k * p.n_s * p.dim;
+	const float *et = p.Et + k * p.n_t * p.dim;
+	float *des = p.dEs + k * p.n_s * p.dim;
+	float *det = p.dEt + k * p.n_t * p.dim;
+	for (int q = 0; q + 1 < n; q++) {
+		const int u0 = P[2 * q], v0 = P[2 * q + 1];
+		if (u0 < 0 || v0 < 0) break;
+		const int u1 = P[2 * q + 2], v1 = P[2 * q + 3];
+		if (!(u1 == u0 - 1 && v1 == v0 - 1)) continue;
+		for (int c = lane; c < p.dim; c += 32) {
+			des[int64_t(u0) * p.dim + c] += g * et[int64_t(v0) * p.dim + c];
+			det[int64_t(v0) * p.dim + c] += g * es[int64_t(u0) * p.dim + c];
+		}
+	}
+}
+
+// DTW on two series with d(u, v) = |x_u - y_v|: every visited cell adds
+// g * sign(x_u - y_v) to dx_u and subtracts it from dy_v (one thread per pair).
+struct SeriesGradParams {
+	int64_t batch;
+	const int32_t *paths;
+	const int64_t *path_off;
+	const int32_t *path_len;
+	const float *grad;
+	const float *x, *y;
+	float *dx, *dy;
+	int64_t n_s, n_t;
+};
+
+__global__ void path_series_grad_kernel(SeriesGradParams p) {
+	const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (k >= p.batch) return;
+	const float g = p.grad[k];
+	const int n = p.path_len[k];
+	const int32_t *P = p.paths + p.path_off[k];
+	const float *x = p.x + k * p.n_s;
+	const float *y = p.y + k * p.n_t;
+	float *dx = p.dx + k * p.n_s;
+	float *dy = p.dy + k * p.n_t;
+	for (int q = 0; q < n; q++) {
+		const int u = P[2 * q], v = P[2 * q + 1];
+		if (u < 0 || v < 0) break;
+		const float diff = x[u] - y[v];
+		const float sg = diff > 0.0f ? g : (diff < 0.0f ? -g : 0.0f);
+		dx[u] += sg;
+		dy[v] -= sg;
+	}
+}
+
+}  // namespace
+
+extern "C" pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, const int32_t *paths,
+                                                 const int64_t *path_offsets, const int32_t *path_len,
+                                                 const float *grad_scores, const float *Es, const float *Et,
+                                                 int64_t n_s, int64_t n_t, float *dEs, float *dEt, void *stream) {
+	if (batch < 0 || dim <= 0 || !paths || !path_offsets || !path_len || !grad_scores || !Es || !Et || !dEs || !dEt)
+		return PA_ERR_INVALID_ARGUMENT;
+	if (batch == 0) return PA_OK;
+	EmbGradParams p{batch, dim, paths, path_offsets, path_len, grad_scores, Es, Et, dEs, dEt, n_s, n_t};
+	const int64_t threads = batch * 32;
+	path_embedding_grad_kernel<<<int((threads + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}
+
+extern "C" pa_status pa_path_series_gradients(int64_t batch, const int32_t *paths, const int64_t *path_offsets,
+                                              const int32_t *path_len, const float *grad_scores, const float *x,
+                                              const float *y, int64_t n_s, int64_t n_t, float *dx, float *dy,
+                                              void *stream) {
+	if (batch < 0 || !paths || !path_offsets || !path_len || !grad_scores || !x || !y || !dx || !dy)
+		return PA_ERR_INVALID_ARGUMENT;
+	if (batch == 0) return PA_OK;
+	SeriesGradParams p{batch, paths, path_offsets, path_len, grad_scores, x, y, dx, dy, n_s, n_t};
+	path_series_grad_kernel<<<int((batch + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
 }

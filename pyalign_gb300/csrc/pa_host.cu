@@ -308,6 +308,16 @@ struct pa_solver {
 	    d_path_len, d_vals, d_val_off, d_best, d_gen, d_wsb_off, d_wsb_tb, d_wsb_vals, d_wsb_sub,
 	    d_wsb_sub_off, d_codes_max;
 	PinBuf h_stage, h_out;
+	// per-call pair metadata, staged in one pinned buffer and sent with one copy
+	DevBuf d_meta;
+	PinBuf h_meta;
+	cudaEvent_t meta_ev = nullptr;    // the staging buffer is free again once this completes
+	bool meta_pending = false;
+	struct {
+		int32_t *ls, *lt, *order;
+		int64_t *mask_off, *map_off, *path_off, *val_off, *dense_off;
+	} m{};
+	std::vector<std::pair<uint64_t, int>> occ_cache;  // (kernel variant, smem) -> blocks per SM
 	DevBuf d_border_mode[3];          // borders per arithmetic mode: float, int tagged, int plain
 	bool border_ready[3] = {false, false, false};
 	std::vector<unsigned char> h_tab;  // staging of the converted similarity table
@@ -315,6 +325,7 @@ struct pa_solver {
 	~pa_solver() {
 		for (auto &e : ev)
 			if (e) cudaEventDestroy(e);
+		if (meta_ev) cudaEventDestroy(meta_ev);
 		if (own_stream) cudaStreamDestroy(own_stream);
 	}
 };
@@ -340,6 +351,7 @@ pa_status ensure_device(pa_solver *s) {
 	PA_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
 	if (!s->stream) s->stream = s->own_stream;
 	for (auto &e : s->ev) PA_CUDA(cudaEventCreate(&e));
+	PA_CUDA(cudaEventCreateWithFlags(&s->meta_ev, cudaEventDisableTiming));
 	return PA_OK;
 }
 
@@ -407,9 +419,9 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	cudaStream_t st = s->stream;
 	DpParams<V> p{};
 	p.npairs = int32_t(npairs);
-	p.order = s->d_order.as<int32_t>();
-	p.len_s = s->d_ls.as<int32_t>();
-	p.len_t = s->d_lt.as<int32_t>();
+	p.order = s->m.order;
+	p.len_s = s->m.ls;
+	p.len_t = s->m.lt;
 	p.sub_kind = in.form == F_DENSE ? SUB_DENSE : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
 	p.neg_inf = ISINT ? V(-(1 << 29)) : V(-INFINITY);
 	p.G = plan.G;
@@ -439,7 +451,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 		p.ne = cvt<V>(in.ne * s->sign, ISINT, scale, diag_tag);
 	} else {
 		p.dense = in.location == PA_DEVICE ? in.sim : s->d_dense.as<float>();
-		p.dense_off = s->d_dense_off.as<int64_t>();
+		p.dense_off = s->m.dense_off;
 		p.dense_si = in.dense_si ? in.dense_si : in.n_t * in.batch;
 		p.dense_sj = in.dense_si ? in.dense_sj : in.batch;
 		p.dense_sign = s->sign;
@@ -502,10 +514,10 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.seed = s->d_seed.as<int32_t>();
 	p.has_seed = s->d_has.as<int32_t>();
 	p.masks = s->d_masks.p;
-	p.mask_off = s->d_mask_off.as<int64_t>();
+	p.mask_off = s->m.mask_off;
 	p.best_in = best_in_dev;
 	p.values = want_values ? s->d_vals.as<float>() : nullptr;
-	p.val_off = s->d_val_off.as<int64_t>();
+	p.val_off = s->m.val_off;
 	p.work_counter = s->d_counter.as<int32_t>();
 	p.status = s->d_status.as<int32_t>();
 
@@ -514,9 +526,14 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	                        ? size_t(in.table_rows * in.table_cols) * sizeof(V)
 	                        : 0;
 	int bps = 0;
-	cudaError_t e;
+	cudaError_t e = cudaSuccess;
 	const int loc = s->loc;
-	if (ISINT) {
+	const uint64_t okey = (uint64_t(ISINT) << 60) | (uint64_t(gk) << 56) | (uint64_t(loc) << 52) |
+	                      (uint64_t(tb) << 48) | (uint64_t(want_values) << 44) | uint64_t(smem);
+	for (const auto &kv : s->occ_cache)
+		if (kv.first == okey) bps = kv.second;
+	if (bps > 0) {
+	} else if (ISINT) {
 		e = gk == GAP_LINEAR ? occupancy_dp_i_linear(loc, tb, want_values, smem, &bps)
 		    : gk == GAP_AFFINE ? occupancy_dp_i_affine(loc, tb, want_values, smem, &bps)
 		                       : occupancy_dp_i_dtw(loc, tb, want_values, smem, &bps);
@@ -527,6 +544,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	}
 	PA_CUDA(e);
 	bps = std::max(bps, 1);
+	if (s->occ_cache.size() < 64) s->occ_cache.push_back({okey, bps});
 	const int gpw = 32 / plan.G;
 	const int64_t groups_needed = (npairs + gpw - 1) / gpw;  // warps needed
 	int64_t grid = int64_t(s->sm_count) * bps;
@@ -644,8 +662,8 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	std::vector<float> tab;
 	WsbParams w{};
 	w.npairs = int32_t(B);
-	w.len_s = s->d_ls.as<int32_t>();
-	w.len_t = s->d_lt.as<int32_t>();
+	w.len_s = s->m.ls;
+	w.len_t = s->m.lt;
 	w.local = s->loc;
 	w.sub_kind = in.form == F_DENSE ? SUB_DENSE : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
 	if (in.form != F_DENSE) {
@@ -838,15 +856,44 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		if (e != cudaSuccess || n == 0) return e;
 		return pa_copy(s, d.p, h, n, cudaMemcpyHostToDevice, st);
 	};
-	// the host vectors above must live until the copies complete: synchronise below
-	PA_CUDA(up(s->d_ls, ls.data(), ls.size() * 4));
-	PA_CUDA(up(s->d_lt, lt.data(), lt.size() * 4));
-	PA_CUDA(up(s->d_order, order.data(), order.size() * 4));
-	PA_CUDA(up(s->d_mask_off, mask_off.data(), mask_off.size() * 8));
-	PA_CUDA(up(s->d_map_off, map_off.data(), map_off.size() * 8));
-	PA_CUDA(up(s->d_path_off, path_off.data(), path_off.size() * 8));
-	PA_CUDA(up(s->d_val_off, val_off.data(), val_off.size() * 8));
-	PA_CUDA(up(s->d_dense_off, dense_off.data(), dense_off.size() * 8));
+	// pair metadata: packed into one pinned staging buffer, one host-to-device copy
+	{
+		const size_t n32 = size_t(B), n64 = size_t(B) + 1;
+		const size_t bytes = ((3 * n32 * 4 + 7) & ~size_t(7)) + 5 * n64 * 8;
+		if (s->meta_pending) {
+			PA_CUDA(cudaEventSynchronize(s->meta_ev));  // the previous call's copy has read it
+			s->meta_pending = false;
+		}
+		PA_CUDA(s->h_meta.ensure(bytes));
+		PA_CUDA(s->d_meta.ensure(bytes));
+		unsigned char *h = s->h_meta.as<unsigned char>();
+		unsigned char *d = s->d_meta.as<unsigned char>();
+		size_t o = 0;
+		auto put = [&](const void *src, size_t nbytes, size_t align) {
+			o = (o + align - 1) & ~(align - 1);
+			if (nbytes) std::memcpy(h + o, src, nbytes);
+			unsigned char *dp = d + o;
+			o += nbytes;
+			return dp;
+		};
+		s->m.ls = reinterpret_cast<int32_t *>(put(ls.data(), n32 * 4, 4));
+		s->m.lt = reinterpret_cast<int32_t *>(put(lt.data(), n32 * 4, 4));
+		s->m.order = reinterpret_cast<int32_t *>(put(order.data(), n32 * 4, 4));
+		s->m.mask_off = reinterpret_cast<int64_t *>(put(mask_off.data(), n64 * 8, 8));
+		// the caller's output offsets replace the internal ones when results go to its buffers
+		const int64_t *mo = (maps_out && map_offsets) ? map_offsets : map_off.data();
+		s->m.map_off = reinterpret_cast<int64_t *>(put(mo, (maps_out && map_offsets ? n32 : n64) * 8, 8));
+		o += (maps_out && map_offsets) ? 8 : 0;
+		const int64_t *po = (method == M_PATHS && user_paths) ? user_paths->path_off : path_off.data();
+		s->m.path_off = reinterpret_cast<int64_t *>(put(po, (method == M_PATHS && user_paths ? n32 : n64) * 8, 8));
+		o += (method == M_PATHS && user_paths) ? 8 : 0;
+		s->m.val_off = reinterpret_cast<int64_t *>(put(val_off.data(), n64 * 8, 8));
+		s->m.dense_off = reinterpret_cast<int64_t *>(put(dense_off.data(), n32 * 8, 8));
+		o += 8;
+		PA_CUDA(pa_copy(s, d, h, o, cudaMemcpyHostToDevice, st));
+		PA_CUDA(cudaEventRecord(s->meta_ev, st));
+		s->meta_pending = true;
+	}
 	PA_CUDA(s->d_score.ensure(size_t(B) * 4));
 	PA_CUDA(s->d_seed.ensure(size_t(B) * 8));
 	PA_CUDA(s->d_has.ensure(size_t(B) * 4));
@@ -902,34 +949,42 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		}
 		WalkParams w{};
 		w.npairs = int32_t(B);
-		w.len_s = s->d_ls.as<int32_t>();
-		w.len_t = s->d_lt.as<int32_t>();
+		w.len_s = s->m.ls;
+		w.len_t = s->m.lt;
 		w.seed = s->d_seed.as<int32_t>();
 		w.has_seed = s->d_has.as<int32_t>();
 		w.masks = s->d_masks.as<uint32_t>();
-		w.mask_off = s->d_mask_off.as<int64_t>();
+		w.mask_off = s->m.mask_off;
 		w.G = plan.G;
 		w.gap = s->gap;
 		w.local = s->loc == LOC_LOCAL;
 		w.maps = to_user ? maps_out : s->d_maps.as<int32_t>();
-		w.map_off = s->d_map_off.as<int64_t>();
-		if (to_user && map_offsets) {
-			PA_CUDA(up(s->d_map_off, map_offsets, size_t(B) * 8));
-		}
+		w.map_off = s->m.map_off;
+
 		w.paths = want_paths ? s->d_paths.as<int32_t>() : nullptr;
-		w.path_off = s->d_path_off.as<int64_t>();
+		w.path_off = s->m.path_off;
 		w.path_len = want_paths ? s->d_path_len.as<int32_t>() : nullptr;
 		if (paths_to_user) {
 			w.maps = nullptr;
 			w.paths = user_paths->paths;
 			w.path_len = user_paths->path_len;
-			PA_CUDA(up(s->d_path_off, user_paths->path_off, size_t(B) * 8));
+
 		}
 		walk_kernel<<<int((B + 127) / 128), 128, 0, st>>>(w);
 		PA_CUDA(cudaGetLastError());
 		launches++;
 	}
 	PA_CUDA(cudaEventRecord(s->ev[3], st));
+
+	if (paths_to_user) {
+		// device-resident form: results stay on the device, nothing to wait for here
+		if (user_paths->scores)
+			PA_CUDA(cudaMemcpyAsync(user_paths->scores, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
+		s->last_launches = launches;
+		for (auto &ms : s->last_ms) ms = 0.0f;
+		if (out) *out = nullptr;
+		return PA_OK;
+	}
 
 	// ---- download
 	res.scores.resize(size_t(B));
@@ -951,10 +1006,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			res.maps.resize(size_t(map_off[size_t(B)]));
 			PA_CUDA(pa_copy(s, res.maps.data(), s->d_maps.p, res.maps.size() * 4, cudaMemcpyDeviceToHost, st));
 		}
-		if (paths_to_user) {
-			if (user_paths->scores)
-				PA_CUDA(cudaMemcpyAsync(user_paths->scores, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
-		} else if (want_paths) {
+		if (want_paths) {
 			res.path_off = path_off;
 			res.paths.resize(size_t(path_off[size_t(B)]));
 			res.path_len.resize(size_t(B));

@@ -192,3 +192,54 @@ def test_embedding_gradients_flow(torch_ag):
     ag.alignment_score(S, lengths, 0.5, 0.1).sum().backward()
     assert torch.isfinite(Es.grad).all() and Es.grad.abs().sum() > 0
     assert torch.isfinite(Et.grad).all() and Et.grad.abs().sum() > 0
+
+
+def test_fused_embedding_gradients_match_dense_route(torch_ag):
+    """embedding_alignment_score's path-walk backward equals dS @ Et with dS the path
+    indicator of the dense route (one aligned j per i, so the sums are single terms)."""
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(9)
+    B, ns, nt, d = 32, 50, 44, 64
+    Es = torch.randn(B, ns, d, device="cuda", generator=g)
+    Et = torch.randn(B, nt, d, device="cuda", generator=g)
+    rng = np.random.default_rng(4)
+    lengths = np.stack([rng.integers(1, ns + 1, B), rng.integers(1, nt + 1, B)], axis=1)
+    for locality in ("global", "local", "semiglobal"):
+        a = Es.clone().requires_grad_(True)
+        b = Et.clone().requires_grad_(True)
+        go = torch.tensor(0.5, requires_grad=True)
+        ge = torch.tensor(0.1, requires_grad=True)
+        sc = ag.embedding_alignment_score(a, b, lengths, go, ge, locality, normalize=False)
+        sc.sum().backward()
+        Eb, Fb = Es.to(torch.bfloat16).float(), Et.to(torch.bfloat16).float()
+        S = torch.bmm(Fb, Eb.transpose(1, 2)).transpose(1, 2).contiguous().requires_grad_(True)
+        go2 = torch.tensor(0.5, requires_grad=True)
+        ge2 = torch.tensor(0.1, requires_grad=True)
+        sc2 = ag.alignment_score(S, lengths, go2, ge2, locality)
+        sc2.sum().backward()
+        assert torch.equal(sc, sc2)
+        dS = S.grad.double()
+        assert torch.allclose(a.grad.double(), torch.bmm(dS, Fb.double()), atol=1e-6)
+        assert torch.allclose(b.grad.double(), torch.bmm(dS.transpose(1, 2), Eb.double()), atol=1e-6)
+        assert abs(go.grad.item() - go2.grad.item()) < 1e-4 and abs(ge.grad.item() - ge2.grad.item()) < 1e-4
+
+
+def test_fused_series_dtw_gradients_match_dense_route(torch_ag):
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(3)
+    B, ns, nt = 16, 70, 90
+    x0 = torch.cumsum(torch.randn(B, ns, device="cuda", generator=g), 1)
+    y0 = torch.cumsum(torch.randn(B, nt, device="cuda", generator=g), 1)
+    rng = np.random.default_rng(8)
+    lengths = np.stack([rng.integers(1, ns + 1, B), rng.integers(1, nt + 1, B)], axis=1)
+    x = x0.clone().requires_grad_(True)
+    y = y0.clone().requires_grad_(True)
+    sc = ag.dtw_series_score(x, y, lengths)
+    sc.sum().backward()
+    x2 = x0.clone().requires_grad_(True)
+    y2 = y0.clone().requires_grad_(True)
+    D = (x2[:, :, None] - y2[:, None, :]).abs()
+    sc2 = ag.alignment_score(D, lengths, locality="global", direction="minimize", dtw=True)
+    sc2.sum().backward()
+    assert torch.equal(sc, sc2)
+    assert torch.allclose(x.grad, x2.grad, atol=1e-5) and torch.allclose(y.grad, y2.grad, atol=1e-5)
