@@ -212,7 +212,9 @@ def test_fused_embedding_gradients_match_dense_route(torch_ag):
         sc = ag.embedding_alignment_score(a, b, lengths, go, ge, locality, normalize=False)
         sc.sum().backward()
         Eb, Fb = Es.to(torch.bfloat16).float(), Et.to(torch.bfloat16).float()
-        S = torch.bmm(Fb, Eb.transpose(1, 2)).transpose(1, 2).contiguous().requires_grad_(True)
+        # the same BF16 product (FP32 accumulation) as the fused forward
+        S = torch.bmm(Et.to(torch.bfloat16), Es.to(torch.bfloat16).transpose(1, 2)).float()
+        S = S.transpose(1, 2).contiguous().requires_grad_(True)
         go2 = torch.tensor(0.5, requires_grad=True)
         ge2 = torch.tensor(0.1, requires_grad=True)
         sc2 = ag.alignment_score(S, lengths, go2, ge2, locality)
