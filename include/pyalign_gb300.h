@@ -266,14 +266,22 @@ pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t direction, i
                             const float *grad_scores, float *dS, const int64_t *ds_offsets, int64_t stride_s,
                             int64_t stride_t, float *dgap, void *stream);
 
-/* Fused backward for S(i, j) = <Es[i], Et[j]> (per-token embeddings, contiguous
- * (batch, n_s, dim) and (batch, n_t, dim) float32): adds grad_scores[k] * Et[j] to dEs[i]
- * and grad_scores[k] * Es[i] to dEt[j] for every aligned cell (i, j) of pair k's path,
- * without materialising dS.  Device memory; allocates nothing. */
-pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, const int32_t *paths,
+/* Embedding similarity S(i, j) = <en_s[i], en_t[j]> with en = E / |E| (normalize != 0,
+ * cosine) or en = E (dot).  pa_normalize_rows_bf16 writes the BF16 factor en (rows x dim)
+ * and 1/|E| per row (1 when not normalising) in one pass over E (rows x dim float32).
+ * pa_path_embedding_gradients is the fused backward: for every aligned cell (i, j) of pair
+ * k's path it writes dEs[i] and dEt[j] (the gradients w.r.t. the raw E, through the
+ * normalisation), without materialising dS; other rows are left untouched (pass zeros).
+ * Es/Et (batch, n, dim) float32, Es_bf16/Et_bf16 their BF16 factors, inv_s/inv_t the
+ * inverse norms.  Device memory; allocates nothing. */
+pa_status pa_normalize_rows_bf16(const float *E, int64_t rows, int32_t dim, int32_t normalize, void *out_bf16,
+                                 float *inv_norm, void *stream);
+pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
                                       const int64_t *path_offsets, const int32_t *path_len,
-                                      const float *grad_scores, const float *Es, const float *Et, int64_t n_s,
-                                      int64_t n_t, float *dEs, float *dEt, void *stream);
+                                      const float *grad_scores, const float *Es, const float *Et,
+                                      const void *Es_bf16, const void *Et_bf16, const float *inv_s,
+                                      const float *inv_t, int64_t n_s, int64_t n_t, float *dEs, float *dEt,
+                                      void *stream);
 
 /* Fused backward of DTW on two series with d(u, v) = |x_u - y_v| (x: (batch, n_s),
  * y: (batch, n_t) float32): every visited cell adds grad * sign(x_u - y_v) to dx_u and

@@ -69,7 +69,10 @@ def _lib():
         L.pa_path_gradients.restype = i32
         L.pa_path_gradients.argtypes = [i32, i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp]
         L.pa_path_embedding_gradients.restype = i32
-        L.pa_path_embedding_gradients.argtypes = [i64, i32, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp]
+        L.pa_path_embedding_gradients.argtypes = [i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, i64,
+                                                  vp, vp, vp]
+        L.pa_normalize_rows_bf16.restype = i32
+        L.pa_normalize_rows_bf16.argtypes = [vp, i64, i32, i32, vp, vp, vp]
         L.pa_path_series_gradients.restype = i32
         L.pa_path_series_gradients.argtypes = [i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp]
         L._pa_grad_bound = True
@@ -190,52 +193,61 @@ def cosine_similarity_batch(Es, Et):
 
 
 class EmbeddingAlignmentScore(torch.autograd.Function):
-    """Alignment score of S = <Es, Et^T> (per-token embeddings); the backward walks the
-    optimal paths and writes dEs, dEt directly (pa_path_embedding_gradients): O(path * d)
-    instead of a dense dS and two batched products."""
+    """Alignment score of S = <en_s, en_t^T> for per-token embeddings (en = E/|E| for the
+    cosine, E for the dot product), the product in BF16 with FP32 accumulation.  The
+    backward walks the optimal paths and writes the gradients of the aligned rows of E
+    directly, through the normalisation (pa_path_embedding_gradients): O(path * d) work
+    instead of a dense dS, two batched products and a dense normalisation backward."""
 
     @staticmethod
-    def forward(ctx, Es, Et, lengths, gap_open, gap_extend, locality, direction, linear):
+    def forward(ctx, Es, Et, lengths, gap_open, gap_extend, locality, direction, linear, normalize):
         Es = Es.contiguous().float()
         Et = Et.contiguous().float()
-        # S^T = Et Es^T in BF16 with FP32 accumulation; the transposed view is S
-        S = torch.bmm(Et.to(torch.bfloat16), Es.to(torch.bfloat16).transpose(1, 2)).float().transpose(1, 2)
+        B, n_s, dim = Es.shape
+        n_t = Et.shape[1]
+        L = _lib()
+        stream = torch.cuda.current_stream().cuda_stream
+        Esb = torch.empty(Es.shape, dtype=torch.bfloat16, device=Es.device)
+        Etb = torch.empty(Et.shape, dtype=torch.bfloat16, device=Et.device)
+        inv_s = torch.empty(B * n_s, dtype=torch.float32, device=Es.device)
+        inv_t = torch.empty(B * n_t, dtype=torch.float32, device=Et.device)
+        _alg.check(L.pa_normalize_rows_bf16(Es.data_ptr(), B * n_s, dim, int(normalize), Esb.data_ptr(),
+                                            inv_s.data_ptr(), stream))
+        _alg.check(L.pa_normalize_rows_bf16(Et.data_ptr(), B * n_t, dim, int(normalize), Etb.data_ptr(),
+                                            inv_t.data_ptr(), stream))
+        # S^T = en_t en_s^T; its transposed view is S with stride 1 along s
+        S = torch.bmm(Etb, Esb.transpose(1, 2)).float().transpose(1, 2)
         gap = (float(gap_open), None) if linear else (float(gap_open), float(gap_extend))
         scores, paths, plen, poff, _ = _forward_paths(S, lengths, gap, locality, direction, False)
-        ctx.save_for_backward(Es, Et, paths, plen, poff)
-        ctx.meta = (locality, direction, linear)
+        ctx.save_for_backward(Es, Et, Esb, Etb, inv_s, inv_t, paths, plen, poff)
+        ctx.meta = (locality, direction, linear, normalize)
         return scores
 
     @staticmethod
     def backward(ctx, grad):
-        Es, Et, paths, plen, poff = ctx.saved_tensors
-        locality, direction, linear = ctx.meta
+        Es, Et, Esb, Etb, inv_s, inv_t, paths, plen, poff = ctx.saved_tensors
+        locality, direction, linear, normalize = ctx.meta
         grad = grad.contiguous().float()
         B, n_s, dim = Es.shape
         n_t = Et.shape[1]
-        # the product was taken in BF16: its gradient uses the same rounded factors
-        Esb = Es.to(torch.bfloat16).float()
-        Etb = Et.to(torch.bfloat16).float()
         dEs = torch.zeros_like(Es)
         dEt = torch.zeros_like(Et)
         _alg.check(_lib().pa_path_embedding_gradients(
-            B, dim, paths.data_ptr(), poff.data_ptr(), plen.data_ptr(), grad.data_ptr(), Esb.data_ptr(),
-            Etb.data_ptr(), n_s, n_t, dEs.data_ptr(), dEt.data_ptr(), torch.cuda.current_stream().cuda_stream))
+            B, dim, int(normalize), paths.data_ptr(), poff.data_ptr(), plen.data_ptr(), grad.data_ptr(),
+            Es.data_ptr(), Et.data_ptr(), Esb.data_ptr(), Etb.data_ptr(), inv_s.data_ptr(), inv_t.data_ptr(),
+            n_s, n_t, dEs.data_ptr(), dEt.data_ptr(), torch.cuda.current_stream().cuda_stream))
         d_open, d_ext = _gap_grads(False, linear, locality, direction, B, paths, plen, poff, grad)
-        return dEs, dEt, None, d_open, d_ext, None, None, None
+        return dEs, dEt, None, d_open, d_ext, None, None, None, None
 
 
 def embedding_alignment_score(Es, Et, lengths, gap_open, gap_extend=None, locality="global",
                               direction="maximize", normalize=True):
     """Differentiable alignment scores on the cosine (normalize=True) or dot similarity of
     per-token embeddings Es (batch, len_s, d) and Et (batch, len_t, d), padded."""
-    if normalize:
-        Es = torch.nn.functional.normalize(Es, dim=-1)
-        Et = torch.nn.functional.normalize(Et, dim=-1)
     linear = gap_extend is None
     go = gap_open if isinstance(gap_open, torch.Tensor) else torch.tensor(float(gap_open))
     ge = gap_extend if isinstance(gap_extend, torch.Tensor) else torch.tensor(float(gap_extend or 0.0))
-    return EmbeddingAlignmentScore.apply(Es, Et, lengths, go, ge, locality, direction, linear)
+    return EmbeddingAlignmentScore.apply(Es, Et, lengths, go, ge, locality, direction, linear, normalize)
 
 
 class SeriesDTW(torch.autograd.Function):

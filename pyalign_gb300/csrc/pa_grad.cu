@@ -7,6 +7,7 @@
 // (pyalign/gaps.py:164-193 with solver.h:2858-2881).  For DTW the score is the sum of the
 // distances of every visited cell (solver.h:3233-3250).  Global alignments also pay the
 // border gap their path ends in (solver.h:2918-2951).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "../../include/pyalign_gb300.h"
@@ -97,25 +98,50 @@ extern "C" pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t d
 }
 
 // ---------------------------------------------------------------------------------------
-// Fused backward for similarity-matrix problems built from per-token embeddings,
-// S(i, j) = <Es[i], Et[j]>: dScore/dEs[i] = sum over the aligned cells (i, j) of the
-// path of g * Et[j] (and symmetrically for Et), without materialising dS.  In one path the
-// aligned cells have distinct i and distinct j, so a warp per pair writes without atomics;
-// lanes run over the embedding dimension.
+// Similarity-matrix problems built from per-token embeddings, S(i, j) = <en_s[i], en_t[j]>
+// with en = E / |E| (cosine) or en = E (dot), multiplied in BF16 with FP32 accumulation.
+//
+// normalize_rows_bf16_kernel: one warp per row writes the BF16 factor and 1/|E| in one
+// pass over E.  path_embedding_grad_kernel: dScore/dE[i] for the aligned cells (i, j) of
+// each pair's optimal path only -- the gradient of S w.r.t. en_s[i] is g * en_t_bf16[j]
+// (the BF16 cast passes gradients through), then the normalisation backward
+// (g - (g . en) en) / |E| -- without materialising dS.  In one path the aligned cells
+// have distinct i and distinct j, so a warp per pair writes without atomics.
 
 namespace {
 
+__global__ void normalize_rows_bf16_kernel(const float *E, int64_t rows, int32_t dim, int32_t normalize,
+                                           __nv_bfloat16 *out, float *inv_norm) {
+	const int64_t r = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (r >= rows) return;
+	const float *x = E + r * dim;
+	float ss = 0.0f;
+	for (int c = lane; c < dim; c += 32) ss += x[c] * x[c];
+	for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+	const float inv = normalize ? 1.0f / fmaxf(sqrtf(ss), 1e-12f) : 1.0f;
+	for (int c = lane; c < dim; c += 32) out[r * dim + c] = __float2bfloat16_rn(x[c] * inv);
+	if (lane == 0) inv_norm[r] = inv;
+}
+
 struct EmbGradParams {
 	int64_t batch;
-	int32_t dim;
+	int32_t dim, normalize;
 	const int32_t *paths;
 	const int64_t *path_off;
 	const int32_t *path_len;
 	const float *grad;
-	const float *Es, *Et;  // (batch, n_s, dim), (batch, n_t, dim) contiguous
-	float *dEs, *dEt;
+	const float *Es, *Et;                 // raw embeddings (batch, n, dim)
+	const __nv_bfloat16 *Esb, *Etb;       // the BF16 factors of the product
+	const float *inv_s, *inv_t;           // 1/|E| per row (1 when not normalising)
+	float *dEs, *dEt;                     // zero except on aligned rows
 	int64_t n_s, n_t;
 };
+
+__device__ __forceinline__ float warp_sum(float x) {
+	for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+	return x;
+}
 
 __global__ void path_embedding_grad_kernel(EmbGradParams p) {
 	const int64_t k = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -124,18 +150,33 @@ __global__ void path_embedding_grad_kernel(EmbGradParams p) {
 	const float g = p.grad[k];
 	const int n = p.path_len[k];
 	const int32_t *P = p.paths + p.path_off[k];
-	const float *es = p.Es + k * p.n_s * p.dim;
-	const float *et = p.Et + k * p.n_t * p.dim;
-	float *des = p.dEs + k * p.n_s * p.dim;
-	float *det = p.dEt + k * p.n_t * p.dim;
+	const int64_t bs = k * p.n_s, bt = k * p.n_t;
 	for (int q = 0; q + 1 < n; q++) {
 		const int u0 = P[2 * q], v0 = P[2 * q + 1];
 		if (u0 < 0 || v0 < 0) break;
 		const int u1 = P[2 * q + 2], v1 = P[2 * q + 3];
 		if (!(u1 == u0 - 1 && v1 == v0 - 1)) continue;
+		const int64_t ri = (bs + u0) * p.dim, rj = (bt + v0) * p.dim;
+		const float is = p.inv_s[bs + u0], it = p.inv_t[bt + v0];
+		float dots = 0.0f, dott = 0.0f;
 		for (int c = lane; c < p.dim; c += 32) {
-			des[int64_t(u0) * p.dim + c] += g * et[int64_t(v0) * p.dim + c];
-			det[int64_t(v0) * p.dim + c] += g * es[int64_t(u0) * p.dim + c];
+			dots += g * __bfloat162float(p.Etb[rj + c]) * p.Es[ri + c] * is;
+			dott += g * __bfloat162float(p.Esb[ri + c]) * p.Et[rj + c] * it;
+		}
+		if (p.normalize) {
+			dots = warp_sum(dots);
+			dott = warp_sum(dott);
+		}
+		for (int c = lane; c < p.dim; c += 32) {
+			const float gs = g * __bfloat162float(p.Etb[rj + c]);
+			const float gt = g * __bfloat162float(p.Esb[ri + c]);
+			if (p.normalize) {
+				p.dEs[ri + c] = (gs - dots * p.Es[ri + c] * is) * is;
+				p.dEt[rj + c] = (gt - dott * p.Et[rj + c] * it) * it;
+			} else {
+				p.dEs[ri + c] = gs;
+				p.dEt[rj + c] = gt;
+			}
 		}
 	}
 }
@@ -175,14 +216,28 @@ __global__ void path_series_grad_kernel(SeriesGradParams p) {
 
 }  // namespace
 
-extern "C" pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, const int32_t *paths,
+extern "C" pa_status pa_normalize_rows_bf16(const float *E, int64_t rows, int32_t dim, int32_t normalize,
+                                            void *out_bf16, float *inv_norm, void *stream) {
+	if (rows < 0 || dim <= 0 || !E || !out_bf16 || !inv_norm) return PA_ERR_INVALID_ARGUMENT;
+	if (rows == 0) return PA_OK;
+	normalize_rows_bf16_kernel<<<int((rows * 32 + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+	    E, rows, dim, normalize, reinterpret_cast<__nv_bfloat16 *>(out_bf16), inv_norm);
+	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}
+
+extern "C" pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
                                                  const int64_t *path_offsets, const int32_t *path_len,
                                                  const float *grad_scores, const float *Es, const float *Et,
-                                                 int64_t n_s, int64_t n_t, float *dEs, float *dEt, void *stream) {
-	if (batch < 0 || dim <= 0 || !paths || !path_offsets || !path_len || !grad_scores || !Es || !Et || !dEs || !dEt)
+                                                 const void *Es_bf16, const void *Et_bf16, const float *inv_s,
+                                                 const float *inv_t, int64_t n_s, int64_t n_t, float *dEs, float *dEt,
+                                                 void *stream) {
+	if (batch < 0 || dim <= 0 || !paths || !path_offsets || !path_len || !grad_scores || !Es || !Et || !Es_bf16 ||
+	    !Et_bf16 || !inv_s || !inv_t || !dEs || !dEt)
 		return PA_ERR_INVALID_ARGUMENT;
 	if (batch == 0) return PA_OK;
-	EmbGradParams p{batch, dim, paths, path_offsets, path_len, grad_scores, Es, Et, dEs, dEt, n_s, n_t};
+	EmbGradParams p{batch, dim, normalize, paths, path_offsets, path_len, grad_scores, Es, Et,
+	                reinterpret_cast<const __nv_bfloat16 *>(Es_bf16), reinterpret_cast<const __nv_bfloat16 *>(Et_bf16),
+	                inv_s, inv_t, dEs, dEt, n_s, n_t};
 	const int64_t threads = batch * 32;
 	path_embedding_grad_kernel<<<int((threads + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;

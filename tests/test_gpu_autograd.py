@@ -195,8 +195,9 @@ def test_embedding_gradients_flow(torch_ag):
 
 
 def test_fused_embedding_gradients_match_dense_route(torch_ag):
-    """embedding_alignment_score's path-walk backward equals dS @ Et with dS the path
-    indicator of the dense route (one aligned j per i, so the sums are single terms)."""
+    """embedding_alignment_score's path-walk backward (dot similarity) equals dS @ Et with dS
+    the path indicator of the dense route (one aligned j per i, so the sums are single
+    terms)."""
     torch, ag = torch_ag
     g = torch.Generator(device="cuda").manual_seed(9)
     B, ns, nt, d = 32, 50, 44, 64
@@ -245,3 +246,28 @@ def test_fused_series_dtw_gradients_match_dense_route(torch_ag):
     sc2.sum().backward()
     assert torch.equal(sc, sc2)
     assert torch.allclose(x.grad, x2.grad, atol=1e-5) and torch.allclose(y.grad, y2.grad, atol=1e-5)
+
+
+def test_fused_cosine_gradients_match_torch_normalize(torch_ag):
+    """With normalize=True the fused backward equals torch's autograd through F.normalize
+    applied to dS @ en_t (the dense route), to float32 rounding."""
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(21)
+    B, ns, nt, d = 16, 40, 36, 128
+    Es = torch.randn(B, ns, d, device="cuda", generator=g)
+    Et = torch.randn(B, nt, d, device="cuda", generator=g)
+    lengths = np.full((B, 2), (ns, nt))
+    a = Es.clone().requires_grad_(True)
+    b = Et.clone().requires_grad_(True)
+    sc = ag.embedding_alignment_score(a, b, lengths, 0.5, 0.1, "global", normalize=True)
+    sc.sum().backward()
+    a2 = Es.clone().requires_grad_(True)
+    b2 = Et.clone().requires_grad_(True)
+    en_s = torch.nn.functional.normalize(a2, dim=-1)
+    en_t = torch.nn.functional.normalize(b2, dim=-1)
+    S = torch.bmm(en_t.to(torch.bfloat16), en_s.to(torch.bfloat16).transpose(1, 2)).float().transpose(1, 2)
+    sc2 = ag.alignment_score(S, lengths, 0.5, 0.1, "global")
+    sc2.sum().backward()
+    assert torch.allclose(sc, sc2, atol=1e-4)
+    assert torch.allclose(a.grad, a2.grad, atol=2e-3, rtol=1e-2)
+    assert torch.allclose(b.grad, b2.grad, atol=2e-3, rtol=1e-2)
