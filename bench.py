@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fwd-bwd-pairs", type=int, default=4096, help="pairs of the fwd+bwd measurement (0: skip)")
+    ap.add_argument("--other-configs", type=int, default=1, help="also measure the other workloads (0: skip)")
     ap.add_argument("--plain-pairs", type=int, default=2048,
                     help="pairs timed on the plain path (one launch per 4-pair batch)")
     return ap.parse_args()
@@ -222,6 +223,119 @@ def cpu_baseline(a, b, ls, lt, table, seconds):
     n = max(threads, min(n, len(ls)))
     cells, dt = run(np.arange(n))
     return cells / dt / 1e9, threads, f"first {n} pairs of the workload ({cells:.3e} cells, {dt:.1f} s)"
+
+
+# --------------------------------------------------------------------------- other workloads
+
+def _time_device(torch, fn, steps=3, warmup=1):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0 / steps
+
+
+def other_configs(torch, alg, L, seed):
+    """The other synthetic workloads of the solve, through pa_solve_batch / the native
+    module with device-resident codes: (1) global linear gap 1, eq +1 / ne -1, 4096 pairs
+    of 64 letters over 20, score + one traceback; (3) semiglobal affine open 10 / extend 1
+    on 256 pairs of 5000 x 10000 residues of a 20-letter alphabet (per-batch Dirichlet(1)
+    frequencies, symmetric integer matrix: diagonal U[4, 11], off-diagonal U[-4, 2]),
+    score only, and the first 20 all-optimal alignments of 2 pairs."""
+    import types
+    out = {}
+    P = ctypes.POINTER
+    rng = np.random.default_rng(seed)
+
+    def run_batch(opts, a, b, ls, lt, table=None, eq=None, ne=None, maps=True):
+        B = a.shape[0]
+        mod = alg.m16 if max(a.shape[1], b.shape[1]) < 16000 else alg.m32
+        solver = mod.create_solver(a.shape[1], b.shape[1], mod.create_options(opts))
+        alg.check(L.pa_solver_set_stream(solver.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        a_d = torch.from_numpy(a.view(np.int32)).cuda()
+        b_d = torch.from_numpy(b.view(np.int32)).cuda()
+        t_d = torch.from_numpy(table).cuda() if table is not None else None
+        length = np.ascontiguousarray(np.stack([ls, lt]), dtype=np.int32)
+        sizes = np.minimum(ls, lt).astype(np.int64)
+        offs = np.zeros(B, np.int64)
+        offs[1:] = np.cumsum(sizes)[:-1]
+        sc = torch.empty(B, dtype=torch.float32, device="cuda")
+        mp = torch.empty(max(1, int(sizes.sum())), dtype=torch.int32, device="cuda")
+        bt = alg.Batch(form=1 if table is not None else 2, location=1, batch=B, n_s=a.shape[1], n_t=b.shape[1],
+                       a=ctypes.cast(a_d.data_ptr(), P(ctypes.c_uint32)), b=ctypes.cast(b_d.data_ptr(), P(ctypes.c_uint32)),
+                       table=ctypes.cast(t_d.data_ptr(), P(ctypes.c_float)) if t_d is not None else None,
+                       table_rows=table.shape[0] if table is not None else 0,
+                       table_cols=table.shape[1] if table is not None else 0,
+                       eq=eq or 0.0, ne=ne or 0.0, length=length.ctypes.data_as(P(ctypes.c_int32)))
+
+        def step():
+            alg.check(L.pa_solve_batch(solver.handle, ctypes.byref(bt), ctypes.c_void_p(sc.data_ptr()),
+                                       ctypes.c_void_p(mp.data_ptr()) if maps else None,
+                                       offs.ctypes.data_as(P(ctypes.c_int64))))
+        t = _time_device(torch, step)
+        ms4 = (ctypes.c_float * 4)()
+        nl = ctypes.c_int32(0)
+        L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
+        cells = float((ls.astype(np.int64) * lt).sum())
+        return {"value": cells / t / 1e9, "unit": "GCUPS", "ms": t * 1000, "dp_ms": ms4[1], "traceback_ms": ms4[2]}
+
+    def opts(alg_, locality, detail, gap, batch, count="ONE"):
+        return {"solver": alg_.Type.ALIGNMENT, "direction": alg_.Direction.MAXIMIZE, "batch": True,
+                "batch_size": batch, "return_dup": False, "locality": alg_.Locality.__members__[locality],
+                "codomain": types.SimpleNamespace(detail=alg_.Detail.__members__[detail], count=alg_.Count.__members__[count]),
+                "gap_cost": gap}
+
+    class Lin:
+        def __init__(self, g):
+            self.g = g
+
+        def to_special_case(self):
+            return {"linear": self.g}
+
+    # config 1
+    B1 = 4096
+    a1 = rng.integers(0, 20, size=(B1, 64)).astype(np.uint32)
+    b1 = rng.integers(0, 20, size=(B1, 64)).astype(np.uint32)
+    l1 = np.full(B1, 64, np.int32)
+    out["global_linear_64x64"] = dict(run_batch(opts(alg, "GLOBAL", "ALIGNMENT", Lin(1.0), B1), a1, b1, l1, l1,
+                                                eq=1.0, ne=-1.0),
+                                      workload="4096 pairs of 64 x 64, 20 letters, global linear gap 1, eq +1 / ne -1, score + one traceback")
+    # config 3
+    B3 = 256
+    freq = rng.dirichlet(np.ones(20))
+    a3 = rng.choice(20, size=(B3, 5000), p=freq).astype(np.uint32)
+    b3 = rng.choice(20, size=(B3, 10000), p=freq).astype(np.uint32)
+    m = rng.integers(-4, 3, size=(20, 20))
+    m = np.triu(m, 1) + np.triu(m, 1).T
+    np.fill_diagonal(m, rng.integers(4, 12, size=20))
+    t3 = m.astype(np.float32)
+    ls3 = np.full(B3, 5000, np.int32)
+    lt3 = np.full(B3, 10000, np.int32)
+    out["semiglobal_affine_5000x10000_score"] = dict(
+        run_batch(opts(alg, "SEMIGLOBAL", "SCORE", AffineGap(10.0, 1.0), B3), a3, b3, ls3, lt3, table=t3, maps=False),
+        workload="256 pairs of 5000 x 10000, 20 letters, semiglobal affine 10/1, score only")
+    # all optimal alignments (first 20 of 2 pairs), through the native module's iterator
+    mod = alg.m16
+    solver = mod.create_solver(5000, 10000, mod.create_options(
+        opts(alg, "SEMIGLOBAL", "ALIGNMENT", AffineGap(10.0, 1.0), 2, count="ALL")))
+    t0 = time.perf_counter()
+    res = solver.solve_indexed_for_alignment_iterator(a3[:2], b3[:2], t3, np.stack([ls3[:2], lt3[:2]]).astype(np.uint16))
+    n_items = 0
+    for it in res:
+        for _ in range(20):
+            if it.next() is None:
+                break
+            n_items += 1
+    dt = time.perf_counter() - t0
+    out["semiglobal_affine_5000x10000_all_optimal"] = {
+        "value": 2 * 5000 * 10000 / dt / 1e9, "unit": "GCUPS", "ms": dt * 1000, "alignments": n_items,
+        "workload": "2 pairs of 5000 x 10000, all-optimal masks on the GPU, first 20 alignments each (host DFS)"}
+    return out
 
 
 # --------------------------------------------------------------------------- fwd + bwd
@@ -525,6 +639,7 @@ def run_ours(args):
                 "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"}
 
     fb = fwd_bwd(torch, args.fwd_bwd_pairs, args.seed + 5) if args.fwd_bwd_pairs > 0 else None
+    others = other_configs(torch, alg, L, args.seed + 7) if args.other_configs else None
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -548,6 +663,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "plain_gpu": plain,
         "fwd_bwd": fb,
+        "other_configs": others,
         "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms)},
         "clocks": clocks.summary(),
     }
