@@ -46,6 +46,11 @@ constexpr int MAX_SMEM_TABLE = 64;  // alphabet size kept in shared memory
 
 // status bits written by kernels (host turns them into errors)
 constexpr int ST_BAD_CODE = 1;
+constexpr int ST_TIMEOUT = 2;   // a chained stripe waited too long for the stripe above it
+
+// Stripe-chained mode: columns a stripe publishes at a time, and the bound of one wait.
+constexpr int PUB_CHUNK = 32;
+constexpr int WAIT_LIMIT = 1 << 23;
 
 template <typename V>
 struct DpParams {
@@ -95,7 +100,56 @@ struct DpParams {
 	int64_t scratch_stride;  // elements per slot
 	int32_t *work_counter;
 	int32_t *status;
+	// stripe-chained mode (units != 0): a ticket is one stripe of one pair; tickets are
+	// numbered stripe-major, level_start[q] is the first ticket of stripe q (nlevels + 1
+	// entries), and stripe q of the pair at rank w in the order is ticket level_start[q] + w.
+	// A stripe reads the boundary row of the stripe above it once that stripe's progress
+	// counter (columns finished) covers the column; the scratch rows are per pair rank.
+	int32_t units;          // informational: the kernel variant decides
+	int32_t ntickets;
+	int32_t nlevels;
+	const int32_t *level_start;
+	int32_t *progress;      // per ticket, zeroed before the launch
+	int4 *chain;            // per ticket: running seed of the stripes so far (value bits, i, j)
 };
+
+__device__ __forceinline__ int32_t ld_acquire(const int32_t *a) {
+	int32_t v;
+	asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void st_release(int32_t *a, int32_t v) {
+	asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+
+// Wait until *prog >= need; returns the value seen.  The wait is bounded: past WAIT_LIMIT
+// polls (or once another wait gave up) it sets ST_TIMEOUT and returns INT32_MAX, so the
+// kernel finishes with flagged, meaningless results instead of hanging.
+static __device__ __noinline__ int32_t wait_progress(const int32_t *prog, int32_t need, int32_t *status) {
+	for (int it = 0; it < WAIT_LIMIT; it++) {
+		const int32_t v = ld_acquire(prog);
+		if (v >= need) return v;
+		if (it >= 64) {
+			if ((it & 63) == 0 && (*reinterpret_cast<volatile int32_t *>(status) & ST_TIMEOUT)) return INT32_MAX;
+			__nanosleep(256);
+		}
+	}
+	atomicOr(status, ST_TIMEOUT);
+	return INT32_MAX;
+}
+
+template <typename V>
+__device__ __forceinline__ int32_t vbits(V x) {
+	if constexpr (std::is_same<V, float>::value) return __float_as_int(x);
+	else return x;
+}
+
+template <typename V>
+__device__ __forceinline__ V vfrom(int32_t x) {
+	if constexpr (std::is_same<V, float>::value) return __int_as_float(x);
+	else return x;
+}
 
 template <typename V>
 struct V2T;
@@ -161,7 +215,7 @@ __device__ __forceinline__ uint32_t gt_mask(int32_t a, int32_t b) {
 	return d;
 }
 
-template <typename V, int GAP, int LOC, int TB, bool VALS>
+template <typename V, int GAP, int LOC, int TB, bool VALS, bool CHAIN>
 __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 	constexpr bool ISINT = std::is_same<V, int32_t>::value;
 	constexpr bool TAG = ISINT && TB != TB_ALL;  // int32 tagged values
@@ -186,18 +240,33 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 	const int gpw = 32 / G;            // groups per warp
 	const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const int slot = warp_global * gpw + grp;
-	V2 *scr = reinterpret_cast<V2 *>(p.scratch) + int64_t(slot) * p.scratch_stride;
 	const int64_t half = p.scratch_stride / 2;
 	const V NEG = p.neg_inf;
 	const int rpp = G * R;  // rows per pass
 	const int sub_kind = p.sub_kind;
+	constexpr bool units = CHAIN;  // stripe-chained mode (G == 32)
+	const int ntickets = units ? p.ntickets : p.npairs;
 
 	for (;;) {
 		int base = 0;
 		if (lane == 0) base = atomicAdd(p.work_counter, gpw);
 		base = __shfl_sync(0xffffffffu, base, 0);
-		if (base >= p.npairs) break;
-		const int w = base + grp;
+		if (base >= ntickets) break;
+		// group mode: the pair at rank base + grp, all of its stripes.  Stripe-chained mode:
+		// stripe q_lo of the pair at rank w, waiting on ticket prod (stripe q_lo - 1).
+		int w = base + grp, q_lo = 0, prod = -1;
+		if constexpr (units) {
+			int lo = 0, hi = p.nlevels - 1;
+			while (lo < hi) {
+				const int mid = (lo + hi + 1) >> 1;
+				if (p.level_start[mid] <= base) lo = mid;
+				else hi = mid - 1;
+			}
+			q_lo = lo;
+			w = base - p.level_start[lo];
+			if (lo > 0) prod = p.level_start[lo - 1] + w;
+		}
+		V2 *scr = reinterpret_cast<V2 *>(p.scratch) + int64_t(units ? w : slot) * p.scratch_stride;
 		const int pair = w < p.npairs ? p.order[w] : -1;
 		const int ls = pair >= 0 ? p.len_s[pair] : 0;
 		const int lt = pair >= 0 ? p.len_t[pair] : 0;
@@ -219,7 +288,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 		const int64_t layer_sz = int64_t(ls + 1) * lstride;
 
 		// --- solution values: borders (solver.h:2806-2814, 2918-2967, 3116-3125, 3205-3210)
-		if (VALS && vals) {
+		if (VALS && vals && q_lo == 0) {
 			for (int j = sub - 1; j < lt; j += G) {
 				vals[j + 1] = to_ref(p.top_D[j + 1], TAG, p.out_sign);
 				if (GAP == GAP_AFFINE) {
@@ -246,13 +315,25 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 		V glob = NEG;                // global: D(ls-1, lt-1)
 		bool have_glob = false;
 
-		for (int q = 0; q < wpass; q++) {
+		const int q_hi = units ? min(q_lo + 1, npass) : wpass;
+		for (int q = q_lo; q < q_hi; q++) {
 			const bool pass_active = q < npass;
 			const int row0 = q * rpp + sub * R;
 			const int nvalid = ls - row0;  // rows of this lane that are < ls (may be <= 0 or >= R)
 			const V2 *bin = scr + (q & 1) * half;
 			V2 *bout = scr + ((q + 1) & 1) * half;
 			const bool write_boundary = sub == G - 1 && q + 1 < npass;
+			// stripe-chained: the boundary row comes from another warp, column by column
+			const int32_t *prog_in = (units && q > 0) ? p.progress + prod : nullptr;
+			int32_t avail = 0;        // columns of bin known to be written
+			int pub_next = PUB_CHUNK;  // next progress value to publish
+			V2 bnext;                  // lane 0: bin of the next column
+			bnext.x = NEG;
+			bnext.y = NEG;
+			if (units && sub == 0 && pass_active && q > 0) {
+				avail = wait_progress(prog_in, 1, p.status);
+				bnext = __ldcg(bin);
+			}
 
 			// query codes, and the int8 substitution profile of each row (SUB_PROFILE)
 			uint32_t qa[R];
@@ -312,6 +393,13 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 					if (q == 0) {
 						upD = p.top_D[j + 1];
 						upP = NEG;
+					} else if constexpr (units) {
+						upD = bnext.x;
+						upP = bnext.y;
+						if (j + 1 < lt) {  // prefetch the next column's boundary
+							if (avail < j + 2) avail = wait_progress(prog_in, j + 2, p.status);
+							bnext = __ldcg(bin + j + 1);
+						}
 					} else {
 						const V2 bv2 = bin[j];
 						upD = bv2.x;
@@ -470,7 +558,13 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 					}
 					outD = uD;
 					outP = uP;
-					if (write_boundary) bout[j] = V2{outD, outP};
+					if (write_boundary) {
+						bout[j] = V2{outD, outP};
+						if (units && j + 1 == pub_next) {  // columns < j + 1 are written
+							if (j + 1 < lt) st_release(p.progress + base, j + 1);
+							pub_next += PUB_CHUNK;
+						}
+					}
 
 					if (TB == TB_ONE) {
 						uint32_t *m = reinterpret_cast<uint32_t *>(p.masks) + p.mask_off[pair];
@@ -554,7 +648,33 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			}
 		}
 
-		if (sub == 0 && pair >= 0) {
+		// ---- stripe-chained: fold in the seed of the stripes above, pass it on
+		bool last_unit = true;
+		if (units && pair >= 0) {  // constant-folded away in group mode
+			last_unit = q_lo >= npass - 1;
+			if (q_lo > 0 && (LOC == LOC_LOCAL || LOC == LOC_SEMI) && !(LOC == LOC_LOCAL && TB == TB_ALL)) {
+				const int32_t *pi = p.progress + prod;
+				if (ld_acquire(pi) < lt) wait_progress(pi, lt, p.status);
+				const int4 rc = __ldcg(p.chain + prod);
+				const V ov = vfrom<V>(rc.x);
+				if (LOC == LOC_LOCAL) {
+					if (ov > l_best || (ov == l_best && (rc.y > l_bi || (rc.y == l_bi && rc.z > l_bj)))) {
+						l_best = ov; l_bi = rc.y; l_bj = rc.z;
+					}
+				} else if (rc.y >= 0 && (col_bi < 0 || ov > col_best || (ov == col_best && rc.y < col_bi))) {
+					col_best = ov; col_bi = rc.y;
+				}
+			}
+			if (!last_unit && sub == G - 1) {
+				int4 rc;
+				if (LOC == LOC_LOCAL) rc = make_int4(vbits(l_best), l_bi, l_bj, 0);
+				else rc = make_int4(vbits(col_best), col_bi, -1, 0);
+				p.chain[base] = rc;
+				st_release(p.progress + base, lt);  // every column, and the record
+			}
+		}
+
+		if (sub == 0 && pair >= 0 && last_unit) {
 			int si = -1, sj = -1, has = 0;
 			float sc = -INFINITY * p.out_sign;
 			if (!empty) {

@@ -306,7 +306,7 @@ struct pa_solver {
 	DevBuf d_a, d_b, d_tab, d_dense, d_dense_off, d_ls, d_lt, d_order, d_mask_off, d_score, d_seed, d_has,
 	    d_masks, d_scratch, d_counter, d_status, d_border, d_maps, d_map_off, d_paths, d_path_off,
 	    d_path_len, d_vals, d_val_off, d_best, d_gen, d_wsb_off, d_wsb_tb, d_wsb_vals, d_wsb_sub,
-	    d_wsb_sub_off, d_codes_max;
+	    d_wsb_sub_off, d_codes_max, d_progress, d_chain;
 	PinBuf h_stage, h_out;
 	// per-call pair metadata, staged in one pinned buffer and sent with one copy
 	DevBuf d_meta;
@@ -314,7 +314,7 @@ struct pa_solver {
 	cudaEvent_t meta_ev = nullptr;    // the staging buffer is free again once this completes
 	bool meta_pending = false;
 	struct {
-		int32_t *ls, *lt, *order;
+		int32_t *ls, *lt, *order, *level_start;
 		int64_t *mask_off, *map_off, *path_off, *val_off, *dense_off;
 	} m{};
 	std::vector<std::pair<uint64_t, int>> occ_cache;  // (kernel variant, smem) -> blocks per SM
@@ -362,6 +362,8 @@ struct Plan {
 	int G = 32;
 	int key_shift = 0;
 	int64_t max_ls = 0, max_lt = 0;
+	bool units = false;        // stripe-chained mode (G = 32): one ticket per stripe
+	int32_t ntickets = 0, nlevels = 0;
 };
 
 // Group width G (lanes per pair, R = 8 rows each) that minimises the cells a launch
@@ -401,6 +403,32 @@ int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, int
 	return bestG;
 }
 
+// Group mode (a group of G lanes sweeps all stripes of its pair) or stripe-chained mode (a
+// warp per stripe, consecutive stripes of a pair on different warps, each waiting on the
+// boundary row of the one above).  Both are estimated in warp-steps: the work spread over
+// the resident warps, or the longest dependent chain, whichever is larger.  Group mode's
+// chain is a whole pair; the stripe-chained chain is one sweep plus a PUB_CHUNK + 32 column
+// lag per stripe.  Chaining pays when a launch has too few pairs to fill the GPU.
+bool choose_units(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, int sm_count, int G) {
+	if (const char *e = std::getenv("PA_DP_MODE")) {  // experiments and tests
+		if (std::strcmp(e, "units") == 0) return true;
+		if (std::strcmp(e, "groups") == 0) return false;
+	}
+	const double slots = double(sm_count) * 16.0;
+	const int64_t rg = int64_t(G) * R, ru = 32 * R;
+	double work_g = 0, work_u = 0, chain_g = 0, chain_u = 0;
+	for (size_t k = 0; k < ls.size(); k++) {
+		if (ls[k] == 0 || lt[k] == 0) continue;
+		const int64_t ng = (ls[k] + rg - 1) / rg, nu = (ls[k] + ru - 1) / ru;
+		work_g += double(ng) * double(lt[k] + G - 1) * double(G) / 32.0;
+		work_u += double(nu) * double(lt[k] + 31);
+		chain_g = std::max(chain_g, double(ng) * double(lt[k] + G - 1));
+		chain_u = std::max(chain_u, double(lt[k] + 31) + double(nu) * double(PUB_CHUNK + 32));
+	}
+	const double tg = std::max(work_g / slots, chain_g), tu = std::max(work_u / slots, chain_u);
+	return tu < 0.8 * tg;
+}
+
 template <typename V>
 V cvt(float x, bool use_int, int scale, int tag) {
 	if (use_int) {
@@ -408,6 +436,50 @@ V cvt(float x, bool use_int, int scale, int tag) {
 		return V(int32_t(std::nearbyint(x)) * scale + tag);
 	}
 	return V(x);
+}
+
+// The kernel family of a (value type, gap kind, mode).
+template <typename V>
+cudaError_t dp_launch(int gk, bool chain, int loc, int tb, bool vals, const DpParams<V> &p, int grid, size_t smem,
+                      cudaStream_t st) {
+	if constexpr (std::is_same<V, int32_t>::value) {
+		if (chain)
+			return gk == GAP_LINEAR ? launch_dp_i_linear_chain(loc, tb, vals, p, grid, smem, st)
+			       : gk == GAP_AFFINE ? launch_dp_i_affine_chain(loc, tb, vals, p, grid, smem, st)
+			                          : launch_dp_i_dtw_chain(loc, tb, vals, p, grid, smem, st);
+		return gk == GAP_LINEAR ? launch_dp_i_linear(loc, tb, vals, p, grid, smem, st)
+		       : gk == GAP_AFFINE ? launch_dp_i_affine(loc, tb, vals, p, grid, smem, st)
+		                          : launch_dp_i_dtw(loc, tb, vals, p, grid, smem, st);
+	} else {
+		if (chain)
+			return gk == GAP_LINEAR ? launch_dp_f_linear_chain(loc, tb, vals, p, grid, smem, st)
+			       : gk == GAP_AFFINE ? launch_dp_f_affine_chain(loc, tb, vals, p, grid, smem, st)
+			                          : launch_dp_f_dtw_chain(loc, tb, vals, p, grid, smem, st);
+		return gk == GAP_LINEAR ? launch_dp_f_linear(loc, tb, vals, p, grid, smem, st)
+		       : gk == GAP_AFFINE ? launch_dp_f_affine(loc, tb, vals, p, grid, smem, st)
+		                          : launch_dp_f_dtw(loc, tb, vals, p, grid, smem, st);
+	}
+}
+
+template <typename V>
+cudaError_t dp_occupancy(int gk, bool chain, int loc, int tb, bool vals, size_t smem, int *bps) {
+	if constexpr (std::is_same<V, int32_t>::value) {
+		if (chain)
+			return gk == GAP_LINEAR ? occupancy_dp_i_linear_chain(loc, tb, vals, smem, bps)
+			       : gk == GAP_AFFINE ? occupancy_dp_i_affine_chain(loc, tb, vals, smem, bps)
+			                          : occupancy_dp_i_dtw_chain(loc, tb, vals, smem, bps);
+		return gk == GAP_LINEAR ? occupancy_dp_i_linear(loc, tb, vals, smem, bps)
+		       : gk == GAP_AFFINE ? occupancy_dp_i_affine(loc, tb, vals, smem, bps)
+		                          : occupancy_dp_i_dtw(loc, tb, vals, smem, bps);
+	} else {
+		if (chain)
+			return gk == GAP_LINEAR ? occupancy_dp_f_linear_chain(loc, tb, vals, smem, bps)
+			       : gk == GAP_AFFINE ? occupancy_dp_f_affine_chain(loc, tb, vals, smem, bps)
+			                          : occupancy_dp_f_dtw_chain(loc, tb, vals, smem, bps);
+		return gk == GAP_LINEAR ? occupancy_dp_f_linear(loc, tb, vals, smem, bps)
+		       : gk == GAP_AFFINE ? occupancy_dp_f_affine(loc, tb, vals, smem, bps)
+		                          : occupancy_dp_f_dtw(loc, tb, vals, smem, bps);
+	}
 }
 
 template <typename V>
@@ -530,41 +602,37 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	const int loc = s->loc;
 	const uint64_t okey = (uint64_t(ISINT) << 60) | (uint64_t(gk) << 56) | (uint64_t(loc) << 52) |
 	                      (uint64_t(tb) << 48) | (uint64_t(want_values) << 44) | uint64_t(smem);
+	const bool ch = plan.units;
 	for (const auto &kv : s->occ_cache)
-		if (kv.first == okey) bps = kv.second;
-	if (bps > 0) {
-	} else if (ISINT) {
-		e = gk == GAP_LINEAR ? occupancy_dp_i_linear(loc, tb, want_values, smem, &bps)
-		    : gk == GAP_AFFINE ? occupancy_dp_i_affine(loc, tb, want_values, smem, &bps)
-		                       : occupancy_dp_i_dtw(loc, tb, want_values, smem, &bps);
-	} else {
-		e = gk == GAP_LINEAR ? occupancy_dp_f_linear(loc, tb, want_values, smem, &bps)
-		    : gk == GAP_AFFINE ? occupancy_dp_f_affine(loc, tb, want_values, smem, &bps)
-		                       : occupancy_dp_f_dtw(loc, tb, want_values, smem, &bps);
-	}
+		if (kv.first == (okey | (uint64_t(ch) << 40))) bps = kv.second;
+	if (bps == 0) e = dp_occupancy<V>(gk, ch, loc, tb, want_values, smem, &bps);
 	PA_CUDA(e);
 	bps = std::max(bps, 1);
-	if (s->occ_cache.size() < 64) s->occ_cache.push_back({okey, bps});
+	if (s->occ_cache.size() < 64) s->occ_cache.push_back({okey | (uint64_t(ch) << 40), bps});
 	const int gpw = 32 / plan.G;
-	const int64_t groups_needed = (npairs + gpw - 1) / gpw;  // warps needed
+	const int64_t groups_needed = plan.units ? plan.ntickets : (npairs + gpw - 1) / gpw;  // warps needed
 	int64_t grid = int64_t(s->sm_count) * bps;
 	grid = std::min<int64_t>(grid, (groups_needed + WARPS - 1) / WARPS);
 	grid = std::max<int64_t>(grid, 1);
-	const int64_t slots = grid * WARPS * gpw;
+	// scratch rows: per group slot, or per pair in the stripe-chained mode
+	const int64_t slots = plan.units ? std::max<int64_t>(npairs, 1) : grid * WARPS * gpw;
 	p.scratch_stride = 2 * std::max<int64_t>(plan.max_lt, 1);
 	PA_CUDA(s->d_scratch.ensure(size_t(slots * p.scratch_stride) * 2 * sizeof(V)));
 	p.scratch = s->d_scratch.p;
+	if (plan.units) {
+		p.units = 1;
+		p.ntickets = plan.ntickets;
+		p.nlevels = plan.nlevels;
+		p.level_start = s->m.level_start;
+		PA_CUDA(s->d_progress.ensure(size_t(plan.ntickets) * 4));
+		PA_CUDA(s->d_chain.ensure(size_t(plan.ntickets) * 16));
+		p.progress = s->d_progress.as<int32_t>();
+		p.chain = s->d_chain.as<int4>();
+		PA_CUDA(cudaMemsetAsync(s->d_progress.p, 0, size_t(plan.ntickets) * 4, st));
+	}
 
 	PA_CUDA(cudaMemsetAsync(s->d_counter.p, 0, sizeof(int32_t), st));
-	if (ISINT) {
-		e = gk == GAP_LINEAR ? launch_dp_i_linear(loc, tb, want_values, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
-		    : gk == GAP_AFFINE ? launch_dp_i_affine(loc, tb, want_values, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st)
-		                       : launch_dp_i_dtw(loc, tb, want_values, *reinterpret_cast<DpParams<int32_t> *>(&p), int(grid), smem, st);
-	} else {
-		e = gk == GAP_LINEAR ? launch_dp_f_linear(loc, tb, want_values, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
-		    : gk == GAP_AFFINE ? launch_dp_f_affine(loc, tb, want_values, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st)
-		                       : launch_dp_f_dtw(loc, tb, want_values, *reinterpret_cast<DpParams<float> *>(&p), int(grid), smem, st);
-	}
+	e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st);
 	PA_CUDA(e);
 	(*launches)++;
 	return PA_OK;
@@ -822,6 +890,10 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	plan.max_lt = max_lt;
 	plan.G = choose_G(ls, lt, s->sm_count);
 	plan.tb = tb;
+	if (s->gap != GAP_GENERAL) {
+		plan.units = choose_units(ls, lt, s->sm_count, plan.G);
+		if (plan.units) plan.G = 32;
+	}
 	res.G = plan.G;
 	// processing order: by number of stripes, then |t|, largest first (a counting sort), so
 	// the groups that share a warp get pairs of the same shape and long pairs start early
@@ -838,6 +910,29 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		for (int64_t k = 0; k < B; k++) count[size_t(key(k)) + 1]++;
 		for (int64_t c = 0; c < nkeys; c++) count[size_t(c) + 1] += count[size_t(c)];
 		for (int64_t k = 0; k < B; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
+	}
+	// stripe-chained tickets: level q holds stripe q of every pair with more than q stripes
+	// (an empty pair counts as one stripe, which writes its border result); the order puts
+	// those pairs first, so stripe q of rank w is ticket level_start[q] + w
+	std::vector<int32_t> level_start;
+	if (plan.units) {
+		const int64_t rpp_u = int64_t(plan.G) * R;
+		std::vector<int64_t> hist;
+		for (int64_t k = 0; k < B; k++) {
+			const int64_t np = std::max<int64_t>(1, (ls[size_t(k)] + rpp_u - 1) / rpp_u);
+			if (int64_t(hist.size()) <= np) hist.resize(size_t(np) + 1, 0);
+			hist[size_t(np)]++;
+		}
+		const int64_t nlev = int64_t(hist.size()) - 1;
+		level_start.assign(size_t(nlev) + 1, 0);
+		int64_t above = B;  // pairs with more than q stripes
+		for (int64_t q = 0; q < nlev; q++) {
+			level_start[size_t(q) + 1] = int32_t(level_start[size_t(q)] + above);
+			above -= hist[size_t(q) + 1];
+		}
+		if (int64_t(level_start.back()) >= (int64_t(1) << 31) - 64) return fail(PA_ERR_LENGTH, "too many stripes in one launch");
+		plan.nlevels = int32_t(nlev);
+		plan.ntickets = level_start.back();
 	}
 	std::vector<int64_t> mask_off(size_t(B) + 1, 0), map_off(size_t(B) + 1, 0), path_off(size_t(B) + 1, 0),
 	    val_off(size_t(B) + 1, 0), dense_off(size_t(B), 0);
@@ -859,7 +954,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	// pair metadata: packed into one pinned staging buffer, one host-to-device copy
 	{
 		const size_t n32 = size_t(B), n64 = size_t(B) + 1;
-		const size_t bytes = ((3 * n32 * 4 + 7) & ~size_t(7)) + 5 * n64 * 8;
+		const size_t bytes = ((3 * n32 * 4 + level_start.size() * 4 + 7) & ~size_t(7)) + 5 * n64 * 8 + 16;
 		if (s->meta_pending) {
 			PA_CUDA(cudaEventSynchronize(s->meta_ev));  // the previous call's copy has read it
 			s->meta_pending = false;
@@ -879,6 +974,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		s->m.ls = reinterpret_cast<int32_t *>(put(ls.data(), n32 * 4, 4));
 		s->m.lt = reinterpret_cast<int32_t *>(put(lt.data(), n32 * 4, 4));
 		s->m.order = reinterpret_cast<int32_t *>(put(order.data(), n32 * 4, 4));
+		s->m.level_start = reinterpret_cast<int32_t *>(put(level_start.data(), level_start.size() * 4, 4));
 		s->m.mask_off = reinterpret_cast<int64_t *>(put(mask_off.data(), n64 * 8, 8));
 		// the caller's output offsets replace the internal ones when results go to its buffers
 		const int64_t *mo = (maps_out && map_offsets) ? map_offsets : map_off.data();
@@ -1035,6 +1131,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	for (int k = 0; k < 4; k++) cudaEventElapsedTime(&s->last_ms[k], s->ev[k], s->ev[k + 1]);
 	s->last_launches = launches;
 	if (status & ST_BAD_CODE) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a or b");
+	if (status & ST_TIMEOUT) return fail(PA_ERR_TIMEOUT, "a chained stripe timed out waiting for the stripe above it");
 
 	// ---- codomain semantics on the host side
 	if (goal == GOAL_ALL && method == M_SCORE) {

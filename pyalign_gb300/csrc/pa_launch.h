@@ -14,6 +14,12 @@ PA_DECL(i, int32_t, dtw)
 PA_DECL(f, float, linear)
 PA_DECL(f, float, affine)
 PA_DECL(f, float, dtw)
+PA_DECL(i, int32_t, linear_chain)
+PA_DECL(i, int32_t, affine_chain)
+PA_DECL(i, int32_t, dtw_chain)
+PA_DECL(f, float, linear_chain)
+PA_DECL(f, float, affine_chain)
+PA_DECL(f, float, dtw_chain)
 #undef PA_DECL
 
 }  // namespace pa
