@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fwd-bwd-pairs", type=int, default=4096, help="pairs of the fwd+bwd measurement (0: skip)")
     ap.add_argument("--other-configs", type=int, default=1, help="also measure the other workloads (0: skip)")
+    ap.add_argument("--precision-pairs", type=int, default=8192, help="pairs of the precision measurement (0: skip)")
     ap.add_argument("--plain-pairs", type=int, default=2048,
                     help="pairs timed on the plain path (one launch per 4-pair batch)")
     return ap.parse_args()
@@ -416,6 +417,83 @@ def fwd_bwd(torch, pairs, seed, steps=3):
                     "workload": f"{nd} pairs, DTW |x-y| on Gaussian random walks, L~U[128,1024]"}}
 
 
+def precision_config(torch, pairs, seed, steps=3):
+    """The precision form: global Gotoh (open 0.5, extend 0.1, maximize) on S = cos of
+    per-token embeddings (d = 256, N(0, 1) then L2-normalised, lengths U[32, 512]) with the
+    similarity product on the tensor cores (pa_similarity_bf16: BF16 factors, FP32
+    accumulation in TMEM) and the float32 DP, plus the DTW variant (minimize) on 1 - cos
+    written by the same kernel's epilogue.  Reports the product alone (TFLOP/s over the
+    ragged cells' 2 d flops), the DP alone and normalise + product + DP (GCUPS over real
+    cells), and the score error of the float32 DP against the FP64 replay of each pair's
+    recovered path (pa_path_scores_f64), relative to |score| and to the summed terms."""
+    from pyalign_gb300 import autograd as ag
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    n, d = 512, 256
+    lengths = rng.integers(32, n + 1, size=(pairs, 2))
+    ls, lt = lengths[:, 0].astype(np.int64), lengths[:, 1].astype(np.int64)
+    cells = float((ls * lt).sum())
+    Es = torch.randn(pairs, n, d, device="cuda", generator=g)
+    Et = torch.randn(pairs, n, d, device="cuda", generator=g)
+    St = torch.empty((pairs, n, n), dtype=torch.float32, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
+    stream = torch.cuda.current_stream()
+
+    def product(alpha=1.0, beta=0.0):
+        Esb, _ = ag.normalized_bf16(Es)
+        Etb, _ = ag.normalized_bf16(Et)
+        return ag.similarity_bf16(Esb, Etb, lengths, out=St, alpha=alpha, beta=beta), Esb, Etb
+
+    S, Esb, Etb = product()
+    ag._forward_paths(S, lengths, (0.5, 0.1), "global", "maximize", False)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(steps):
+        ag.similarity_bf16(Esb, Etb, lengths, out=St)
+    ev[1].record(stream)
+    for _ in range(steps):
+        ag._forward_paths(S, lengths, (0.5, 0.1), "global", "maximize", False)
+    ev[2].record(stream)
+    for _ in range(steps):
+        S, _, _ = product()
+        ag._forward_paths(S, lengths, (0.5, 0.1), "global", "maximize", False)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    t_gemm = ev[0].elapsed_time(ev[1]) / 1000 / steps
+    t_dp = ev[1].elapsed_time(ev[2]) / 1000 / steps
+    t_all = ev[2].elapsed_time(ev[3]) / 1000 / steps
+    sc32, rep, scale = ag.path_scores_f64(S, lengths, 0.5, 0.1, "global", "maximize", with_scale=True)
+    err_score = float(((sc32.double() - rep).abs() / rep.abs()).max())
+    err_scale = float(((sc32.double() - rep).abs() / scale).max())
+
+    D, _, _ = product(-1.0, 1.0)
+    ag._forward_paths(D, lengths, None, "global", "minimize", True)
+    torch.cuda.synchronize()
+    ev[4].record(stream)
+    for _ in range(steps):
+        D, _, _ = product(-1.0, 1.0)
+        ag._forward_paths(D, lengths, None, "global", "minimize", True)
+    ev[5].record(stream)
+    torch.cuda.synchronize()
+    t_dtw = ev[4].elapsed_time(ev[5]) / 1000 / steps
+    dsc, drep = ag.path_scores_f64(D, lengths, locality="global", direction="minimize", dtw=True)
+    derr = float(((dsc.double() - drep).abs() / drep.abs()).max())
+    status = ag.tensor_core_status()
+    tiles = float((((lt + 127) // 128) * ((ls + 127) // 128)).sum())
+    return {
+        "value": cells / t_all / 1e9, "unit": "GCUPS",
+        "workload": f"{pairs} pairs, L~U[32,{n}], d={d}, cos on the tensor cores, global Gotoh 0.5/0.1 (FP32 DP)",
+        "product": {"ms": t_gemm * 1e3, "tflops": 2.0 * d * cells / t_gemm / 1e12,
+                    "tile_tflops": 2.0 * d * tiles * 128 * 128 / t_gemm / 1e12,
+                    "out_gbs": 4.0 * cells / t_gemm / 1e9, "status": status},
+        "dp_gcups": cells / t_dp / 1e9, "dp_ms": t_dp * 1e3, "total_ms": t_all * 1e3,
+        "error_vs_fp64_replay": {"max_rel_score": err_score, "max_rel_terms": err_scale},
+        "dtw": {"value": cells / t_dtw / 1e9, "unit": "GCUPS", "ms": t_dtw * 1e3,
+                "error_vs_fp64_replay": {"max_rel_score": derr},
+                "workload": "DTW (minimize) on 1 - cos of the same pairs, distance from the product's epilogue"},
+    }
+
+
 # --------------------------------------------------------------------------- arms
 
 def run_reference(args):
@@ -640,6 +718,7 @@ def run_ours(args):
 
     fb = fwd_bwd(torch, args.fwd_bwd_pairs, args.seed + 5) if args.fwd_bwd_pairs > 0 else None
     others = other_configs(torch, alg, L, args.seed + 7) if args.other_configs else None
+    prec = precision_config(torch, args.precision_pairs, args.seed + 2) if args.precision_pairs > 0 else None
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -664,6 +743,7 @@ def run_ours(args):
         "plain_gpu": plain,
         "fwd_bwd": fb,
         "other_configs": others,
+        "precision": prec,
         "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms)},
         "clocks": clocks.summary(),
     }

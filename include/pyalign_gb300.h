@@ -108,8 +108,10 @@ void pa_solver_destroy(pa_solver *solver);
 /* Replaces Solver::batch_size (factory.h:422, pyalign.h:25). */
 int32_t pa_solver_batch_size(const pa_solver *solver);
 
-/* Run the solver's device work on `stream` (a cudaStream_t; NULL = the solver's own
- * non-blocking stream). */
+/* Run the solver's device work on `stream`, a cudaStream_t; NULL is CUDA's default stream,
+ * as for a kernel launch, so work on it is ordered with the caller's work on that stream.
+ * Until this is called the solver uses a non-blocking stream of its own (its calls that
+ * return host results synchronise it before returning). */
 pa_status pa_solver_set_stream(pa_solver *solver, void *stream);
 
 /* ---- the 15 solve entry points (factory.h:424-507; pyalign.h:26-40) ----
@@ -289,6 +291,36 @@ pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normal
 pa_status pa_path_series_gradients(int64_t batch, const int32_t *paths, const int64_t *path_offsets,
                                    const int32_t *path_len, const float *grad_scores, const float *x,
                                    const float *y, int64_t n_s, int64_t n_t, float *dx, float *dy, void *stream);
+
+/* Similarity matrices of per-token embeddings on the tensor cores (tcgen05, BF16 operands,
+ * FP32 accumulation): St[k * pitch_pair + j * pitch_row + i] = beta + alpha * <Et[k, j],
+ * Es[k, i]> (one rounding; alpha = 1, beta = 0 for the similarity itself, alpha = -1,
+ * beta = 1 for the distance 1 - cos) for j < len_t[k], i < len_s[k]; other elements are not
+ * written.  Es (batch, n_s, dim) and
+ * Et (batch, n_t, dim) are row-major BF16 (16-byte aligned, dim a multiple of 16);
+ * tile_start (batch + 1) holds the prefix sums of ceil(len_t / 128) * ceil(len_s / 128)
+ * and total_tiles its last entry.  The dense similarity of MatrixForm problems
+ * (pyalign/solve.py:342-379, factory.h:573-576), written transposed (S^T) so the DP reads it
+ * with stride 1 along s; the oracle is a float64 product.  len_s, len_t, tile_start, St and
+ * status are device memory; a wait that times out ORs 2 into *status.  Allocates nothing;
+ * runs on `stream`. */
+pa_status pa_similarity_bf16(const void *Es, const void *Et, int64_t batch, int64_t n_s, int64_t n_t, int32_t dim,
+                             const int32_t *len_s, const int32_t *len_t, const int32_t *tile_start,
+                             int64_t total_tiles, float *St, int64_t pitch_pair, int64_t pitch_row, float alpha,
+                             float beta, int32_t *status, void *stream);
+
+/* Score of each pair's recovered path re-evaluated in FP64: the similarities of its aligned
+ * cells (every visited cell for DTW) plus or minus its gap costs w(k) = open + extend (k - 1),
+ * border gaps of global paths included -- the float64 restatement of the score that the
+ * float32 DP accumulated along the same path.  paths as from pa_solve_dense_paths (device);
+ * sim read as sim[sim_offsets[k] + u * stride_s + v * stride_t]; gaps[4] = open_s, extend_s,
+ * open_t, extend_t (host).  scale (device, may be NULL) receives the magnitude of the terms
+ * the score sums -- sum |S| over those cells plus the path's total gap cost -- the natural
+ * denominator of an error for scores near zero.  Allocates nothing; runs on `stream`. */
+pa_status pa_path_scores_f64(int32_t type, int32_t locality, int32_t direction, int64_t batch, const int32_t *paths,
+                             const int64_t *path_offsets, const int32_t *path_len, const float *sim,
+                             const int64_t *sim_offsets, int64_t stride_s, int64_t stride_t, const double *gaps,
+                             double *scores, double *scale, void *stream);
 
 /* Device time of the phases of the last solve on this solver, in milliseconds
  * (0: upload, 1: DP kernels, 2: traceback kernels, 3: download), and the number of

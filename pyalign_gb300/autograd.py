@@ -75,8 +75,110 @@ def _lib():
         L.pa_normalize_rows_bf16.argtypes = [vp, i64, i32, i32, vp, vp, vp]
         L.pa_path_series_gradients.restype = i32
         L.pa_path_series_gradients.argtypes = [i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp]
+        L.pa_similarity_bf16.restype = i32
+        f32 = ctypes.c_float
+        L.pa_similarity_bf16.argtypes = [vp, vp, i64, i64, i64, i32, vp, vp, vp, i64, vp, i64, i64, f32, f32, vp, vp]
+        L.pa_path_scores_f64.restype = i32
+        L.pa_path_scores_f64.argtypes = [i32, i32, i32, i64, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp, vp]
         L._pa_grad_bound = True
     return L
+
+
+_STATUS = {}
+
+
+def _status(device):
+    st = _STATUS.get(device)
+    if st is None:
+        st = torch.zeros(1, dtype=torch.int32, device=device)
+        _STATUS[device] = st
+    return st
+
+
+def tensor_core_status(device=None):
+    """Error bits the tensor-core similarity kernel raised since the last call (2: a wait
+    for the tensor cores timed out); reading synchronises the device and clears them."""
+    st = _status(torch.device(device or "cuda", torch.cuda.current_device()))
+    v = int(st.item())
+    st.zero_()
+    return v
+
+
+def _lengths(lengths, B):
+    ln = np.ascontiguousarray(np.asarray(lengths).reshape(B, 2).T, dtype=np.int32)
+    return ln
+
+
+def similarity_bf16(Esb, Etb, lengths, out=None, alpha=1.0, beta=0.0):
+    """S = beta + alpha <Es[i], Et[j]> per pair from BF16 factors (batch, n, dim), on the
+    tensor cores (pa_similarity_bf16), FP32 accumulation (alpha = -1, beta = 1 gives the
+    distance 1 - cos).  Only the cells inside each pair's lengths are written: the rest of
+    `out` (a fresh torch.empty by default) is left as it was.  Returns S as a
+    (batch, n_s, n_t) transposed view of S^T, stride 1 along s."""
+    B, n_s, dim = Esb.shape
+    n_t = Etb.shape[1]
+    if Esb.dtype != torch.bfloat16 or Etb.dtype != torch.bfloat16 or not Esb.is_contiguous() \
+            or not Etb.is_contiguous() or Etb.shape[0] != B or Etb.shape[2] != dim:
+        raise ValueError("Es, Et must be contiguous BF16 (batch, n, dim) tensors of one batch and dim")
+    if dim % 16:
+        raise ValueError("dim must be a multiple of 16")
+    ln = _lengths(lengths, B)
+    if (ln[0] > n_s).any() or (ln[1] > n_t).any() or (ln < 0).any():
+        raise ValueError("lengths exceed the embeddings")
+    tiles = ((ln[1].astype(np.int64) + 127) // 128) * ((ln[0].astype(np.int64) + 127) // 128)
+    meta = np.zeros(3 * B + 1, np.int32)
+    meta[:B] = ln[0]
+    meta[B:2 * B] = ln[1]
+    meta[2 * B + 1:] = np.cumsum(tiles)
+    total = int(meta[-1])
+    dmeta = torch.from_numpy(meta).to(Esb.device, non_blocking=False)
+    if out is None:
+        out = torch.empty((B, n_t, n_s), dtype=torch.float32, device=Esb.device)
+    elif out.shape != (B, n_t, n_s) or out.dtype != torch.float32 or out.stride(2) != 1 or not out.is_cuda:
+        raise ValueError("out must be a (batch, n_t, n_s) float32 CUDA tensor with unit stride along s")
+    st = _status(Esb.device)
+    _alg.check(_lib().pa_similarity_bf16(
+        Esb.data_ptr(), Etb.data_ptr(), B, n_s, n_t, dim, dmeta.data_ptr(), dmeta.data_ptr() + 4 * B,
+        dmeta.data_ptr() + 8 * B, total, out.data_ptr(), out.stride(0), out.stride(1), float(alpha), float(beta),
+        st.data_ptr(),
+        torch.cuda.current_stream().cuda_stream))
+    return out.transpose(1, 2)
+
+
+def _pad16(E):
+    d = E.shape[-1]
+    return E if d % 16 == 0 else torch.nn.functional.pad(E, (0, 16 - d % 16))
+
+
+def path_scores_f64(S, lengths, gap_open=None, gap_extend=None, locality="global", direction="maximize",
+                    dtw=False, with_scale=False):
+    """The optimal scores of the float32 DP and, for the same recovered paths, their scores
+    re-evaluated in FP64 on the GPU (pa_path_scores_f64): (scores float32, replay float64),
+    plus with_scale the magnitude of the summed terms (sum |S| + gap costs) per path.  The
+    distance between the two scores is the DP's float32 accumulation error."""
+    linear = gap_extend is None
+    gap = None if dtw else ((float(gap_open), None) if linear else (float(gap_open), float(gap_extend)))
+    if S.stride(1) != 1 and S.stride(2) != 1:
+        S = S.contiguous()
+    scores, paths, plen, poff, _ = _forward_paths(S, lengths, gap, locality, direction, dtw)
+    B = S.shape[0]
+    A = _alg
+    if dtw:
+        g = None
+    elif linear:
+        g = np.array([gap[0], gap[0], gap[0], gap[0]], np.float64)
+    else:
+        g = np.array([gap[0], gap[1], gap[0], gap[1]], np.float64)
+    soff = torch.from_numpy(S.storage_offset() + np.arange(B, dtype=np.int64) * S.stride(0)).to(S.device)
+    base = S.data_ptr() - S.storage_offset() * S.element_size()
+    out = torch.empty(B, dtype=torch.float64, device=S.device)
+    scale = torch.empty(B, dtype=torch.float64, device=S.device) if with_scale else None
+    _alg.check(_lib().pa_path_scores_f64(
+        int(A.Type.DTW if dtw else A.Type.ALIGNMENT), int(A.Locality.__members__[locality.upper()]),
+        int(A.Direction.__members__[direction.upper()]), B, paths.data_ptr(), poff.data_ptr(), plen.data_ptr(),
+        base, soff.data_ptr(), S.stride(1), S.stride(2), None if g is None else g.ctypes.data, out.data_ptr(),
+        None if scale is None else scale.data_ptr(), torch.cuda.current_stream().cuda_stream))
+    return (scores, out, scale) if with_scale else (scores, out)
 
 
 def _forward_paths(S, lengths, gap, locality, direction, dtw):
@@ -182,14 +284,63 @@ def alignment_score(S, lengths, gap_open=None, gap_extend=None, locality="global
     return AlignmentScore.apply(S, lengths, go, ge, locality, direction, dtw, linear)
 
 
-def cosine_similarity_batch(Es, Et):
+def normalized_bf16(E, normalize=True):
+    """The BF16 factor of E (batch, n, d) for the similarity product -- E / |E| per row when
+    normalising -- and 1 / |E| per row, in one pass (pa_normalize_rows_bf16).  d is padded
+    with zeros to a multiple of 16 (the tensor-core K step)."""
+    E = _pad16(E.contiguous().float())
+    B, n, dim = E.shape
+    Eb = torch.empty(E.shape, dtype=torch.bfloat16, device=E.device)
+    inv = torch.empty(B * n, dtype=torch.float32, device=E.device)
+    _alg.check(_lib().pa_normalize_rows_bf16(E.data_ptr(), B * n, dim, int(normalize), Eb.data_ptr(),
+                                             inv.data_ptr(), torch.cuda.current_stream().cuda_stream))
+    return Eb, inv
+
+
+class CosineSimilarity(torch.autograd.Function):
+    """S = <en_s, en_t> with en = E / |E|, the product on the tensor cores.  Backward: the
+    dense route, dEn_s = dS en_t and dEn_t = dS^T en_s (the BF16 cast passes gradients
+    through), then the normalisation backward (g - (g . en) en) / |E|."""
+
+    @staticmethod
+    def forward(ctx, Es, Et, lengths):
+        B, n_s, d = Es.shape
+        n_t = Et.shape[1]
+        Esb, inv_s = normalized_bf16(Es)
+        Etb, inv_t = normalized_bf16(Et)
+        if lengths is None:
+            lengths = np.tile(np.array([[n_s, n_t]], np.int32), (B, 1))
+            out = None
+        else:
+            out = torch.zeros((B, n_t, n_s), dtype=torch.float32, device=Es.device)
+        ctx.save_for_backward(Esb, Etb, inv_s, inv_t)
+        ctx.d = d
+        return similarity_bf16(Esb, Etb, lengths, out=out)
+
+    @staticmethod
+    def backward(ctx, dS):
+        Esb, Etb, inv_s, inv_t = ctx.saved_tensors
+        B, n_s, dp = Esb.shape
+        n_t = Etb.shape[1]
+        en_s, en_t = Esb.float(), Etb.float()
+        g_s = torch.bmm(dS.float(), en_t)
+        g_t = torch.bmm(dS.float().transpose(1, 2), en_s)
+        inv_s = inv_s.view(B, n_s, 1)
+        inv_t = inv_t.view(B, n_t, 1)
+        # en here is the BF16 factor; the normalisation backward uses the exact en = E / |E|
+        # only through (g . en) en, where the BF16 rounding is below float32 noise of g
+        d_s = (g_s - (g_s * en_s).sum(-1, keepdim=True) * en_s) * inv_s
+        d_t = (g_t - (g_t * en_t).sum(-1, keepdim=True) * en_t) * inv_t
+        return d_s[..., :ctx.d], d_t[..., :ctx.d], None
+
+
+def cosine_similarity_batch(Es, Et, lengths=None):
     """S = cos(E_s, E_t) per pair: L2-normalised embeddings multiplied in BF16 with FP32
-    accumulation.  Es: (batch, len_s, d), Et: (batch, len_t, d).  Returned as a transposed
-    view of S^T (stride 1 along s), the layout the DP reads fastest."""
-    Es = torch.nn.functional.normalize(Es, dim=-1)
-    Et = torch.nn.functional.normalize(Et, dim=-1)
-    St = torch.bmm(Et.to(torch.bfloat16), Es.to(torch.bfloat16).transpose(1, 2)).float()
-    return St.transpose(1, 2)
+    accumulation on the tensor cores.  Es: (batch, len_s, d), Et: (batch, len_t, d);
+    lengths (batch, 2) limits the product to each pair's cells (the rest of S is zero).
+    Returned as a transposed view of S^T (stride 1 along s), the layout the DP reads
+    fastest.  Differentiable with respect to Es and Et."""
+    return CosineSimilarity.apply(Es, Et, lengths)
 
 
 class EmbeddingAlignmentScore(torch.autograd.Function):
@@ -201,26 +352,19 @@ class EmbeddingAlignmentScore(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, Es, Et, lengths, gap_open, gap_extend, locality, direction, linear, normalize):
-        Es = Es.contiguous().float()
-        Et = Et.contiguous().float()
-        B, n_s, dim = Es.shape
-        n_t = Et.shape[1]
-        L = _lib()
-        stream = torch.cuda.current_stream().cuda_stream
-        Esb = torch.empty(Es.shape, dtype=torch.bfloat16, device=Es.device)
-        Etb = torch.empty(Et.shape, dtype=torch.bfloat16, device=Et.device)
-        inv_s = torch.empty(B * n_s, dtype=torch.float32, device=Es.device)
-        inv_t = torch.empty(B * n_t, dtype=torch.float32, device=Et.device)
-        _alg.check(L.pa_normalize_rows_bf16(Es.data_ptr(), B * n_s, dim, int(normalize), Esb.data_ptr(),
-                                            inv_s.data_ptr(), stream))
-        _alg.check(L.pa_normalize_rows_bf16(Et.data_ptr(), B * n_t, dim, int(normalize), Etb.data_ptr(),
-                                            inv_t.data_ptr(), stream))
-        # S^T = en_t en_s^T; its transposed view is S with stride 1 along s
-        S = torch.bmm(Etb, Esb.transpose(1, 2)).float().transpose(1, 2)
+        dim_in = Es.shape[-1]
+        Es = _pad16(Es.contiguous().float())
+        Et = _pad16(Et.contiguous().float())
+        Esb, inv_s = normalized_bf16(Es, normalize)
+        Etb, inv_t = normalized_bf16(Et, normalize)
+        # S^T = en_t en_s^T on the tensor cores, only the cells inside the lengths; its
+        # transposed view is S with stride 1 along s
+        S = similarity_bf16(Esb, Etb, lengths)
         gap = (float(gap_open), None) if linear else (float(gap_open), float(gap_extend))
         scores, paths, plen, poff, _ = _forward_paths(S, lengths, gap, locality, direction, False)
         ctx.save_for_backward(Es, Et, Esb, Etb, inv_s, inv_t, paths, plen, poff)
         ctx.meta = (locality, direction, linear, normalize)
+        ctx.dim_in = dim_in
         return scores
 
     @staticmethod
@@ -230,6 +374,7 @@ class EmbeddingAlignmentScore(torch.autograd.Function):
         grad = grad.contiguous().float()
         B, n_s, dim = Es.shape
         n_t = Et.shape[1]
+        d_in = ctx.dim_in
         dEs = torch.zeros_like(Es)
         dEt = torch.zeros_like(Et)
         _alg.check(_lib().pa_path_embedding_gradients(
@@ -237,7 +382,7 @@ class EmbeddingAlignmentScore(torch.autograd.Function):
             Es.data_ptr(), Et.data_ptr(), Esb.data_ptr(), Etb.data_ptr(), inv_s.data_ptr(), inv_t.data_ptr(),
             n_s, n_t, dEs.data_ptr(), dEt.data_ptr(), torch.cuda.current_stream().cuda_stream))
         d_open, d_ext = _gap_grads(False, linear, locality, direction, B, paths, plen, poff, grad)
-        return dEs, dEt, None, d_open, d_ext, None, None, None, None
+        return dEs[..., :d_in], dEt[..., :d_in], None, d_open, d_ext, None, None, None, None
 
 
 def embedding_alignment_score(Es, Et, lengths, gap_open, gap_extend=None, locality="global",

@@ -37,7 +37,12 @@ namespace pa {
 enum GapKind { GAP_LINEAR = 0, GAP_AFFINE = 1, GAP_DTW = 2, GAP_GENERAL = 3 };
 enum LocKind { LOC_LOCAL = 0, LOC_GLOBAL = 1, LOC_SEMI = 2 };
 enum TbKind { TB_NONE = 0, TB_ONE = 1, TB_ALL = 2 };
-enum SubKind { SUB_TABLE = 0, SUB_BINARY = 1, SUB_DENSE = 2, SUB_PROFILE = 3 };
+enum SubKind { SUB_TABLE = 0, SUB_BINARY = 1, SUB_DENSE = 2, SUB_PROFILE = 3, SUB_COLPROF = 4 };
+
+// SUB_COLPROF: per thread and letter c, the int8 scores of the thread's R rows against c,
+// kept in shared memory after the table as colprof[c * BLOCK + thread] (8 bytes): one
+// conflict-free 64-bit load per step replaces R table lookups (alphabets up to 32 letters).
+constexpr int MAX_COLPROF = 32;
 
 constexpr int R = 8;              // rows per lane
 constexpr int BLOCK = 128;        // threads per block
@@ -232,6 +237,8 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 	}
 	__syncthreads();
 	const V *tab = table_in_smem ? stab : p.table;
+	uint2 *colprof = reinterpret_cast<uint2 *>(
+	    smem_raw + ((size_t(table_in_smem ? p.table_rows * p.table_cols : 0) * sizeof(V) + 15) & ~size_t(15)));
 
 	const int G = p.G;
 	const int lane = threadIdx.x & 31;
@@ -344,7 +351,19 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 				qa[r] = (pass_active && i < ls && arow) ? arow[i] : 0u;
 				plo[r] = phi[r] = 0u;
 			}
-			if (sub_kind == SUB_PROFILE) {
+			if (sub_kind == SUB_COLPROF) {
+				const int cols = p.table_cols;
+				for (int c = 0; c < cols; c++) {
+					uint32_t lo = 0, hi = 0;
+#pragma unroll
+					for (int r = 0; r < R; r++) {
+						const uint32_t byte = uint32_t(int32_t(tab[qa[r] * cols + c])) & 0xffu;
+						if (r < 4) lo |= byte << (8 * r);
+						else hi |= byte << (8 * (r - 4));
+					}
+					colprof[c * BLOCK + threadIdx.x] = make_uint2(lo, hi);
+				}
+			} else if (sub_kind == SUB_PROFILE) {
 				const int cols = p.table_cols;
 #pragma unroll
 				for (int r = 0; r < R; r++) {
@@ -409,7 +428,11 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 				if (act) {
 					// substitution values of the R rows at column j
 					V S[R];
-					if (sub_kind == SUB_PROFILE) {
+					if (sub_kind == SUB_COLPROF) {
+						const uint2 pr = colprof[tcode * BLOCK + threadIdx.x];
+#pragma unroll
+						for (int r = 0; r < R; r++) S[r] = V(prmt(pr.x, pr.y, sext_selector(uint32_t(r))));
+					} else if (sub_kind == SUB_PROFILE) {
 						const uint32_t sel = sext_selector(tcode);
 #pragma unroll
 						for (int r = 0; r < R; r++) S[r] = V(prmt(plo[r], phi[r], sel));

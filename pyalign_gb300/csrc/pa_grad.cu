@@ -254,3 +254,92 @@ extern "C" pa_status pa_path_series_gradients(int64_t batch, const int32_t *path
 	path_series_grad_kernel<<<int((batch + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
 }
+
+// ---------------------------------------------------------------------------------------
+// FP64 replay of a recovered path's score.  The float32 DP accumulates its score in float32
+// along the path; for long alignments that sum drifts from the exact value.  Re-evaluating
+// the same path in float64 -- aligned cells' similarities (every visited cell for DTW), gap
+// runs as w(k) = open + extend (k - 1), border gaps of global paths as in the backward
+// above -- gives the float64 score of that path, and its distance to the DP's score is the
+// DP's accumulation error.
+
+namespace {
+
+struct ReplayParams {
+	int64_t batch;
+	int32_t dtw, global;
+	double gap_sign;  // -1 maximize, +1 minimize
+	const int32_t *paths;
+	const int64_t *path_off;
+	const int32_t *path_len;
+	const float *sim;
+	const int64_t *sim_off;
+	int64_t ss, st;
+	double open_s, ext_s, open_t, ext_t;
+	double *out;
+	double *scale;
+};
+
+__global__ void path_replay_f64_kernel(ReplayParams p) {
+	const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (k >= p.batch) return;
+	const int n = p.path_len[k];
+	const int32_t *P = p.paths + p.path_off[k];
+	const float *S = p.sim + p.sim_off[k];
+	double sum = 0.0, gaps = 0.0, mag = 0.0;
+	for (int q = 0; q + 1 < n; q++) {
+		const int u0 = P[2 * q], v0 = P[2 * q + 1], u1 = P[2 * q + 2], v1 = P[2 * q + 3];
+		if (u0 < 0 || v0 < 0) break;
+		if (p.dtw || (u1 == u0 - 1 && v1 == v0 - 1)) {
+			const double x = double(S[int64_t(u0) * p.ss + int64_t(v0) * p.st]);
+			sum += x;
+			mag += fabs(x);
+		} else if (v1 == v0 && u1 < u0) {
+			gaps += p.open_s + p.ext_s * double(u0 - u1 - 1);
+		} else if (u1 == u0 && v1 < v0) {
+			gaps += p.open_t + p.ext_t * double(v0 - v1 - 1);
+		}
+	}
+	if (n > 0 && p.global && !p.dtw) {
+		const int ul = P[2 * (n - 1)], vl = P[2 * (n - 1) + 1];
+		if (ul < 0 && vl >= 0) gaps += p.open_t + p.ext_t * double(vl);
+		else if (vl < 0 && ul >= 0) gaps += p.open_s + p.ext_s * double(ul);
+	}
+	p.out[k] = n > 0 ? sum + p.gap_sign * gaps : 0.0;
+	if (p.scale) p.scale[k] = mag + fabs(gaps);
+}
+
+}  // namespace
+
+extern "C" pa_status pa_path_scores_f64(int32_t type, int32_t locality, int32_t direction, int64_t batch,
+                                        const int32_t *paths, const int64_t *path_offsets, const int32_t *path_len,
+                                        const float *sim, const int64_t *sim_offsets, int64_t stride_s,
+                                        int64_t stride_t, const double *gaps, double *scores, double *scale,
+                                        void *stream) {
+	if (batch < 0 || !paths || !path_offsets || !path_len || !sim || !sim_offsets || !scores ||
+	    (type != PA_TYPE_DTW && !gaps))
+		return PA_ERR_INVALID_ARGUMENT;
+	if (batch == 0) return PA_OK;
+	ReplayParams p{};
+	p.batch = batch;
+	p.dtw = type == PA_TYPE_DTW;
+	p.global = type == PA_TYPE_DTW || locality == PA_GLOBAL;
+	p.gap_sign = direction == PA_MINIMIZE ? 1.0 : -1.0;
+	p.paths = paths;
+	p.path_off = path_offsets;
+	p.path_len = path_len;
+	p.sim = sim;
+	p.sim_off = sim_offsets;
+	p.ss = stride_s;
+	p.st = stride_t;
+	if (gaps) {
+		p.open_s = gaps[0];
+		p.ext_s = gaps[1];
+		p.open_t = gaps[2];
+		p.ext_t = gaps[3];
+	}
+	p.out = scores;
+	p.scale = scale;
+	path_replay_f64_kernel<<<int((batch + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}

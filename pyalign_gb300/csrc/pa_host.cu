@@ -298,6 +298,7 @@ struct pa_solver {
 	int sm_count = 0;
 	cudaStream_t own_stream = nullptr;
 	cudaStream_t stream = nullptr;
+	bool stream_set = false;  // pa_solver_set_stream was called (stream may be NULL then)
 	cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 	float last_ms[4] = {0, 0, 0, 0};
 	int32_t last_launches = 0;
@@ -349,7 +350,7 @@ pa_status ensure_device(pa_solver *s) {
 	PA_CUDA(cudaGetDevice(&s->device));
 	PA_CUDA(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
 	PA_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
-	if (!s->stream) s->stream = s->own_stream;
+	if (!s->stream_set) s->stream = s->own_stream;
 	for (auto &e : s->ev) PA_CUDA(cudaEventCreate(&e));
 	PA_CUDA(cudaEventCreateWithFlags(&s->meta_ev, cudaEventDisableTiming));
 	return PA_OK;
@@ -574,8 +575,16 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 				tabv[k] = cvt<V>(host_table[k] * s->sign, ISINT, scale, diag_tag);
 				if (ISINT && (int64_t(tabv[k]) < -128 || int64_t(tabv[k]) > 127)) fits_int8 = false;
 			}
-			// an int8 query profile read with one prmt per cell (alphabets of <= 8 letters)
+			// int8 profiles read with one prmt per cell: per row in registers (alphabets of
+			// <= 8 letters) or per letter in shared memory (<= 32 letters)
+			bool colprof_ok = ISINT && tag && in.table_cols <= MAX_COLPROF && in.table_rows <= MAX_SMEM_TABLE;
+			for (size_t k = 0; k < nt_ && colprof_ok; k++)
+				if (int64_t(tabv[k]) < -128 || int64_t(tabv[k]) > 127) colprof_ok = false;
+			const char *sk = std::getenv("PA_SUBST");  // experiments: "table", "colprof"
 			if (fits_int8) p.sub_kind = SUB_PROFILE;
+			else if (colprof_ok) p.sub_kind = SUB_COLPROF;
+			if (sk && std::strcmp(sk, "table") == 0) p.sub_kind = SUB_TABLE;
+			if (sk && std::strcmp(sk, "colprof") == 0 && colprof_ok) p.sub_kind = SUB_COLPROF;
 			PA_CUDA(s->d_tab.ensure(nt_ * sizeof(V)));
 			PA_CUDA(pa_copy(s, s->d_tab.p, tabv, nt_ * sizeof(V), cudaMemcpyHostToDevice, st));
 			p.table = s->d_tab.as<V>();
@@ -594,9 +603,10 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.status = s->d_status.as<int32_t>();
 
 	// ---- grid and scratch
-	const size_t smem = (in.form == F_INDEXED && in.table_rows <= MAX_SMEM_TABLE && in.table_cols <= MAX_SMEM_TABLE)
-	                        ? size_t(in.table_rows * in.table_cols) * sizeof(V)
-	                        : 0;
+	size_t smem = (in.form == F_INDEXED && in.table_rows <= MAX_SMEM_TABLE && in.table_cols <= MAX_SMEM_TABLE)
+	                  ? size_t(in.table_rows * in.table_cols) * sizeof(V)
+	                  : 0;
+	if (p.sub_kind == SUB_COLPROF) smem = ((smem + 15) & ~size_t(15)) + size_t(in.table_cols) * BLOCK * 8;
 	int bps = 0;
 	cudaError_t e = cudaSuccess;
 	const int loc = s->loc;
@@ -1342,7 +1352,8 @@ int32_t pa_solver_batch_size(const pa_solver *s) { return s ? s->batch_size : 0;
 pa_status pa_solver_set_stream(pa_solver *s, void *stream) {
 	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
 	if (pa_status st = ensure_device(s)) return st;
-	s->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : s->own_stream;
+	s->stream = reinterpret_cast<cudaStream_t>(stream);  // NULL: CUDA's default stream
+	s->stream_set = true;
 	return PA_OK;
 }
 

@@ -1,0 +1,254 @@
+// Ragged batched similarity product on the 5th-generation tensor cores (sm_103a):
+//   St[k][j][i] = beta + alpha * <Et[k][j], Es[k][i]>   for j < len_t[k], i < len_s[k]
+// BF16 operands, FP32 accumulation in tensor memory.  This is the similarity matrix of
+// per-token embeddings that the dense (MatrixForm) alignment problems read, written as S^T
+// so that the DP kernel reads it with stride 1 along s.
+//
+// One CTA of 128 threads computes a 128 x 128 tile of one pair at a time (persistent grid,
+// tiles numbered pair by pair through tile_start).  Per K chunk of up to 128 elements the
+// threads copy both operand tiles into shared memory in the canonical K-major layout without
+// swizzle -- 8-row x 16-byte core matrices, 128 bytes apart along K (leading byte offset)
+// and (K chunk / 8) * 128 bytes apart along M/N (stride byte offset) -- and one thread
+// issues K/16 tcgen05.mma (M = 128, N = 128, K = 16) into a 128-column TMEM accumulator and
+// commits them to an mbarrier.  The four warps then read their 32 TMEM lanes (tile rows)
+// with tcgen05.ld and store the rows that fall inside the pair.  Three CTAs share an SM
+// (64 KB of operands each, 3 x 128 of the 512 TMEM columns), so one CTA's copies overlap
+// another's MMAs and epilogue.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "../../include/pyalign_gb300.h"
+
+namespace {
+
+constexpr int TM = 128;           // tile rows (t positions): MMA M, TMEM lanes
+constexpr int TN = 128;           // tile columns (s positions): MMA N, TMEM columns
+constexpr int KC = 128;           // K elements staged per chunk
+constexpr int THREADS = 128;
+constexpr int OPBYTES = TM * KC * 2;             // one operand tile: 32 KB
+constexpr int SMEM_BYTES = 2 * OPBYTES + 1024;   // operands + barrier/TMEM slot, 1 KB aligned
+constexpr int ST_TIMEOUT = 2;
+
+struct SimParams {
+	const __nv_bfloat16 *Es;  // (batch, n_s, dim)
+	const __nv_bfloat16 *Et;  // (batch, n_t, dim)
+	int64_t n_s, n_t;
+	int32_t dim;
+	const int32_t *len_s, *len_t;  // device
+	const int32_t *tile_start;     // device, batch + 1
+	int64_t batch, total_tiles;
+	float *St;
+	int64_t pitch_pair, pitch_row;
+	float alpha, beta;  // epilogue: beta + alpha * dot (1 - cos for DTW distances)
+	int32_t *status;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+	return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: start, leading and stride byte offsets (all >> 4),
+// descriptor version 1 at bit 46, no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+	return uint64_t((addr >> 4) & 0x3fff) | (uint64_t((lbo >> 4) & 0x3fff) << 16) |
+	       (uint64_t((sbo >> 4) & 0x3fff) << 32) | (uint64_t(1) << 46);
+}
+
+// Instruction descriptor of kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9,
+// 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(TN >> 3) << 17) | (uint32_t(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\t"
+	    "setp.ne.b32 p, %4, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+	    "l"(da), "l"(db), "r"(IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// Bounded wait for the mbarrier phase with the given parity: false after about two seconds.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+	const long long t0 = clock64();
+	for (;;) {
+		uint32_t done;
+		asm volatile(
+		    "{\n\t.reg .pred p;\n\t"
+		    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		    "selp.u32 %0, 1, 0, p;\n\t}\n"
+		    : "=r"(done)
+		    : "r"(bar), "r"(parity)
+		    : "memory");
+		if (done) return true;
+		if (clock64() - t0 > (1ll << 32)) return false;
+	}
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+	asm volatile(
+	    "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+	    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+	    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+	    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+	      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+	      "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+	      "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+	    : "r"(taddr));
+	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Copy rows [r0, r0 + 128) x K elements [kc, kc + kw) of X (rows of `dim` BF16, `rows`
+// valid, zero beyond) into the canonical K-major layout: 16-byte piece (r, c) at
+// (r / 8) * (kw / 8) * 128 + c * 128 + (r % 8) * 16.  Eight consecutive threads fill one
+// 128-byte core matrix.
+__device__ __forceinline__ void stage(unsigned char *dst, const __nv_bfloat16 *X, int64_t r0, int64_t rows, int dim,
+                                      int kc, int kw) {
+	const int nkc = kw >> 3;
+	const int pieces = TM * nkc;
+	for (int c = threadIdx.x; c < pieces; c += THREADS) {
+		const int r8 = c & 7, rest = c >> 3;
+		const int kq = rest % nkc, g = rest / nkc;
+		const int r = g * 8 + r8;
+		uint4 v = make_uint4(0, 0, 0, 0);
+		if (r0 + r < rows) v = *reinterpret_cast<const uint4 *>(X + (r0 + r) * int64_t(dim) + kc + kq * 8);
+		*reinterpret_cast<uint4 *>(dst + (g * nkc + kq) * 128 + r8 * 16) = v;
+	}
+}
+
+__global__ void __launch_bounds__(THREADS, 1) sim_bf16_kernel(SimParams p) {
+	extern __shared__ __align__(1024) unsigned char smem[];
+	unsigned char *sA = smem;
+	unsigned char *sB = smem + OPBYTES;
+	uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * OPBYTES);
+	uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + 2 * OPBYTES + 16);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+		             "r"(TN)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	if (threadIdx.x == 0) {
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = *tslot;
+	const uint32_t bar_a = smem_addr(bar);
+	uint32_t phase = 0;
+	bool ok = true;
+
+	for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+		// the pair of tile t: the last k with tile_start[k] <= t
+		int64_t lo = 0, hi = p.batch - 1;
+		while (lo < hi) {
+			const int64_t mid = (lo + hi + 1) >> 1;
+			if (p.tile_start[mid] <= t) lo = mid;
+			else hi = mid - 1;
+		}
+		const int64_t k = lo;
+		const int64_t ls = p.len_s[k], lt = p.len_t[k];
+		const int64_t tiles_n = (ls + TN - 1) / TN;
+		const int64_t local = t - p.tile_start[k];
+		const int64_t m0 = (local / tiles_n) * TM, n0 = (local % tiles_n) * TN;
+		const __nv_bfloat16 *A = p.Et + k * p.n_t * p.dim;
+		const __nv_bfloat16 *B = p.Es + k * p.n_s * p.dim;
+
+		for (int kc = 0; kc < p.dim && ok; kc += KC) {
+			const int kw = min(KC, p.dim - kc);
+			stage(sA, A, m0, lt, p.dim, kc, kw);
+			stage(sB, B, n0, ls, p.dim, kc, kw);
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+			__syncthreads();
+			if (threadIdx.x == 0) {
+				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				const uint32_t sbo = uint32_t(kw >> 3) * 128u;
+				for (int kk = 0; kk < kw / 16; kk++) {
+					const uint64_t da = smem_desc(smem_addr(sA) + kk * 256, 128, sbo);
+					const uint64_t db = smem_desc(smem_addr(sB) + kk * 256, 128, sbo);
+					mma_bf16(tmem, da, db, (kc > 0 || kk > 0) ? 1u : 0u);
+				}
+				mma_commit(bar_a);
+			}
+			// every thread takes the same decision, so the barriers below stay matched
+			if (!__syncthreads_and(mbar_wait(bar_a, phase) ? 1 : 0)) {
+				if (threadIdx.x == 0) atomicOr(p.status, ST_TIMEOUT);
+				ok = false;
+			}
+			phase ^= 1u;
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+		}
+		if (ok) {
+			// epilogue: warp w holds tile rows 32w..32w+31 (TMEM lanes), one row per thread
+			const int64_t j = m0 + warp * 32 + lane;
+			float *row = p.St + k * p.pitch_pair + j * p.pitch_row + n0;
+			const int64_t ncols = ls - n0;  // valid columns of this tile (> 0)
+			for (int cc = 0; cc < TN; cc += 32) {
+				uint32_t v[32];
+				tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(cc), v);
+				if (j < lt) {
+#pragma unroll
+					for (int q = 0; q < 32; q++)
+						if (cc + q < ncols) row[cc + q] = __fmaf_rn(p.alpha, __uint_as_float(v[q]), p.beta);
+				}
+			}
+		}
+		asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+		__syncthreads();
+	}
+	__syncthreads();
+	if (warp == 0) {
+		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TN) : "memory");
+	}
+}
+
+}  // namespace
+
+extern "C" pa_status pa_similarity_bf16(const void *Es, const void *Et, int64_t batch, int64_t n_s, int64_t n_t,
+                                        int32_t dim, const int32_t *len_s, const int32_t *len_t,
+                                        const int32_t *tile_start, int64_t total_tiles, float *St,
+                                        int64_t pitch_pair, int64_t pitch_row, float alpha, float beta,
+                                        int32_t *status, void *stream) {
+	if (batch < 0 || n_s < 0 || n_t < 0 || total_tiles < 0) return PA_ERR_INVALID_ARGUMENT;
+	if (batch == 0 || total_tiles == 0) return PA_OK;
+	if (!Es || !Et || !len_s || !len_t || !tile_start || !St || !status) return PA_ERR_INVALID_ARGUMENT;
+	if (dim <= 0 || dim % 16 != 0) return PA_ERR_INVALID_ARGUMENT;  // K steps of 16, 16-byte rows
+	if ((reinterpret_cast<uintptr_t>(Es) | reinterpret_cast<uintptr_t>(Et)) & 15) return PA_ERR_INVALID_ARGUMENT;
+	int dev = 0, sms = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return PA_ERR_NO_DEVICE;
+	if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return PA_ERR_CUDA;
+	static bool attr_set[64] = {};
+	if (dev < 64 && !attr_set[dev]) {
+		if (cudaFuncSetAttribute(sim_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
+		    cudaSuccess)
+			return PA_ERR_CUDA;
+		attr_set[dev] = true;
+	}
+	SimParams p;
+	p.Es = static_cast<const __nv_bfloat16 *>(Es);
+	p.Et = static_cast<const __nv_bfloat16 *>(Et);
+	p.n_s = n_s;
+	p.n_t = n_t;
+	p.dim = dim;
+	p.len_s = len_s;
+	p.len_t = len_t;
+	p.tile_start = tile_start;
+	p.batch = batch;
+	p.total_tiles = total_tiles;
+	p.St = St;
+	p.pitch_pair = pitch_pair;
+	p.pitch_row = pitch_row;
+	p.alpha = alpha;
+	p.beta = beta;
+	p.status = status;
+	const int64_t grid = total_tiles < int64_t(3) * sms ? total_tiles : int64_t(3) * sms;
+	sim_bf16_kernel<<<int(grid), THREADS, SMEM_BYTES, static_cast<cudaStream_t>(stream)>>>(p);
+	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}

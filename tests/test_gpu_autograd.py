@@ -213,9 +213,10 @@ def test_fused_embedding_gradients_match_dense_route(torch_ag):
         sc = ag.embedding_alignment_score(a, b, lengths, go, ge, locality, normalize=False)
         sc.sum().backward()
         Eb, Fb = Es.to(torch.bfloat16).float(), Et.to(torch.bfloat16).float()
-        # the same BF16 product (FP32 accumulation) as the fused forward
-        S = torch.bmm(Et.to(torch.bfloat16), Es.to(torch.bfloat16).transpose(1, 2)).float()
-        S = S.transpose(1, 2).contiguous().requires_grad_(True)
+        # the same BF16 tensor-core product (FP32 accumulation) as the fused forward
+        St0 = torch.zeros((B, nt, ns), dtype=torch.float32, device="cuda")
+        S = ag.similarity_bf16(Es.to(torch.bfloat16), Et.to(torch.bfloat16), lengths, out=St0)
+        S = S.contiguous().requires_grad_(True)
         go2 = torch.tensor(0.5, requires_grad=True)
         ge2 = torch.tensor(0.1, requires_grad=True)
         sc2 = ag.alignment_score(S, lengths, go2, ge2, locality)
@@ -265,7 +266,8 @@ def test_fused_cosine_gradients_match_torch_normalize(torch_ag):
     b2 = Et.clone().requires_grad_(True)
     en_s = torch.nn.functional.normalize(a2, dim=-1)
     en_t = torch.nn.functional.normalize(b2, dim=-1)
-    S = torch.bmm(en_t.to(torch.bfloat16), en_s.to(torch.bfloat16).transpose(1, 2)).float().transpose(1, 2)
+    # the float32 product of the BF16 factors (the tensor-core kernel keeps FP32 outputs)
+    S = torch.bmm(en_t.to(torch.bfloat16).float(), en_s.to(torch.bfloat16).float().transpose(1, 2)).transpose(1, 2)
     sc2 = ag.alignment_score(S, lengths, 0.5, 0.1, "global")
     sc2.sum().backward()
     assert torch.allclose(sc, sc2, atol=1e-4)

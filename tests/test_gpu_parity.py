@@ -227,3 +227,28 @@ def test_bag_at_once_batch_form(gpu_alg, oracle_alg):
         assert scores[k] == ref[k].score, k
         want = ref[k].s_to_t if ln[0, k] <= ln[1, k] else ref[k].t_to_s
         assert np.array_equal(maps[offs[k]:offs[k] + sizes[k]], want), k
+
+
+@pytest.mark.parametrize("subst", ["profile", "table"])
+@pytest.mark.parametrize("gap", ["linear", "affine"])
+@pytest.mark.parametrize("locality", ["local", "global", "semiglobal"])
+def test_twenty_letter_table(gpu_alg, oracle_alg, monkeypatch, subst, gap, locality):
+    """A 20-letter integer table: read through the per-letter int8 profile in shared memory
+    (the default for integer tables of up to 32 letters) and through plain table lookups."""
+    if subst == "table":
+        monkeypatch.setenv("PA_SUBST", "table")
+    rng = np.random.default_rng(zlib.crc32(f"twenty/{gap}/{locality}".encode()))
+    m = rng.integers(-4, 3, size=(20, 20))
+    m = np.triu(m, 1) + np.triu(m, 1).T
+    np.fill_diagonal(m, rng.integers(4, 12, size=20))
+    table = m.astype(np.float32)
+    pairs = random_pairs(rng, 12, 0, 300, alphabet=20, related=0.6)
+    for method, count in (("alignment", "one"), ("score", "one"), ("alignment_iterator", "all")):
+        opts = options(gpu_alg, locality=locality, detail="score" if method == "score" else "alignment",
+                       count=count, gap=GAPS[gap])
+        d = _run_both(gpu_alg, oracle_alg, opts, method, "indexed", pairs, table=table, iter_cap=20)
+        assert d is None, f"{method}: {d}"
+        mopts = options(gpu_alg, locality=locality, direction="minimize",
+                        detail="score" if method == "score" else "alignment", count=count, gap=GAPS[gap])
+        d = _run_both(gpu_alg, oracle_alg, mopts, method, "indexed", pairs, table=-table, iter_cap=20)
+        assert d is None, f"minimize {method}: {d}"
