@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <stack>
 #include <string>
@@ -801,6 +802,102 @@ pa_status download_wsb(pa_solver *s, ResultData &res) {
 	return PA_OK;
 }
 
+// ---------------------------------------------------------------------------------------
+// Autotuner.  A DP launch runs in group mode with G = 4, 8, 16 or 32 lanes per pair or in
+// the stripe-chained mode; which is fastest depends on how many pairs there are and how
+// long they are (measured on GB300: 12,288 pairs of lengths in [100, 1000] run 1.8x faster
+// with G = 16 than with G = 8, 65,536 such pairs run fastest with G = 8, 256 pairs of
+// 5000 x 10000 4x faster chained).  The first call with a new workload signature -- pair
+// count, mean and largest lengths in half-octave/octave buckets, gap kind, locality,
+// traceback kind, arithmetic, input form -- times each candidate on the real input and
+// keeps the fastest for every later call with that signature, process-wide.  Every plan
+// computes the same results (the order of pairs and the grouping never change a value).
+// PA_TUNE=0 turns the timing off (the analytic choice stands), as do the experiment
+// overrides PA_DP_MODE and PA_GROUP_WIDTH.
+struct TuneEntry {
+	uint64_t key;
+	int G;
+	bool units;
+};
+std::mutex g_tune_mu;
+std::vector<TuneEntry> g_tune;
+constexpr double TUNE_MIN_CELLS = 2e7;  // smaller launches keep the analytic choice
+
+uint64_t tune_key(const pa_solver *s, const Input &in, const Plan &plan, const std::vector<int32_t> &ls,
+                  const std::vector<int32_t> &lt, double *cells) {
+	int64_t n = 0, mls = 0, mlt = 0;
+	double sls = 0, slt = 0, c = 0;
+	for (size_t k = 0; k < ls.size(); k++) {
+		if (ls[k] == 0 || lt[k] == 0) continue;
+		n++;
+		sls += ls[k];
+		slt += lt[k];
+		c += double(ls[k]) * double(lt[k]);
+		mls = std::max<int64_t>(mls, ls[k]);
+		mlt = std::max<int64_t>(mlt, lt[k]);
+	}
+	*cells = c;
+	auto oct = [](double x) -> uint64_t { return x < 1 ? 0 : uint64_t(std::floor(std::log2(x))) & 63; };
+	auto half = [](double x) -> uint64_t { return x < 1 ? 0 : uint64_t(std::floor(2 * std::log2(x))) & 63; };
+	const uint64_t tabk = in.form != F_INDEXED ? 0 : in.table_cols <= 8 ? 1 : in.table_cols <= MAX_COLPROF ? 2 : 3;
+	return oct(double(n)) | (half(n ? sls / n : 0) << 6) | (half(n ? slt / n : 0) << 12) | (oct(double(mls)) << 18) |
+	       (oct(double(mlt)) << 24) | (uint64_t(s->gap & 3) << 30) | (uint64_t(s->loc & 3) << 32) |
+	       (uint64_t(plan.tb & 3) << 34) | (uint64_t(plan.use_int) << 36) | (uint64_t(in.form & 3) << 37) |
+	       (tabk << 39) | (uint64_t(s->sm_count & 1023) << 41) | (uint64_t(s->device & 63) << 51);
+}
+
+template <typename Stage, typename Dp>
+pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, const Input &in,
+                    Plan &plan, Stage &stage, Dp &dp) {
+	const char *te = std::getenv("PA_TUNE");
+	if ((te && std::strcmp(te, "0") == 0) || std::getenv("PA_DP_MODE") || std::getenv("PA_GROUP_WIDTH")) return PA_OK;
+	double cells = 0;
+	const uint64_t key = tune_key(s, in, plan, ls, lt, &cells);
+	{
+		std::lock_guard<std::mutex> lk(g_tune_mu);
+		for (const auto &t : g_tune)
+			if (t.key == key) {
+				plan.G = t.G;
+				plan.units = t.units;
+				return PA_OK;
+			}
+	}
+	if (cells < TUNE_MIN_CELLS) return PA_OK;
+	// candidates: every group width whose stripe is not far taller than the pairs, and the
+	// stripe-chained mode when the longest pairs span several 256-row stripes
+	std::vector<std::pair<int, bool>> cand;
+	for (int G : {32, 16, 8, 4})
+		if (G == 4 || int64_t(G) * R <= 2 * plan.max_ls) cand.push_back({G, false});
+	if (plan.max_ls > 2 * 32 * R) cand.push_back({32, true});
+	if (cand.size() < 2) return PA_OK;
+	cudaStream_t st = s->stream;
+	float best = INFINITY;
+	int bestG = plan.G;
+	bool bestU = plan.units;
+	for (const auto &c : cand) {
+		Plan pl = plan;
+		pl.G = c.first;
+		pl.units = c.second;
+		if (pa_status e = stage(pl)) return e;
+		PA_CUDA(cudaEventRecord(s->ev[1], st));
+		if (pa_status e = dp(pl, pl.tb, false, nullptr)) return e;
+		PA_CUDA(cudaEventRecord(s->ev[2], st));
+		PA_CUDA(cudaEventSynchronize(s->ev[2]));
+		float ms = 0;
+		PA_CUDA(cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]));
+		if (ms < best) {
+			best = ms;
+			bestG = pl.G;
+			bestU = pl.units;
+		}
+	}
+	plan.G = bestG;
+	plan.units = bestU;
+	std::lock_guard<std::mutex> lk(g_tune_mu);
+	if (g_tune.size() < 4096) g_tune.push_back({key, bestG, bestU});
+	return PA_OK;
+}
+
 pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_out, pa_result **out,
                      int32_t *maps_out = nullptr, const int64_t *map_offsets = nullptr,
                      const UserPaths *user_paths = nullptr) {
@@ -894,7 +991,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		if (B * in.n_t > 0 && int64_t(mx[1]) >= in.table_cols) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in b");
 	}
 
-	// per-pair metadata
+	// ---- plan: group width and mode, arithmetic; the tuner may try several plans
 	Plan plan;
 	plan.max_ls = max_ls;
 	plan.max_lt = max_lt;
@@ -903,118 +1000,6 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	if (s->gap != GAP_GENERAL) {
 		plan.units = choose_units(ls, lt, s->sm_count, plan.G);
 		if (plan.units) plan.G = 32;
-	}
-	res.G = plan.G;
-	// processing order: by number of stripes, then |t|, largest first (a counting sort), so
-	// the groups that share a warp get pairs of the same shape and long pairs start early
-	std::vector<int32_t> order(static_cast<size_t>(B));
-	{
-		const int64_t rpp = int64_t(plan.G) * R;
-		const int64_t kt = max_lt + 1;
-		const int64_t nkeys = ((max_ls + rpp - 1) / rpp + 1) * kt;
-		std::vector<int32_t> count(size_t(nkeys) + 1, 0);
-		auto key = [&](int64_t k) {
-			const int64_t np = (ls[size_t(k)] + rpp - 1) / rpp;
-			return nkeys - 1 - (np * kt + lt[size_t(k)]);  // descending
-		};
-		for (int64_t k = 0; k < B; k++) count[size_t(key(k)) + 1]++;
-		for (int64_t c = 0; c < nkeys; c++) count[size_t(c) + 1] += count[size_t(c)];
-		for (int64_t k = 0; k < B; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
-	}
-	// stripe-chained tickets: level q holds stripe q of every pair with more than q stripes
-	// (an empty pair counts as one stripe, which writes its border result); the order puts
-	// those pairs first, so stripe q of rank w is ticket level_start[q] + w
-	std::vector<int32_t> level_start;
-	if (plan.units) {
-		const int64_t rpp_u = int64_t(plan.G) * R;
-		std::vector<int64_t> hist;
-		for (int64_t k = 0; k < B; k++) {
-			const int64_t np = std::max<int64_t>(1, (ls[size_t(k)] + rpp_u - 1) / rpp_u);
-			if (int64_t(hist.size()) <= np) hist.resize(size_t(np) + 1, 0);
-			hist[size_t(np)]++;
-		}
-		const int64_t nlev = int64_t(hist.size()) - 1;
-		level_start.assign(size_t(nlev) + 1, 0);
-		int64_t above = B;  // pairs with more than q stripes
-		for (int64_t q = 0; q < nlev; q++) {
-			level_start[size_t(q) + 1] = int32_t(level_start[size_t(q)] + above);
-			above -= hist[size_t(q) + 1];
-		}
-		if (int64_t(level_start.back()) >= (int64_t(1) << 31) - 64) return fail(PA_ERR_LENGTH, "too many stripes in one launch");
-		plan.nlevels = int32_t(nlev);
-		plan.ntickets = level_start.back();
-	}
-	std::vector<int64_t> mask_off(size_t(B) + 1, 0), map_off(size_t(B) + 1, 0), path_off(size_t(B) + 1, 0),
-	    val_off(size_t(B) + 1, 0), dense_off(size_t(B), 0);
-	const int rpp = plan.G * R;
-	for (int64_t k = 0; k < B; k++) {
-		const int64_t a = ls[size_t(k)], b = lt[size_t(k)];
-		const int64_t npass = (a == 0 || b == 0) ? 0 : (a + rpp - 1) / rpp;
-		mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * (b + plan.G - 1) * plan.G;
-		map_off[size_t(k) + 1] = map_off[size_t(k)] + std::min(a, b);
-		path_off[size_t(k) + 1] = path_off[size_t(k)] + 2 * (a + b + 2);
-		val_off[size_t(k) + 1] = val_off[size_t(k)] + int64_t(res.layers) * (a + 1) * (b + 1);
-		dense_off[size_t(k)] = in.dense_off_host ? in.dense_off_host[k] : k;
-	}
-	auto up = [&](DevBuf &d, const void *h, size_t n) -> cudaError_t {
-		cudaError_t e = d.ensure(n);
-		if (e != cudaSuccess || n == 0) return e;
-		return pa_copy(s, d.p, h, n, cudaMemcpyHostToDevice, st);
-	};
-	// pair metadata: packed into one pinned staging buffer, one host-to-device copy
-	{
-		const size_t n32 = size_t(B), n64 = size_t(B) + 1;
-		const size_t bytes = ((3 * n32 * 4 + level_start.size() * 4 + 7) & ~size_t(7)) + 5 * n64 * 8 + 16;
-		if (s->meta_pending) {
-			PA_CUDA(cudaEventSynchronize(s->meta_ev));  // the previous call's copy has read it
-			s->meta_pending = false;
-		}
-		PA_CUDA(s->h_meta.ensure(bytes));
-		PA_CUDA(s->d_meta.ensure(bytes));
-		unsigned char *h = s->h_meta.as<unsigned char>();
-		unsigned char *d = s->d_meta.as<unsigned char>();
-		size_t o = 0;
-		auto put = [&](const void *src, size_t nbytes, size_t align) {
-			o = (o + align - 1) & ~(align - 1);
-			if (nbytes) std::memcpy(h + o, src, nbytes);
-			unsigned char *dp = d + o;
-			o += nbytes;
-			return dp;
-		};
-		s->m.ls = reinterpret_cast<int32_t *>(put(ls.data(), n32 * 4, 4));
-		s->m.lt = reinterpret_cast<int32_t *>(put(lt.data(), n32 * 4, 4));
-		s->m.order = reinterpret_cast<int32_t *>(put(order.data(), n32 * 4, 4));
-		s->m.level_start = reinterpret_cast<int32_t *>(put(level_start.data(), level_start.size() * 4, 4));
-		s->m.mask_off = reinterpret_cast<int64_t *>(put(mask_off.data(), n64 * 8, 8));
-		// the caller's output offsets replace the internal ones when results go to its buffers
-		const int64_t *mo = (maps_out && map_offsets) ? map_offsets : map_off.data();
-		s->m.map_off = reinterpret_cast<int64_t *>(put(mo, (maps_out && map_offsets ? n32 : n64) * 8, 8));
-		o += (maps_out && map_offsets) ? 8 : 0;
-		const int64_t *po = (method == M_PATHS && user_paths) ? user_paths->path_off : path_off.data();
-		s->m.path_off = reinterpret_cast<int64_t *>(put(po, (method == M_PATHS && user_paths ? n32 : n64) * 8, 8));
-		o += (method == M_PATHS && user_paths) ? 8 : 0;
-		s->m.val_off = reinterpret_cast<int64_t *>(put(val_off.data(), n64 * 8, 8));
-		s->m.dense_off = reinterpret_cast<int64_t *>(put(dense_off.data(), n32 * 8, 8));
-		o += 8;
-		PA_CUDA(pa_copy(s, d, h, o, cudaMemcpyHostToDevice, st));
-		PA_CUDA(cudaEventRecord(s->meta_ev, st));
-		s->meta_pending = true;
-	}
-	PA_CUDA(s->d_score.ensure(size_t(B) * 4));
-	PA_CUDA(s->d_seed.ensure(size_t(B) * 8));
-	PA_CUDA(s->d_has.ensure(size_t(B) * 4));
-	PA_CUDA(s->d_counter.ensure(4));
-	PA_CUDA(s->d_status.ensure(4));
-	PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, st));
-	const size_t mask_elem = tb == TB_ALL ? 16 : 4;
-	if (tb != TB_NONE) PA_CUDA(s->d_masks.ensure(size_t(mask_off[size_t(B)]) * mask_elem));
-	if (want_values) PA_CUDA(s->d_vals.ensure(size_t(val_off[size_t(B)]) * 4));
-	PA_CUDA(cudaEventRecord(s->ev[1], st));
-
-	// ---- DP
-	if (s->gap == GAP_GENERAL) {
-		if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
-	} else {
 		double bound = 0;
 		bool use_int = int_mode_ok(s, in, host_table.data(), max_ls, max_lt, &bound);
 		if (use_int && s->loc == LOC_LOCAL && tb == TB_ONE) {
@@ -1025,19 +1010,139 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			if ((bound * 4.0 + 4.0) * double(int64_t(1) << shift) >= 2147483647.0) use_int = false;
 		}
 		plan.use_int = use_int;
+	}
+	std::vector<int32_t> order, level_start;
+	std::vector<int64_t> mask_off, map_off, path_off, val_off, dense_off;
+	// per-pair metadata of a plan: processing order, stripe tickets, output offsets, staged
+	// to the device; output buffers sized
+	auto stage = [&](Plan &plan) -> pa_status {
+		// processing order: by number of stripes, then |t|, largest first (a counting sort), so
+		// the groups that share a warp get pairs of the same shape and long pairs start early
+		order.assign(size_t(B), 0);
+		{
+			const int64_t rpp = int64_t(plan.G) * R;
+			const int64_t kt = max_lt + 1;
+			const int64_t nkeys = ((max_ls + rpp - 1) / rpp + 1) * kt;
+			std::vector<int32_t> count(size_t(nkeys) + 1, 0);
+			auto key = [&](int64_t k) {
+				const int64_t np = (ls[size_t(k)] + rpp - 1) / rpp;
+				return nkeys - 1 - (np * kt + lt[size_t(k)]);  // descending
+			};
+			for (int64_t k = 0; k < B; k++) count[size_t(key(k)) + 1]++;
+			for (int64_t c = 0; c < nkeys; c++) count[size_t(c) + 1] += count[size_t(c)];
+			for (int64_t k = 0; k < B; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
+		}
+		// stripe-chained tickets: level q holds stripe q of every pair with more than q stripes
+		// (an empty pair counts as one stripe, which writes its border result); the order puts
+		// those pairs first, so stripe q of rank w is ticket level_start[q] + w
+		level_start.clear();
+		if (plan.units) {
+			const int64_t rpp_u = int64_t(plan.G) * R;
+			std::vector<int64_t> hist;
+			for (int64_t k = 0; k < B; k++) {
+				const int64_t np = std::max<int64_t>(1, (ls[size_t(k)] + rpp_u - 1) / rpp_u);
+				if (int64_t(hist.size()) <= np) hist.resize(size_t(np) + 1, 0);
+				hist[size_t(np)]++;
+			}
+			const int64_t nlev = int64_t(hist.size()) - 1;
+			level_start.assign(size_t(nlev) + 1, 0);
+			int64_t above = B;  // pairs with more than q stripes
+			for (int64_t q = 0; q < nlev; q++) {
+				level_start[size_t(q) + 1] = int32_t(level_start[size_t(q)] + above);
+				above -= hist[size_t(q) + 1];
+			}
+			if (int64_t(level_start.back()) >= (int64_t(1) << 31) - 64) return fail(PA_ERR_LENGTH, "too many stripes in one launch");
+			plan.nlevels = int32_t(nlev);
+			plan.ntickets = level_start.back();
+		}
+		mask_off.assign(size_t(B) + 1, 0);
+		map_off.assign(size_t(B) + 1, 0);
+		path_off.assign(size_t(B) + 1, 0);
+		val_off.assign(size_t(B) + 1, 0);
+		dense_off.assign(size_t(B), 0);
+		const int rpp = plan.G * R;
+		for (int64_t k = 0; k < B; k++) {
+			const int64_t a = ls[size_t(k)], b = lt[size_t(k)];
+			const int64_t npass = (a == 0 || b == 0) ? 0 : (a + rpp - 1) / rpp;
+			mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * (b + plan.G - 1) * plan.G;
+			map_off[size_t(k) + 1] = map_off[size_t(k)] + std::min(a, b);
+			path_off[size_t(k) + 1] = path_off[size_t(k)] + 2 * (a + b + 2);
+			val_off[size_t(k) + 1] = val_off[size_t(k)] + int64_t(res.layers) * (a + 1) * (b + 1);
+			dense_off[size_t(k)] = in.dense_off_host ? in.dense_off_host[k] : k;
+		}
+		// pair metadata: packed into one pinned staging buffer, one host-to-device copy
+		{
+			const size_t n32 = size_t(B), n64 = size_t(B) + 1;
+			const size_t bytes = ((3 * n32 * 4 + level_start.size() * 4 + 7) & ~size_t(7)) + 5 * n64 * 8 + 16;
+			if (s->meta_pending) {
+				PA_CUDA(cudaEventSynchronize(s->meta_ev));  // the previous call's copy has read it
+				s->meta_pending = false;
+			}
+			PA_CUDA(s->h_meta.ensure(bytes));
+			PA_CUDA(s->d_meta.ensure(bytes));
+			unsigned char *h = s->h_meta.as<unsigned char>();
+			unsigned char *d = s->d_meta.as<unsigned char>();
+			size_t o = 0;
+			auto put = [&](const void *src, size_t nbytes, size_t align) {
+				o = (o + align - 1) & ~(align - 1);
+				if (nbytes) std::memcpy(h + o, src, nbytes);
+				unsigned char *dp = d + o;
+				o += nbytes;
+				return dp;
+			};
+			s->m.ls = reinterpret_cast<int32_t *>(put(ls.data(), n32 * 4, 4));
+			s->m.lt = reinterpret_cast<int32_t *>(put(lt.data(), n32 * 4, 4));
+			s->m.order = reinterpret_cast<int32_t *>(put(order.data(), n32 * 4, 4));
+			s->m.level_start = reinterpret_cast<int32_t *>(put(level_start.data(), level_start.size() * 4, 4));
+			s->m.mask_off = reinterpret_cast<int64_t *>(put(mask_off.data(), n64 * 8, 8));
+			// the caller's output offsets replace the internal ones when results go to its buffers
+			const int64_t *mo = (maps_out && map_offsets) ? map_offsets : map_off.data();
+			s->m.map_off = reinterpret_cast<int64_t *>(put(mo, (maps_out && map_offsets ? n32 : n64) * 8, 8));
+			o += (maps_out && map_offsets) ? 8 : 0;
+			const int64_t *po = (method == M_PATHS && user_paths) ? user_paths->path_off : path_off.data();
+			s->m.path_off = reinterpret_cast<int64_t *>(put(po, (method == M_PATHS && user_paths ? n32 : n64) * 8, 8));
+			o += (method == M_PATHS && user_paths) ? 8 : 0;
+			s->m.val_off = reinterpret_cast<int64_t *>(put(val_off.data(), n64 * 8, 8));
+			s->m.dense_off = reinterpret_cast<int64_t *>(put(dense_off.data(), n32 * 8, 8));
+			o += 8;
+			PA_CUDA(pa_copy(s, d, h, o, cudaMemcpyHostToDevice, st));
+			PA_CUDA(cudaEventRecord(s->meta_ev, st));
+			s->meta_pending = true;
+		}
+		PA_CUDA(s->d_score.ensure(size_t(B) * 4));
+		PA_CUDA(s->d_seed.ensure(size_t(B) * 8));
+		PA_CUDA(s->d_has.ensure(size_t(B) * 4));
+		PA_CUDA(s->d_counter.ensure(4));
+		PA_CUDA(s->d_status.ensure(4));
+		PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, st));
+		const size_t mask_elem = tb == TB_ALL ? 16 : 4;
+		if (tb != TB_NONE) PA_CUDA(s->d_masks.ensure(size_t(mask_off[size_t(B)]) * mask_elem));
+		if (want_values) PA_CUDA(s->d_vals.ensure(size_t(val_off[size_t(B)]) * 4));
+		return PA_OK;
+	};
+	auto dp = [&](const Plan &pl, int tbk, bool vals, const float *best_in) -> pa_status {
+		return pl.use_int ? run_dp<int32_t>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches)
+		                  : run_dp<float>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches);
+	};
+	if (s->gap != GAP_GENERAL && tb != TB_ALL && !want_values) {
+		if (pa_status e = tune_plan(s, ls, lt, in, plan, stage, dp)) return e;
+	}
+	if (pa_status e = stage(plan)) return e;
+	res.G = plan.G;
+	PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, st));
+	PA_CUDA(cudaEventRecord(s->ev[1], st));
+
+	// ---- DP
+	if (s->gap == GAP_GENERAL) {
+		if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
+	} else {
 		if (tb == TB_ALL && s->loc == LOC_LOCAL) {
 			// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
-			pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, TB_NONE, host_table.data(), B, false, nullptr, &launches)
-			                       : run_dp<float>(s, in, plan, TB_NONE, host_table.data(), B, false, nullptr, &launches);
-			if (e2) return e2;
+			if (pa_status e2 = dp(plan, TB_NONE, false, nullptr)) return e2;
 			PA_CUDA(s->d_best.ensure(size_t(B) * 4));
 			PA_CUDA(pa_copy(s, s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
 		}
-		pa_status e2 = use_int ? run_dp<int32_t>(s, in, plan, tb, host_table.data(), B, want_values,
-		                                         s->d_best.as<float>(), &launches)
-		                       : run_dp<float>(s, in, plan, tb, host_table.data(), B, want_values,
-		                                       s->d_best.as<float>(), &launches);
-		if (e2) return e2;
+		if (pa_status e2 = dp(plan, tb, want_values, s->d_best.as<float>())) return e2;
 	}
 	PA_CUDA(cudaEventRecord(s->ev[2], st));
 

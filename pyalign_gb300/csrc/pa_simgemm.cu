@@ -106,19 +106,31 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 // 128-byte core matrix.
 __device__ __forceinline__ void stage(unsigned char *dst, const __nv_bfloat16 *X, int64_t r0, int64_t rows, int dim,
                                       int kc, int kw) {
-	const int nkc = kw >> 3;
-	const int pieces = TM * nkc;
-	for (int c = threadIdx.x; c < pieces; c += THREADS) {
-		const int r8 = c & 7, rest = c >> 3;
-		const int kq = rest % nkc, g = rest / nkc;
-		const int r = g * 8 + r8;
-		uint4 v = make_uint4(0, 0, 0, 0);
-		if (r0 + r < rows) v = *reinterpret_cast<const uint4 *>(X + (r0 + r) * int64_t(dim) + kc + kq * 8);
-		*reinterpret_cast<uint4 *>(dst + (g * nkc + kq) * 128 + r8 * 16) = v;
+	const int nkc = kw >> 3;  // pieces per thread: TM * nkc / THREADS = nkc (TM == THREADS)
+	constexpr int BATCH = 8;  // loads in flight per thread before their stores
+	for (int c0 = 0; c0 < nkc; c0 += BATCH) {
+		uint4 v[BATCH];
+#pragma unroll
+		for (int u = 0; u < BATCH; u++) {
+			const int c = (c0 + u) * THREADS + threadIdx.x;
+			const int r8 = c & 7, rest = c >> 3;
+			const int kq = rest % nkc, g = rest / nkc;
+			const int r = g * 8 + r8;
+			v[u] = make_uint4(0, 0, 0, 0);
+			if (c0 + u < nkc && r0 + r < rows)
+				v[u] = __ldg(reinterpret_cast<const uint4 *>(X + (r0 + r) * int64_t(dim) + kc + kq * 8));
+		}
+#pragma unroll
+		for (int u = 0; u < BATCH; u++) {
+			const int c = (c0 + u) * THREADS + threadIdx.x;
+			const int r8 = c & 7, rest = c >> 3;
+			const int kq = rest % nkc, g = rest / nkc;
+			if (c0 + u < nkc) *reinterpret_cast<uint4 *>(dst + (g * nkc + kq) * 128 + r8 * 16) = v[u];
+		}
 	}
 }
 
-__global__ void __launch_bounds__(THREADS, 1) sim_bf16_kernel(SimParams p) {
+__global__ void __launch_bounds__(THREADS, 3) sim_bf16_kernel(SimParams p) {
 	extern __shared__ __align__(1024) unsigned char smem[];
 	unsigned char *sA = smem;
 	unsigned char *sB = smem + OPBYTES;
@@ -184,19 +196,25 @@ __global__ void __launch_bounds__(THREADS, 1) sim_bf16_kernel(SimParams p) {
 			phase ^= 1u;
 			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 		}
-		if (ok) {
-			// epilogue: warp w holds tile rows 32w..32w+31 (TMEM lanes), one row per thread
-			const int64_t j = m0 + warp * 32 + lane;
-			float *row = p.St + k * p.pitch_pair + j * p.pitch_row + n0;
+		if (ok && m0 + warp * 32 < lt) {
+			// epilogue: warp w holds tile rows 32w..32w+31 (TMEM lanes), one row per thread.
+			// Per 32 columns each thread parks its row in shared memory (the A operand's
+			// space, free once the MMAs completed; row pitch 33 words, conflict-free both
+			// ways) and the warp writes the rows back one at a time as 128-byte segments.
+			float *buf = reinterpret_cast<float *>(sA) + warp * 32 * 33;
 			const int64_t ncols = ls - n0;  // valid columns of this tile (> 0)
-			for (int cc = 0; cc < TN; cc += 32) {
+			const int rows = int(min(int64_t(32), lt - (m0 + warp * 32)));
+			float *out = p.St + k * p.pitch_pair + (m0 + warp * 32) * p.pitch_row + n0;
+			for (int cc = 0; cc < TN && cc < ncols; cc += 32) {
 				uint32_t v[32];
 				tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(cc), v);
-				if (j < lt) {
 #pragma unroll
-					for (int q = 0; q < 32; q++)
-						if (cc + q < ncols) row[cc + q] = __fmaf_rn(p.alpha, __uint_as_float(v[q]), p.beta);
+				for (int q = 0; q < 32; q++) buf[lane * 33 + q] = __fmaf_rn(p.alpha, __uint_as_float(v[q]), p.beta);
+				__syncwarp();
+				if (cc + lane < ncols) {
+					for (int rr = 0; rr < rows; rr++) out[rr * p.pitch_row + cc + lane] = buf[rr * 33 + lane];
 				}
+				__syncwarp();
 			}
 		}
 		asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

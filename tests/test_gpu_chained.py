@@ -135,3 +135,29 @@ def test_chained_matches_group_mode_large(gpu_alg, monkeypatch, locality):
                 out[(mode, detail)] = [(r.score, r.s_to_t.tolist()) for r in res]
     assert np.array_equal(out[("groups", "score")], out[("units", "score")])
     assert out[("groups", "alignment")] == out[("units", "alignment")]
+
+
+def test_autotuned_plan_matches_analytic_plan(gpu_alg, monkeypatch):
+    """The autotuner times the group widths and the chained mode on the first call with a
+    new workload signature; whichever it keeps, scores and alignments are those of the
+    analytic plan (PA_TUNE=0)."""
+    rng = np.random.default_rng(71)
+    n = 1536
+    ls = rng.integers(100, 700, size=n)
+    lt = rng.integers(100, 700, size=n)
+    a = np.zeros((n, 700), np.uint32)
+    b = np.zeros((n, 700), np.uint32)
+    for k in range(n):
+        a[k, :ls[k]] = rng.integers(0, 4, size=ls[k])
+        b[k, :lt[k]] = rng.integers(0, 4, size=lt[k])
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    ln = np.stack([ls, lt]).astype(np.uint16)
+    out = {}
+    for tune in ("0", "1"):
+        monkeypatch.setenv("PA_TUNE", tune)
+        opts = options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"], batch_size=n)
+        solver = gpu_alg.m16.create_solver(700, 700, gpu_alg.m16.create_options(opts))
+        res = solver.solve_indexed_for_alignment(a, b, table, ln)
+        out[tune] = [(r.score, r.s_to_t.tolist()) for r in res]
+    assert out["0"] == out["1"]
