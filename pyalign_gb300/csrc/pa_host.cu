@@ -416,6 +416,7 @@ bool choose_units(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt
 		if (std::strcmp(e, "units") == 0) return true;
 		if (std::strcmp(e, "groups") == 0) return false;
 	}
+	if (std::getenv("PA_GROUP_WIDTH")) return false;  // a forced group width means group mode
 	const double slots = double(sm_count) * 16.0;
 	const int64_t rg = int64_t(G) * R, ru = 32 * R;
 	double work_g = 0, work_u = 0, chain_g = 0, chain_u = 0;
