@@ -401,6 +401,13 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			const int r_last = nvalid - 1;
 
 			uint32_t tnext = (pass_active && brow) ? brow[0] : 0u;  // code of column 0 (lt >= 1 here)
+			// this lane's traceback word of step s is mrow[s * G] (hoisted out of the step loop)
+			uint32_t *mrow1 = nullptr;
+			uint4 *mrow4 = nullptr;
+			if (TB == TB_ONE && pass_active)
+				mrow1 = reinterpret_cast<uint32_t *>(p.masks) + p.mask_off[pair] + int64_t(q) * nsteps_pair * G + sub;
+			if (TB == TB_ALL && pass_active)
+				mrow4 = reinterpret_cast<uint4 *>(p.masks) + p.mask_off[pair] + int64_t(q) * nsteps_pair * G + sub;
 			for (int s = 0; s < wsteps; s++) {
 				const int j = s - sub;
 				V upD = __shfl_up_sync(0xffffffffu, outD, 1, G);
@@ -590,11 +597,9 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 					}
 
 					if (TB == TB_ONE) {
-						uint32_t *m = reinterpret_cast<uint32_t *>(p.masks) + p.mask_off[pair];
-						m[(int64_t(q) * nsteps_pair + s) * G + sub] = mword;
+						mrow1[s * G] = mword;
 					} else if (TB == TB_ALL) {
-						uint4 *m = reinterpret_cast<uint4 *>(p.masks) + p.mask_off[pair];
-						m[(int64_t(q) * nsteps_pair + s) * G + sub] = make_uint4(mall[0], mall[1], mall[2], mall[3]);
+						mrow4[s * G] = make_uint4(mall[0], mall[1], mall[2], mall[3]);
 					}
 
 					if (LOC == LOC_SEMI || LOC == LOC_GLOBAL) {

@@ -1182,7 +1182,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			w.path_len = user_paths->path_len;
 
 		}
-		walk_kernel<<<int((B + 127) / 128), 128, 0, st>>>(w);
+		walk_kernel<<<int((B + 3) / 4), 128, 0, st>>>(w);  // a warp per pair
 		PA_CUDA(cudaGetLastError());
 		launches++;
 	}

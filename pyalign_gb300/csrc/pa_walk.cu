@@ -3,51 +3,70 @@
 
 namespace pa {
 
-__device__ __forceinline__ uint32_t nibble_at(const uint32_t *W, int i, int j, int G, int S) {
-	const int rpp = G * R;
-	const int q = i / rpp;
-	const int rem = i - q * rpp;
-	const int sb = rem / R;
-	const int r = rem - sb * R;
-	const uint32_t w = W[(int64_t(q) * S + (j + sb)) * G + sb];
-	// row r's nibble (D source code | P-extend << 2 | Q-extend << 3) at bits 4(R-1-r)
-	return (w >> (4 * (R - 1 - r))) & 15u;
-}
-
-// One thread per pair.  Steps follow TracebackIterators<false>::Iterator::next
+// One warp per pair.  Steps follow TracebackIterators<false>::Iterator::next
 // (solver.h:1497-1536): record the point, stop when u < 0 or v < 0 or (local) the value is
 // not strictly positive -- which is exactly the "zero" source code 3 -- else follow the
 // traceback: diagonal, vertical or horizontal; for affine gaps the P/Q tracebacks jump to
 // the cell where the gap was opened (tb_P = tb_P(i-1, j) while the P-extend bit is set,
 // solver.h:2995-3016).  Diagonal steps are the alignment edges (solver.h:809-847).
+//
+// The walk is a chain of dependent mask reads, so its speed is the latency of one read.
+// The warp therefore caches a window of the masks: lane l holds the word of the 8-row block
+// (u >> 3) - (l >> 4) at column v - (l & 15), i.e. 16 rows x 16 columns up-left of the cell
+// where the window was placed, loaded in one round trip.  Every lane runs the same walk
+// (all values are warp-uniform) and takes a cell's word from its lane with a shuffle; a
+// cell outside the window re-places it there.  A diagonal or gap run thus costs one memory
+// round trip per 8-16 steps instead of one per step.
 __global__ void walk_kernel(WalkParams p) {
-	const int pair = blockIdx.x * blockDim.x + threadIdx.x;
-	if (pair >= p.npairs) return;
+	const int pair = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+	const int lane = threadIdx.x & 31;
+	if (pair >= p.npairs) return;  // whole warps
 	const int ls = p.len_s[pair], lt = p.len_t[pair];
 	const int nmap = min(ls, lt);
 	int32_t *map = p.maps ? p.maps + p.map_off[pair] : nullptr;
 	if (map)
-		for (int k = 0; k < nmap; k++) map[k] = -1;
+		for (int k = lane; k < nmap; k += 32) map[k] = -1;
+	__syncwarp();  // the fill is ordered before lane 0's writes below
 	int32_t *path = p.paths ? p.paths + p.path_off[pair] : nullptr;
 	if (!p.has_seed[pair]) {
-		if (p.path_len) p.path_len[pair] = 0;
+		if (p.path_len && lane == 0) p.path_len[pair] = 0;
 		return;
 	}
 	int u = p.seed[2 * pair], v = p.seed[2 * pair + 1];
-	int np = 0;
-	if (path) { path[0] = u; path[1] = v; }
-	np = 1;
+	if (path && lane == 0) { path[0] = u; path[1] = v; }
+	int np = 1;
 	const uint32_t *W = p.masks + p.mask_off[pair];
 	const int G = p.G;
 	const int S = lt + G - 1;
 	const bool s2t = ls <= lt;
 	const bool affine = p.gap == GAP_AFFINE;
+	int ub = -1000000, vb = -1000000;  // window: row blocks ub-1..ub, columns vb-15..vb
+	uint32_t win = 0;
+	// nibble of cell (i, j), i, j >= 0 and warp-uniform (R = 8 rows per block)
+	auto nib = [&](int i, int j) -> uint32_t {
+		int dr = ub - (i >> 3), dc = vb - j;
+		if (dr < 0 || dr > 1 || dc < 0 || dc > 15) {
+			ub = i >> 3;
+			vb = j;
+			dr = 0;
+			dc = 0;
+			const int rb = ub - (lane >> 4), col = vb - (lane & 15);
+			win = 0u;
+			if (rb >= 0 && col >= 0) {
+				const int q = rb / G, sb = rb - q * G;
+				win = W[(int64_t(q) * S + (col + sb)) * G + sb];
+			}
+		}
+		const uint32_t w = __shfl_sync(0xffffffffu, win, dr * 16 + dc);
+		// row r's nibble (D source code | P-extend << 2 | Q-extend << 3) at bits 4(R-1-r)
+		return (w >> (4 * (R - 1 - (i & (R - 1))))) & 15u;
+	};
 	while (u >= 0 && v >= 0) {
-		const uint32_t code = nibble_at(W, u, v, G, S) & 3u;
+		const uint32_t code = nib(u, v) & 3u;
 		if (p.local && code == 3u) break;
 		int nu = u, nv = v;
 		if (code == 2u) {
-			if (map) {
+			if (map && lane == 0) {
 				if (s2t) map[u] = v;
 				else map[v] = u;
 			}
@@ -56,7 +75,7 @@ __global__ void walk_kernel(WalkParams p) {
 		} else if (code == 1u) {
 			if (affine) {
 				int k = u;
-				while (k > 0 && (nibble_at(W, k, v, G, S) & 4u)) k--;
+				while (k > 0 && (nib(k, v) & 4u)) k--;
 				nu = k - 1;
 			} else {
 				nu = u - 1;
@@ -64,7 +83,7 @@ __global__ void walk_kernel(WalkParams p) {
 		} else {
 			if (affine) {
 				int k = v;
-				while (k > 0 && (nibble_at(W, u, k, G, S) & 8u)) k--;
+				while (k > 0 && (nib(u, k) & 8u)) k--;
 				nv = k - 1;
 			} else {
 				nv = v - 1;
@@ -72,10 +91,10 @@ __global__ void walk_kernel(WalkParams p) {
 		}
 		u = nu;
 		v = nv;
-		if (path) { path[2 * np] = u; path[2 * np + 1] = v; }
+		if (path && lane == 0) { path[2 * np] = u; path[2 * np + 1] = v; }
 		np++;
 	}
-	if (p.path_len) p.path_len[pair] = np;
+	if (p.path_len && lane == 0) p.path_len[pair] = np;
 }
 
 __global__ void codes_max_kernel(const uint32_t *x, int64_t n, uint32_t *out) {
