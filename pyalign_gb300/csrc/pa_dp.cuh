@@ -220,6 +220,119 @@ __device__ __forceinline__ uint32_t gt_mask(int32_t a, int32_t b) {
 	return d;
 }
 
+// End of a pair (group mode) or of a stripe ticket (stripe-chained mode): reduce the seed
+// candidates over the group, fold in and pass on the seed of the stripes above (chained),
+// and -- for the last stripe -- write the score and the traceback seed (solver.h:2035-2124,
+// 2174-2220, 2266-2326).
+template <typename V, int LOC, int TB, bool TAG, bool CHAIN>
+__device__ __forceinline__ void finish_pair(const DpParams<V> &p, int G, int sub, int pair, int ls, int lt, bool empty,
+                                            int npass, int q_lo, int prod, int base, V NEG, V l_best, int l_bi,
+                                            int l_bj, V row_best, int row_bj, V col_best, int col_bi, V glob,
+                                            bool have_glob) {
+	// ---- group reductions and outputs
+	if (LOC == LOC_LOCAL) {
+		for (int o = 1; o < G; o <<= 1) {
+			const V ov = __shfl_xor_sync(0xffffffffu, l_best, o, G);
+			const int oi = __shfl_xor_sync(0xffffffffu, l_bi, o, G);
+			const int oj = __shfl_xor_sync(0xffffffffu, l_bj, o, G);
+			const bool take = ov > l_best || (ov == l_best && (oi > l_bi || (oi == l_bi && oj > l_bj)));
+			if (take) { l_best = ov; l_bi = oi; l_bj = oj; }
+		}
+	} else if (LOC == LOC_SEMI) {
+		for (int o = 1; o < G; o <<= 1) {
+			const V orv = __shfl_xor_sync(0xffffffffu, row_best, o, G);
+			const int orj = __shfl_xor_sync(0xffffffffu, row_bj, o, G);
+			if (orj >= 0 && (row_bj < 0 || orv > row_best)) { row_best = orv; row_bj = orj; }
+			const V ocv = __shfl_xor_sync(0xffffffffu, col_best, o, G);
+			const int oci = __shfl_xor_sync(0xffffffffu, col_bi, o, G);
+			if (oci >= 0 && (col_bi < 0 || ocv > col_best || (ocv == col_best && oci < col_bi))) {
+				col_best = ocv; col_bi = oci;
+			}
+		}
+	} else {
+		for (int o = 1; o < G; o <<= 1) {
+			const V og = __shfl_xor_sync(0xffffffffu, glob, o, G);
+			const int oh = __shfl_xor_sync(0xffffffffu, int(have_glob), o, G);
+			if (oh && !have_glob) { glob = og; have_glob = true; }
+		}
+	}
+
+	// ---- stripe-chained: fold in the seed of the stripes above, pass it on
+	bool last_unit = true;
+	if (CHAIN && pair >= 0) {
+		last_unit = q_lo >= npass - 1;
+		if (q_lo > 0 && (LOC == LOC_LOCAL || LOC == LOC_SEMI) && !(LOC == LOC_LOCAL && TB == TB_ALL)) {
+			const int32_t *pi = p.progress + prod;
+			if (ld_acquire(pi) < lt) wait_progress(pi, lt, p.status);
+			const int4 rc = __ldcg(p.chain + prod);
+			const V ov = vfrom<V>(rc.x);
+			if (LOC == LOC_LOCAL) {
+				if (ov > l_best || (ov == l_best && (rc.y > l_bi || (rc.y == l_bi && rc.z > l_bj)))) {
+					l_best = ov; l_bi = rc.y; l_bj = rc.z;
+				}
+			} else if (rc.y >= 0 && (col_bi < 0 || ov > col_best || (ov == col_best && rc.y < col_bi))) {
+				col_best = ov; col_bi = rc.y;
+			}
+		}
+		if (!last_unit && sub == G - 1) {
+			int4 rc;
+			if (LOC == LOC_LOCAL) rc = make_int4(vbits(l_best), l_bi, l_bj, 0);
+			else rc = make_int4(vbits(col_best), col_bi, -1, 0);
+			p.chain[base] = rc;
+			st_release(p.progress + base, lt);  // every column, and the record
+		}
+	}
+
+	if (sub == 0 && pair >= 0 && last_unit) {
+		int si = -1, sj = -1, has = 0;
+		float sc = -INFINITY * p.out_sign;
+		if (!empty) {
+			if (LOC == LOC_LOCAL) {
+				if (TB == TB_ALL) {
+					has = 1;
+					sc = p.best_in[pair];
+				} else if (l_best > NEG) {
+					has = 1; si = l_bi; sj = l_bj;
+					sc = to_ref(l_best, TAG, p.out_sign);
+				}
+			} else if (LOC == LOC_SEMI) {
+				has = 1;
+				if (row_bj >= 0 && (col_bi < 0 || !(col_best > row_best))) {
+					si = ls - 1; sj = row_bj; sc = to_ref(row_best, TAG, p.out_sign);
+				} else {
+					si = col_bi; sj = lt - 1; sc = to_ref(col_best, TAG, p.out_sign);
+				}
+			} else {
+				has = 1; si = ls - 1; sj = lt - 1;
+				sc = to_ref(glob, TAG, p.out_sign);
+			}
+		} else {
+			// no cells: the seed is a border cell or does not exist
+			if (LOC == LOC_GLOBAL) {
+				has = 1; si = ls - 1; sj = lt - 1;
+				const V x = ls == 0 ? p.top_D[lt] : p.left_D[ls];
+				sc = to_ref(x, TAG, p.out_sign);
+			} else if (LOC == LOC_SEMI) {
+				// Optima over D(ls-1, 0..lt-1) then D(0..ls-1, lt-1) (solver.h:2284-2292)
+				V b = NEG;
+				for (int jj = 0; jj < lt; jj++) {
+					const V x = p.top_D[jj + 1];
+					if (x > b) { b = x; si = ls - 1; sj = jj; }
+				}
+				for (int ii = 0; ii < ls; ii++) {
+					const V x = p.left_D[ii + 1];
+					if (x > b) { b = x; si = ii; sj = lt - 1; }
+				}
+				if (b > NEG) { has = 1; sc = to_ref(b, TAG, p.out_sign); }
+			}
+		}
+		p.score[pair] = sc;
+		p.seed[2 * pair] = si;
+		p.seed[2 * pair + 1] = sj;
+		p.has_seed[pair] = has;
+	}
+}
+
 template <typename V, int GAP, int LOC, int TB, bool VALS, bool CHAIN>
 __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 	constexpr bool ISINT = std::is_same<V, int32_t>::value;
@@ -648,108 +761,8 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			__syncwarp();
 		}
 
-		// ---- group reductions and outputs
-		if (LOC == LOC_LOCAL) {
-			for (int o = 1; o < G; o <<= 1) {
-				const V ov = __shfl_xor_sync(0xffffffffu, l_best, o, G);
-				const int oi = __shfl_xor_sync(0xffffffffu, l_bi, o, G);
-				const int oj = __shfl_xor_sync(0xffffffffu, l_bj, o, G);
-				const bool take = ov > l_best || (ov == l_best && (oi > l_bi || (oi == l_bi && oj > l_bj)));
-				if (take) { l_best = ov; l_bi = oi; l_bj = oj; }
-			}
-		} else if (LOC == LOC_SEMI) {
-			for (int o = 1; o < G; o <<= 1) {
-				const V orv = __shfl_xor_sync(0xffffffffu, row_best, o, G);
-				const int orj = __shfl_xor_sync(0xffffffffu, row_bj, o, G);
-				if (orj >= 0 && (row_bj < 0 || orv > row_best)) { row_best = orv; row_bj = orj; }
-				const V ocv = __shfl_xor_sync(0xffffffffu, col_best, o, G);
-				const int oci = __shfl_xor_sync(0xffffffffu, col_bi, o, G);
-				if (oci >= 0 && (col_bi < 0 || ocv > col_best || (ocv == col_best && oci < col_bi))) {
-					col_best = ocv; col_bi = oci;
-				}
-			}
-		} else {
-			for (int o = 1; o < G; o <<= 1) {
-				const V og = __shfl_xor_sync(0xffffffffu, glob, o, G);
-				const int oh = __shfl_xor_sync(0xffffffffu, int(have_glob), o, G);
-				if (oh && !have_glob) { glob = og; have_glob = true; }
-			}
-		}
-
-		// ---- stripe-chained: fold in the seed of the stripes above, pass it on
-		bool last_unit = true;
-		if (units && pair >= 0) {  // constant-folded away in group mode
-			last_unit = q_lo >= npass - 1;
-			if (q_lo > 0 && (LOC == LOC_LOCAL || LOC == LOC_SEMI) && !(LOC == LOC_LOCAL && TB == TB_ALL)) {
-				const int32_t *pi = p.progress + prod;
-				if (ld_acquire(pi) < lt) wait_progress(pi, lt, p.status);
-				const int4 rc = __ldcg(p.chain + prod);
-				const V ov = vfrom<V>(rc.x);
-				if (LOC == LOC_LOCAL) {
-					if (ov > l_best || (ov == l_best && (rc.y > l_bi || (rc.y == l_bi && rc.z > l_bj)))) {
-						l_best = ov; l_bi = rc.y; l_bj = rc.z;
-					}
-				} else if (rc.y >= 0 && (col_bi < 0 || ov > col_best || (ov == col_best && rc.y < col_bi))) {
-					col_best = ov; col_bi = rc.y;
-				}
-			}
-			if (!last_unit && sub == G - 1) {
-				int4 rc;
-				if (LOC == LOC_LOCAL) rc = make_int4(vbits(l_best), l_bi, l_bj, 0);
-				else rc = make_int4(vbits(col_best), col_bi, -1, 0);
-				p.chain[base] = rc;
-				st_release(p.progress + base, lt);  // every column, and the record
-			}
-		}
-
-		if (sub == 0 && pair >= 0 && last_unit) {
-			int si = -1, sj = -1, has = 0;
-			float sc = -INFINITY * p.out_sign;
-			if (!empty) {
-				if (LOC == LOC_LOCAL) {
-					if (TB == TB_ALL) {
-						has = 1;
-						sc = p.best_in[pair];
-					} else if (l_best > NEG) {
-						has = 1; si = l_bi; sj = l_bj;
-						sc = to_ref(l_best, TAG, p.out_sign);
-					}
-				} else if (LOC == LOC_SEMI) {
-					has = 1;
-					if (row_bj >= 0 && (col_bi < 0 || !(col_best > row_best))) {
-						si = ls - 1; sj = row_bj; sc = to_ref(row_best, TAG, p.out_sign);
-					} else {
-						si = col_bi; sj = lt - 1; sc = to_ref(col_best, TAG, p.out_sign);
-					}
-				} else {
-					has = 1; si = ls - 1; sj = lt - 1;
-					sc = to_ref(glob, TAG, p.out_sign);
-				}
-			} else {
-				// no cells: the seed is a border cell or does not exist
-				if (LOC == LOC_GLOBAL) {
-					has = 1; si = ls - 1; sj = lt - 1;
-					const V x = ls == 0 ? p.top_D[lt] : p.left_D[ls];
-					sc = to_ref(x, TAG, p.out_sign);
-				} else if (LOC == LOC_SEMI) {
-					// Optima over D(ls-1, 0..lt-1) then D(0..ls-1, lt-1) (solver.h:2284-2292)
-					V b = NEG;
-					for (int jj = 0; jj < lt; jj++) {
-						const V x = p.top_D[jj + 1];
-						if (x > b) { b = x; si = ls - 1; sj = jj; }
-					}
-					for (int ii = 0; ii < ls; ii++) {
-						const V x = p.left_D[ii + 1];
-						if (x > b) { b = x; si = ii; sj = lt - 1; }
-					}
-					if (b > NEG) { has = 1; sc = to_ref(b, TAG, p.out_sign); }
-				}
-			}
-			p.score[pair] = sc;
-			p.seed[2 * pair] = si;
-			p.seed[2 * pair + 1] = sj;
-			p.has_seed[pair] = has;
-		}
+		finish_pair<V, LOC, TB, TAG, CHAIN>(p, G, sub, pair, ls, lt, empty, npass, q_lo, prod, base, NEG, l_best, l_bi,
+		                                    l_bj, row_best, row_bj, col_best, col_bi, glob, have_glob);
 	}
 }
 
@@ -771,6 +784,7 @@ struct WalkParams {
 	const uint32_t *masks;
 	const int64_t *mask_off;
 	int32_t G;
+	int32_t cols;   // columns per lane step of the DP that wrote the masks (1: dp_kernel, 2: dp2_kernel)
 	int32_t gap;    // GapKind
 	int32_t local;  // 1: stop at value-0 cells
 	int32_t *maps;  // min(ls, lt) per pair at map_off

@@ -366,7 +366,12 @@ struct Plan {
 	int64_t max_ls = 0, max_lt = 0;
 	bool units = false;        // stripe-chained mode (G = 32): one ticket per stripe
 	int32_t ntickets = 0, nlevels = 0;
+	int C = 1;                 // columns per lane step: 2 = dp2_kernel (int32 tagged, no values)
 };
+
+// Launches the two-column kernel can run: int32 tagged scoring without all-optimal masks
+// or Solution values.
+bool cols2_ok(const Plan &plan, bool want_values) { return plan.use_int && plan.tb != TB_ALL && !want_values; }
 
 // Group width G (lanes per pair, R = 8 rows each) that minimises the cells a launch
 // computes: the real cells plus the padding rows of each pair's last stripe and the G-1
@@ -444,8 +449,12 @@ V cvt(float x, bool use_int, int scale, int tag) {
 // The kernel family of a (value type, gap kind, mode).
 template <typename V>
 cudaError_t dp_launch(int gk, bool chain, int loc, int tb, bool vals, const DpParams<V> &p, int grid, size_t smem,
-                      cudaStream_t st) {
+                      cudaStream_t st, int cols = 1) {
 	if constexpr (std::is_same<V, int32_t>::value) {
+		if (cols == 2)
+			return gk == GAP_LINEAR ? launch_dp2_linear(loc, tb, chain, p, grid, smem, st)
+			       : gk == GAP_AFFINE ? launch_dp2_affine(loc, tb, chain, p, grid, smem, st)
+			                          : launch_dp2_dtw(loc, tb, chain, p, grid, smem, st);
 		if (chain)
 			return gk == GAP_LINEAR ? launch_dp_i_linear_chain(loc, tb, vals, p, grid, smem, st)
 			       : gk == GAP_AFFINE ? launch_dp_i_affine_chain(loc, tb, vals, p, grid, smem, st)
@@ -465,8 +474,12 @@ cudaError_t dp_launch(int gk, bool chain, int loc, int tb, bool vals, const DpPa
 }
 
 template <typename V>
-cudaError_t dp_occupancy(int gk, bool chain, int loc, int tb, bool vals, size_t smem, int *bps) {
+cudaError_t dp_occupancy(int gk, bool chain, int loc, int tb, bool vals, size_t smem, int *bps, int cols = 1) {
 	if constexpr (std::is_same<V, int32_t>::value) {
+		if (cols == 2)
+			return gk == GAP_LINEAR ? occupancy_dp2_linear(loc, tb, chain, smem, bps)
+			       : gk == GAP_AFFINE ? occupancy_dp2_affine(loc, tb, chain, smem, bps)
+			                          : occupancy_dp2_dtw(loc, tb, chain, smem, bps);
 		if (chain)
 			return gk == GAP_LINEAR ? occupancy_dp_i_linear_chain(loc, tb, vals, smem, bps)
 			       : gk == GAP_AFFINE ? occupancy_dp_i_affine_chain(loc, tb, vals, smem, bps)
@@ -615,12 +628,14 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	const uint64_t okey = (uint64_t(ISINT) << 60) | (uint64_t(gk) << 56) | (uint64_t(loc) << 52) |
 	                      (uint64_t(tb) << 48) | (uint64_t(want_values) << 44) | uint64_t(smem);
 	const bool ch = plan.units;
+	const int cols = (ISINT && plan.C == 2 && tb != TB_ALL && !want_values) ? 2 : 1;
+	const uint64_t ckey = okey | (uint64_t(ch) << 40) | (uint64_t(cols == 2) << 41);
 	for (const auto &kv : s->occ_cache)
-		if (kv.first == (okey | (uint64_t(ch) << 40))) bps = kv.second;
-	if (bps == 0) e = dp_occupancy<V>(gk, ch, loc, tb, want_values, smem, &bps);
+		if (kv.first == ckey) bps = kv.second;
+	if (bps == 0) e = dp_occupancy<V>(gk, ch, loc, tb, want_values, smem, &bps, cols);
 	PA_CUDA(e);
 	bps = std::max(bps, 1);
-	if (s->occ_cache.size() < 64) s->occ_cache.push_back({okey | (uint64_t(ch) << 40), bps});
+	if (s->occ_cache.size() < 64) s->occ_cache.push_back({ckey, bps});
 	const int gpw = 32 / plan.G;
 	const int64_t groups_needed = plan.units ? plan.ntickets : (npairs + gpw - 1) / gpw;  // warps needed
 	int64_t grid = int64_t(s->sm_count) * bps;
@@ -644,7 +659,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	}
 
 	PA_CUDA(cudaMemsetAsync(s->d_counter.p, 0, sizeof(int32_t), st));
-	e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st);
+	e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st, cols);
 	PA_CUDA(e);
 	(*launches)++;
 	return PA_OK;
@@ -1011,6 +1026,9 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			if ((bound * 4.0 + 4.0) * double(int64_t(1) << shift) >= 2147483647.0) use_int = false;
 		}
 		plan.use_int = use_int;
+		plan.C = cols2_ok(plan, want_values) ? 2 : 1;
+		if (const char *e = std::getenv("PA_DP_COLS"))  // experiments and tests
+			if (std::atoi(e) == 1) plan.C = 1;
 	}
 	std::vector<int32_t> order, level_start;
 	std::vector<int64_t> mask_off, map_off, path_off, val_off, dense_off;
@@ -1065,7 +1083,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		for (int64_t k = 0; k < B; k++) {
 			const int64_t a = ls[size_t(k)], b = lt[size_t(k)];
 			const int64_t npass = (a == 0 || b == 0) ? 0 : (a + rpp - 1) / rpp;
-			mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * (b + plan.G - 1) * plan.G;
+			const int64_t steps = plan.C == 2 ? (b + 1) / 2 + plan.G - 1 : b + plan.G - 1;
+			mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * steps * plan.G * plan.C;
 			map_off[size_t(k) + 1] = map_off[size_t(k)] + std::min(a, b);
 			path_off[size_t(k) + 1] = path_off[size_t(k)] + 2 * (a + b + 2);
 			val_off[size_t(k) + 1] = val_off[size_t(k)] + int64_t(res.layers) * (a + 1) * (b + 1);
@@ -1168,6 +1187,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		w.masks = s->d_masks.as<uint32_t>();
 		w.mask_off = s->m.mask_off;
 		w.G = plan.G;
+		w.cols = plan.C;
 		w.gap = s->gap;
 		w.local = s->loc == LOC_LOCAL;
 		w.maps = to_user ? maps_out : s->d_maps.as<int32_t>();

@@ -22,4 +22,13 @@ PA_DECL(f, float, affine_chain)
 PA_DECL(f, float, dtw_chain)
 #undef PA_DECL
 
+#define PA_DECL2(GAP)                                                                                      \
+	cudaError_t launch_dp2_##GAP(int loc, int tb, bool chain, const DpParams<int32_t> &p, int grid, size_t smem, \
+	                             cudaStream_t st);                                                     \
+	cudaError_t occupancy_dp2_##GAP(int loc, int tb, bool chain, size_t smem, int *blocks_per_sm);
+PA_DECL2(linear)
+PA_DECL2(affine)
+PA_DECL2(dtw)
+#undef PA_DECL2
+
 }  // namespace pa

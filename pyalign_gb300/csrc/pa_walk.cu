@@ -37,7 +37,8 @@ __global__ void walk_kernel(WalkParams p) {
 	int np = 1;
 	const uint32_t *W = p.masks + p.mask_off[pair];
 	const int G = p.G;
-	const int S = lt + G - 1;
+	const bool two = p.cols == 2;  // dp2_kernel layout: a uint2 per lane and step, columns j, j + 1
+	const int S = two ? ((lt + 1) >> 1) + G - 1 : lt + G - 1;
 	const bool s2t = ls <= lt;
 	const bool affine = p.gap == GAP_AFFINE;
 	int ub = -1000000, vb = -1000000;  // window: row blocks ub-1..ub, columns vb-15..vb
@@ -54,7 +55,8 @@ __global__ void walk_kernel(WalkParams p) {
 			win = 0u;
 			if (rb >= 0 && col >= 0) {
 				const int q = rb / G, sb = rb - q * G;
-				win = W[(int64_t(q) * S + (col + sb)) * G + sb];
+				win = two ? W[((int64_t(q) * S + ((col >> 1) + sb)) * G + sb) * 2 + (col & 1)]
+				          : W[(int64_t(q) * S + (col + sb)) * G + sb];
 			}
 		}
 		const uint32_t w = __shfl_sync(0xffffffffu, win, dr * 16 + dc);

@@ -252,3 +252,33 @@ def test_twenty_letter_table(gpu_alg, oracle_alg, monkeypatch, subst, gap, local
                         detail="score" if method == "score" else "alignment", count=count, gap=GAPS[gap])
         d = _run_both(gpu_alg, oracle_alg, mopts, method, "indexed", pairs, table=-table, iter_cap=20)
         assert d is None, f"minimize {method}: {d}"
+
+
+@pytest.mark.parametrize("gap", ["linear", "affine", "dtw"])
+@pytest.mark.parametrize("locality", ["local", "global", "semiglobal"])
+def test_one_and_two_column_kernels(gpu_alg, oracle_alg, monkeypatch, gap, locality):
+    """Integer scoring runs the two-column kernel (a lane updates columns j and j + 1 per
+    step) by default; PA_DP_COLS=1 selects the one-column kernel.  Both against the oracle,
+    odd and even |t|, several stripes, score and one traceback."""
+    if gap == "dtw" and locality != "global":
+        pytest.skip("DTW is global")
+    rng = np.random.default_rng(zlib.crc32(f"cols/{gap}/{locality}".encode()))
+    pairs = random_pairs(rng, 14, 0, 300, alphabet=4, related=0.6)
+    pairs[0] = (pairs[0][0][:1], pairs[0][1][:1])
+    pairs[1] = (pairs[1][0][:257], pairs[1][1][:3])
+    for cols in ("1", "2"):
+        monkeypatch.setenv("PA_DP_COLS", cols)
+        for method in ("score", "alignment"):
+            if gap == "dtw":
+                opts = options(gpu_alg, dtw=True, direction="minimize",
+                               detail="score" if method == "score" else "alignment")
+                table = np.abs(np.subtract.outer(np.arange(4.0), np.arange(4.0))).astype(np.float32)
+            else:
+                opts = options(gpu_alg, locality=locality, detail="score" if method == "score" else "alignment",
+                               gap=GAPS[gap])
+                table = _table(rng, 4)
+            d = _run_both(gpu_alg, oracle_alg, opts, method, "indexed", pairs, table=table)
+            assert d is None, f"cols={cols} {method}: {d}"
+            if gap != "dtw":
+                d = _run_both(gpu_alg, oracle_alg, opts, method, "binary", pairs, eq=2.0, ne=-3.0)
+                assert d is None, f"cols={cols} binary {method}: {d}"
