@@ -24,9 +24,14 @@ def torch_ag():
     return torch, autograd
 
 
+@pytest.mark.parametrize("kernel", ["pipelined", "plain"])
 @pytest.mark.parametrize("dim", [16, 64, 128, 256, 272])
-def test_similarity_matches_float32_product(torch_ag, dim):
+def test_similarity_matches_float32_product(torch_ag, monkeypatch, dim, kernel):
+    """Both kernels: the pipelined one (TMA loads, warp-specialised, double-buffered TMEM),
+    the default, and the plain one (PA_SIM_KERNEL=plain)."""
     torch, ag = torch_ag
+    if kernel == "plain":
+        monkeypatch.setenv("PA_SIM_KERNEL", "plain")
     g = torch.Generator(device="cuda").manual_seed(dim)
     B, ns, nt = 9, 300, 280
     Es = torch.randn(B, ns, dim, device="cuda", generator=g).to(torch.bfloat16)
