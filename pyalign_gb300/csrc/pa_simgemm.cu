@@ -293,6 +293,41 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
 	    : "memory");
 }
 
+// The tiles of one CTA, a contiguous range [t0, t1), walked pair by pair: one warp-wide
+// search for the pair of t0, then per tile only a counter, and per pair three loads
+// (its tile count and lengths).  All three roles walk the same sequence.
+struct TileWalk {
+	int64_t t, t1, k, local, ntiles_k, tiles_n, ls, lt;
+	__device__ __forceinline__ void load_pair(const SimParams &p) {
+		ntiles_k = p.tile_start[k + 1] - p.tile_start[k];
+		ls = p.len_s[k];
+		lt = p.len_t[k];
+		tiles_n = (ls + TN - 1) / TN;
+	}
+	__device__ __forceinline__ void begin(const SimParams &p, int64_t t0, int64_t tend) {
+		t = t0;
+		t1 = tend;
+		if (t >= t1) return;
+		int64_t m0_, n0_, ls_, lt_;
+		tile_of(p, t, k, m0_, n0_, ls_, lt_);  // warp-wide search
+		local = t - p.tile_start[k];
+		load_pair(p);
+	}
+	__device__ __forceinline__ bool valid() const { return t < t1; }
+	__device__ __forceinline__ int64_t m0() const { return (local / tiles_n) * TM; }
+	__device__ __forceinline__ int64_t n0() const { return (local % tiles_n) * TN; }
+	__device__ __forceinline__ void next(const SimParams &p) {
+		if (++t >= t1) return;
+		if (++local >= ntiles_k) {  // next pair with tiles
+			do {
+				k++;
+				local = 0;
+				load_pair(p);
+			} while (ntiles_k == 0);
+		}
+	}
+};
+
 __global__ void __launch_bounds__(PTHREADS, 1)
     sim_bf16_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                         SimParams p) {
@@ -332,17 +367,20 @@ __global__ void __launch_bounds__(PTHREADS, 1)
 	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 	const uint32_t tmem = *tslot;
 	const int nchunks = (p.dim + PK - 1) / PK;
+	const int64_t per = (p.total_tiles + gridDim.x - 1) / gridDim.x;
+	const int64_t t_begin = min(int64_t(blockIdx.x) * per, p.total_tiles);
+	const int64_t t_end = min(t_begin + per, p.total_tiles);
+	TileWalk tw;
+	tw.begin(p, t_begin, t_end);  // every warp, all lanes
 
 	if (warp == 0) {
 		// ---- producer (the warp decodes tiles, lane 0 issues the copies)
 		int s = 0;
 		uint32_t ph = 0;
 		bool ok = true;
-		for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
-			int64_t k, m0, n0, ls, lt;
-			tile_of(p, t, k, m0, n0, ls, lt);
+		for (; tw.valid() && ok; tw.next(p)) {
 			if (lane == 0) {
-				const int ya = int(k * p.n_t + m0), yb = int(k * p.n_s + n0);
+				const int ya = int(tw.k * p.n_t + tw.m0()), yb = int(tw.k * p.n_s + tw.n0());
 				for (int c = 0; c < nchunks; c++) {
 					if (!pwait(empty(s), ph ^ 1u)) { atomicOr(p.status, ST_TIMEOUT); ok = false; break; }
 					asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full(s)),
@@ -361,7 +399,7 @@ __global__ void __launch_bounds__(PTHREADS, 1)
 		int s = 0, a = 0;
 		uint32_t ph = 0, aph = 0;
 		bool ok = true;
-		for (int64_t t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+		for (; tw.valid() && ok; tw.next(p)) {
 			if (lane == 0) {
 				if (!pwait(freed(a), aph ^ 1u)) {
 					atomicOr(p.status, ST_TIMEOUT);
@@ -394,9 +432,8 @@ __global__ void __launch_bounds__(PTHREADS, 1)
 		float *buf = epi + (warp - 2) * 32 * 33;
 		int a = 0;
 		uint32_t aph = 0;
-		for (int64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
-			int64_t k, m0, n0, ls, lt;
-			tile_of(p, t, k, m0, n0, ls, lt);
+		for (; tw.valid(); tw.next(p)) {
+			const int64_t k = tw.k, m0 = tw.m0(), n0 = tw.n0(), ls = tw.ls, lt = tw.lt;
 			if (!__all_sync(0xffffffffu, pwait(ready(a), aph))) {
 				if (lane == 0) atomicOr(p.status, ST_TIMEOUT);
 				break;
