@@ -514,6 +514,16 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			const int r_last = nvalid - 1;
 
 			uint32_t tnext = (pass_active && brow) ? brow[0] : 0u;  // code of column 0 (lt >= 1 here)
+			// dense S with stride 1 along s: a lane whose 8 rows all lie in the pair reads them as
+			// two 16-byte loads, one column ahead of its use (drow + row0 + j * sj)
+			const bool dvec = sub_kind == SUB_DENSE && pass_active && nvalid >= R && p.dense_si == 1 &&
+			                  (p.dense_sj & 3) == 0 && ((reinterpret_cast<uintptr_t>(drow) & 15) == 0);
+			const float *dcol = dvec ? drow + row0 : nullptr;
+			float4 dn0 = make_float4(0.f, 0.f, 0.f, 0.f), dn1 = dn0;
+			if (dvec) {
+				dn0 = __ldg(reinterpret_cast<const float4 *>(dcol));
+				dn1 = __ldg(reinterpret_cast<const float4 *>(dcol) + 1);
+			}
 			// this lane's traceback word of step s is mrow[s * G] (hoisted out of the step loop)
 			uint32_t *mrow1 = nullptr;
 			uint4 *mrow4 = nullptr;
@@ -562,6 +572,20 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 					} else if (sub_kind == SUB_TABLE) {
 #pragma unroll
 						for (int r = 0; r < R; r++) S[r] = tab[qa[r] * p.table_cols + tcode];
+					} else if (dvec) {
+						S[0] = V(dn0.x * p.dense_sign);
+						S[1] = V(dn0.y * p.dense_sign);
+						S[2] = V(dn0.z * p.dense_sign);
+						S[3] = V(dn0.w * p.dense_sign);
+						S[4] = V(dn1.x * p.dense_sign);
+						S[5] = V(dn1.y * p.dense_sign);
+						S[6] = V(dn1.z * p.dense_sign);
+						S[7] = V(dn1.w * p.dense_sign);
+						if (j + 1 < lt) {
+							const float4 *nx = reinterpret_cast<const float4 *>(dcol + int64_t(j + 1) * p.dense_sj);
+							dn0 = __ldg(nx);
+							dn1 = __ldg(nx + 1);
+						}
 					} else {
 #pragma unroll
 						for (int r = 0; r < R; r++) {
