@@ -21,7 +21,11 @@
  *    and traceback matrices are int32 (the Python layer narrows them for m16).
  *  - A solver is not re-entrant (like the reference, factory.h:682-973); results and
  *    iterators own their data and stay valid after later solve calls.
- *  - All device work of a solver runs on its CUDA stream (pa_solver_set_stream).
+ *  - All device work of a solver runs on its CUDA stream (pa_solver_set_stream).  A
+ *    device-resident solve that repeats the solver's previous one exactly (lengths, shapes,
+ *    buffers, options) reuses its plan and, from the second repetition on, runs as a CUDA
+ *    graph captured on a private stream; inputs are read at every launch (PA_GRAPHS=0
+ *    disables the cache).
  */
 #ifndef PYALIGN_GB300_H
 #define PYALIGN_GB300_H

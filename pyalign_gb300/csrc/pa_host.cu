@@ -324,10 +324,41 @@ struct pa_solver {
 	bool border_ready[3] = {false, false, false};
 	std::vector<unsigned char> h_tab;  // staging of the converted similarity table
 
+	// Repeated solves: the signature of the last device-resident solve and, once the same
+	// solve came twice in a row, a CUDA graph of its device work (see solve_impl).
+	struct Repeat {
+		bool valid = false;
+		int method = -1, form = -1;
+		int64_t B = 0, n_s = 0, n_t = 0, trows = 0, tcols = 0, dsi = 0, dsj = 0;
+		const void *a = nullptr, *b = nullptr, *sim = nullptr, *table = nullptr;
+		float eq = 0, ne = 0;
+		int32_t *maps_out = nullptr, *paths = nullptr, *path_len = nullptr;
+		float *scores = nullptr;
+		cudaStream_t stream = nullptr;
+		std::vector<int32_t> ls, lt;
+		std::vector<float> table_host;
+		std::vector<int64_t> user_map_off, user_path_off, dense_off;
+		// the plan and what the downloads need from it
+		int G = 0, C = 1, launches = 0, key_shift = 0, ntickets = 0, nlevels = 0;
+		bool units = false, use_int = false;
+		std::vector<int64_t> mask_off, map_off, path_off, val_off;
+		cudaGraphExec_t exec = nullptr;
+	} rep;
+	cudaStream_t cap_stream = nullptr;  // private stream the graph is captured on
+	bool capturing = false;
+
+	void drop_graph() {
+		if (rep.exec) cudaGraphExecDestroy(rep.exec);
+		rep.exec = nullptr;
+		rep.valid = false;
+	}
+
 	~pa_solver() {
+		drop_graph();
 		for (auto &e : ev)
 			if (e) cudaEventDestroy(e);
 		if (meta_ev) cudaEventDestroy(meta_ev);
+		if (cap_stream) cudaStreamDestroy(cap_stream);
 		if (own_stream) cudaStreamDestroy(own_stream);
 	}
 };
@@ -601,7 +632,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			if (sk && std::strcmp(sk, "table") == 0) p.sub_kind = SUB_TABLE;
 			if (sk && std::strcmp(sk, "colprof") == 0 && colprof_ok) p.sub_kind = SUB_COLPROF;
 			PA_CUDA(s->d_tab.ensure(nt_ * sizeof(V)));
-			PA_CUDA(pa_copy(s, s->d_tab.p, tabv, nt_ * sizeof(V), cudaMemcpyHostToDevice, st));
+			if (!s->capturing) PA_CUDA(pa_copy(s, s->d_tab.p, tabv, nt_ * sizeof(V), cudaMemcpyHostToDevice, st));
 			p.table = s->d_tab.as<V>();
 		}
 	}
@@ -1144,35 +1175,67 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		return pl.use_int ? run_dp<int32_t>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches)
 		                  : run_dp<float>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches);
 	};
-	if (s->gap != GAP_GENERAL && tb != TB_ALL && !want_values) {
-		if (pa_status e = tune_plan(s, ls, lt, in, plan, stage, dp)) return e;
-	}
-	if (pa_status e = stage(plan)) return e;
-	res.G = plan.G;
-	PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, st));
-	PA_CUDA(cudaEventRecord(s->ev[1], st));
+	// ---- repeated solves: the same device-resident solve as the last call on this solver
+	// (same lengths, shapes, buffers, options, table, offsets and stream) skips planning and
+	// staging -- the device metadata, converted table and plan of that call are still in
+	// place -- and from its second repetition on runs as one CUDA graph of the device work,
+	// captured on a private stream.  Any other call first drops the cached state, since it
+	// rewrites the buffers the graph reads.  PA_GRAPHS=0 turns this off.
+	const char *genv = std::getenv("PA_GRAPHS");
+	const bool repeatable = in.location == PA_DEVICE && s->gap != GAP_GENERAL && tb != TB_ALL && !want_values &&
+	                        (method == M_SCORE || method == M_ALIGNMENT || method == M_PATHS) &&
+	                        !(genv && std::strcmp(genv, "0") == 0);
+	const bool paths_to_user = method == M_PATHS && user_paths;
+	auto same_rep = [&]() -> bool {
+		const pa_solver::Repeat &r = s->rep;
+		if (!r.valid || r.method != method || r.form != in.form || r.B != B || r.n_s != in.n_s || r.n_t != in.n_t)
+			return false;
+		if (r.a != in.a || r.b != in.b || r.sim != in.sim || r.table != in.table || r.trows != in.table_rows ||
+		    r.tcols != in.table_cols || r.dsi != in.dense_si || r.dsj != in.dense_sj || r.stream != st)
+			return false;
+		if (std::memcmp(&r.eq, &in.eq, 4) || std::memcmp(&r.ne, &in.ne, 4)) return false;
+		if (r.maps_out != maps_out || r.ls != ls || r.lt != lt || r.table_host != host_table) return false;
+		if (r.scores != (paths_to_user ? user_paths->scores : nullptr)) return false;
+		if (paths_to_user && (r.paths != user_paths->paths || r.path_len != user_paths->path_len ||
+		                      std::memcmp(r.user_path_off.data(), user_paths->path_off, size_t(B) * 8)))
+			return false;
+		if (maps_out && map_offsets && (r.user_map_off.size() != size_t(B) ||
+		                                std::memcmp(r.user_map_off.data(), map_offsets, size_t(B) * 8)))
+			return false;
+		if (in.dense_off_host && (r.dense_off.size() != size_t(B) ||
+		                          std::memcmp(r.dense_off.data(), in.dense_off_host, size_t(B) * 8)))
+			return false;
+		return true;
+	};
+	const bool hit = repeatable && same_rep();
+	if (!hit) s->drop_graph();
 
-	// ---- DP
-	if (s->gap == GAP_GENERAL) {
-		if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
-	} else {
-		if (tb == TB_ALL && s->loc == LOC_LOCAL) {
-			// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
-			if (pa_status e2 = dp(plan, TB_NONE, false, nullptr)) return e2;
-			PA_CUDA(s->d_best.ensure(size_t(B) * 4));
-			PA_CUDA(pa_copy(s, s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
-		}
-		if (pa_status e2 = dp(plan, tb, want_values, s->d_best.as<float>())) return e2;
-	}
-	PA_CUDA(cudaEventRecord(s->ev[2], st));
-
-	// ---- traceback walk (one optimal path)
 	const bool need_walk = tb == TB_ONE && s->gap != GAP_GENERAL &&
 	                       (method == M_ALIGNMENT || method == M_ALIGNMENT_ITER || method == M_SOLUTION ||
 	                        method == M_SOLUTION_ITER || method == M_PATHS);
-	const bool paths_to_user = method == M_PATHS && user_paths;
-	if (need_walk) {
-		const bool to_user = maps_out && in.location == PA_DEVICE;
+	// the device work after staging: status reset, DP, traceback walk, the scores of the
+	// device-resident path form.  The phase events are recorded in it; inside a capture they
+	// become external event nodes of the graph, so the timings stay exact on replays.
+	auto record = [&](cudaEvent_t e, cudaStream_t sw) -> cudaError_t {
+		return s->capturing ? cudaEventRecordWithFlags(e, sw, cudaEventRecordExternal) : cudaEventRecord(e, sw);
+	};
+	auto device_work = [&](cudaStream_t sw, bool timed) -> pa_status {
+		PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, sw));
+		if (timed) PA_CUDA(record(s->ev[1], sw));
+		if (s->gap == GAP_GENERAL) {
+			if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
+		} else {
+			if (tb == TB_ALL && s->loc == LOC_LOCAL) {
+				// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
+				if (pa_status e2 = dp(plan, TB_NONE, false, nullptr)) return e2;
+				PA_CUDA(s->d_best.ensure(size_t(B) * 4));
+				PA_CUDA(pa_copy(s, s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, sw));
+			}
+			if (pa_status e2 = dp(plan, tb, want_values, s->d_best.as<float>())) return e2;
+		}
+		if (timed) PA_CUDA(record(s->ev[2], sw));
+		if (need_walk) {
+			const bool to_user = maps_out && in.location == PA_DEVICE;
 		PA_CUDA(s->d_maps.ensure(size_t(map_off[size_t(B)]) * 4));
 		if (want_paths) {
 			PA_CUDA(s->d_paths.ensure(size_t(path_off[size_t(B)]) * 4));
@@ -1202,16 +1265,113 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			w.path_len = user_paths->path_len;
 
 		}
-		walk_kernel<<<int((B + 3) / 4), 128, 0, st>>>(w);  // a warp per pair
+		walk_kernel<<<int((B + 3) / 4), 128, 0, sw>>>(w);  // a warp per pair
 		PA_CUDA(cudaGetLastError());
 		launches++;
+		}
+		if (paths_to_user && user_paths->scores)
+			PA_CUDA(cudaMemcpyAsync(user_paths->scores, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, sw));
+		return PA_OK;
+	};
+
+	if (hit) {
+		pa_solver::Repeat &r = s->rep;
+		plan.G = r.G;
+		plan.C = r.C;
+		plan.units = r.units;
+		plan.use_int = r.use_int;
+		plan.key_shift = r.key_shift;
+		plan.ntickets = r.ntickets;
+		plan.nlevels = r.nlevels;
+		mask_off = r.mask_off;
+		map_off = r.map_off;
+		path_off = r.path_off;
+		val_off = r.val_off;
+		if (!r.exec) {
+			// second identical solve: capture its device work once, then launch it as a graph
+			if (!s->cap_stream) PA_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+			cudaGraph_t graph = nullptr;
+			const cudaStream_t saved = s->stream;
+			int before = launches;
+			PA_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+			s->stream = s->cap_stream;
+			s->capturing = true;
+			pa_status e = device_work(s->cap_stream, true);
+			s->capturing = false;
+			s->stream = saved;
+			const cudaError_t ce = cudaStreamEndCapture(s->cap_stream, &graph);
+			if (e == PA_OK && ce == cudaSuccess && graph) {
+				if (cudaGraphInstantiate(&r.exec, graph, 0) != cudaSuccess) r.exec = nullptr;
+			}
+			if (graph) cudaGraphDestroy(graph);
+			cudaGetLastError();  // a failed capture leaves no sticky error
+			r.launches = launches - before;
+			launches = before;
+			if (!r.exec) {
+				s->drop_graph();
+				return fail(PA_ERR_CUDA, "capturing the repeated solve as a CUDA graph failed (PA_GRAPHS=0 disables it)");
+			}
+		}
+		PA_CUDA(cudaGraphLaunch(r.exec, st));  // records ev[1], ev[2] around the DP
+		launches += r.launches;
+	} else {
+		if (s->gap != GAP_GENERAL && tb != TB_ALL && !want_values) {
+			if (pa_status e = tune_plan(s, ls, lt, in, plan, stage, dp)) return e;
+		}
+		if (pa_status e = stage(plan)) return e;
+		if (pa_status e = device_work(st, true)) return e;
 	}
+	res.G = plan.G;
 	PA_CUDA(cudaEventRecord(s->ev[3], st));
+	if (repeatable && !hit) {
+		// remember this solve for the next call
+		pa_solver::Repeat &r = s->rep;
+		r.valid = true;
+		r.method = method;
+		r.form = in.form;
+		r.B = B;
+		r.n_s = in.n_s;
+		r.n_t = in.n_t;
+		r.trows = in.table_rows;
+		r.tcols = in.table_cols;
+		r.dsi = in.dense_si;
+		r.dsj = in.dense_sj;
+		r.a = in.a;
+		r.b = in.b;
+		r.sim = in.sim;
+		r.table = in.table;
+		r.eq = in.eq;
+		r.ne = in.ne;
+		r.stream = st;
+		r.maps_out = maps_out;
+		r.scores = paths_to_user ? user_paths->scores : nullptr;
+		r.paths = paths_to_user ? user_paths->paths : nullptr;
+		r.path_len = paths_to_user ? user_paths->path_len : nullptr;
+		r.ls = ls;
+		r.lt = lt;
+		r.table_host = host_table;
+		r.user_map_off.assign(maps_out && map_offsets ? map_offsets : nullptr,
+		                      maps_out && map_offsets ? map_offsets + B : nullptr);
+		r.user_path_off.assign(paths_to_user ? user_paths->path_off : nullptr,
+		                       paths_to_user ? user_paths->path_off + B : nullptr);
+		r.dense_off.assign(in.dense_off_host ? in.dense_off_host : nullptr,
+		                   in.dense_off_host ? in.dense_off_host + B : nullptr);
+		r.G = plan.G;
+		r.C = plan.C;
+		r.units = plan.units;
+		r.use_int = plan.use_int;
+		r.key_shift = plan.key_shift;
+		r.ntickets = plan.ntickets;
+		r.nlevels = plan.nlevels;
+		r.mask_off = mask_off;
+		r.map_off = map_off;
+		r.path_off = path_off;
+		r.val_off = val_off;
+		r.exec = nullptr;
+	}
 
 	if (paths_to_user) {
 		// device-resident form: results stay on the device, nothing to wait for here
-		if (user_paths->scores)
-			PA_CUDA(cudaMemcpyAsync(user_paths->scores, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, st));
 		s->last_launches = launches;
 		for (auto &ms : s->last_ms) ms = 0.0f;
 		if (out) *out = nullptr;

@@ -1,0 +1,140 @@
+"""Repeated device-resident solves and their CUDA graph (needs a GPU).
+
+A solver that gets the same device-resident solve twice in a row (same lengths, buffers,
+options) skips planning and staging and, from the second repetition on, launches the
+device work as one CUDA graph.  The graph reads the inputs at launch, so new contents in
+the same buffers must be seen; other lengths must re-plan.  Every result is compared with
+the same solve on a solver that never caches (PA_GRAPHS=0), bit for bit.
+"""
+
+import ctypes
+import types
+
+import numpy as np
+import pytest
+
+from _cases import Gap
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    torch = pytest.importorskip("torch")
+    from pyalign_gb300 import build
+    build.build()
+    if not torch.cuda.is_available():
+        pytest.fail("no CUDA device visible")
+    from pyalign_gb300 import algorithm as alg
+    from pyalign_gb300 import autograd as ag
+    return torch, alg, ag
+
+
+def _batch_solver(alg, torch, n, n_s, n_t):
+    opts = {"solver": alg.Type.ALIGNMENT, "direction": alg.Direction.MAXIMIZE, "batch": True, "batch_size": n,
+            "return_dup": False, "locality": alg.Locality.LOCAL,
+            "codomain": types.SimpleNamespace(detail=alg.Detail.ALIGNMENT, count=alg.Count.ONE),
+            "gap_cost": Gap("affine", 5.0, 2.0)}
+    solver = alg.m16.create_solver(n_s, n_t, alg.m16.create_options(opts))
+    alg.check(alg.lib().pa_solver_set_stream(solver.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return solver
+
+
+def _timings(alg, solver):
+    ms4 = (ctypes.c_float * 4)()
+    nl = ctypes.c_int32(0)
+    alg.check(alg.lib().pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl)))
+    return list(ms4)
+
+
+def _solve_batch(alg, torch, solver, a_d, b_d, t_d, ln, sc, mp):
+    """pa_solve_batch with device codes/table and the device outputs sc, mp (reset first);
+    returns (scores, maps)."""
+    P = ctypes.POINTER
+    n = a_d.shape[0]
+    sizes = np.minimum(ln[0], ln[1]).astype(np.int64)
+    offs = np.zeros(n, np.int64)
+    offs[1:] = np.cumsum(sizes)[:-1]
+    sc.fill_(float("nan"))
+    mp.fill_(-7)
+    length = np.ascontiguousarray(ln, dtype=np.int32)
+    bt = alg.Batch(form=1, location=1, batch=n, n_s=a_d.shape[1], n_t=b_d.shape[1],
+                   a=ctypes.cast(a_d.data_ptr(), P(ctypes.c_uint32)), b=ctypes.cast(b_d.data_ptr(), P(ctypes.c_uint32)),
+                   table=ctypes.cast(t_d.data_ptr(), P(ctypes.c_float)), table_rows=4, table_cols=4,
+                   length=length.ctypes.data_as(P(ctypes.c_int32)))
+    alg.check(alg.lib().pa_solve_batch(solver.handle, ctypes.byref(bt), ctypes.c_void_p(sc.data_ptr()),
+                                       ctypes.c_void_p(mp.data_ptr()), offs.ctypes.data_as(P(ctypes.c_int64))))
+    torch.cuda.synchronize()
+    m = int(sizes.sum())
+    return sc.cpu().numpy(), mp[:m].cpu().numpy()
+
+
+def test_repeated_batch_solves(env, monkeypatch):
+    torch, alg, ag = env
+    rng = np.random.default_rng(5)
+    n, n_s, n_t = 512, 300, 320
+    ln = np.stack([rng.integers(1, n_s + 1, n), rng.integers(1, n_t + 1, n)]).astype(np.int32)
+    a = rng.integers(0, 4, size=(n, n_s)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, n_t)).astype(np.uint32)
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    a_d = torch.from_numpy(a.view(np.int32)).cuda()
+    b_d = torch.from_numpy(b.view(np.int32)).cuda()
+    t_d = torch.from_numpy(table).cuda()
+    sc = torch.empty(n, device="cuda")
+    mp = torch.empty(int(np.minimum(ln[0], ln[1]).sum()), dtype=torch.int32, device="cuda")
+    sc_r, mp_r = torch.empty_like(sc), torch.empty_like(mp)
+
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    ref_solver = _batch_solver(alg, torch, n, n_s, n_t)
+    want = _solve_batch(alg, torch, ref_solver, a_d, b_d, t_d, ln, sc_r, mp_r)
+    monkeypatch.delenv("PA_GRAPHS")
+
+    solver = _batch_solver(alg, torch, n, n_s, n_t)
+    for rep in range(4):  # planned, cached plan + captured graph, graph, graph
+        got = _solve_batch(alg, torch, solver, a_d, b_d, t_d, ln, sc, mp)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), rep
+        ms = _timings(alg, solver)
+        assert ms[1] > 0 and ms[2] > 0, (rep, ms)  # the phases are timed on replays too
+
+    # new contents in the same buffers: the graph reads them at launch
+    a_d.copy_(torch.from_numpy(rng.integers(0, 4, size=(n, n_s)).astype(np.int32)))
+    got = _solve_batch(alg, torch, solver, a_d, b_d, t_d, ln, sc, mp)
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    want2 = _solve_batch(alg, torch, ref_solver, a_d, b_d, t_d, ln, sc_r, mp_r)
+    monkeypatch.delenv("PA_GRAPHS")
+    assert np.array_equal(got[0], want2[0]) and np.array_equal(got[1], want2[1])
+    assert not np.array_equal(want2[0], want[0])
+
+    # other lengths: planned anew
+    ln2 = ln.copy()
+    ln2[0, :7] = 1
+    got = _solve_batch(alg, torch, solver, a_d, b_d, t_d, ln2, sc, mp)
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    want3 = _solve_batch(alg, torch, ref_solver, a_d, b_d, t_d, ln2, sc_r, mp_r)
+    assert np.array_equal(got[0], want3[0]) and np.array_equal(got[1], want3[1])
+
+
+def test_repeated_dense_paths_and_gradients(env, monkeypatch):
+    """The autograd front end (pa_solve_dense_paths): repeated forward + backward on one
+    similarity buffer whose contents change in place."""
+    torch, alg, ag = env
+    g = torch.Generator(device="cuda").manual_seed(3)
+    B, ns, nt = 96, 200, 170
+    rng = np.random.default_rng(9)
+    lengths = np.stack([rng.integers(1, ns + 1, B), rng.integers(1, nt + 1, B)], axis=1)
+    S = torch.randn(B, ns, nt, device="cuda", generator=g)
+
+    def run():
+        return ag.alignment_score(S, lengths, 0.5, 0.1, "global").clone()
+
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    want = run()
+    monkeypatch.delenv("PA_GRAPHS")
+    for rep in range(4):
+        assert torch.equal(run(), want), rep
+    S.mul_(-1.0).add_(0.25)
+    got = run()
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    assert torch.equal(got, run())
+    assert not torch.equal(got, want)
