@@ -186,6 +186,9 @@ void pa_result_destroy(pa_result *r);
 int64_t pa_result_size(const pa_result *r);
 int64_t pa_result_len_s(const pa_result *r, int64_t lane);
 int64_t pa_result_len_t(const pa_result *r, int64_t lane);
+/* All lanes' lengths at once (len_s, len_t: pa_result_size entries each): the per-lane
+ * shapes pyalign reads for every result object (solve.py:376-379), in one call. */
+pa_status pa_result_lengths(const pa_result *r, int32_t *len_s, int32_t *len_t);
 
 /* Alignment of a lane (codomain Alignment or Solution): Alignment::score/s_to_t/t_to_s
  * (factory.h:130-193).  `map` receives min(|s|, |t|) entries: s_to_t when |s| <= |t|,

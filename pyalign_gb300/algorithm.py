@@ -102,6 +102,8 @@ def lib():
         L.pa_result_score.argtypes = [_P, _c_i64]
         L.pa_result_alignment.argtypes = [_P, _c_i64, _PI]
         L.pa_result_export.argtypes = [_P, _PF, _PI, _PL]
+        L.pa_result_lengths.restype = _c_i32
+        L.pa_result_lengths.argtypes = [_P, _PI, _PI]
         L.pa_result_layers.restype = _c_i32
         L.pa_result_layers.argtypes = [_P, _c_i64]
         L.pa_result_max_degree_1.restype = _c_i32
@@ -269,12 +271,29 @@ def _narrow(a, dtype):
     return a.astype(np.int32, copy=False)
 
 
-class Alignment:
-    """Alignment (factory.h:130-193): score plus s_to_t / t_to_s, -1 where unaligned."""
+class _AlignmentBatch:
+    """The exported results of one solve call that lazy Alignment objects read from: all
+    scores, all maps (int32; a lane's slice is narrowed to the index type when read),
+    per-lane offsets and lengths."""
 
-    __slots__ = ("_ls", "_lt", "_score", "_s_to_t", "_t_to_s", "_dtype")
+    __slots__ = ("scores", "maps", "offs", "sizes", "ls", "lt", "dtype")
+
+    def __init__(self, scores, maps, offs, sizes, ls, lt, dtype):
+        self.scores, self.maps, self.offs, self.sizes = scores, maps, offs, sizes
+        self.ls, self.lt, self.dtype = ls, lt, dtype
+
+
+class Alignment:
+    """Alignment (factory.h:130-193): score plus s_to_t / t_to_s, -1 where unaligned.
+
+    Alignments of a batch are created lazily (`_lazy`): they hold their batch and lane until
+    a field is read, so a call returning 65,536 of them costs one export, not 65,536
+    array conversions (pyalign wraps each one, solve.py:376-379)."""
+
+    __slots__ = ("_ls", "_lt", "_score", "_s_to_t", "_t_to_s", "_dtype", "_src", "_k")
 
     def __init__(self, ls, lt, score, mp, index_dtype):
+        self._src = None
         self._ls, self._lt = ls, lt
         self._score = float(score)
         self._dtype = index_dtype
@@ -284,8 +303,30 @@ class Alignment:
         else:
             self._s_to_t, self._t_to_s = None, mp
 
+    @classmethod
+    def _lazy(cls, batch, k):
+        a = cls.__new__(cls)
+        a._src = batch
+        a._k = k
+        return a
+
+    def _load(self):
+        b, k = self._src, self._k
+        self._src = None
+        self._ls, self._lt = int(b.ls[k]), int(b.lt[k])
+        self._score = float(b.scores[k])
+        self._dtype = b.dtype
+        o = int(b.offs[k])
+        mp = _narrow(b.maps[o:o + int(b.sizes[k])], b.dtype)
+        if self._ls <= self._lt:
+            self._s_to_t, self._t_to_s = mp, None
+        else:
+            self._s_to_t, self._t_to_s = None, mp
+
     @property
     def score(self):
+        if self._src is not None:
+            self._load()
         return self._score
 
     @staticmethod
@@ -297,12 +338,16 @@ class Alignment:
 
     @property
     def s_to_t(self):
+        if self._src is not None:
+            self._load()
         if self._s_to_t is None:
             self._s_to_t = self._invert(self._t_to_s, self._ls, self._dtype)
         return self._s_to_t
 
     @property
     def t_to_s(self):
+        if self._src is not None:
+            self._load()
         if self._t_to_s is None:
             self._t_to_s = self._invert(self._s_to_t, self._lt, self._dtype)
         return self._t_to_s
@@ -565,9 +610,11 @@ class Solver:
     def _lanes(self, res):
         L = lib()
         n = L.pa_result_size(res.ptr)
-        ls = [L.pa_result_len_s(res.ptr, k) for k in range(n)]
-        lt = [L.pa_result_len_t(res.ptr, k) for k in range(n)]
-        return n, ls, lt
+        ls = np.zeros((n,), dtype=np.int32)
+        lt = np.zeros((n,), dtype=np.int32)
+        if n:
+            check(L.pa_result_lengths(res.ptr, _ip(ls), _ip(lt)))
+        return n, ls.tolist(), lt.tolist()
 
     def _alignments(self, res):
         n, ls, lt = self._lanes(res)
@@ -578,8 +625,9 @@ class Solver:
         maps = np.zeros((int(sizes.sum()),), dtype=np.int32)
         scores = np.zeros((n,), dtype=np.float32)
         check(lib().pa_result_export(res.ptr, _fp(scores), _ip(maps), offs.ctypes.data_as(_PL)))
-        return tuple(Alignment(ls[k], lt[k], scores[k], maps[offs[k]:offs[k] + sizes[k]], self._index_dtype)
-                     for k in range(n))
+        batch = _AlignmentBatch(scores, maps, offs, sizes, ls, lt, self._index_dtype)
+        lazy = Alignment._lazy
+        return tuple(lazy(batch, k) for k in range(n))
 
     def _iterators(self, res, cls):
         n, ls, lt = self._lanes(res)

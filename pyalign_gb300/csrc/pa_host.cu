@@ -404,7 +404,7 @@ struct Plan {
 // or Solution values.
 bool cols2_ok(const Plan &plan, bool want_values) { return plan.use_int && plan.tb != TB_ALL && !want_values; }
 
-// Group width G (lanes per pair, R = 8 rows each) that minimises the cells a launch
+// Group width G (lanes per pair, R = 8 rows each; G = 1 is a lane per pair) that minimises the cells a launch
 // computes: the real cells plus the padding rows of each pair's last stripe and the G-1
 // skew steps of every stripe.  Narrower groups share a warp with other pairs and pay more
 // per-stripe overhead: a 6% penalty per halving (measured: G = 8 beats G = 4 on uniform
@@ -413,14 +413,14 @@ bool cols2_ok(const Plan &plan, bool want_values) { return plan.use_int && plan.
 int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, int sm_count) {
 	if (const char *e = std::getenv("PA_GROUP_WIDTH")) {  // experiments and tuning
 		const int g = std::atoi(e);
-		if (g == 4 || g == 8 || g == 16 || g == 32) return g;
+		if (g == 1 || g == 2 || g == 4 || g == 8 || g == 16 || g == 32) return g;
 	}
-	static const int cand[4] = {32, 16, 8, 4};
+	static const int cand[6] = {32, 16, 8, 4, 2, 1};  // 1: a lane per pair
 	int64_t pairs = 0;
 	for (size_t k = 0; k < ls.size(); k++) pairs += (ls[k] > 0 && lt[k] > 0);
 	double best = 0;
 	int bestG = 32;
-	for (int c = 0; c < 4; c++) {
+	for (int c = 0; c < 6; c++) {
 		const int G = cand[c];
 		const int64_t rpp = int64_t(G) * R;
 		double cells = 0;
@@ -913,8 +913,8 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 	// candidates: every group width whose stripe is not far taller than the pairs, and the
 	// stripe-chained mode when the longest pairs span several 256-row stripes
 	std::vector<std::pair<int, bool>> cand;
-	for (int G : {32, 16, 8, 4})
-		if (G == 4 || int64_t(G) * R <= 2 * plan.max_ls) cand.push_back({G, false});
+	for (int G : {32, 16, 8, 4, 2, 1})
+		if (G == 4 || (int64_t(G) * R <= 2 * plan.max_ls && (G >= 4 || plan.max_ls <= 256))) cand.push_back({G, false});
 	if (plan.max_ls > 2 * 32 * R) cand.push_back({32, true});
 	if (cand.size() < 2) return PA_OK;
 	cudaStream_t st = s->stream;
@@ -1792,6 +1792,12 @@ void pa_result_destroy(pa_result *r) { delete r; }
 int64_t pa_result_size(const pa_result *r) { return r ? r->d->batch : 0; }
 int64_t pa_result_len_s(const pa_result *r, int64_t lane) { return r->d->ls[size_t(lane)]; }
 int64_t pa_result_len_t(const pa_result *r, int64_t lane) { return r->d->lt[size_t(lane)]; }
+pa_status pa_result_lengths(const pa_result *r, int32_t *len_s, int32_t *len_t) {
+	if (!r || !len_s || !len_t) return fail(PA_ERR_INVALID_ARGUMENT, "null argument");
+	std::memcpy(len_s, r->d->ls.data(), r->d->ls.size() * 4);
+	std::memcpy(len_t, r->d->lt.data(), r->d->lt.size() * 4);
+	return PA_OK;
+}
 
 int32_t pa_result_has_alignment(const pa_result *r, int64_t lane) {
 	const ResultData &d = *r->d;

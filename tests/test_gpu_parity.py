@@ -282,3 +282,23 @@ def test_one_and_two_column_kernels(gpu_alg, oracle_alg, monkeypatch, gap, local
             if gap != "dtw":
                 d = _run_both(gpu_alg, oracle_alg, opts, method, "binary", pairs, eq=2.0, ne=-3.0)
                 assert d is None, f"cols={cols} binary {method}: {d}"
+
+
+@pytest.mark.parametrize("width", ["1", "2"])
+@pytest.mark.parametrize("locality", ["local", "global", "semiglobal"])
+def test_lane_per_pair_widths(gpu_alg, oracle_alg, monkeypatch, width, locality):
+    """Group widths below four lanes (1: a lane per pair, its 8 rows per stripe) that the
+    autotuner offers for short pairs; integer and float scoring against the oracle."""
+    monkeypatch.setenv("PA_GROUP_WIDTH", width)
+    rng = np.random.default_rng(zlib.crc32(f"narrow/{width}/{locality}".encode()))
+    pairs = random_pairs(rng, 40, 0, 60, alphabet=4, related=0.6)
+    for method in ("score", "alignment", "solution"):
+        detail = "score" if method == "score" else ("solution" if method == "solution" else "alignment")
+        opts = options(gpu_alg, locality=locality, detail=detail, gap=GAPS["affine"])
+        d = _run_both(gpu_alg, oracle_alg, opts, method, "binary", pairs, eq=2.0, ne=-3.0)
+        assert d is None, f"{method}: {d}"
+        d = _run_both(gpu_alg, oracle_alg, opts, method, "indexed", pairs, table=_table(rng, 4, integer=False))
+        assert d is None, f"float {method}: {d}"
+    opts = options(gpu_alg, locality=locality, detail="alignment", count="all", gap=GAPS["linear"])
+    d = _run_both(gpu_alg, oracle_alg, opts, "alignment_iterator", "binary", pairs[:12], eq=1.0, ne=-1.0, iter_cap=20)
+    assert d is None, f"all optimal: {d}"
