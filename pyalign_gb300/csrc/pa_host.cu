@@ -16,6 +16,7 @@
 #include <numeric>
 #include <stack>
 #include <string>
+#include <unordered_map>
 #include <unordered_set>
 #include <vector>
 
@@ -153,7 +154,39 @@ struct ResultData {
 	std::vector<int32_t> paths, path_len;
 	std::vector<int64_t> mask_off;
 	std::vector<uint32_t> masks_one;  // TB_ONE words (solutions)
-	std::vector<uint32_t> masks_all;  // TB_ALL: 4 words per lane-step
+	// TB_ALL: 4 words per lane-step, left on the device (the result owns the buffer) and
+	// read by the host DFS in 64 KB chunks on demand: the DFS touches the cells near the
+	// optimal paths only, a few MB of masks that can be 16 bytes per cell in total
+	void *dev_masks_all = nullptr;
+	int64_t dev_masks_words = 0;
+	static constexpr int64_t CHUNK = 16384;  // words per chunk
+	mutable std::unordered_map<int64_t, std::vector<uint32_t>> mchunks;
+	mutable int64_t mchunk_bytes = 0;
+	ResultData() = default;
+	ResultData(const ResultData &) = delete;  // owns dev_masks_all
+	ResultData &operator=(const ResultData &) = delete;
+	~ResultData() {
+		if (dev_masks_all) cudaFree(dev_masks_all);
+	}
+	uint32_t mask_word(int64_t w) const {
+		const int64_t c = w / CHUNK;
+		auto it = mchunks.find(c);
+		if (it == mchunks.end()) {
+			if (mchunk_bytes > (int64_t(256) << 20)) {  // bound the cache
+				mchunks.clear();
+				mchunk_bytes = 0;
+			}
+			const int64_t n = std::min(CHUNK, dev_masks_words - c * CHUNK);
+			std::vector<uint32_t> buf(size_t(std::max<int64_t>(n, 1)), 0u);
+			if (n > 0 &&
+			    cudaMemcpy(buf.data(), static_cast<const uint32_t *>(dev_masks_all) + c * CHUNK, size_t(n) * 4,
+			               cudaMemcpyDeviceToHost) != cudaSuccess)
+				std::fill(buf.begin(), buf.end(), 0u);
+			mchunk_bytes += n * 4;
+			it = mchunks.emplace(c, std::move(buf)).first;
+		}
+		return it->second[size_t(w - c * CHUNK)];
+	}
 	std::vector<int64_t> val_off;
 	std::vector<float> values;
 	// general (WSB) gap: traceback codes and values per lane
@@ -178,7 +211,7 @@ struct ResultData {
 		const int q = i / rpp, rem = i - q * rpp, sb = rem / R, r = rem - sb * R;
 		const int64_t S = lt[lane] + G - 1;
 		const size_t e = size_t(mask_off[lane] + (int64_t(q) * S + (j + sb)) * G + sb);
-		const uint32_t w = masks_all[4 * e + size_t(r >> 1)];
+		const uint32_t w = mask_word(int64_t(4 * e) + (r >> 1));
 		return (w >> (16 * (r & 1))) & 0xffffu;
 	}
 	// WSB one-optimal traceback code of D(i, j): kind (0 none, 1 diag, 2 vertical k, 3 horizontal k)
@@ -1407,8 +1440,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		}
 	}
 	if (tb == TB_ALL && s->gap != GAP_GENERAL) {
-		res.masks_all.resize(size_t(mask_off[size_t(B)]) * 4);
-		PA_CUDA(pa_copy(s, res.masks_all.data(), s->d_masks.p, res.masks_all.size() * 4, cudaMemcpyDeviceToHost, st));
+		// the result takes the mask buffer over (the solver allocates a new one next time)
+		res.dev_masks_all = s->d_masks.p;
+		res.dev_masks_words = mask_off[size_t(B)] * 4;
+		s->d_masks.p = nullptr;
+		s->d_masks.cap = 0;
 	}
 	if (tb == TB_ONE && want_values && s->gap != GAP_GENERAL) {
 		res.masks_one.resize(size_t(mask_off[size_t(B)]));
