@@ -42,7 +42,7 @@ BYTES_PER_CELL = 0.5
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--pairs", type=int, default=65536)
@@ -123,60 +123,87 @@ def options_dict(alg, batch_size):
 # --------------------------------------------------------------------------- clocks
 
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling during the timed region (read-only)."""
+    """nvidia-smi clock/throttle sampling (read-only) every 20 ms, started before the
+    warm-up; each sample carries the host time it arrived, and a summary keeps only the
+    samples inside the marked timed region."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 20
 
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.samples = []          # (host monotonic time, line)
+        self.regions = {}
+        self.first = threading.Event()
 
     def __enter__(self):
+        return self.start()
+
+    def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            self.first.wait(timeout=10.0)   # nvidia-smi's start-up must not eat the timed region
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.samples.append((time.monotonic(), line.strip()))
+            self.first.set()
+
+    def begin(self, name):
+        self.regions[name] = [time.monotonic(), None]
+
+    def end(self, name):
+        self.regions[name][1] = time.monotonic()
 
     def __exit__(self, *exc):
+        self.stop()
+
+    def stop(self):
         if self.proc:
+            time.sleep(2.0 * self.PERIOD_MS / 1000.0)   # the sample after the last mark
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
-        sm, mx, reasons = [], [], set()
+    def summary(self, name):
+        t0, t1 = self.regions.get(name, (None, None))
+        sm, mx, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for t, line in self.samples:
+            if t0 is None or t1 is None or not (t0 <= t <= t1):
+                continue
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 7:
                 continue
             try:
                 sm.append(float(parts[0]))
                 mx.append(float(parts[1]))
+                pw.append(float(parts[2]))
             except ValueError:
                 continue
             for nm, v in zip(names, parts[3:7]):
                 if v.lower() == "active":
                     reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+               "period_ms": self.PERIOD_MS, "window_s": None if t1 is None else t1 - t0}
+        if sm:
+            out.update({"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": max(mx),
+                        "power_w_median": statistics.median(pw), "reasons": sorted(reasons),
+                        "samples": len(sm)})
+        return out
 
 
 # --------------------------------------------------------------------------- CPU baseline
@@ -601,6 +628,7 @@ def run_ours(args):
         return float(t.item())
 
     # ---- device-resident timing
+    clocks = ClockSampler(local).start()
     for _ in range(args.warmup):
         step_device()
     barrier()
@@ -608,16 +636,17 @@ def run_ours(args):
     ms4 = (ctypes.c_float * 4)()
     nl = ctypes.c_int32(0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        e0.record(stream)
-        for _ in range(args.steps):
-            step_device()
-            L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
-            dp_ms.append(ms4[1])
-            walk_ms.append(ms4[2])
-            launches += nl.value
-        e1.record(stream)
-        barrier()
+    clocks.begin("device")
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_device()
+        L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
+        dp_ms.append(ms4[1])
+        walk_ms.append(ms4[2])
+        launches += nl.value
+    e1.record(stream)
+    barrier()
+    clocks.end("device")
     elapsed = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
     value = cells * world * args.steps / elapsed / 1e9
 
@@ -673,11 +702,14 @@ def run_ours(args):
     for _ in range(max(1, args.warmup)):
         step_host()
     barrier()
+    clocks.begin("e2e")
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step_host()
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
+    clocks.end("e2e")
+    clocks.stop()
     e2e = cells * world * args.steps / e2e_s / 1e9
     h2d, d2h = ctypes.c_int64(0), ctypes.c_int64(0)
     L.pa_solver_last_bytes(solver.handle, ctypes.byref(h2d), ctypes.byref(d2h))
@@ -745,7 +777,7 @@ def run_ours(args):
         "other_configs": others,
         "precision": prec,
         "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms)},
-        "clocks": clocks.summary(),
+        "clocks": dict(clocks.summary("device"), e2e=clocks.summary("e2e")),
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
