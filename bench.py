@@ -310,7 +310,8 @@ def other_configs(torch, alg, L, seed):
         nl = ctypes.c_int32(0)
         L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
         cells = float((ls.astype(np.int64) * lt).sum())
-        return {"value": cells / t / 1e9, "unit": "GCUPS", "ms": t * 1000, "dp_ms": ms4[1], "traceback_ms": ms4[2]}
+        return {"value": cells / t / 1e9, "unit": "GCUPS", "ms": t * 1000, "dp_ms": ms4[1], "traceback_ms": ms4[2],
+                "plan": solver.last_plan()}
 
     def opts(alg_, locality, detail, gap, batch, count="ONE"):
         return {"solver": alg_.Type.ALIGNMENT, "direction": alg_.Direction.MAXIMIZE, "batch": True,
@@ -565,6 +566,7 @@ def run_ours(args):
     pbuild.build()
     L = alg.lib()
     L.pa_measure_int32_peak.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+    L.pa_measure_int16x2_peak.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     L.pa_solver_last_bytes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
 
     # each rank solves its own batch (pairs are independent: weak scaling, no collective)
@@ -632,7 +634,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         step_device()
     barrier()
-    dp_ms, walk_ms, launches = [], [], 0
+    dp_ms, walk_ms, up_ms, down_ms, launches = [], [], [], [], 0
     ms4 = (ctypes.c_float * 4)()
     nl = ctypes.c_int32(0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -641,14 +643,17 @@ def run_ours(args):
     for _ in range(args.steps):
         step_device()
         L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
+        up_ms.append(ms4[0])
         dp_ms.append(ms4[1])
         walk_ms.append(ms4[2])
+        down_ms.append(ms4[3])
         launches += nl.value
     e1.record(stream)
     barrier()
     clocks.end("device")
     elapsed = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
     value = cells * world * args.steps / elapsed / 1e9
+    plan = solver.last_plan()
 
     # correctness spot check of the device results against the host path below
     sc_dev = sc_d.cpu().numpy().copy()
@@ -721,10 +726,16 @@ def run_ours(args):
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the DP kernel (int32 ALU bound; traceback stores are the HBM side)
-    peak = ctypes.c_float(0)
+    # ---- roofline of the DP kernel (integer ALU bound; traceback stores are the HBM side).
+    # The denominator is the measured peak of the arithmetic the chosen kernel computes in:
+    # int32 lanes, or packed 16-bit pairs (two lane operations per instruction).
+    packed = plan["arithmetic"] == "int16x2"
+    peak32, peak16 = ctypes.c_float(0), ctypes.c_float(0)
     pms = ctypes.c_float(0)
-    alg.check(L.pa_measure_int32_peak(ctypes.byref(peak), ctypes.byref(pms)))
+    alg.check(L.pa_measure_int32_peak(ctypes.byref(peak32), ctypes.byref(pms)))
+    alg.check(L.pa_measure_int16x2_peak(ctypes.byref(peak16), ctypes.byref(pms)))
+    peak = peak16 if packed else peak32
+    peak_fn = "pa_measure_int16x2_peak" if packed else "pa_measure_int32_peak"
     dp_s = statistics.mean(dp_ms) / 1000.0
     achieved_ops = cells * OPS_PER_CELL / dp_s / 1e9
     peaks = {}
@@ -736,14 +747,15 @@ def run_ours(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     alg_bytes = cells * BYTES_PER_CELL + float((ls.astype(np.int64) + lt.astype(np.int64)).sum()) * 4
     traffic = None
-    prof = os.path.join(REPO, "profiles", "dp_affine_local_traffic.json")
+    prof = os.path.join(REPO, "profiles", "dp16_affine_local_traffic.json" if packed else "dp_affine_local_traffic.json")
     if os.path.exists(prof):
         with open(prof) as f:
             pj = json.load(f)
         traffic = pj["dram_bytes_per_cell"] * cells
     roof_alu = {"bound": "alu", "achieved": achieved_ops, "peak": float(peak.value), "unit": "Gop/s",
                 "frac": achieved_ops / float(peak.value), "traffic": traffic,
-                "ops_per_cell": OPS_PER_CELL, "peak_source": "measured in-run (pa_measure_int32_peak)"}
+                "ops_per_cell": OPS_PER_CELL, "peak_source": f"measured in-run ({peak_fn})",
+                "int32_peak": float(peak32.value), "int16x2_peak": float(peak16.value)}
     roof_hbm = {"bound": "hbm", "achieved": alg_bytes / dp_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": alg_bytes / dp_s / 1e9 / hbm_peak, "traffic": traffic,
                 "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback"}
@@ -776,7 +788,9 @@ def run_ours(args):
         "fwd_bwd": fb,
         "other_configs": others,
         "precision": prec,
-        "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms)},
+        "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms),
+                               "before_dp": statistics.mean(up_ms), "after_traceback": statistics.mean(down_ms)},
+        "plan": plan,
         "clocks": dict(clocks.summary("device"), e2e=clocks.summary("e2e")),
     }
     print(json.dumps(line), flush=True)

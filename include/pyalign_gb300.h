@@ -334,6 +334,14 @@ pa_status pa_path_scores_f64(int32_t type, int32_t locality, int32_t direction, 
  * kernels launched.  Measured with CUDA events on the solver's stream. */
 pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel_launches);
 
+/* The DP plan of the last solve on this solver (diagnostic): plan4[0] = kernel family
+ * (0: one column per lane step, 1: two columns per lane step, 2: stripe-chained, 3: packed
+ * 16-bit twin pairs, one column per step, 4: general gap costs, 5: packed 16-bit twin pairs,
+ * two columns per step), plan4[1] = lanes per pair group G, plan4[2] =
+ * arithmetic (0: float32, 1: int32, 2: packed int16), plan4[3] = 1 when the solve ran as a
+ * replayed CUDA graph.  No counterpart in the reference. */
+pa_status pa_solver_last_plan(const pa_solver *s, int32_t *plan4);
+
 /* Bytes copied host->device and device->host by the last solve call of this solver
  * (inputs, per-pair metadata, results). */
 pa_status pa_solver_last_bytes(const pa_solver *s, int64_t *h2d, int64_t *d2h);
@@ -342,6 +350,10 @@ pa_status pa_solver_last_bytes(const pa_solver *s, int64_t *h2d, int64_t *d2h);
  * DP cell update, used as the denominator of the DP kernels' roofline.  No counterpart in
  * the reference (it has no GPU code). */
 pa_status pa_measure_int32_peak(float *gops, float *ms);
+
+/* Diagnostic: the same mix on packed 16-bit pairs (add.s16x2 / max.s16x2), counted as two
+ * operations per instruction: the roofline denominator of the packed 16-bit twin kernel. */
+pa_status pa_measure_int16x2_peak(float *gops, float *ms);
 
 /* ---- allocation-free score solve ----
  * No counterpart in the reference (its solver allocates its matrices on the host).

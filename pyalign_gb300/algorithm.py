@@ -78,6 +78,7 @@ def lib():
         L.pa_solver_batch_size.argtypes = [_P]
         L.pa_solver_set_stream.argtypes = [_P, _P]
         L.pa_solver_last_timings.argtypes = [_P, _PF, _PI]
+        L.pa_solver_last_plan.argtypes = [_P, _PI]
         dense = [_P, _PF, _c_i64, _c_i64, _c_i64, _PI]
         indexed = [_P, _PU, _PU, _c_i64, _c_i64, _c_i64, _PF, _c_i64, _c_i64, _PI]
         binary = [_P, _PU, _PU, _c_i64, _c_i64, _c_i64, _c_f32, _c_f32, _PI]
@@ -546,6 +547,15 @@ class Solver:
         n = ctypes.c_int32(0)
         lib().pa_solver_last_timings(self._h, ms, ctypes.byref(n))
         return list(ms), n.value
+
+    KERNELS = ("one-column", "two-column", "stripe-chained", "16-bit twins", "general gaps", "16-bit twins, two-column")
+
+    def last_plan(self):
+        """(kernel family, lanes per pair group, arithmetic, graph replay) of the last solve."""
+        v = (ctypes.c_int32 * 4)()
+        lib().pa_solver_last_plan(self._h, v)
+        return {"kernel": self.KERNELS[v[0]], "G": v[1], "arithmetic": ("float32", "int32", "int16x2")[v[2]],
+                "graph": bool(v[3])}
 
     # --- argument marshalling (pytensor casts of factory.h:424-507)
     @staticmethod

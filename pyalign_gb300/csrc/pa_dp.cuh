@@ -116,7 +116,28 @@ struct DpParams {
 	const int32_t *level_start;
 	int32_t *progress;      // per ticket, zeroed before the launch
 	int4 *chain;            // per ticket: running seed of the stripes so far (value bits, i, j)
+	// packed 16-bit twin kernel (dp16_kernel, pa_dp16.cuh): gap addends and the sentinel as
+	// value * 16 + tag in both halves, borders likewise (left16[i+1] = D(i,-1), top16[j+1] =
+	// D(-1,j)); the table holds value * 16 + 8
+	uint32_t h_open_s, h_ext_s, h_open_t, h_ext_t, h_up, h_left, h_neg;
+	const uint32_t *left16;
+	const uint32_t *top16;
+	// indexed form: the largest code of a and of b (written by codes_max_kernel earlier in
+	// the stream) and the bounds they must stay below; a launch with a code out of bounds
+	// does no work and sets ST_BAD_CODE (codes_valid)
+	const uint32_t *codes_max;
+	uint32_t code_lim_a, code_lim_b;
 };
+
+// False (and ST_BAD_CODE set) when a code of the launch lies outside the similarity table:
+// every thread reads the same two words, so a whole launch returns before any table access.
+template <typename P>
+__device__ __forceinline__ bool codes_valid(const P &p) {
+	if (!p.codes_max) return true;
+	const bool ok = p.codes_max[0] < p.code_lim_a && p.codes_max[1] < p.code_lim_b;
+	if (!ok && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(p.status, ST_BAD_CODE);
+	return ok;
+}
 
 __device__ __forceinline__ int32_t ld_acquire(const int32_t *a) {
 	int32_t v;
@@ -339,6 +360,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 	constexpr bool TAG = ISINT && TB != TB_ALL;  // int32 tagged values
 	constexpr bool KEYSEED = TAG && TB == TB_ONE && LOC == LOC_LOCAL;  // packed (value, j) seed keys
 	typedef typename V2T<V>::type V2;
+	if (!codes_valid(p)) return;
 
 	extern __shared__ unsigned char smem_raw[];
 	V *stab = reinterpret_cast<V *>(smem_raw);
@@ -809,6 +831,8 @@ struct WalkParams {
 	const int64_t *mask_off;
 	int32_t G;
 	int32_t cols;   // columns per lane step of the DP that wrote the masks (1: dp_kernel, 2: dp2_kernel)
+	int32_t fmt16;  // 1: nibbles of dp16_kernel (code in bits 2-3, P-open bit 0, Q-open bit 1)
+	const int32_t *status;  // the DP's status: a launch that flagged ST_BAD_CODE has no masks
 	int32_t gap;    // GapKind
 	int32_t local;  // 1: stop at value-0 cells
 	int32_t *maps;  // min(ls, lt) per pair at map_off

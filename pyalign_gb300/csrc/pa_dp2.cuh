@@ -65,6 +65,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp2_kernel(DpParams<int32_t> p) {
 	constexpr bool TAG = true;
 	constexpr bool KEYSEED = TB == TB_ONE && LOC == LOC_LOCAL;
 	static_assert(TB != TB_ALL, "all-optimal masks use dp_kernel");
+	if (!codes_valid(p)) return;
 
 	extern __shared__ unsigned char smem_raw[];
 	V *stab = reinterpret_cast<V *>(smem_raw);

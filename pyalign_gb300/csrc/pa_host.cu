@@ -336,6 +336,7 @@ struct pa_solver {
 	cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 	float last_ms[4] = {0, 0, 0, 0};
 	int32_t last_launches = 0;
+	int32_t last_plan[4] = {0, 0, 0, 0};  // kernel family, G, arithmetic, graph replay
 	int64_t bytes_h2d = 0, bytes_d2h = 0;
 
 	DevBuf d_a, d_b, d_tab, d_dense, d_dense_off, d_ls, d_lt, d_order, d_mask_off, d_score, d_seed, d_has,
@@ -353,8 +354,8 @@ struct pa_solver {
 		int64_t *mask_off, *map_off, *path_off, *val_off, *dense_off;
 	} m{};
 	std::vector<std::pair<uint64_t, int>> occ_cache;  // (kernel variant, smem) -> blocks per SM
-	DevBuf d_border_mode[3];          // borders per arithmetic mode: float, int tagged, int plain
-	bool border_ready[3] = {false, false, false};
+	DevBuf d_border_mode[4];          // borders per arithmetic mode: float, int tagged, int plain, packed 16-bit
+	bool border_ready[4] = {false, false, false, false};
 	std::vector<unsigned char> h_tab;  // staging of the converted similarity table
 
 	// Repeated solves: the signature of the last device-resident solve and, once the same
@@ -373,7 +374,8 @@ struct pa_solver {
 		std::vector<int64_t> user_map_off, user_path_off, dense_off;
 		// the plan and what the downloads need from it
 		int G = 0, C = 1, launches = 0, key_shift = 0, ntickets = 0, nlevels = 0;
-		bool units = false, use_int = false;
+		bool units = false, use_int = false, h16 = false;
+		int32_t h_neg = 0;
 		std::vector<int64_t> mask_off, map_off, path_off, val_off;
 		cudaGraphExec_t exec = nullptr;
 	} rep;
@@ -431,7 +433,78 @@ struct Plan {
 	bool units = false;        // stripe-chained mode (G = 32): one ticket per stripe
 	int32_t ntickets = 0, nlevels = 0;
 	int C = 1;                 // columns per lane step: 2 = dp2_kernel (int32 tagged, no values)
+	bool h16 = false;          // packed 16-bit twin pairs (dp16_kernel); h_neg is its sentinel
+	int32_t h_neg = 0;
+	int C32 = 1;               // columns per lane step of the int32/float kernels for this launch
 };
+
+// The packed 16-bit twin kernel (pa_dp16.cuh) computes a launch exactly when every value
+// it forms fits an int16 as value * 16 + tag, with room below the smallest real value for
+// the sentinel and the addends applied to it.  Bounds, in value units: no D exceeds the
+// largest similarity times the shorter length (plus the largest border); no real D, P or Q
+// falls below the smallest border minus the costs of one gap down and one gap across the
+// whole matrix (local alignment: below minus one gap opening and extension, the zero floor
+// holds the rest).  It also needs an indexed form with at most 4 letters of t (int8
+// profiles of 4 bytes, one prmt per two cells), similarities in [-8, 7] (int8 after the
+// scaling), gap costs of at least 1 (rows past a pair's |s| must stay below its optimum),
+// lengths of t below 65536 (16-bit column field), local or global alignment and no
+// all-optimal masks or Solution values.  PA_DP16=0 turns it off.
+bool h16_plan(const pa_solver *s, const Input &in, const float *host_table, const std::vector<int32_t> &ls,
+              const std::vector<int32_t> &lt, int tb, bool want_values, bool use_int, int32_t *neg_out) {
+	if (const char *e = std::getenv("PA_DP16"))
+		if (std::strcmp(e, "0") == 0) return false;
+	if (!use_int || want_values || tb == TB_ALL || in.form != F_INDEXED) return false;
+	if (in.table_cols > 4 || in.table_rows > MAX_SMEM_TABLE || in.table_cols < 1) return false;
+	if (s->loc != LOC_LOCAL && s->loc != LOC_GLOBAL) return false;
+	if (s->gap != GAP_LINEAR && s->gap != GAP_AFFINE) return false;
+	const pa_options &o = s->opt;
+	double us, ut, w1s, w1t;
+	if (s->gap == GAP_LINEAR) {
+		us = w1s = o.linear_s;
+		ut = w1t = o.linear_t;
+	} else {
+		us = o.affine_u_s;
+		ut = o.affine_u_t;
+		w1s = double(o.affine_u_s) + o.affine_v_s;
+		w1t = double(o.affine_u_t) + o.affine_v_t;
+	}
+	if (!(us >= 1 && ut >= 1 && w1s >= 1 && w1t >= 1)) return false;
+	double smax = -INFINITY;
+	for (int64_t k = 0; k < in.table_rows * in.table_cols; k++) {
+		const double v = double(host_table[k]) * s->sign;
+		if (v * 16 + 8 < -128 || v * 16 + 8 > 127) return false;
+		smax = std::max(smax, v);
+	}
+	int64_t mshort = 0, mls = 0, mlt = 0;
+	for (size_t k = 0; k < ls.size(); k++) {
+		if (ls[k] == 0 || lt[k] == 0) continue;
+		mshort = std::max<int64_t>(mshort, std::min(ls[k], lt[k]));
+		mls = std::max<int64_t>(mls, ls[k]);
+		mlt = std::max<int64_t>(mlt, lt[k]);
+	}
+	if (mlt >= 65536) return false;
+	double bmin = 0, bmax = 0;
+	for (int64_t k = 0; k <= mls && k < int64_t(s->left_D.size()); k++) {
+		if (!std::isfinite(s->left_D[size_t(k)])) return false;
+		bmin = std::min(bmin, double(s->left_D[size_t(k)]));
+		bmax = std::max(bmax, double(s->left_D[size_t(k)]));
+	}
+	for (int64_t k = 0; k <= mlt && k < int64_t(s->top_D.size()); k++) {
+		if (!std::isfinite(s->top_D[size_t(k)])) return false;
+		bmin = std::min(bmin, double(s->top_D[size_t(k)]));
+		bmax = std::max(bmax, double(s->top_D[size_t(k)]));
+	}
+	const double hi = std::max(0.0, smax) * double(mshort) + bmax;
+	const double one_step = std::max({w1s + us, w1t + ut, 8.0});
+	const double lo = s->loc == LOC_LOCAL ? -one_step
+	                                      : bmin - (w1s + us * double(mls)) - (w1t + ut * double(mlt)) - one_step;
+	const double neg = 16.0 * std::ceil(std::max(w1s, w1t) + std::max(us, ut) + 10.0) - 32768.0;
+	if (hi * 16.0 + 15.0 > 32767.0 || lo * 16.0 <= neg + 16.0) return false;
+	*neg_out = int32_t(neg);
+	return true;
+}
+
+uint32_t h16_pack(int32_t v) { return (uint32_t(uint16_t(int16_t(v))) * 0x10001u); }
 
 // Launches the two-column kernel can run: int32 tagged scoring without all-optimal masks
 // or Solution values.
@@ -586,6 +659,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.out_sign = s->sign;
 	const int gk = s->gap;  // GAP_LINEAR / GAP_AFFINE / GAP_DTW
 	const int diag_tag = (tag && gk != GAP_DTW) ? 2 : 0;
+	const bool h16 = ISINT && plan.h16;
 
 	// ---- sequences and substitution
 	if (in.form != F_DENSE) {
@@ -620,6 +694,21 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 		p.c_open_t = cvt<V>(-w1t, ISINT, scale, 0);
 		p.c_ext_t = cvt<V>(-o.affine_u_t, ISINT, scale, 0);
 	}
+	if (h16) {
+		// value * 16 + tag: P's open candidate carries code 1 (bits 2-3) and its open bit 0,
+		// Q's carries code 0 and its open bit 1
+		auto hv = [](float x, int tg) { return h16_pack(int32_t(std::nearbyint(x)) * 16 + tg); };
+		if (gk == GAP_LINEAR) {
+			p.h_up = hv(-o.linear_s, 4);
+			p.h_left = hv(-o.linear_t, 0);
+		} else {
+			p.h_open_s = hv(-(o.affine_u_s + o.affine_v_s), 5);
+			p.h_ext_s = hv(-o.affine_u_s, 0);
+			p.h_open_t = hv(-(o.affine_u_t + o.affine_v_t), 2);
+			p.h_ext_t = hv(-o.affine_u_t, 0);
+		}
+		p.h_neg = h16_pack(plan.h_neg);
+	}
 	// ---- borders: converted once per solver and arithmetic mode, then kept on the device
 	{
 		const size_t ns = s->left_D.size(), nt = s->top_D.size();
@@ -643,6 +732,21 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 		p.left_P = b + ns;
 		p.top_D = b + 2 * ns;
 		p.top_Q = b + 2 * ns + nt;
+		if (h16) {
+			// packed borders of the 16-bit kernel (its launches have finite borders)
+			if (!s->border_ready[3]) {
+				std::vector<uint32_t> hb(ns + nt);
+				for (size_t k = 0; k < ns; k++)
+					hb[k] = std::isfinite(s->left_D[k]) ? h16_pack(int32_t(std::nearbyint(s->left_D[k])) * 16) : 0u;
+				for (size_t k = 0; k < nt; k++)
+					hb[ns + k] = std::isfinite(s->top_D[k]) ? h16_pack(int32_t(std::nearbyint(s->top_D[k])) * 16) : 0u;
+				PA_CUDA(s->d_border_mode[3].ensure(hb.size() * 4));
+				PA_CUDA(cudaMemcpy(s->d_border_mode[3].p, hb.data(), hb.size() * 4, cudaMemcpyHostToDevice));
+				s->border_ready[3] = true;
+			}
+			p.left16 = s->d_border_mode[3].as<uint32_t>();
+			p.top16 = p.left16 + ns;
+		}
 		if (in.form == F_INDEXED) {
 			// the table (small) is converted on the host: scaled, tagged, direction-normalised;
 			// the staging buffer belongs to the solver, so the copy needs no synchronisation
@@ -651,7 +755,8 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			V *tabv = reinterpret_cast<V *>(s->h_tab.data());
 			bool fits_int8 = ISINT && tag && in.table_cols <= 8 && in.table_rows <= MAX_SMEM_TABLE;
 			for (size_t k = 0; k < nt_; k++) {
-				tabv[k] = cvt<V>(host_table[k] * s->sign, ISINT, scale, diag_tag);
+				tabv[k] = h16 ? V(int32_t(std::nearbyint(host_table[k] * s->sign)) * 16 + 8)
+				              : cvt<V>(host_table[k] * s->sign, ISINT, scale, diag_tag);
 				if (ISINT && (int64_t(tabv[k]) < -128 || int64_t(tabv[k]) > 127)) fits_int8 = false;
 			}
 			// int8 profiles read with one prmt per cell: per row in registers (alphabets of
@@ -680,6 +785,11 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.val_off = s->m.val_off;
 	p.work_counter = s->d_counter.as<int32_t>();
 	p.status = s->d_status.as<int32_t>();
+	if (in.form == F_INDEXED) {
+		p.codes_max = s->d_codes_max.as<uint32_t>();
+		p.code_lim_a = (in.batch * in.n_s > 0) ? uint32_t(in.table_rows) : 0xFFFFFFFFu;
+		p.code_lim_b = (in.batch * in.n_t > 0) ? uint32_t(in.table_cols) : 0xFFFFFFFFu;
+	}
 
 	// ---- grid and scratch
 	size_t smem = (in.form == F_INDEXED && in.table_rows <= MAX_SMEM_TABLE && in.table_cols <= MAX_SMEM_TABLE)
@@ -693,15 +803,20 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	                      (uint64_t(tb) << 48) | (uint64_t(want_values) << 44) | uint64_t(smem);
 	const bool ch = plan.units;
 	const int cols = (ISINT && plan.C == 2 && tb != TB_ALL && !want_values) ? 2 : 1;
-	const uint64_t ckey = okey | (uint64_t(ch) << 40) | (uint64_t(cols == 2) << 41);
+	const uint64_t ckey = okey | (uint64_t(ch) << 40) | (uint64_t(cols == 2) << 41) | (uint64_t(h16) << 42);
 	for (const auto &kv : s->occ_cache)
 		if (kv.first == ckey) bps = kv.second;
-	if (bps == 0) e = dp_occupancy<V>(gk, ch, loc, tb, want_values, smem, &bps, cols);
+	if (bps == 0) {
+		if (h16) e = gk == GAP_LINEAR ? occupancy_dp16_linear(loc, tb, cols, smem, &bps)
+		                              : occupancy_dp16_affine(loc, tb, cols, smem, &bps);
+		else e = dp_occupancy<V>(gk, ch, loc, tb, want_values, smem, &bps, cols);
+	}
 	PA_CUDA(e);
 	bps = std::max(bps, 1);
 	if (s->occ_cache.size() < 64) s->occ_cache.push_back({ckey, bps});
 	const int gpw = 32 / plan.G;
-	const int64_t groups_needed = plan.units ? plan.ntickets : (npairs + gpw - 1) / gpw;  // warps needed
+	const int64_t units_needed = h16 ? (npairs + 1) / 2 : npairs;  // twins or pairs
+	const int64_t groups_needed = plan.units ? plan.ntickets : (units_needed + gpw - 1) / gpw;  // warps needed
 	int64_t grid = int64_t(s->sm_count) * bps;
 	grid = std::min<int64_t>(grid, (groups_needed + WARPS - 1) / WARPS);
 	grid = std::max<int64_t>(grid, 1);
@@ -723,7 +838,13 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	}
 
 	PA_CUDA(cudaMemsetAsync(s->d_counter.p, 0, sizeof(int32_t), st));
-	e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st, cols);
+	if constexpr (std::is_same<V, int32_t>::value) {
+		if (h16) e = gk == GAP_LINEAR ? launch_dp16_linear(loc, tb, cols, p, int(grid), smem, st)
+		                              : launch_dp16_affine(loc, tb, cols, p, int(grid), smem, st);
+		else e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st, cols);
+	} else {
+		e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st, cols);
+	}
 	PA_CUDA(e);
 	(*launches)++;
 	return PA_OK;
@@ -898,6 +1019,8 @@ struct TuneEntry {
 	uint64_t key;
 	int G;
 	bool units;
+	bool h16;
+	int C;
 };
 std::mutex g_tune_mu;
 std::vector<TuneEntry> g_tune;
@@ -939,25 +1062,43 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 			if (t.key == key) {
 				plan.G = t.G;
 				plan.units = t.units;
+				plan.h16 = plan.h16 && t.h16;  // the 16-bit kernel still needs this launch's bounds
+				plan.C = plan.h16 ? t.C : plan.C32;
 				return PA_OK;
 			}
 	}
 	if (cells < TUNE_MIN_CELLS) return PA_OK;
 	// candidates: every group width whose stripe is not far taller than the pairs, and the
 	// stripe-chained mode when the longest pairs span several 256-row stripes
-	std::vector<std::pair<int, bool>> cand;
+	// (G, chained, 16-bit twins, columns per step): the 16-bit kernel, with one or two columns
+	// per step, where this launch's bounds admit it
+	const int C0 = plan.C32;
+	struct Cand {
+		int G;
+		bool units, h16;
+		int C;
+	};
+	std::vector<Cand> cand;
 	for (int G : {32, 16, 8, 4, 2, 1})
-		if (G == 4 || (int64_t(G) * R <= 2 * plan.max_ls && (G >= 4 || plan.max_ls <= 256))) cand.push_back({G, false});
-	if (plan.max_ls > 2 * 32 * R) cand.push_back({32, true});
+		if (G == 4 || (int64_t(G) * R <= 2 * plan.max_ls && (G >= 4 || plan.max_ls <= 256))) {
+			cand.push_back({G, false, false, C0});
+			if (plan.h16) {
+				cand.push_back({G, false, true, 1});
+				if (C0 == 2) cand.push_back({G, false, true, 2});
+			}
+		}
+	if (plan.max_ls > 2 * 32 * R) cand.push_back({32, true, false, C0});
 	if (cand.size() < 2) return PA_OK;
 	cudaStream_t st = s->stream;
 	float best = INFINITY;
-	int bestG = plan.G;
-	bool bestU = plan.units;
+	int bestG = plan.G, bestC = plan.C;
+	bool bestU = plan.units, bestH = plan.h16;
 	for (const auto &c : cand) {
 		Plan pl = plan;
-		pl.G = c.first;
-		pl.units = c.second;
+		pl.G = c.G;
+		pl.units = c.units;
+		pl.h16 = c.h16;
+		pl.C = c.C;
 		if (pa_status e = stage(pl)) return e;
 		PA_CUDA(cudaEventRecord(s->ev[1], st));
 		if (pa_status e = dp(pl, pl.tb, false, nullptr)) return e;
@@ -969,12 +1110,16 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 			best = ms;
 			bestG = pl.G;
 			bestU = pl.units;
+			bestH = pl.h16;
+			bestC = pl.C;
 		}
 	}
 	plan.G = bestG;
 	plan.units = bestU;
+	plan.h16 = bestH;
+	plan.C = bestC;
 	std::lock_guard<std::mutex> lk(g_tune_mu);
-	if (g_tune.size() < 4096) g_tune.push_back({key, bestG, bestU});
+	if (g_tune.size() < 4096) g_tune.push_back({key, bestG, bestU, bestH, bestC});
 	return PA_OK;
 }
 
@@ -1064,20 +1209,55 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		if (B * in.n_s > 0) codes_max_kernel<<<grid, 256, 0, st>>>(da, B * in.n_s, s->d_codes_max.as<uint32_t>());
 		if (B * in.n_t > 0) codes_max_kernel<<<grid, 256, 0, st>>>(db, B * in.n_t, s->d_codes_max.as<uint32_t>() + 1);
 		PA_CUDA(cudaGetLastError());
-		uint32_t mx[2] = {0, 0};
-		PA_CUDA(pa_copy(s, mx, s->d_codes_max.p, 8, cudaMemcpyDeviceToHost, st));
-		PA_CUDA(cudaStreamSynchronize(st));
-		if (B * in.n_s > 0 && int64_t(mx[0]) >= in.table_rows) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a");
-		if (B * in.n_t > 0 && int64_t(mx[1]) >= in.table_cols) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in b");
+		launches += int(B * in.n_s > 0) + int(B * in.n_t > 0);
+		// no wait here: the DP kernels read the maxima at launch and do nothing (ST_BAD_CODE)
+		// when a code is out of bounds; the error is raised after the solve's one sync
 	}
 
+	// ---- repeated solves: the same solve as the last call on this solver (same lengths,
+	// shapes, buffers, options, table, offsets and stream) skips planning and staging -- the
+	// device metadata, converted table and plan of that call are still in place.  A repeated
+	// device-resident solve runs, from its second repetition on, as one CUDA graph of the
+	// device work, captured on a private stream; with host buffers the inputs are copied in
+	// as always and the work is launched directly.  Any other call first drops the cached
+	// state, since it rewrites the buffers the repeat reads.  PA_GRAPHS=0 turns this off.
+	const char *genv = std::getenv("PA_GRAPHS");
+	const bool repeatable = s->gap != GAP_GENERAL && tb != TB_ALL && !want_values &&
+	                        (method == M_SCORE || method == M_ALIGNMENT || method == M_PATHS) &&
+	                        !(genv && std::strcmp(genv, "0") == 0);
+	const bool paths_to_user = method == M_PATHS && user_paths;
+	auto same_rep = [&]() -> bool {
+		const pa_solver::Repeat &r = s->rep;
+		if (!r.valid || r.method != method || r.form != in.form || r.B != B || r.n_s != in.n_s || r.n_t != in.n_t)
+			return false;
+		if (r.a != in.a || r.b != in.b || r.sim != in.sim || r.table != in.table || r.trows != in.table_rows ||
+		    r.tcols != in.table_cols || r.dsi != in.dense_si || r.dsj != in.dense_sj || r.stream != st)
+			return false;
+		if (std::memcmp(&r.eq, &in.eq, 4) || std::memcmp(&r.ne, &in.ne, 4)) return false;
+		if (r.maps_out != maps_out || r.ls != ls || r.lt != lt || r.table_host != host_table) return false;
+		if (r.scores != (paths_to_user ? user_paths->scores : nullptr)) return false;
+		if (paths_to_user && (r.paths != user_paths->paths || r.path_len != user_paths->path_len ||
+		                      std::memcmp(r.user_path_off.data(), user_paths->path_off, size_t(B) * 8)))
+			return false;
+		if (maps_out && map_offsets && (r.user_map_off.size() != size_t(B) ||
+		                                std::memcmp(r.user_map_off.data(), map_offsets, size_t(B) * 8)))
+			return false;
+		if (in.dense_off_host && (r.dense_off.size() != size_t(B) ||
+		                          std::memcmp(r.dense_off.data(), in.dense_off_host, size_t(B) * 8)))
+			return false;
+		return true;
+	};
+	const bool hit = repeatable && same_rep();
+	if (!hit) s->drop_graph();
+
 	// ---- plan: group width and mode, arithmetic; the tuner may try several plans
+	// (a repeated solve takes the plan of the call it repeats: no planning)
 	Plan plan;
 	plan.max_ls = max_ls;
 	plan.max_lt = max_lt;
-	plan.G = choose_G(ls, lt, s->sm_count);
 	plan.tb = tb;
-	if (s->gap != GAP_GENERAL) {
+	if (!hit) plan.G = choose_G(ls, lt, s->sm_count);
+	if (!hit && s->gap != GAP_GENERAL) {
 		plan.units = choose_units(ls, lt, s->sm_count, plan.G);
 		if (plan.units) plan.G = 32;
 		double bound = 0;
@@ -1093,6 +1273,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		plan.C = cols2_ok(plan, want_values) ? 2 : 1;
 		if (const char *e = std::getenv("PA_DP_COLS"))  // experiments and tests
 			if (std::atoi(e) == 1) plan.C = 1;
+		int32_t hneg = 0;
+		plan.C32 = plan.C;
+		plan.h16 = !plan.units && h16_plan(s, in, host_table.data(), ls, lt, tb, want_values, use_int, &hneg);
+		plan.h_neg = hneg;
+		if (plan.h16) plan.C = plan.C32;  // two columns per step unless PA_DP_COLS=1
 	}
 	std::vector<int32_t> order, level_start;
 	std::vector<int64_t> mask_off, map_off, path_off, val_off, dense_off;
@@ -1208,40 +1393,6 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		return pl.use_int ? run_dp<int32_t>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches)
 		                  : run_dp<float>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches);
 	};
-	// ---- repeated solves: the same device-resident solve as the last call on this solver
-	// (same lengths, shapes, buffers, options, table, offsets and stream) skips planning and
-	// staging -- the device metadata, converted table and plan of that call are still in
-	// place -- and from its second repetition on runs as one CUDA graph of the device work,
-	// captured on a private stream.  Any other call first drops the cached state, since it
-	// rewrites the buffers the graph reads.  PA_GRAPHS=0 turns this off.
-	const char *genv = std::getenv("PA_GRAPHS");
-	const bool repeatable = in.location == PA_DEVICE && s->gap != GAP_GENERAL && tb != TB_ALL && !want_values &&
-	                        (method == M_SCORE || method == M_ALIGNMENT || method == M_PATHS) &&
-	                        !(genv && std::strcmp(genv, "0") == 0);
-	const bool paths_to_user = method == M_PATHS && user_paths;
-	auto same_rep = [&]() -> bool {
-		const pa_solver::Repeat &r = s->rep;
-		if (!r.valid || r.method != method || r.form != in.form || r.B != B || r.n_s != in.n_s || r.n_t != in.n_t)
-			return false;
-		if (r.a != in.a || r.b != in.b || r.sim != in.sim || r.table != in.table || r.trows != in.table_rows ||
-		    r.tcols != in.table_cols || r.dsi != in.dense_si || r.dsj != in.dense_sj || r.stream != st)
-			return false;
-		if (std::memcmp(&r.eq, &in.eq, 4) || std::memcmp(&r.ne, &in.ne, 4)) return false;
-		if (r.maps_out != maps_out || r.ls != ls || r.lt != lt || r.table_host != host_table) return false;
-		if (r.scores != (paths_to_user ? user_paths->scores : nullptr)) return false;
-		if (paths_to_user && (r.paths != user_paths->paths || r.path_len != user_paths->path_len ||
-		                      std::memcmp(r.user_path_off.data(), user_paths->path_off, size_t(B) * 8)))
-			return false;
-		if (maps_out && map_offsets && (r.user_map_off.size() != size_t(B) ||
-		                                std::memcmp(r.user_map_off.data(), map_offsets, size_t(B) * 8)))
-			return false;
-		if (in.dense_off_host && (r.dense_off.size() != size_t(B) ||
-		                          std::memcmp(r.dense_off.data(), in.dense_off_host, size_t(B) * 8)))
-			return false;
-		return true;
-	};
-	const bool hit = repeatable && same_rep();
-	if (!hit) s->drop_graph();
 
 	const bool need_walk = tb == TB_ONE && s->gap != GAP_GENERAL &&
 	                       (method == M_ALIGNMENT || method == M_ALIGNMENT_ITER || method == M_SOLUTION ||
@@ -1284,6 +1435,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		w.mask_off = s->m.mask_off;
 		w.G = plan.G;
 		w.cols = plan.C;
+		w.fmt16 = plan.h16 ? 1 : 0;
+		w.status = s->d_status.as<int32_t>();
 		w.gap = s->gap;
 		w.local = s->loc == LOC_LOCAL;
 		w.maps = to_user ? maps_out : s->d_maps.as<int32_t>();
@@ -1311,6 +1464,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		pa_solver::Repeat &r = s->rep;
 		plan.G = r.G;
 		plan.C = r.C;
+		plan.h16 = r.h16;
+		plan.h_neg = r.h_neg;
 		plan.units = r.units;
 		plan.use_int = r.use_int;
 		plan.key_shift = r.key_shift;
@@ -1320,7 +1475,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		map_off = r.map_off;
 		path_off = r.path_off;
 		val_off = r.val_off;
-		if (!r.exec) {
+		if (in.location == PA_HOST) {
+			// host buffers: the inputs were copied to the solver's own buffers above; the plan
+			// and the staged metadata of the last call are reused, the work is launched as is
+			if (pa_status e = device_work(st, true)) return e;
+		} else if (!r.exec) {
 			// second identical solve: capture its device work once, then launch it as a graph
 			if (!s->cap_stream) PA_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
 			cudaGraph_t graph = nullptr;
@@ -1345,8 +1504,10 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 				return fail(PA_ERR_CUDA, "capturing the repeated solve as a CUDA graph failed (PA_GRAPHS=0 disables it)");
 			}
 		}
-		PA_CUDA(cudaGraphLaunch(r.exec, st));  // records ev[1], ev[2] around the DP
-		launches += r.launches;
+		if (in.location == PA_DEVICE) {
+			PA_CUDA(cudaGraphLaunch(r.exec, st));  // records ev[1], ev[2] around the DP
+			launches += r.launches;
+		}
 	} else {
 		if (s->gap != GAP_GENERAL && tb != TB_ALL && !want_values) {
 			if (pa_status e = tune_plan(s, ls, lt, in, plan, stage, dp)) return e;
@@ -1355,6 +1516,10 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		if (pa_status e = device_work(st, true)) return e;
 	}
 	res.G = plan.G;
+	s->last_plan[0] = s->gap == GAP_GENERAL ? 4 : plan.h16 ? (plan.C == 2 ? 5 : 3) : plan.units ? 2 : plan.C == 2 ? 1 : 0;
+	s->last_plan[1] = plan.G;
+	s->last_plan[2] = plan.h16 ? 2 : plan.use_int ? 1 : 0;
+	s->last_plan[3] = hit && s->rep.exec ? 1 : 0;
 	PA_CUDA(cudaEventRecord(s->ev[3], st));
 	if (repeatable && !hit) {
 		// remember this solve for the next call
@@ -1391,6 +1556,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		                   in.dense_off_host ? in.dense_off_host + B : nullptr);
 		r.G = plan.G;
 		r.C = plan.C;
+		r.h16 = plan.h16;
+		r.h_neg = plan.h_neg;
 		r.units = plan.units;
 		r.use_int = plan.use_int;
 		r.key_shift = plan.key_shift;
@@ -1462,6 +1629,12 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	PA_CUDA(cudaStreamSynchronize(st));
 	for (int k = 0; k < 4; k++) cudaEventElapsedTime(&s->last_ms[k], s->ev[k], s->ev[k + 1]);
 	s->last_launches = launches;
+	if ((status & ST_BAD_CODE) && in.form == F_INDEXED && s->gap != GAP_GENERAL) {
+		uint32_t mx[2] = {0, 0};
+		PA_CUDA(cudaMemcpy(mx, s->d_codes_max.p, 8, cudaMemcpyDeviceToHost));
+		if (B * in.n_s > 0 && int64_t(mx[0]) >= in.table_rows) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a");
+		return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in b");
+	}
 	if (status & ST_BAD_CODE) return fail(PA_ERR_INVALID_ARGUMENT, "out of bounds index in a or b");
 	if (status & ST_TIMEOUT) return fail(PA_ERR_TIMEOUT, "a chained stripe timed out waiting for the stripe above it");
 
@@ -1683,6 +1856,13 @@ pa_status pa_solver_last_bytes(const pa_solver *s, int64_t *h2d, int64_t *d2h) {
 	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
 	if (h2d) *h2d = s->bytes_h2d;
 	if (d2h) *d2h = s->bytes_d2h;
+	return PA_OK;
+}
+
+pa_status pa_solver_last_plan(const pa_solver *s, int32_t *plan4) {
+	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
+	if (plan4)
+		for (int k = 0; k < 4; k++) plan4[k] = s->last_plan[k];
 	return PA_OK;
 }
 

@@ -31,4 +31,12 @@ PA_DECL2(affine)
 PA_DECL2(dtw)
 #undef PA_DECL2
 
+#define PA_DECL16(GAP)                                                                                  \
+	cudaError_t launch_dp16_##GAP(int loc, int tb, int cols, const DpParams<int32_t> &p, int grid, size_t smem, \
+	                              cudaStream_t st);                                                 \
+	cudaError_t occupancy_dp16_##GAP(int loc, int tb, int cols, size_t smem, int *blocks_per_sm);
+PA_DECL16(linear)
+PA_DECL16(affine)
+#undef PA_DECL16
+
 }  // namespace pa

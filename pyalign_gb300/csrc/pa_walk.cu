@@ -13,14 +13,18 @@ namespace pa {
 // The walk is a chain of dependent mask reads, so its speed is the latency of one read.
 // The warp therefore caches a window of the masks: lane l holds the word of the 8-row block
 // (u >> 3) - (l >> 4) at column v - (l & 15), i.e. 16 rows x 16 columns up-left of the cell
-// where the window was placed, loaded in one round trip.  Every lane runs the same walk
-// (all values are warp-uniform) and takes a cell's word from its lane with a shuffle; a
-// cell outside the window re-places it there.  A diagonal or gap run thus costs one memory
-// round trip per 8-16 steps instead of one per step.
+// where the window was placed, loaded in one round trip; a cell outside the window
+// re-places it there.  Runs are resolved 16 cells at a time: for a run of diagonal steps
+// lane k decodes cell (u - k, v - k) and one ballot gives the run's length (lanes then write
+// their map entries and path points in parallel), and the start of an affine gap -- the
+// first cell up or left whose extend bit is clear -- is found the same way.  A diagonal or
+// gap run thus costs one memory round trip per 8-16 cells and a few instructions per 16
+// cells instead of per cell.
 __global__ void walk_kernel(WalkParams p) {
 	const int pair = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
 	const int lane = threadIdx.x & 31;
 	if (pair >= p.npairs) return;  // whole warps
+	if (p.status && (*p.status & ST_BAD_CODE)) return;  // the DP did not run: no seeds, no masks
 	const int ls = p.len_s[pair], lt = p.len_t[pair];
 	const int nmap = min(ls, lt);
 	int32_t *map = p.maps ? p.maps + p.map_off[pair] : nullptr;
@@ -38,58 +42,89 @@ __global__ void walk_kernel(WalkParams p) {
 	const uint32_t *W = p.masks + p.mask_off[pair];
 	const int G = p.G;
 	const bool two = p.cols == 2;  // dp2_kernel layout: a uint2 per lane and step, columns j, j + 1
+	const bool fmt16 = p.fmt16 != 0;
 	const int S = two ? ((lt + 1) >> 1) + G - 1 : lt + G - 1;
 	const bool s2t = ls <= lt;
 	const bool affine = p.gap == GAP_AFFINE;
 	int ub = -1000000, vb = -1000000;  // window: row blocks ub-1..ub, columns vb-15..vb
 	uint32_t win = 0;
-	// nibble of cell (i, j), i, j >= 0 and warp-uniform (R = 8 rows per block)
-	auto nib = [&](int i, int j) -> uint32_t {
-		int dr = ub - (i >> 3), dc = vb - j;
-		if (dr < 0 || dr > 1 || dc < 0 || dc > 15) {
-			ub = i >> 3;
-			vb = j;
-			dr = 0;
-			dc = 0;
-			const int rb = ub - (lane >> 4), col = vb - (lane & 15);
-			win = 0u;
-			if (rb >= 0 && col >= 0) {
-				const int q = rb / G, sb = rb - q * G;
-				win = two ? W[((int64_t(q) * S + ((col >> 1) + sb)) * G + sb) * 2 + (col & 1)]
-				          : W[(int64_t(q) * S + (col + sb)) * G + sb];
-			}
+	// place the window with cell (i, j) at its bottom-right corner (warp-uniform i, j)
+	auto place = [&](int i, int j) {
+		ub = i >> 3;
+		vb = j;
+		const int rb = ub - (lane >> 4), col = vb - (lane & 15);
+		win = 0u;
+		if (rb >= 0 && col >= 0) {
+			const int q = rb / G, sb = rb - q * G;
+			win = two ? W[((int64_t(q) * S + ((col >> 1) + sb)) * G + sb) * 2 + (col & 1)]
+			          : W[(int64_t(q) * S + (col + sb)) * G + sb];
 		}
-		const uint32_t w = __shfl_sync(0xffffffffu, win, dr * 16 + dc);
-		// row r's nibble (D source code | P-extend << 2 | Q-extend << 3) at bits 4(R-1-r)
-		return (w >> (4 * (R - 1 - (i & (R - 1))))) & 15u;
+	};
+	auto inwin = [&](int i, int j) {
+		const int dr = ub - (i >> 3), dc = vb - j;
+		return i >= 0 && j >= 0 && dr >= 0 && dr <= 1 && dc >= 0 && dc <= 15;
+	};
+	// nibble of this lane's cell (i, j), valid where ok (the cell lies in the window): every
+	// lane reads its own cell with one shuffle.  Row r's nibble (D source code | P-extend << 2
+	// | Q-extend << 3) sits at bits 4(R-1-r); the 16-bit kernel's nibbles hold the code in
+	// bits 2-3 and the open bits in 0-1.
+	auto nib_at = [&](int i, int j, bool ok) -> uint32_t {
+		const int src = ok ? (ub - (i >> 3)) * 16 + (vb - j) : 0;
+		const uint32_t w = __shfl_sync(0xffffffffu, win, src);
+		const uint32_t n = (w >> (4 * (R - 1 - (i & (R - 1))))) & 15u;
+		return fmt16 ? ((n >> 2) | ((~n & 3u) << 2)) : n;
+	};
+	// first cell of a gap run: from (i, j) up (di = 1) or left (dj = 1) while the cell's
+	// extend bit (mask) is set and the index is positive; lane m looks m cells ahead, one
+	// ballot resolves up to 16 cells (the scalar loop: k = i; while (k > 0 && ext(k)) k--)
+	auto gap_start = [&](int i, int j, int di, int dj, uint32_t mask) -> int {
+		for (;;) {
+			if (!inwin(i, j)) place(i, j);
+			const int r = i - di * lane, c = j - dj * lane;
+			const bool ok = lane < 16 && inwin(r, c);
+			const uint32_t n = nib_at(r, c, ok);
+			const bool stop = ok && ((di ? r : c) == 0 || !(n & mask));
+			const uint32_t bs = __ballot_sync(0xffffffffu, stop);
+			const uint32_t bo = __ballot_sync(0xffffffffu, ok);
+			const int first_stop = bs ? __ffs(int(bs)) - 1 : 32;
+			const int first_out = __ffs(int(~bo)) - 1;
+			if (first_stop < first_out) return (di ? i : j) - first_stop;
+			i -= di * first_out;
+			j -= dj * first_out;
+		}
 	};
 	while (u >= 0 && v >= 0) {
-		const uint32_t code = nib(u, v) & 3u;
+		if (!inwin(u, v)) place(u, v);
+		// a run of diagonal steps: lane k < 16 looks at (u - k, v - k), one ballot finds how
+		// many consecutive cells from (u, v) have the diagonal code
+		const int iu = u - lane, iv = v - lane;
+		const bool ok = lane < 16 && inwin(iu, iv);
+		const uint32_t n = nib_at(iu, iv, ok);
+		const uint32_t bal = __ballot_sync(0xffffffffu, ok && (n & 3u) == 2u);
+		const int run = __ffs(int(~bal)) - 1;
+		if (run > 0) {
+			if (lane < run) {
+				if (map) {
+					if (s2t) map[iu] = iv;
+					else map[iv] = iu;
+				}
+				if (path) {
+					path[2 * (np + lane)] = iu - 1;
+					path[2 * (np + lane) + 1] = iv - 1;
+				}
+			}
+			u -= run;
+			v -= run;
+			np += run;
+			continue;
+		}
+		const uint32_t code = __shfl_sync(0xffffffffu, n, 0) & 3u;  // (u, v) is lane 0's cell
 		if (p.local && code == 3u) break;
 		int nu = u, nv = v;
-		if (code == 2u) {
-			if (map && lane == 0) {
-				if (s2t) map[u] = v;
-				else map[v] = u;
-			}
-			nu = u - 1;
-			nv = v - 1;
-		} else if (code == 1u) {
-			if (affine) {
-				int k = u;
-				while (k > 0 && (nib(k, v) & 4u)) k--;
-				nu = k - 1;
-			} else {
-				nu = u - 1;
-			}
+		if (code == 1u) {
+			nu = (affine ? gap_start(u, v, 1, 0, 4u) : u) - 1;
 		} else {
-			if (affine) {
-				int k = v;
-				while (k > 0 && (nib(u, k) & 8u)) k--;
-				nv = k - 1;
-			} else {
-				nv = v - 1;
-			}
+			nv = (affine ? gap_start(u, v, 0, 1, 8u) : v) - 1;
 		}
 		u = nu;
 		v = nv;
@@ -99,10 +134,26 @@ __global__ void walk_kernel(WalkParams p) {
 	if (p.path_len && lane == 0) p.path_len[pair] = np;
 }
 
+// Largest code of an array, folded into *out with atomicMax.  Streams 16-byte words with
+// four loads in flight per thread (the reads are the whole cost: 4 bytes per code), after a
+// scalar head up to the first 16-byte boundary and before a scalar tail.
 __global__ void codes_max_kernel(const uint32_t *x, int64_t n, uint32_t *out) {
+	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	const int64_t nth = int64_t(gridDim.x) * blockDim.x;
+	const int64_t head = min(n, int64_t(((16 - (reinterpret_cast<uintptr_t>(x) & 15)) & 15) >> 2));
 	uint32_t m = 0;
-	const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-	for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) m = max(m, x[k]);
+	if (tid < head) m = x[tid];
+	const uint4 *v = reinterpret_cast<const uint4 *>(x + head);
+	const int64_t nv = (n - head) >> 2;
+	for (int64_t k = tid; k < nv; k += 4 * nth) {
+		uint4 q[4];
+#pragma unroll
+		for (int u = 0; u < 4; u++) q[u] = k + u * nth < nv ? __ldcs(v + k + u * nth) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+		for (int u = 0; u < 4; u++) m = max(m, max(max(q[u].x, q[u].y), max(q[u].z, q[u].w)));
+	}
+	const int64_t t0 = head + 4 * nv;
+	if (t0 + tid < n) m = max(m, x[t0 + tid]);  // at most 3 tail codes
 	for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
 	if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }

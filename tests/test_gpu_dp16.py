@@ -1,0 +1,187 @@
+"""The packed 16-bit twin-pair DP kernel against the oracle (needs a GPU).
+
+The solver runs two pairs per lane in the two 16-bit halves of every register whenever a
+launch's value bounds fit 16 bits (indexed form, at most 4 letters of t, similarities in
+[-8, 7], gap costs >= 1, local or global, one traceback or none).  Here every such case is
+compared with the oracle bit for bit: ragged twins (the two pairs of a twin differ in |s|
+and |t|), empty pairs, single rows and columns, stripe-multiple lengths, an odd pair count
+(the last twin has one pair), all-mismatch pairs whose local optimum is 0, several group
+widths, maximize and minimize.  The kernel family that ran is read back from the solver, and
+launches outside the bounds must fall back to the int32 kernels.  A bench-like bag is
+compared with the int32 kernels GPU against GPU.
+"""
+
+import zlib
+
+import numpy as np
+import pytest
+
+from _cases import Gap, call, compare, options, pack, random_pairs
+
+pytestmark = pytest.mark.gpu
+
+GAPS = {"linear": Gap("linear", 2.0), "affine": Gap("affine", 5.0, 2.0)}
+TWINS = {"1": "16-bit twins", "2": "16-bit twins, two-column"}
+
+
+@pytest.fixture(scope="module")
+def gpu_alg():
+    from pyalign_gb300 import build
+    build.build()
+    from pyalign_gb300 import algorithm as alg
+    if alg.lib().pa_device_count() == 0:
+        pytest.fail("no CUDA device visible")
+    return alg
+
+
+@pytest.fixture()
+def analytic(monkeypatch):
+    """The analytic plan in group mode (few-pair launches would otherwise be stripe-chained)."""
+    monkeypatch.setenv("PA_TUNE", "0")
+    monkeypatch.setenv("PA_DP_MODE", "groups")
+
+
+@pytest.fixture(params=["1", "2"])
+def cols(request, monkeypatch):
+    """One or two columns per lane step."""
+    if request.param == "1":
+        monkeypatch.setenv("PA_DP_COLS", "1")
+    return request.param
+
+
+def _table(rng, direction):
+    t = rng.integers(-4, 0, size=(4, 4)).astype(np.float32)
+    np.fill_diagonal(t, rng.integers(2, 7, size=4))
+    return -t if direction == "minimize" else t
+
+
+def _pairs(rng, n):
+    pairs = random_pairs(rng, n, 1, 300, alphabet=4, related=0.6)
+    pairs[0] = (pairs[0][0][:0], pairs[0][1])                 # empty s
+    pairs[1] = (pairs[1][0], pairs[1][1][:0])                 # empty t
+    pairs[2] = (pairs[2][0][:1], pairs[2][1])                 # one row
+    pairs[3] = (pairs[3][0], pairs[3][1][:1])                 # one column
+    pairs[4] = (pairs[4][0][:64], pairs[4][1][:64])           # one stripe of G = 8 exactly
+    pairs[5] = (pairs[5][0][:65], pairs[5][1])                # one row into the next stripe
+    pairs[6] = (np.zeros(40, np.uint32), np.ones(37, np.uint32))   # all mismatches: optimum 0
+    pairs[7] = (np.zeros(9, np.uint32), np.zeros(250, np.uint32))  # twin partner of very different shape
+    return pairs
+
+
+def _run(gpu_alg, oracle_alg, opts, method, pairs, table):
+    n = len(pairs)
+    a, b, ln = pack(pairs, n)
+    cap = (max(a.shape[1], 1), max(b.shape[1], 1))
+    o = dict(opts, batch_size=n, batch=True)
+    solver, g = call(gpu_alg, o, cap, method, "indexed", a, b, ln, table=table)
+    plan = solver.last_plan()
+    _, r = call(oracle_alg, o, cap, method, "indexed", a, b, ln, table=table)
+    return plan, compare(method, g, r, n)
+
+
+@pytest.mark.parametrize("gap", ["linear", "affine"])
+@pytest.mark.parametrize("locality", ["local", "global"])
+@pytest.mark.parametrize("method", ["score", "alignment"])
+@pytest.mark.parametrize("direction", ["maximize", "minimize"])
+def test_dp16_parity(analytic, cols, gpu_alg, oracle_alg, gap, locality, method, direction):
+    rng = np.random.default_rng(zlib.crc32(f"dp16/{gap}/{locality}/{method}/{direction}".encode()))
+    pairs = _pairs(rng, 61)
+    detail = "score" if method == "score" else "alignment"
+    opts = options(gpu_alg, locality=locality, direction=direction, detail=detail, gap=GAPS[gap])
+    plan, d = _run(gpu_alg, oracle_alg, opts, method, pairs, _table(rng, direction))
+    assert plan["kernel"] == TWINS[cols], plan
+    assert d is None, d
+
+
+@pytest.mark.parametrize("G", ["1", "2", "4", "16", "32"])
+def test_dp16_group_widths(monkeypatch, cols, gpu_alg, oracle_alg, G):
+    monkeypatch.setenv("PA_GROUP_WIDTH", G)
+    rng = np.random.default_rng(int(G) + 500)
+    pairs = _pairs(rng, 45)
+    opts = options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"])
+    plan, d = _run(gpu_alg, oracle_alg, opts, "alignment", pairs, _table(rng, "maximize"))
+    assert plan["kernel"] == TWINS[cols] and plan["G"] == int(G), plan
+    assert d is None, d
+
+
+def test_dp16_bounds_fall_back(analytic, gpu_alg, oracle_alg):
+    """Outside the 16-bit bounds the int32 kernels run, with the same results."""
+    rng = np.random.default_rng(77)
+    pairs = _pairs(rng, 20)
+    opts = options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"])
+    table = _table(rng, "maximize")
+    table[0, 0] = 9.0                                         # similarity outside [-8, 7]
+    plan, d = _run(gpu_alg, oracle_alg, opts, "alignment", pairs, table)
+    assert not plan["kernel"].startswith("16-bit"), plan
+    assert d is None, d
+    # a local optimum that may exceed 2047: 7 * 300 > 2047
+    table = np.full((4, 4), -2.0, np.float32)
+    np.fill_diagonal(table, 7.0)
+    long_pairs = [(np.zeros(300, np.uint32), np.zeros(300, np.uint32))] + pairs[:5]
+    plan, d = _run(gpu_alg, oracle_alg, opts, "alignment", long_pairs, table)
+    assert not plan["kernel"].startswith("16-bit"), plan
+    assert d is None, d
+    # a zero gap extension (rows past |s| would not stay below the optimum)
+    opts0 = options(gpu_alg, locality="local", detail="alignment", gap=Gap("affine", 3.0, 0.0))
+    plan, d = _run(gpu_alg, oracle_alg, opts0, "alignment", pairs, _table(rng, "maximize"))
+    assert not plan["kernel"].startswith("16-bit"), plan
+    assert d is None, d
+
+
+@pytest.mark.parametrize("locality", ["local", "global"])
+def test_dp16_matches_int32_large(gpu_alg, monkeypatch, cols, locality):
+    """3000 pairs of |s|, |t| ~ U[100, 1000] (DNA +2/-3, affine 5/2; global only up to the
+    lengths the bounds admit): scores and alignments of the 16-bit kernel equal the int32
+    kernels', GPU against GPU."""
+    rng = np.random.default_rng(808)
+    n = 3000
+    hi = 1000 if locality == "local" else 250
+    ls = rng.integers(100 if locality == "local" else 20, hi + 1, size=n)
+    lt = rng.integers(100 if locality == "local" else 20, hi + 1, size=n)
+    a = rng.integers(0, 4, size=(n, hi)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, hi)).astype(np.uint32)
+    half = n // 2
+    b[:half, :hi] = a[:half, :hi]                             # related half: mutated copies
+    mut = rng.random(size=(half, hi)) < 0.1
+    b[:half][mut] = rng.integers(0, 4, size=int(mut.sum()))
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    ln = np.stack([ls, lt]).astype(np.uint16)
+    monkeypatch.setenv("PA_TUNE", "0")
+    monkeypatch.setenv("PA_DP_MODE", "groups")
+    out = {}
+    for dp16 in ("1", "0"):
+        monkeypatch.setenv("PA_DP16", dp16)
+        for detail in ("score", "alignment"):
+            opts = options(gpu_alg, locality=locality, detail=detail, gap=GAPS["affine"], batch_size=n)
+            solver = gpu_alg.m16.create_solver(hi, hi, gpu_alg.m16.create_options(opts))
+            if detail == "score":
+                out[(dp16, detail)] = np.asarray(solver.solve_indexed_for_score(a, b, table, ln))
+            else:
+                res = solver.solve_indexed_for_alignment(a, b, table, ln)
+                out[(dp16, detail)] = [(r.score, r.s_to_t.tolist()) for r in res]
+            kernel = solver.last_plan()["kernel"]
+            assert (kernel == TWINS[cols]) == (dp16 == "1"), (dp16, kernel)
+    assert np.array_equal(out[("1", "score")], out[("0", "score")])
+    assert out[("1", "alignment")] == out[("0", "alignment")]
+
+
+def test_dp16_bad_codes_then_valid(analytic, gpu_alg, oracle_alg):
+    """A code outside the table raises (the kernels check the launch's code maxima and do no
+    work), and the same solver then solves a valid bag correctly."""
+    rng = np.random.default_rng(5150)
+    pairs = _pairs(rng, 30)
+    n = len(pairs)
+    a, b, ln = pack(pairs, n)
+    table = _table(rng, "maximize")
+    opts = dict(options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"]), batch_size=n, batch=True)
+    solver = gpu_alg.m16.create_solver(a.shape[1], b.shape[1], gpu_alg.m16.create_options(opts))
+    bad = b.copy()
+    bad[3, 0] = 4
+    with pytest.raises(ValueError, match="out of bounds index in b"):
+        solver.solve_indexed_for_alignment(a, bad, table, ln)
+    g = solver.solve_indexed_for_alignment(a, b, table, ln)
+    assert solver.last_plan()["kernel"].startswith("16-bit"), solver.last_plan()
+    _, r = call(oracle_alg, opts, (a.shape[1], b.shape[1]), "alignment", "indexed", a, b, ln, table=table)
+    d = compare("alignment", g, r, n)
+    assert d is None, d

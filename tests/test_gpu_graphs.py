@@ -138,3 +138,54 @@ def test_repeated_dense_paths_and_gradients(env, monkeypatch):
     monkeypatch.setenv("PA_GRAPHS", "0")
     assert torch.equal(got, run())
     assert not torch.equal(got, want)
+
+
+def test_repeated_host_batch_solves(env, monkeypatch):
+    """pa_solve_batch with host buffers: a repeat reuses the plan and staged metadata (no
+    graph); new contents and new lengths are solved exactly as by a solver that never caches."""
+    torch, alg, ag = env
+    P = ctypes.POINTER
+    rng = np.random.default_rng(17)
+    n, n_s, n_t = 700, 260, 300
+    ln = np.stack([rng.integers(0, n_s + 1, n), rng.integers(1, n_t + 1, n)]).astype(np.int32)
+    a = rng.integers(0, 4, size=(n, n_s)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, n_t)).astype(np.uint32)
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+
+    def solve(solver, a, b, ln):
+        sizes = np.minimum(ln[0], ln[1]).astype(np.int64)
+        offs = np.zeros(n, np.int64)
+        offs[1:] = np.cumsum(sizes)[:-1]
+        sc = np.full(n, np.nan, np.float32)
+        mp = np.full(max(1, int(sizes.sum())), -7, np.int32)
+        length = np.ascontiguousarray(ln, dtype=np.int32)
+        bt = alg.Batch(form=1, location=0, batch=n, n_s=n_s, n_t=n_t,
+                       a=a.ctypes.data_as(P(ctypes.c_uint32)), b=b.ctypes.data_as(P(ctypes.c_uint32)),
+                       table=table.ctypes.data_as(P(ctypes.c_float)), table_rows=4, table_cols=4,
+                       length=length.ctypes.data_as(P(ctypes.c_int32)))
+        alg.check(alg.lib().pa_solve_batch(solver.handle, ctypes.byref(bt), sc.ctypes.data_as(ctypes.c_void_p),
+                                           mp.ctypes.data_as(ctypes.c_void_p), offs.ctypes.data_as(P(ctypes.c_int64))))
+        return sc, mp
+
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    ref = _batch_solver(alg, torch, n, n_s, n_t)
+    want = solve(ref, a, b, ln)
+    monkeypatch.delenv("PA_GRAPHS")
+    solver = _batch_solver(alg, torch, n, n_s, n_t)
+    for rep in range(3):
+        got = solve(solver, a, b, ln)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), rep
+        assert not solver.last_plan()["graph"]
+    a[:, :] = rng.integers(0, 4, size=(n, n_s))              # new contents, same host buffer
+    got = solve(solver, a, b, ln)
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    want2 = solve(ref, a, b, ln)
+    monkeypatch.delenv("PA_GRAPHS")
+    assert np.array_equal(got[0], want2[0]) and np.array_equal(got[1], want2[1])
+    ln2 = ln.copy()
+    ln2[1, :11] = 3                                           # new lengths: planned anew
+    got = solve(solver, a, b, ln2)
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    want3 = solve(ref, a, b, ln2)
+    assert np.array_equal(got[0], want3[0]) and np.array_equal(got[1], want3[1])
