@@ -116,10 +116,13 @@ struct DpParams {
 	const int32_t *level_start;
 	int32_t *progress;      // per ticket, zeroed before the launch
 	int4 *chain;            // per ticket: running seed of the stripes so far (value bits, i, j)
-	// packed 16-bit twin kernel (dp16_kernel, pa_dp16.cuh): gap addends and the sentinel as
-	// value * 16 + tag in both halves, borders likewise (left16[i+1] = D(i,-1), top16[j+1] =
-	// D(-1,j)); the table holds value * 16 + 8
-	uint32_t h_open_s, h_ext_s, h_open_t, h_ext_t, h_up, h_left, h_neg;
+	// packed 16-bit twin kernel (dp16_kernel, pa_dp16.cuh): the extend addends (value * 16,
+	// both halves), the opening / linear addends as 32-bit IMAD constants (value * 16 + tag,
+	// the low half's carry folded into the high half), the sentinel and the borders as biased
+	// values (value * 16 + 32768; left16[i+1] = D(i,-1), top16[j+1] = D(-1,j)); the table
+	// holds value * 16 + 8
+	uint32_t h_ext_s, h_ext_t, h_neg;
+	uint32_t k_open_s, k_open_t, k_up, k_left;
 	const uint32_t *left16;
 	const uint32_t *top16;
 	// indexed form: the largest code of a and of b (written by codes_max_kernel earlier in

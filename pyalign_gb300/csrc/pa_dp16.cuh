@@ -8,7 +8,8 @@
 // every add and max is one packed instruction (add.s16x2 / max.s16x2, fused to one
 // add-max or three-way max where the hardware has it) that updates both cells.
 //
-// Value encoding: value * 16 + tag.  Bits 2-3 of the tag are the push priority of the
+// Value encoding: value * 16 + tag, offset by 32768 (offset binary, compared as unsigned
+// 16-bit numbers, so the order is the signed order).  Bits 2-3 of the tag are the push priority of the
 // candidate as in the int32 kernels (zero 3 > diag 2 > P/up 1 > Q/left 0), so one max
 // chain yields the value and the reference's tie winner.  Bit 0 is set on P's "open"
 // candidate (from D above) and bit 1 on Q's (from D to the left); the "extend" candidates
@@ -31,6 +32,15 @@
 // The host admits a launch only when bounds on every value (largest similarity times the
 // shorter length, the borders, the gap costs) fit the 16-bit range with room for the
 // sentinel, so the results equal the int32 kernels' bit for bit.
+//
+// Adds of a constant to a packed value run as one 32-bit IMAD on the FMA pipe instead of a
+// packed add on the ALU pipe, which the max chains keep busy: every biased value stays above
+// the sentinel margin, which exceeds the magnitude of any negative gap addend, so adding such
+// an addend always carries out of the low half, and the host folds that carry into the high
+// half of the constant (k_open_s and friends).  The bounds hold in every cell a launch
+// computes -- the padding rows and columns of twins included (a zero or sentinel floor on
+// every row, the upper bound over the launch's whole rectangle) -- because a wrapped half
+// would carry into its neighbour.
 #pragma once
 
 #include "pa_dp.cuh"
@@ -45,20 +55,20 @@ __device__ __forceinline__ uint32_t h_add(uint32_t a, uint32_t b) {
 
 __device__ __forceinline__ uint32_t h_max(uint32_t a, uint32_t b) {
 	uint32_t d;
-	asm("max.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+	asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
 	return d;
 }
 
 // max(a + b, c) per half
 __device__ __forceinline__ uint32_t h_addmax(uint32_t a, uint32_t b, uint32_t c) {
 	uint32_t d;
-	asm("{.reg .b32 t;\n\tadd.s16x2 t, %1, %2;\n\tmax.s16x2 %0, t, %3;}" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+	asm("{.reg .b32 t;\n\tadd.u16x2 t, %1, %2;\n\tmax.u16x2 %0, t, %3;}" : "=r"(d) : "r"(a), "r"(b), "r"(c));
 	return d;
 }
 
 __device__ __forceinline__ uint32_t h_max3(uint32_t a, uint32_t b, uint32_t c) {
 	uint32_t d;
-	asm("{.reg .b32 t;\n\tmax.s16x2 t, %1, %2;\n\tmax.s16x2 %0, t, %3;}" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+	asm("{.reg .b32 t;\n\tmax.u16x2 t, %1, %2;\n\tmax.u16x2 %0, t, %3;}" : "=r"(d) : "r"(a), "r"(b), "r"(c));
 	return d;
 }
 
@@ -68,8 +78,13 @@ __device__ __forceinline__ uint32_t h_minu(uint32_t a, uint32_t b) {
 	return d;
 }
 
-__device__ __forceinline__ int32_t h_lo(uint32_t x) { return int32_t(int16_t(uint16_t(x & 0xffffu))); }
-__device__ __forceinline__ int32_t h_hi(uint32_t x) { return int32_t(x) >> 16; }
+// the (value * 16 + tag) of the low or high half, bias removed
+__device__ __forceinline__ int32_t h_lo(uint32_t x) { return int32_t(x & 0xffffu) - 32768; }
+__device__ __forceinline__ int32_t h_hi(uint32_t x) { return int32_t(x >> 16) - 32768; }
+// x + k as one IMAD (FMA pipe); k carries the low half's carry (see above)
+__device__ __forceinline__ uint32_t h_addk(uint32_t x, int32_t one, uint32_t k) {
+	return uint32_t(imad(int32_t(x), one, int32_t(k)));
+}
 
 // One cell of each half: (D, P) from above, the D to the left and its Q, the diagonal D, the
 // score S; returns the tagged key, writes D, P, Q (see the encoding above).
@@ -81,13 +96,13 @@ __device__ __forceinline__ uint32_t cell16(const DpParams<int32_t> &p, uint32_t 
 	constexpr uint32_t CLR_PF = 0xFFFEFFFEu;   // P without its open bit
 	constexpr uint32_t CLR_QF = 0xFFFDFFFDu;   // Q without its open bit
 	if (GAP == GAP_AFFINE) {
-		P = h_addmax(uP & CLR_PF, p.h_ext_s, h_add(uD, p.h_open_s));
-		Q = h_addmax(Qleft & CLR_QF, p.h_ext_t, h_add(old, p.h_open_t));
+		P = h_addmax(uP & CLR_PF, p.h_ext_s, h_addk(uD, p.one, p.k_open_s));
+		Q = h_addmax(Qleft & CLR_QF, p.h_ext_t, h_addk(old, p.one, p.k_open_t));
 	} else {
-		P = h_add(uD, p.h_up);
-		Q = h_add(old, p.h_left);
+		P = h_addk(uD, p.one, p.k_up);
+		Q = h_addk(old, p.one, p.k_left);
 	}
-	const uint32_t m = LOC == LOC_LOCAL ? h_max3(P, Q, floor_) : h_max(P, Q);
+	const uint32_t m = h_max3(P, Q, floor_);  // zero floor (local) or sentinel floor
 	const uint32_t key = h_addmax(dsave, S, m);
 	D = key & CLR_TAG;
 	return key;
@@ -137,7 +152,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 	static_assert(LOC == LOC_LOCAL || LOC == LOC_GLOBAL, "local or global");
 	static_assert(TB != TB_ALL, "one traceback or none");
 	static_assert(C == 1 || C == 2, "one or two columns per step");
-	constexpr uint32_t HMIN = 0x80008000u;     // the int16 minimum in both halves
+	constexpr uint32_t HMIN = 0u;              // below every biased value
 	constexpr uint32_t INVALID_ROW = 0x80808080u;
 	constexpr bool SEED = LOC == LOC_LOCAL;
 	if (!codes_valid(p)) return;
@@ -222,7 +237,10 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 				}
 				prA[r] = xa;
 				prB[r] = xb;
-				fl[r] = (vA ? 0x0000000Cu : (NEG & 0x0000FFFFu)) | (vB ? 0x000C0000u : (NEG & 0xFFFF0000u));
+				// zero (tag 12, biased) on local rows, else the sentinel: no value falls below it
+				fl[r] = LOC == LOC_LOCAL
+				            ? ((vA ? 0x0000800Cu : (NEG & 0x0000FFFFu)) | (vB ? 0x800C0000u : (NEG & 0xFFFF0000u)))
+				            : NEG;
 				Dl[r] = (pass_active && i < ls) ? p.left16[i + 1] : NEG;
 				Ql[r] = NEG;
 			}
@@ -240,6 +258,19 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 				const int64_t sB = C == 2 ? ((ltB + 1) >> 1) + G - 1 : ltB + G - 1;
 				if (pass_active && q < npA) mA = m + p.mask_off[pa] + (int64_t(q) * sA * G + sub) * C;
 				if (pass_active && q < npB) mB = m + p.mask_off[pb] + (int64_t(q) * sB * G + sub) * C;
+			}
+			// lane 0: the (D, P) above this pass's first row in the next step's columns, read one
+			// step ahead -- the border row, or the boundary row the group's last lane wrote in the
+			// previous pass (complete before this pass: same warp, __syncwarp between passes)
+			int2 bn0 = make_int2(int32_t(NEG), int32_t(NEG)), bn1 = bn0;
+			if (sub == 0 && pass_active) {
+				if (q == 0) {
+					bn0.x = int32_t(p.top16[1]);
+					if (C == 2 && lt > 1) bn1.x = int32_t(p.top16[2]);
+				} else {
+					bn0 = bin[0];
+					if (C == 2 && lt > 1) bn1 = bin[1];
+				}
 			}
 			uint32_t tnA0 = pass_active ? browA[0] : 0u, tnB0 = pass_active ? browB[0] : 0u;
 			uint32_t tnA1 = (C == 2 && pass_active && lt > 1) ? browA[1] : 0u;
@@ -266,23 +297,13 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 					tnB1 = browB[j0 + 3];
 				}
 				if (sub == 0 && act) {
-					if (q == 0) {
-						upD0 = p.top16[j0 + 1];
-						upP0 = NEG;
-						if (C == 2) {
-							upD1 = act1 ? p.top16[j1 + 1] : NEG;
-							upP1 = NEG;
-						}
-					} else {
-						const int2 b0 = bin[j0];
-						upD0 = uint32_t(b0.x);
-						upP0 = uint32_t(b0.y);
-						if (act1) {
-							const int2 b1 = bin[j1];
-							upD1 = uint32_t(b1.x);
-							upP1 = uint32_t(b1.y);
-						}
-					}
+					upD0 = uint32_t(bn0.x);
+					upP0 = uint32_t(bn0.y);
+					upD1 = uint32_t(bn1.x);
+					upP1 = uint32_t(bn1.y);
+					const int n0 = j0 + C, n1 = j0 + 3;  // the next step's columns
+					if (n0 < lt) bn0 = q == 0 ? make_int2(int32_t(p.top16[n0 + 1]), int32_t(NEG)) : bin[n0];
+					if (C == 2 && n1 < lt) bn1 = q == 0 ? make_int2(int32_t(p.top16[n1 + 1]), int32_t(NEG)) : bin[n1];
 				}
 				if (act) {
 					// prmt selectors: half A = byte tcA of prA sign-extended, half B = byte tcB of prB
@@ -316,11 +337,11 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 						}
 						if (SEED) {
 							const uint32_t t0 = TB == TB_ONE ? uint32_t(r * C) * 0x10001u : 0u;
-							const uint32_t k0 = D0 | t0;
+							const uint32_t k0 = TB == TB_ONE ? h_addk(D0, p.one, t0) : D0;  // D0 | t0
 							if ((r & 1) == 0) even0 = k0;
 							else smax0 = h_max3(smax0, even0, k0);
 							if (C == 2) {
-								const uint32_t k1 = D1 | (TB == TB_ONE ? t0 + 0x10001u : 0u);
+								const uint32_t k1 = TB == TB_ONE ? h_addk(D1, p.one, t0 + 0x10001u) : D1;
 								if ((r & 1) == 0) even1 = k1;
 								else smax1 = h_max3(smax1, even1, k1);
 							}
@@ -400,7 +421,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 				// a later pass has larger rows, so it wins a tie of values
 				const int32_t kA = h_lo(lm), kB = h_hi(lm);
 				const int rsh = C == 2 ? 1 : 0;
-				if (kA != -32768) {
+				if (kA != -32768) {  // the lane saw a cell of the pair
 					const int32_t v = (kA >> 4) * 4;
 					if (v >= bestA) {
 						bestA = v;

@@ -494,7 +494,9 @@ bool h16_plan(const pa_solver *s, const Input &in, const float *host_table, cons
 		bmin = std::min(bmin, double(s->top_D[size_t(k)]));
 		bmax = std::max(bmax, double(s->top_D[size_t(k)]));
 	}
-	const double hi = std::max(0.0, smax) * double(mshort) + bmax;
+	// a twin computes the larger of its two pairs' shapes: bound the upper side over the
+	// launch's whole rectangle (at least the largest shorter length of one pair)
+	const double hi = std::max(0.0, smax) * double(std::max(mshort, std::min(mls, mlt))) + bmax;
 	const double one_step = std::max({w1s + us, w1t + ut, 8.0});
 	const double lo = s->loc == LOC_LOCAL ? -one_step
 	                                      : bmin - (w1s + us * double(mls)) - (w1t + ut * double(mlt)) - one_step;
@@ -504,7 +506,13 @@ bool h16_plan(const pa_solver *s, const Input &in, const float *host_table, cons
 	return true;
 }
 
+// a 16-bit addend in both halves
 uint32_t h16_pack(int32_t v) { return (uint32_t(uint16_t(int16_t(v))) * 0x10001u); }
+// a value (value * 16 + tag) in both halves, biased by 32768
+uint32_t h16_value(int32_t v) { return uint32_t(uint16_t(v + 32768)) * 0x10001u; }
+// a negative addend c as a 32-bit constant: adding it to a biased value always carries out
+// of the low half (the value exceeds -c), so the high half takes c - 1
+uint32_t h16_addk(int32_t c) { return (uint32_t(uint16_t(c - 1)) << 16) | uint32_t(uint16_t(c)); }
 
 // Launches the two-column kernel can run: int32 tagged scoring without all-optimal masks
 // or Solution values.
@@ -697,17 +705,17 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	if (h16) {
 		// value * 16 + tag: P's open candidate carries code 1 (bits 2-3) and its open bit 0,
 		// Q's carries code 0 and its open bit 1
-		auto hv = [](float x, int tg) { return h16_pack(int32_t(std::nearbyint(x)) * 16 + tg); };
+		auto raw = [](float x, int tg) { return int32_t(std::nearbyint(x)) * 16 + tg; };
 		if (gk == GAP_LINEAR) {
-			p.h_up = hv(-o.linear_s, 4);
-			p.h_left = hv(-o.linear_t, 0);
+			p.k_up = h16_addk(raw(-o.linear_s, 4));
+			p.k_left = h16_addk(raw(-o.linear_t, 0));
 		} else {
-			p.h_open_s = hv(-(o.affine_u_s + o.affine_v_s), 5);
-			p.h_ext_s = hv(-o.affine_u_s, 0);
-			p.h_open_t = hv(-(o.affine_u_t + o.affine_v_t), 2);
-			p.h_ext_t = hv(-o.affine_u_t, 0);
+			p.k_open_s = h16_addk(raw(-(o.affine_u_s + o.affine_v_s), 5));
+			p.h_ext_s = h16_pack(raw(-o.affine_u_s, 0));
+			p.k_open_t = h16_addk(raw(-(o.affine_u_t + o.affine_v_t), 2));
+			p.h_ext_t = h16_pack(raw(-o.affine_u_t, 0));
 		}
-		p.h_neg = h16_pack(plan.h_neg);
+		p.h_neg = h16_value(plan.h_neg);
 	}
 	// ---- borders: converted once per solver and arithmetic mode, then kept on the device
 	{
@@ -736,10 +744,13 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			// packed borders of the 16-bit kernel (its launches have finite borders)
 			if (!s->border_ready[3]) {
 				std::vector<uint32_t> hb(ns + nt);
-				for (size_t k = 0; k < ns; k++)
-					hb[k] = std::isfinite(s->left_D[k]) ? h16_pack(int32_t(std::nearbyint(s->left_D[k])) * 16) : 0u;
-				for (size_t k = 0; k < nt; k++)
-					hb[ns + k] = std::isfinite(s->top_D[k]) ? h16_pack(int32_t(std::nearbyint(s->top_D[k])) * 16) : 0u;
+				// (borders beyond the launch's bounds are never read; clamped to stay encodable)
+				auto bv16 = [](float x) {
+					const double v = std::isfinite(x) ? std::nearbyint(double(x)) * 16.0 : -30000.0;
+					return h16_value(int32_t(std::min(30000.0, std::max(-30000.0, v))));
+				};
+				for (size_t k = 0; k < ns; k++) hb[k] = bv16(s->left_D[k]);
+				for (size_t k = 0; k < nt; k++) hb[ns + k] = bv16(s->top_D[k]);
 				PA_CUDA(s->d_border_mode[3].ensure(hb.size() * 4));
 				PA_CUDA(cudaMemcpy(s->d_border_mode[3].p, hb.data(), hb.size() * 4, cudaMemcpyHostToDevice));
 				s->border_ready[3] = true;
