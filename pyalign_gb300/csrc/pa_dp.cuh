@@ -825,7 +825,8 @@ __global__ void codes_max_kernel(const uint32_t *x, int64_t n, uint32_t *out);
 // alignment map: a point is an edge when the next step moves diagonally
 // (path_compressor, solver.h:809-847); P/Q steps jump to the gap-open cell.
 struct WalkParams {
-	int32_t npairs;
+	int32_t npairs;  // pairs pair0 .. pair0 + npairs - 1, a warp each
+	int32_t pair0;
 	const int32_t *len_s;
 	const int32_t *len_t;
 	const int32_t *seed;

@@ -376,11 +376,18 @@ struct pa_solver {
 		int G = 0, C = 1, launches = 0, key_shift = 0, ntickets = 0, nlevels = 0;
 		bool units = false, use_int = false, h16 = false;
 		int32_t h_neg = 0;
+		int nchunks = 1;
 		std::vector<int64_t> mask_off, map_off, path_off, val_off;
 		cudaGraphExec_t exec = nullptr;
 	} rep;
 	cudaStream_t cap_stream = nullptr;  // private stream the graph is captured on
 	bool capturing = false;
+	cudaStream_t copy_stream = nullptr;   // uploads and downloads of a pipelined host-buffer repeat
+	cudaStream_t cmp2 = nullptr;          // its second compute stream (odd chunks)
+	DevBuf d_counter2, d_scratch2;        // work counter and scratch rows of DP launches on cmp2
+	std::vector<cudaEvent_t> ev_chunk;    // its per-chunk ordering events
+	bool skip_table = false;              // run_dp: the converted table is already on the device
+	cudaEvent_t table_ev = nullptr;       // run_dp: recorded once the converted table is copied
 
 	void drop_graph() {
 		if (rep.exec) cudaGraphExecDestroy(rep.exec);
@@ -394,6 +401,9 @@ struct pa_solver {
 			if (e) cudaEventDestroy(e);
 		if (meta_ev) cudaEventDestroy(meta_ev);
 		if (cap_stream) cudaStreamDestroy(cap_stream);
+		for (auto &e : ev_chunk) cudaEventDestroy(e);
+		if (copy_stream) cudaStreamDestroy(copy_stream);
+		if (cmp2) cudaStreamDestroy(cmp2);
 		if (own_stream) cudaStreamDestroy(own_stream);
 	}
 };
@@ -436,6 +446,7 @@ struct Plan {
 	bool h16 = false;          // packed 16-bit twin pairs (dp16_kernel); h_neg is its sentinel
 	int32_t h_neg = 0;
 	int C32 = 1;               // columns per lane step of the int32/float kernels for this launch
+	int nchunks = 1;           // repeated host-buffer solves: pipeline of this many pair ranges
 };
 
 // The packed 16-bit twin kernel (pa_dp16.cuh) computes a launch exactly when every value
@@ -504,6 +515,15 @@ bool h16_plan(const pa_solver *s, const Input &in, const float *host_table, cons
 	if (hi * 16.0 + 15.0 > 32767.0 || lo * 16.0 <= neg + 16.0) return false;
 	*neg_out = int32_t(neg);
 	return true;
+}
+
+// Pair range [k0, k1) of chunk c of a pipelined solve of B pairs in K chunks: sizes grow as
+// 1 : 2 : 4 : ..., so each chunk's upload (about 4x faster per pair than its DP) is hidden
+// behind the previous chunk's DP and only the small first chunk's upload is exposed.
+void chunk_range(int64_t B, int K, int c, int64_t &k0, int64_t &k1) {
+	const int64_t den = (int64_t(1) << K) - 1;
+	k0 = B * ((int64_t(1) << c) - 1) / den;
+	k1 = B * ((int64_t(1) << (c + 1)) - 1) / den;
 }
 
 // a 16-bit addend in both halves
@@ -645,14 +665,18 @@ cudaError_t dp_occupancy(int gk, bool chain, int loc, int tb, bool vals, size_t 
 
 template <typename V>
 pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const float *host_table,
-                 int64_t npairs, bool want_values, const float *best_in_dev, int *launches) {
+                 int64_t npairs, bool want_values, const float *best_in_dev, int *launches, int64_t first = 0,
+                 int codes_slot = 0, int side = 0) {
 	const bool ISINT = std::is_same<V, int32_t>::value;
 	const bool tag = ISINT && tb != TB_ALL;
 	const int scale = tag ? 4 : 1;
-	cudaStream_t st = s->stream;
+	// side 1: a pipeline chunk on the second compute stream, with its own counter and scratch
+	cudaStream_t st = side ? s->cmp2 : s->stream;
+	DevBuf &counter = side ? s->d_counter2 : s->d_counter;
+	DevBuf &scratch = side ? s->d_scratch2 : s->d_scratch;
 	DpParams<V> p{};
 	p.npairs = int32_t(npairs);
-	p.order = s->m.order;
+	p.order = s->m.order + first;  // a pipeline chunk: its pairs occupy order[first, first + npairs)
 	p.len_s = s->m.ls;
 	p.len_t = s->m.lt;
 	p.sub_kind = in.form == F_DENSE ? SUB_DENSE : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
@@ -781,7 +805,9 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 			if (sk && std::strcmp(sk, "table") == 0) p.sub_kind = SUB_TABLE;
 			if (sk && std::strcmp(sk, "colprof") == 0 && colprof_ok) p.sub_kind = SUB_COLPROF;
 			PA_CUDA(s->d_tab.ensure(nt_ * sizeof(V)));
-			if (!s->capturing) PA_CUDA(pa_copy(s, s->d_tab.p, tabv, nt_ * sizeof(V), cudaMemcpyHostToDevice, st));
+			if (!s->capturing && !s->skip_table)
+				PA_CUDA(pa_copy(s, s->d_tab.p, tabv, nt_ * sizeof(V), cudaMemcpyHostToDevice, st));
+			if (s->table_ev) PA_CUDA(cudaEventRecord(s->table_ev, st));
 			p.table = s->d_tab.as<V>();
 		}
 	}
@@ -794,10 +820,11 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.best_in = best_in_dev;
 	p.values = want_values ? s->d_vals.as<float>() : nullptr;
 	p.val_off = s->m.val_off;
-	p.work_counter = s->d_counter.as<int32_t>();
+	PA_CUDA(counter.ensure(4));
+	p.work_counter = counter.as<int32_t>();
 	p.status = s->d_status.as<int32_t>();
 	if (in.form == F_INDEXED) {
-		p.codes_max = s->d_codes_max.as<uint32_t>();
+		p.codes_max = s->d_codes_max.as<uint32_t>() + 2 * codes_slot;
 		p.code_lim_a = (in.batch * in.n_s > 0) ? uint32_t(in.table_rows) : 0xFFFFFFFFu;
 		p.code_lim_b = (in.batch * in.n_t > 0) ? uint32_t(in.table_cols) : 0xFFFFFFFFu;
 	}
@@ -834,8 +861,8 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	// scratch rows: per group slot, or per pair in the stripe-chained mode
 	const int64_t slots = plan.units ? std::max<int64_t>(npairs, 1) : grid * WARPS * gpw;
 	p.scratch_stride = 2 * std::max<int64_t>(plan.max_lt, 1);
-	PA_CUDA(s->d_scratch.ensure(size_t(slots * p.scratch_stride) * 2 * sizeof(V)));
-	p.scratch = s->d_scratch.p;
+	PA_CUDA(scratch.ensure(size_t(slots * p.scratch_stride) * 2 * sizeof(V)));
+	p.scratch = scratch.p;
 	if (plan.units) {
 		p.units = 1;
 		p.ntickets = plan.ntickets;
@@ -848,7 +875,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 		PA_CUDA(cudaMemsetAsync(s->d_progress.p, 0, size_t(plan.ntickets) * 4, st));
 	}
 
-	PA_CUDA(cudaMemsetAsync(s->d_counter.p, 0, sizeof(int32_t), st));
+	PA_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(int32_t), st));
 	if constexpr (std::is_same<V, int32_t>::value) {
 		if (h16) e = gk == GAP_LINEAR ? launch_dp16_linear(loc, tb, cols, p, int(grid), smem, st)
 		                              : launch_dp16_affine(loc, tb, cols, p, int(grid), smem, st);
@@ -1188,20 +1215,6 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	cudaEventRecord(s->ev[0], st);
 	int launches = 0;
 
-	// ---- upload inputs
-	if (in.location == PA_HOST) {
-		if (in.form == F_DENSE) {
-			const size_t n = size_t(in.n_s * in.n_t * B) * sizeof(float);
-			PA_CUDA(s->d_dense.ensure(n));
-			if (n) PA_CUDA(pa_copy(s, s->d_dense.p, in.sim, n, cudaMemcpyHostToDevice, st));
-		} else {
-			const size_t na = size_t(B * in.n_s) * sizeof(uint32_t), nb = size_t(B * in.n_t) * sizeof(uint32_t);
-			PA_CUDA(s->d_a.ensure(na));
-			PA_CUDA(s->d_b.ensure(nb));
-			if (na) PA_CUDA(pa_copy(s, s->d_a.p, in.a, na, cudaMemcpyHostToDevice, st));
-			if (nb) PA_CUDA(pa_copy(s, s->d_b.p, in.b, nb, cudaMemcpyHostToDevice, st));
-		}
-	}
 	// the similarity table is small: keep a host copy (device-resident tables are read back)
 	std::vector<float> host_table;
 	if (in.form == F_INDEXED) {
@@ -1211,18 +1224,6 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		} else if (!host_table.empty()) {
 			std::memcpy(host_table.data(), in.table, host_table.size() * 4);
 		}
-		// codes must index the table (factory.h:602-614); checked on the device
-		PA_CUDA(s->d_codes_max.ensure(8));
-		PA_CUDA(cudaMemsetAsync(s->d_codes_max.p, 0, 8, st));
-		const uint32_t *da = in.location == PA_DEVICE ? in.a : s->d_a.as<uint32_t>();
-		const uint32_t *db = in.location == PA_DEVICE ? in.b : s->d_b.as<uint32_t>();
-		const int grid = std::max(1, std::min(s->sm_count * 4, int((B * std::max(in.n_s, in.n_t) + 255) / 256)));
-		if (B * in.n_s > 0) codes_max_kernel<<<grid, 256, 0, st>>>(da, B * in.n_s, s->d_codes_max.as<uint32_t>());
-		if (B * in.n_t > 0) codes_max_kernel<<<grid, 256, 0, st>>>(db, B * in.n_t, s->d_codes_max.as<uint32_t>() + 1);
-		PA_CUDA(cudaGetLastError());
-		launches += int(B * in.n_s > 0) + int(B * in.n_t > 0);
-		// no wait here: the DP kernels read the maxima at launch and do nothing (ST_BAD_CODE)
-		// when a code is out of bounds; the error is raised after the solve's one sync
 	}
 
 	// ---- repeated solves: the same solve as the last call on this solver (same lengths,
@@ -1260,6 +1261,39 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	};
 	const bool hit = repeatable && same_rep();
 	if (!hit) s->drop_graph();
+	// a repeated solve with host buffers and many pairs runs as a pipeline of chunks (see
+	// below): its uploads and index checks happen chunk by chunk there
+	const bool chunked = hit && in.location == PA_HOST && s->rep.nchunks > 1;
+
+	// ---- upload inputs
+	if (in.location == PA_HOST && !chunked) {
+		if (in.form == F_DENSE) {
+			const size_t n = size_t(in.n_s * in.n_t * B) * sizeof(float);
+			PA_CUDA(s->d_dense.ensure(n));
+			if (n) PA_CUDA(pa_copy(s, s->d_dense.p, in.sim, n, cudaMemcpyHostToDevice, st));
+		} else {
+			const size_t na = size_t(B * in.n_s) * sizeof(uint32_t), nb = size_t(B * in.n_t) * sizeof(uint32_t);
+			PA_CUDA(s->d_a.ensure(na));
+			PA_CUDA(s->d_b.ensure(nb));
+			if (na) PA_CUDA(pa_copy(s, s->d_a.p, in.a, na, cudaMemcpyHostToDevice, st));
+			if (nb) PA_CUDA(pa_copy(s, s->d_b.p, in.b, nb, cudaMemcpyHostToDevice, st));
+		}
+	}
+	if (in.form == F_INDEXED && !chunked) {
+		// codes must index the table (factory.h:602-614); checked on the device
+		PA_CUDA(s->d_codes_max.ensure(8));
+		PA_CUDA(cudaMemsetAsync(s->d_codes_max.p, 0, 8, st));
+		const uint32_t *da = in.location == PA_DEVICE ? in.a : s->d_a.as<uint32_t>();
+		const uint32_t *db = in.location == PA_DEVICE ? in.b : s->d_b.as<uint32_t>();
+		const int grid = std::max(1, std::min(s->sm_count * 4, int((B * std::max(in.n_s, in.n_t) + 255) / 256)));
+		if (B * in.n_s > 0) codes_max_kernel<<<grid, 256, 0, st>>>(da, B * in.n_s, s->d_codes_max.as<uint32_t>());
+		if (B * in.n_t > 0) codes_max_kernel<<<grid, 256, 0, st>>>(db, B * in.n_t, s->d_codes_max.as<uint32_t>() + 1);
+		PA_CUDA(cudaGetLastError());
+		launches += int(B * in.n_s > 0) + int(B * in.n_t > 0);
+		// no wait here: the DP kernels read the maxima at launch and do nothing (ST_BAD_CODE)
+		// when a code is out of bounds; the error is raised after the solve's one sync
+	}
+
 
 	// ---- plan: group width and mode, arithmetic; the tuner may try several plans
 	// (a repeated solve takes the plan of the call it repeats: no planning)
@@ -1297,19 +1331,27 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	auto stage = [&](Plan &plan) -> pa_status {
 		// processing order: by number of stripes, then |t|, largest first (a counting sort), so
 		// the groups that share a warp get pairs of the same shape and long pairs start early
+		// (a pipelined solve sorts each chunk's pair range on its own: chunk c's pairs occupy
+		// order[k0, k1) for its pair indices [k0, k1))
 		order.assign(size_t(B), 0);
 		{
 			const int64_t rpp = int64_t(plan.G) * R;
 			const int64_t kt = max_lt + 1;
 			const int64_t nkeys = ((max_ls + rpp - 1) / rpp + 1) * kt;
-			std::vector<int32_t> count(size_t(nkeys) + 1, 0);
+			std::vector<int32_t> count(size_t(nkeys) + 1);
 			auto key = [&](int64_t k) {
 				const int64_t np = (ls[size_t(k)] + rpp - 1) / rpp;
 				return nkeys - 1 - (np * kt + lt[size_t(k)]);  // descending
 			};
-			for (int64_t k = 0; k < B; k++) count[size_t(key(k)) + 1]++;
-			for (int64_t c = 0; c < nkeys; c++) count[size_t(c) + 1] += count[size_t(c)];
-			for (int64_t k = 0; k < B; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
+			for (int c = 0; c < plan.nchunks; c++) {
+				int64_t k0, k1;
+				chunk_range(B, plan.nchunks, c, k0, k1);
+				std::fill(count.begin(), count.end(), 0);
+				for (int64_t k = k0; k < k1; k++) count[size_t(key(k)) + 1]++;
+				count[0] = int32_t(k0);
+				for (int64_t c2 = 0; c2 < nkeys; c2++) count[size_t(c2) + 1] += count[size_t(c2)];
+				for (int64_t k = k0; k < k1; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
+			}
 		}
 		// stripe-chained tickets: level q holds stripe q of every pair with more than q stripes
 		// (an empty pair counts as one stripe, which writes its border result); the order puts
@@ -1414,28 +1456,9 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	auto record = [&](cudaEvent_t e, cudaStream_t sw) -> cudaError_t {
 		return s->capturing ? cudaEventRecordWithFlags(e, sw, cudaEventRecordExternal) : cudaEventRecord(e, sw);
 	};
-	auto device_work = [&](cudaStream_t sw, bool timed) -> pa_status {
-		PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, sw));
-		if (timed) PA_CUDA(record(s->ev[1], sw));
-		if (s->gap == GAP_GENERAL) {
-			if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
-		} else {
-			if (tb == TB_ALL && s->loc == LOC_LOCAL) {
-				// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
-				if (pa_status e2 = dp(plan, TB_NONE, false, nullptr)) return e2;
-				PA_CUDA(s->d_best.ensure(size_t(B) * 4));
-				PA_CUDA(pa_copy(s, s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, sw));
-			}
-			if (pa_status e2 = dp(plan, tb, want_values, s->d_best.as<float>())) return e2;
-		}
-		if (timed) PA_CUDA(record(s->ev[2], sw));
-		if (need_walk) {
-			const bool to_user = maps_out && in.location == PA_DEVICE;
-		PA_CUDA(s->d_maps.ensure(size_t(map_off[size_t(B)]) * 4));
-		if (want_paths) {
-			PA_CUDA(s->d_paths.ensure(size_t(path_off[size_t(B)]) * 4));
-			PA_CUDA(s->d_path_len.ensure(size_t(B) * 4));
-		}
+	// the traceback walk of all pairs (pair0 / npairs select a range)
+	auto walk_params = [&]() -> WalkParams {
+		const bool to_user = maps_out && in.location == PA_DEVICE;
 		WalkParams w{};
 		w.npairs = int32_t(B);
 		w.len_s = s->m.ls;
@@ -1452,7 +1475,6 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		w.local = s->loc == LOC_LOCAL;
 		w.maps = to_user ? maps_out : s->d_maps.as<int32_t>();
 		w.map_off = s->m.map_off;
-
 		w.paths = want_paths ? s->d_paths.as<int32_t>() : nullptr;
 		w.path_off = s->m.path_off;
 		w.path_len = want_paths ? s->d_path_len.as<int32_t>() : nullptr;
@@ -1460,8 +1482,33 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			w.maps = nullptr;
 			w.paths = user_paths->paths;
 			w.path_len = user_paths->path_len;
-
 		}
+		return w;
+	};
+	auto ensure_walk_buffers = [&]() -> cudaError_t {
+		cudaError_t e = s->d_maps.ensure(size_t(map_off[size_t(B)]) * 4);
+		if (e == cudaSuccess && want_paths) e = s->d_paths.ensure(size_t(path_off[size_t(B)]) * 4);
+		if (e == cudaSuccess && want_paths) e = s->d_path_len.ensure(size_t(B) * 4);
+		return e;
+	};
+	auto device_work = [&](cudaStream_t sw, bool timed) -> pa_status {
+		PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, sw));
+		if (timed) PA_CUDA(record(s->ev[1], sw));
+		if (s->gap == GAP_GENERAL) {
+			if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
+		} else {
+			if (tb == TB_ALL && s->loc == LOC_LOCAL) {
+				// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
+				if (pa_status e2 = dp(plan, TB_NONE, false, nullptr)) return e2;
+				PA_CUDA(s->d_best.ensure(size_t(B) * 4));
+				PA_CUDA(pa_copy(s, s->d_best.p, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, sw));
+			}
+			if (pa_status e2 = dp(plan, tb, want_values, s->d_best.as<float>())) return e2;
+		}
+		if (timed) PA_CUDA(record(s->ev[2], sw));
+		if (need_walk) {
+		PA_CUDA(ensure_walk_buffers());
+		WalkParams w = walk_params();
 		walk_kernel<<<int((B + 3) / 4), 128, 0, sw>>>(w);  // a warp per pair
 		PA_CUDA(cudaGetLastError());
 		launches++;
@@ -1470,6 +1517,111 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			PA_CUDA(cudaMemcpyAsync(user_paths->scores, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToDevice, sw));
 		return PA_OK;
 	};
+	// A repeated solve with host buffers and many pairs, as a pipeline of nchunks pair ranges
+	// (the staged order is chunk-major: chunk c's pairs [k0, k1) occupy order[k0, k1)).  The
+	// copy stream uploads each chunk's codes; the solver's stream, per chunk once its codes
+	// are in, checks their range and runs the DP and the walk over the chunk's pairs; the copy
+	// stream then downloads the chunk's alignment maps.  Uploads of later chunks and downloads
+	// of earlier ones overlap the computation.  Per-chunk index checks write their own maxima
+	// slot, which that chunk's DP launch reads.
+	auto pipeline = [&]() -> pa_status {
+		const int K = plan.nchunks;
+		if (!s->copy_stream) PA_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+		if (!s->cmp2) PA_CUDA(cudaStreamCreateWithFlags(&s->cmp2, cudaStreamNonBlocking));
+		while (int(s->ev_chunk.size()) < 2 * K + 4) {
+			cudaEvent_t e = nullptr;
+			PA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+			s->ev_chunk.push_back(e);
+		}
+		cudaStream_t cs = s->copy_stream;
+		const cudaStream_t side_stream[2] = {st, s->cmp2};
+		cudaEvent_t *ev = s->ev_chunk.data();  // uploads 0..K-1, walks K..2K-1, then 4 joins
+		cudaEvent_t ev_start = ev[2 * K], ev_table = ev[2 * K + 1], ev_cmp2 = ev[2 * K + 2], ev_copy = ev[2 * K + 3];
+		PA_CUDA(s->d_a.ensure(size_t(B * in.n_s) * 4));
+		PA_CUDA(s->d_b.ensure(size_t(B * in.n_t) * 4));
+		PA_CUDA(s->d_codes_max.ensure(size_t(8 * K)));
+		if (need_walk) PA_CUDA(ensure_walk_buffers());
+		int32_t *maps_host = nullptr;
+		if (need_walk) {
+			if (!maps_out) res.maps.resize(size_t(map_off[size_t(B)]));
+			maps_host = maps_out ? maps_out : res.maps.data();
+		}
+		auto range = [&](int c, int64_t &k0, int64_t &k1) { chunk_range(B, K, c, k0, k1); };
+		// the copy stream and the second compute stream start after the work already queued on
+		// the solver's stream, and after this call's status reset
+		PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, st));
+		PA_CUDA(cudaEventRecord(ev_start, st));
+		PA_CUDA(cudaStreamWaitEvent(cs, ev_start, 0));
+		PA_CUDA(cudaStreamWaitEvent(s->cmp2, ev_start, 0));
+		for (int c = 0; c < K; c++) {
+			int64_t k0, k1;
+			range(c, k0, k1);
+			if (in.n_s && k1 > k0)
+				PA_CUDA(pa_copy(s, s->d_a.as<uint32_t>() + k0 * in.n_s, in.a + k0 * in.n_s, size_t((k1 - k0) * in.n_s) * 4,
+				                cudaMemcpyHostToDevice, cs));
+			if (in.n_t && k1 > k0)
+				PA_CUDA(pa_copy(s, s->d_b.as<uint32_t>() + k0 * in.n_t, in.b + k0 * in.n_t, size_t((k1 - k0) * in.n_t) * 4,
+				                cudaMemcpyHostToDevice, cs));
+			PA_CUDA(cudaEventRecord(ev[c], cs));
+		}
+		PA_CUDA(cudaEventRecord(s->ev[1], st));
+		// even chunks on the solver's stream, odd ones on the second compute stream: a chunk's
+		// launch fills the SMs that the previous chunk's tail leaves idle
+		pa_status err = PA_OK;
+		for (int c = 0; c < K && err == PA_OK; c++) {
+			int64_t k0, k1;
+			range(c, k0, k1);
+			const int side = c & 1;
+			const cudaStream_t sc = side_stream[side];
+			PA_CUDA(cudaStreamWaitEvent(sc, ev[c], 0));
+			if (in.form == F_INDEXED) {
+				uint32_t *mx = s->d_codes_max.as<uint32_t>() + 2 * c;
+				PA_CUDA(cudaMemsetAsync(mx, 0, 8, sc));
+				const int64_t na = (k1 - k0) * in.n_s, nb = (k1 - k0) * in.n_t;
+				const int grid = std::max(1, std::min(s->sm_count * 4, int((std::max(na, nb) + 255) / 256)));
+				if (na > 0) codes_max_kernel<<<grid, 256, 0, sc>>>(s->d_a.as<uint32_t>() + k0 * in.n_s, na, mx);
+				if (nb > 0) codes_max_kernel<<<grid, 256, 0, sc>>>(s->d_b.as<uint32_t>() + k0 * in.n_t, nb, mx + 1);
+				PA_CUDA(cudaGetLastError());
+				launches += int(na > 0) + int(nb > 0);
+			}
+			if (c == 1) PA_CUDA(cudaStreamWaitEvent(sc, ev_table, 0));  // the table chunk 0 uploaded
+			if (k1 > k0) {
+				// chunk 0 converts and uploads the table; the others reuse it
+				s->table_ev = c == 0 ? ev_table : nullptr;
+				s->skip_table = c > 0;
+				err = plan.use_int ? run_dp<int32_t>(s, in, plan, tb, host_table.data(), k1 - k0, false, nullptr,
+				                                     &launches, k0, c, side)
+				                   : run_dp<float>(s, in, plan, tb, host_table.data(), k1 - k0, false, nullptr,
+				                                   &launches, k0, c, side);
+				s->table_ev = nullptr;
+				s->skip_table = false;
+				if (err) break;
+			} else if (c == 0) {
+				PA_CUDA(cudaEventRecord(ev_table, sc));
+			}
+			if (need_walk && k1 > k0) {
+				WalkParams w = walk_params();
+				w.pair0 = int32_t(k0);
+				w.npairs = int32_t(k1 - k0);
+				walk_kernel<<<int((k1 - k0 + 3) / 4), 128, 0, sc>>>(w);
+				PA_CUDA(cudaGetLastError());
+				launches++;
+				PA_CUDA(cudaEventRecord(ev[K + c], sc));
+				PA_CUDA(cudaStreamWaitEvent(cs, ev[K + c], 0));
+				const int64_t m0 = map_off[size_t(k0)], m1 = map_off[size_t(k1)];
+				if (m1 > m0)
+					PA_CUDA(pa_copy(s, maps_host + m0, s->d_maps.as<int32_t>() + m0, size_t(m1 - m0) * 4,
+					                cudaMemcpyDeviceToHost, cs));
+			}
+		}
+		// join: the solver's stream continues after the second compute stream and the copies
+		PA_CUDA(cudaEventRecord(ev_cmp2, s->cmp2));
+		PA_CUDA(cudaStreamWaitEvent(st, ev_cmp2, 0));
+		PA_CUDA(cudaEventRecord(s->ev[2], st));
+		PA_CUDA(cudaEventRecord(ev_copy, cs));
+		PA_CUDA(cudaStreamWaitEvent(st, ev_copy, 0));
+		return err;
+	};
 
 	if (hit) {
 		pa_solver::Repeat &r = s->rep;
@@ -1477,6 +1629,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		plan.C = r.C;
 		plan.h16 = r.h16;
 		plan.h_neg = r.h_neg;
+		plan.nchunks = r.nchunks;
 		plan.units = r.units;
 		plan.use_int = r.use_int;
 		plan.key_shift = r.key_shift;
@@ -1486,7 +1639,9 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		map_off = r.map_off;
 		path_off = r.path_off;
 		val_off = r.val_off;
-		if (in.location == PA_HOST) {
+		if (chunked) {
+			if (pa_status e = pipeline()) return e;
+		} else if (in.location == PA_HOST) {
 			// host buffers: the inputs were copied to the solver's own buffers above; the plan
 			// and the staged metadata of the last call are reused, the work is launched as is
 			if (pa_status e = device_work(st, true)) return e;
@@ -1522,6 +1677,24 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	} else {
 		if (s->gap != GAP_GENERAL && tb != TB_ALL && !want_values) {
 			if (pa_status e = tune_plan(s, ls, lt, in, plan, stage, dp)) return e;
+		}
+		// host buffers and many pairs: the repeats of this solve run as a pipeline of chunks
+		// (3 chunks from 32K pairs, 2 from 8K; PA_CHUNKS overrides, up to 12) when the
+		// alignment maps go to the packed offsets (the caller's offsets, if given, equal them)
+		plan.nchunks = 1;
+		if (repeatable && in.location == PA_HOST && in.form != F_DENSE && !plan.units && !want_paths) {
+			int K = B >= 32768 ? 3 : B >= 8192 ? 2 : 1;
+			if (const char *e = std::getenv("PA_CHUNKS")) K = std::atoi(e);
+			bool packed = true;
+			if (maps_out && map_offsets) {
+				int64_t o = 0;
+				for (int64_t k = 0; k < B && packed; k++) {
+					packed = map_offsets[k] == o;
+					o += std::min(ls[size_t(k)], lt[size_t(k)]);
+				}
+			}
+			K = std::min(K, 12);
+			if (K > 1 && packed && B >= (int64_t(1) << K)) plan.nchunks = K;
 		}
 		if (pa_status e = stage(plan)) return e;
 		if (pa_status e = device_work(st, true)) return e;
@@ -1569,6 +1742,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		r.C = plan.C;
 		r.h16 = plan.h16;
 		r.h_neg = plan.h_neg;
+		r.nchunks = plan.nchunks;
 		r.units = plan.units;
 		r.use_int = plan.use_int;
 		r.key_shift = plan.key_shift;
@@ -1601,8 +1775,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	res.map_off = map_off;
 	res.mask_off = mask_off;
 	if (need_walk) {
-		if ((maps_out && in.location == PA_DEVICE) || paths_to_user) {
-			// results stay on the device
+		if ((maps_out && in.location == PA_DEVICE) || paths_to_user || chunked) {
+			// results stay on the device, or the pipeline downloaded them chunk by chunk
 		} else if (maps_out) {
 			PA_CUDA(pa_copy(s, maps_out, s->d_maps.p, size_t(map_off[size_t(B)]) * 4, cudaMemcpyDeviceToHost, st));
 		} else {

@@ -21,9 +21,10 @@ namespace pa {
 // gap run thus costs one memory round trip per 8-16 cells and a few instructions per 16
 // cells instead of per cell.
 __global__ void walk_kernel(WalkParams p) {
-	const int pair = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+	const int wid = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
 	const int lane = threadIdx.x & 31;
-	if (pair >= p.npairs) return;  // whole warps
+	if (wid >= p.npairs) return;  // whole warps
+	const int pair = p.pair0 + wid;
 	if (p.status && (*p.status & ST_BAD_CODE)) return;  // the DP did not run: no seeds, no masks
 	const int ls = p.len_s[pair], lt = p.len_t[pair];
 	const int nmap = min(ls, lt);

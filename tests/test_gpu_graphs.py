@@ -140,10 +140,15 @@ def test_repeated_dense_paths_and_gradients(env, monkeypatch):
     assert not torch.equal(got, want)
 
 
-def test_repeated_host_batch_solves(env, monkeypatch):
+@pytest.mark.parametrize("chunks", [None, "3"])
+def test_repeated_host_batch_solves(env, monkeypatch, chunks):
     """pa_solve_batch with host buffers: a repeat reuses the plan and staged metadata (no
-    graph); new contents and new lengths are solved exactly as by a solver that never caches."""
+    graph) -- with PA_CHUNKS=3 as a pipeline of three pair ranges whose uploads, DPs, walks and
+    map downloads overlap; new contents and new lengths are solved exactly as by a solver that
+    never caches."""
     torch, alg, ag = env
+    if chunks:
+        monkeypatch.setenv("PA_CHUNKS", chunks)
     P = ctypes.POINTER
     rng = np.random.default_rng(17)
     n, n_s, n_t = 700, 260, 300
@@ -189,3 +194,28 @@ def test_repeated_host_batch_solves(env, monkeypatch):
     monkeypatch.setenv("PA_GRAPHS", "0")
     want3 = solve(ref, a, b, ln2)
     assert np.array_equal(got[0], want3[0]) and np.array_equal(got[1], want3[1])
+
+
+def test_pipelined_python_api_repeats(env, monkeypatch, oracle_alg):
+    """The native module's solve_indexed_for_alignment repeated with host arrays, pipelined in
+    four chunks (maps into the result object), against the oracle."""
+    torch, alg, ag = env
+    from _cases import compare, options
+    monkeypatch.setenv("PA_CHUNKS", "4")
+    rng = np.random.default_rng(23)
+    n = 301
+    ls = rng.integers(0, 200, size=n)
+    lt = rng.integers(1, 220, size=n)
+    a = rng.integers(0, 4, size=(n, 200)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, 220)).astype(np.uint32)
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    ln = np.stack([ls, lt]).astype(np.uint16)
+    opts = dict(options(alg, locality="local", detail="alignment", gap=Gap("affine", 5.0, 2.0)), batch_size=n)
+    solver = alg.m16.create_solver(200, 220, alg.m16.create_options(opts))
+    oracle = oracle_alg.m16.create_solver(200, 220, oracle_alg.m16.create_options(opts))
+    want = oracle.solve_indexed_for_alignment(a, b, table, ln)
+    for rep in range(3):
+        got = solver.solve_indexed_for_alignment(a, b, table, ln)
+        d = compare("alignment", got, want, n)
+        assert d is None, (rep, d)
