@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--fwd-bwd-pairs", type=int, default=4096, help="pairs of the fwd+bwd measurement (0: skip)")
     ap.add_argument("--other-configs", type=int, default=1, help="also measure the other workloads (0: skip)")
     ap.add_argument("--precision-pairs", type=int, default=8192, help="pairs of the precision measurement (0: skip)")
+    ap.add_argument("--prepare", type=int, default=1, help="also time problem preparation from strings (0: skip)")
     ap.add_argument("--plain-pairs", type=int, default=2048,
                     help="pairs timed on the plain path (one launch per 4-pair batch)")
     return ap.parse_args()
@@ -365,6 +366,58 @@ def other_configs(torch, alg, L, seed):
         "value": 2 * 5000 * 10000 / dt / 1e9, "unit": "GCUPS", "ms": dt * 1000, "alignments": n_items,
         "workload": "2 pairs of 5000 x 10000, all-optimal masks on the GPU, first 20 alignments each (host DFS)"}
     return out
+
+
+# --------------------------------------------------------------------------- prepare
+
+def prepare_config(torch, a, b, ls, lt, sample=8192):
+    """Problem preparation of the bench bag from strings (pyalign's indexed form,
+    solve.py:382-396): the reference's way -- each string encoded on its own through the
+    alphabet's 256-entry byte index (ByteAlphabetEncoder.encode, factory.py:114-127),
+    restated, timed on a sample of pairs and reported per pair -- against one batch call of
+    pa_encode_latin1 into host rows and into device rows (one upload of the raw bytes)."""
+    from pyalign_gb300 import prepare as prep
+    letters = np.array(list("ACGT"))
+    B = a.shape[0]
+    s_list = ["".join(letters[a[k, :ls[k]]]) for k in range(B)]
+    t_list = ["".join(letters[b[k, :lt[k]]]) for k in range(B)]
+    lut = prep.lut_of("ACGT")
+    n = min(sample, B)
+    rows = np.zeros((n, a.shape[1]), np.uint32)
+    t0 = time.perf_counter()
+    for k in range(n):  # the per-problem encoder's work, string by string
+        r = lut[np.frombuffer(s_list[k].encode("latin1"), dtype=np.uint8)]
+        if np.max(r) == 0xFF:
+            raise ValueError("item not in alphabet")
+        rows[k, :len(r)] = r
+        r = lut[np.frombuffer(t_list[k].encode("latin1"), dtype=np.uint8)]
+        if np.max(r) == 0xFF:
+            raise ValueError("item not in alphabet")
+        rows[k, :len(r)] = r
+    per_problem = (time.perf_counter() - t0) / n
+    host_a = np.zeros(a.shape, np.uint32)
+    host_b = np.zeros(b.shape, np.uint32)
+    t0 = time.perf_counter()
+    prep.encode_latin1(s_list, lut, out=host_a, width=a.shape[1])
+    prep.encode_latin1(t_list, lut, out=host_b, width=b.shape[1])
+    host_s = time.perf_counter() - t0
+    if not (np.array_equal(host_a, a) and np.array_equal(host_b, b)):
+        raise SystemExit("batch encoding differs from the bench codes")
+    dev_a = torch.empty(a.shape, dtype=torch.int32, device="cuda")
+    dev_b = torch.empty(b.shape, dtype=torch.int32, device="cuda")
+    prep.encode_latin1(s_list[:64], lut, out=dev_a, width=a.shape[1])  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prep.encode_latin1(s_list, lut, out=dev_a, width=a.shape[1])
+    prep.encode_latin1(t_list, lut, out=dev_b, width=b.shape[1])
+    torch.cuda.synchronize()
+    dev_s = time.perf_counter() - t0
+    if not torch.equal(dev_a.cpu(), torch.from_numpy(a.view(np.int32))):
+        raise SystemExit("device encoding differs from the bench codes")
+    return {"pairs": B, "per_problem_s": per_problem * B, "per_problem_sample_pairs": n,
+            "batch_host_s": host_s, "batch_device_s": dev_s,
+            "speedup_host": per_problem * B / host_s, "speedup_device": per_problem * B / dev_s,
+            "bytes_uploaded_device": int(ls.sum() + lt.sum()), "codes_bytes": int(a.nbytes + b.nbytes)}
 
 
 # --------------------------------------------------------------------------- fwd + bwd
@@ -763,6 +816,7 @@ def run_ours(args):
     fb = fwd_bwd(torch, args.fwd_bwd_pairs, args.seed + 5) if args.fwd_bwd_pairs > 0 else None
     others = other_configs(torch, alg, L, args.seed + 7) if args.other_configs else None
     prec = precision_config(torch, args.precision_pairs, args.seed + 2) if args.precision_pairs > 0 else None
+    prepd = prepare_config(torch, a, b, ls, lt) if args.prepare else None
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -788,6 +842,7 @@ def run_ours(args):
         "fwd_bwd": fb,
         "other_configs": others,
         "precision": prec,
+        "prepare": prepd,
         "kernel_ms_per_step": {"dp": statistics.mean(dp_ms), "traceback": statistics.mean(walk_ms),
                                "before_dp": statistics.mean(up_ms), "after_traceback": statistics.mean(down_ms)},
         "plan": plan,

@@ -346,6 +346,20 @@ pa_status pa_solver_last_plan(const pa_solver *s, int32_t *plan4);
  * (inputs, per-pair metadata, results). */
 pa_status pa_solver_last_bytes(const pa_solver *s, int64_t *h2d, int64_t *d2h);
 
+/* Batch encoding of byte-alphabet sequences (replaces the per-problem encoding of pyalign's
+ * prepare step, pyalign/solve.py:382-396 -> AlphabetProblem.build_index_sequences,
+ * problems/factory.py:87-90 -> ByteAlphabetEncoder.encode, factory.py:114-127).  count
+ * strings of latin1 bytes, string k = text[offsets[k] .. offsets[k+1]) (host), are mapped
+ * through lut (256 entries, host; 0xff = not in the alphabet -- ByteAlphabetEncoder._index)
+ * into row k of codes (row k at codes + k * row_stride, uint32), zero-padded to width.
+ * location PA_HOST: codes is host memory, encoded by worker threads; PA_DEVICE: codes is
+ * device memory, the bytes are uploaded once and encoded by a kernel on `stream`, and the
+ * call waits for it.  Returns PA_ERR_INVALID_ARGUMENT ("item not in alphabet") when a byte
+ * is not in the alphabet, PA_ERR_LENGTH when a string is longer than width.  No counterpart
+ * in the reference's native module. */
+pa_status pa_encode_latin1(const uint8_t *text, const int64_t *offsets, int64_t count, const uint8_t *lut, int64_t width,
+                           int64_t row_stride, uint32_t *codes, int32_t location, void *stream);
+
 /* Diagnostic: measured int32 throughput of this GPU (Gop/s) for the add/add/max mix of the
  * DP cell update, used as the denominator of the DP kernels' roofline.  No counterpart in
  * the reference (it has no GPU code). */
