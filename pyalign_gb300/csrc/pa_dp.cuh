@@ -237,6 +237,21 @@ __device__ __forceinline__ int32_t imad(int32_t a, int32_t b, int32_t c) {
 	return d;
 }
 
+// Asynchronous 16-byte global -> shared copies (cp.async): commit closes a group, wait<N>
+// returns once at most N of this thread's groups are still in flight.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+	const uint32_t sa = uint32_t(__cvta_generic_to_shared(smem));
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Dense S with stride 1 along s: each lane keeps the next DENSE_RING - 1 columns of its 8
+// rows in flight in a shared-memory ring (2 x 16 bytes per column), DENSE_RING * 32 bytes per
+// thread at the start of the dynamic shared memory.
+constexpr int DENSE_RING = 4;
+
 // 0xffffffff when a > b, else 0.
 __device__ __forceinline__ uint32_t gt_mask(int32_t a, int32_t b) {
 	uint32_t d;
@@ -365,7 +380,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 	typedef typename V2T<V>::type V2;
 	if (!codes_valid(p)) return;
 
-	extern __shared__ unsigned char smem_raw[];
+	extern __shared__ __align__(16) unsigned char smem_raw[];
 	V *stab = reinterpret_cast<V *>(smem_raw);
 	const bool table_in_smem = (p.sub_kind == SUB_TABLE || p.sub_kind == SUB_PROFILE) &&
 	                           p.table_rows <= MAX_SMEM_TABLE && p.table_cols <= MAX_SMEM_TABLE;
@@ -472,12 +487,16 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			const int32_t *prog_in = (units && q > 0) ? p.progress + prod : nullptr;
 			int32_t avail = 0;        // columns of bin known to be written
 			int pub_next = PUB_CHUNK;  // next progress value to publish
-			V2 bnext;                  // lane 0: bin of the next column
+			V2 bnext;                  // lane 0: bin of the next column, read one step ahead
 			bnext.x = NEG;
 			bnext.y = NEG;
-			if (units && sub == 0 && pass_active && q > 0) {
-				avail = wait_progress(prog_in, 1, p.status);
-				bnext = __ldcg(bin);
+			if (sub == 0 && pass_active && q > 0) {
+				if (units) {
+					avail = wait_progress(prog_in, 1, p.status);
+					bnext = __ldcg(bin);
+				} else {
+					bnext = bin[0];  // group mode: written by this warp's last lane in the previous pass
+				}
 			}
 
 			// query codes, and the int8 substitution profile of each row (SUB_PROFILE)
@@ -544,11 +563,20 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			const bool dvec = sub_kind == SUB_DENSE && pass_active && nvalid >= R && p.dense_si == 1 &&
 			                  (p.dense_sj & 3) == 0 && ((reinterpret_cast<uintptr_t>(drow) & 15) == 0);
 			const float *dcol = dvec ? drow + row0 : nullptr;
-			float4 dn0 = make_float4(0.f, 0.f, 0.f, 0.f), dn1 = dn0;
-			if (dvec) {
-				dn0 = __ldg(reinterpret_cast<const float4 *>(dcol));
-				dn1 = __ldg(reinterpret_cast<const float4 *>(dcol) + 1);
-			}
+			// column jj's 8 rows into ring slot jj % DENSE_RING, one commit group per column (an
+			// empty group past the last column keeps the count)
+			float4 *ring = reinterpret_cast<float4 *>(smem_raw) + threadIdx.x * (2 * DENSE_RING);
+			auto fetch = [&](int jj) {
+				if (jj < lt) {
+					const float *src = dcol + int64_t(jj) * p.dense_sj;
+					float4 *dst = ring + 2 * (jj & (DENSE_RING - 1));
+					cp_async16(dst, src);
+					cp_async16(dst + 1, src + 4);
+				}
+				cp_async_commit();
+			};
+			if (dvec)
+				for (int k = 0; k < DENSE_RING - 1; k++) fetch(k);
 			// this lane's traceback word of step s is mrow[s * G] (hoisted out of the step loop)
 			uint32_t *mrow1 = nullptr;
 			uint4 *mrow4 = nullptr;
@@ -575,9 +603,9 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 							bnext = __ldcg(bin + j + 1);
 						}
 					} else {
-						const V2 bv2 = bin[j];
-						upD = bv2.x;
-						upP = bv2.y;
+						upD = bnext.x;
+						upP = bnext.y;
+						if (j + 1 < lt) bnext = bin[j + 1];
 					}
 				}
 				if (act) {
@@ -598,6 +626,11 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 #pragma unroll
 						for (int r = 0; r < R; r++) S[r] = tab[qa[r] * p.table_cols + tcode];
 					} else if (dvec) {
+						// column j's group is complete once at most DENSE_RING - 2 newer ones remain;
+						// the refill goes to the slot read in the previous step
+						cp_async_wait<DENSE_RING - 2>();
+						const float4 dn0 = ring[2 * (j & (DENSE_RING - 1))], dn1 = ring[2 * (j & (DENSE_RING - 1)) + 1];
+						fetch(j + DENSE_RING - 1);
 						S[0] = V(dn0.x * p.dense_sign);
 						S[1] = V(dn0.y * p.dense_sign);
 						S[2] = V(dn0.z * p.dense_sign);
@@ -606,11 +639,6 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 						S[5] = V(dn1.y * p.dense_sign);
 						S[6] = V(dn1.z * p.dense_sign);
 						S[7] = V(dn1.w * p.dense_sign);
-						if (j + 1 < lt) {
-							const float4 *nx = reinterpret_cast<const float4 *>(dcol + int64_t(j + 1) * p.dense_sj);
-							dn0 = __ldg(nx);
-							dn1 = __ldg(nx + 1);
-						}
 					} else {
 #pragma unroll
 						for (int r = 0; r < R; r++) {

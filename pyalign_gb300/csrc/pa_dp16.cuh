@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 	constexpr bool SEED = LOC == LOC_LOCAL;
 	if (!codes_valid(p)) return;
 
-	extern __shared__ unsigned char smem_raw[];
+	extern __shared__ __align__(16) unsigned char smem_raw[];
 	int32_t *stab = reinterpret_cast<int32_t *>(smem_raw);
 	const int cols = p.table_cols;
 	for (int k = threadIdx.x; k < p.table_rows * cols; k += blockDim.x) stab[k] = p.table[k];
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 		// shape the twin computes
 		const int rsA = emptyA ? 0 : lsA, rsB = emptyB ? 0 : lsB;
 		const int ctA = emptyA ? 0 : ltA, ctB = emptyB ? 0 : ltB;
-		const int ls = max(rsA, rsB), lt = max(ctA, ctB);
+		const int ls = max(rsA, rsB), lt = max(ctA, ctB), ctmin = min(ctA, ctB);
 		const int npass = max(npA, npB);
 		const int nsteps = C == 2 ? ((lt + 1) >> 1) + G - 1 : lt + G - 1;
 		int wpass = npass, wsteps = npass ? nsteps : 0;
@@ -382,11 +382,15 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 						}
 					}
 					if (SEED) {
-						const uint32_t cm0 = colmask16(j0, ctA, ctB);
-						uint32_t sv = (smax0 & cm0) | (HMIN & ~cm0);
-						if (C == 2) {
-							const uint32_t cm1 = colmask16(j1, ctA, ctB);
-							sv = h_max(sv, (smax1 & cm1) | (HMIN & ~cm1));
+						// a step's columns lie inside both pairs until the shorter pair's end
+						uint32_t sv = C == 2 ? h_max(smax0, smax1) : smax0;
+						if (j0 + C > ctmin) {
+							const uint32_t cm0 = colmask16(j0, ctA, ctB);
+							sv = (smax0 & cm0) | (HMIN & ~cm0);
+							if (C == 2) {
+								const uint32_t cm1 = colmask16(j1, ctA, ctB);
+								sv = h_max(sv, (smax1 & cm1) | (HMIN & ~cm1));
+							}
 						}
 						seed16<TB, C>(sv, j0, lm, pos);
 					}

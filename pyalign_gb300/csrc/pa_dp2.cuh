@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp2_kernel(DpParams<int32_t> p) {
 	static_assert(TB != TB_ALL, "all-optimal masks use dp_kernel");
 	if (!codes_valid(p)) return;
 
-	extern __shared__ unsigned char smem_raw[];
+	extern __shared__ __align__(16) unsigned char smem_raw[];
 	V *stab = reinterpret_cast<V *>(smem_raw);
 	const bool table_in_smem = (p.sub_kind == SUB_TABLE || p.sub_kind == SUB_PROFILE || p.sub_kind == SUB_COLPROF) &&
 	                           p.table_rows <= MAX_SMEM_TABLE && p.table_cols <= MAX_SMEM_TABLE;
@@ -145,12 +145,17 @@ __global__ void __launch_bounds__(BLOCK, 4) dp2_kernel(DpParams<int32_t> p) {
 			const int32_t *prog_in = (CHAIN && q > 0) ? p.progress + prod : nullptr;
 			int32_t avail = 0;
 			int pub_next = PUB_CHUNK;
-			V2 bn0, bn1;  // lane 0, chained: boundary of the next step's two columns
+			V2 bn0, bn1;  // lane 0: boundary of the next step's two columns, read one step ahead
 			bn0.x = bn0.y = bn1.x = bn1.y = NEG;
-			if (CHAIN && sub == 0 && pass_active && q > 0) {
-				avail = wait_progress(prog_in, min(2, lt), p.status);
-				bn0 = __ldcg(bin);
-				if (lt > 1) bn1 = __ldcg(bin + 1);
+			if (sub == 0 && pass_active && q > 0) {
+				if (CHAIN) {
+					avail = wait_progress(prog_in, min(2, lt), p.status);
+					bn0 = __ldcg(bin);
+					if (lt > 1) bn1 = __ldcg(bin + 1);
+				} else {  // group mode: written by this warp's last lane in the previous pass
+					bn0 = bin[0];
+					if (lt > 1) bn1 = bin[1];
+				}
 			}
 
 			uint32_t qa[R];
@@ -244,13 +249,13 @@ __global__ void __launch_bounds__(BLOCK, 4) dp2_kernel(DpParams<int32_t> p) {
 							if (j0 + 3 < lt) bn1 = __ldcg(bin + j0 + 3);
 						}
 					} else {
-						const V2 b0 = bin[j0];
-						upD0 = b0.x;
-						upP0 = b0.y;
-						if (act1) {
-							const V2 b1 = bin[j1];
-							upD1 = b1.x;
-							upP1 = b1.y;
+						upD0 = bn0.x;
+						upP0 = bn0.y;
+						upD1 = bn1.x;
+						upP1 = bn1.y;
+						if (j0 + 2 < lt) {
+							bn0 = bin[j0 + 2];
+							if (j0 + 3 < lt) bn1 = bin[j0 + 3];
 						}
 					}
 				}

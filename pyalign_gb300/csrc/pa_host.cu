@@ -834,6 +834,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	                  ? size_t(in.table_rows * in.table_cols) * sizeof(V)
 	                  : 0;
 	if (p.sub_kind == SUB_COLPROF) smem = ((smem + 15) & ~size_t(15)) + size_t(in.table_cols) * BLOCK * 8;
+	if (p.sub_kind == SUB_DENSE) smem = size_t(BLOCK) * DENSE_RING * 32;  // the dense S ring (pa_dp.cuh)
 	int bps = 0;
 	cudaError_t e = cudaSuccess;
 	const int loc = s->loc;
