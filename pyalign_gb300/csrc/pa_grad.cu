@@ -181,6 +181,98 @@ __global__ void path_embedding_grad_kernel(EmbGradParams p) {
 	}
 }
 
+// The same gradients, four aligned cells at a time per warp (widths that are a multiple of
+// 32): lanes examine 32 path steps at once and a ballot lists the aligned ones (the scan
+// stops at the first point with a negative coordinate, as above); each 8-lane quarter of
+// the warp then takes one listed cell, reads its rows with 16-byte loads (lane l holds
+// elements 4l + 32t) and reduces over its 8 lanes.  Four independent cells in flight per
+// warp instead of one dependent chain of row loads.
+__device__ __forceinline__ float quarter_sum(float x) {
+	for (int o = 4; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+	return x;
+}
+
+__device__ __forceinline__ float4 bf16x4(const __nv_bfloat16 *p4) {
+	const uint2 w = *reinterpret_cast<const uint2 *>(p4);
+	return make_float4(__uint_as_float(w.x << 16), __uint_as_float(w.x & 0xffff0000u), __uint_as_float(w.y << 16),
+	                   __uint_as_float(w.y & 0xffff0000u));
+}
+
+__global__ void path_embedding_grad_vec_kernel(EmbGradParams p) {
+	const int64_t k = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (k >= p.batch) return;
+	const float g = p.grad[k];
+	const int n = p.path_len[k];
+	const int32_t *P = p.paths + p.path_off[k];
+	const int64_t bs = k * p.n_s, bt = k * p.n_t;
+	const int quarter = lane >> 3, ql = lane & 7;
+	const int chunks = p.dim >> 5;
+	for (int q0 = 0; q0 + 1 < n; q0 += 32) {
+		const int q = q0 + lane;
+		int u0 = -1, v0 = -1;
+		bool neg = false, al = false;
+		if (q + 1 < n) {
+			u0 = P[2 * q];
+			v0 = P[2 * q + 1];
+			neg = u0 < 0 || v0 < 0;
+			al = !neg && P[2 * q + 2] == u0 - 1 && P[2 * q + 3] == v0 - 1;
+		}
+		const uint32_t negm = __ballot_sync(0xffffffffu, neg);
+		const int stop = negm ? __ffs(int(negm)) - 1 : 32;  // steps from the first negative point on are not visited
+		uint32_t am = __ballot_sync(0xffffffffu, al && lane < stop);
+		while (am) {
+			// this quarter's cell: the (quarter + 1)-th listed step; every lane runs every shuffle
+			// below in the same order (a quarter without a cell only skips the memory accesses)
+			uint32_t m = am;
+			for (int c = 0; c < quarter; c++) m &= m - 1;
+			const int src = m ? __ffs(int(m)) - 1 : 32;
+			const int u = __shfl_sync(0xffffffffu, u0, src < 32 ? src : 0);
+			const int v = __shfl_sync(0xffffffffu, v0, src < 32 ? src : 0);
+			for (int c = 0; c < 4 && am; c++) am &= am - 1;  // the four cells of this round
+			const bool has = src < 32 && u >= 0 && u < p.n_s && v >= 0 && v < p.n_t;
+			const int64_t ri = (bs + (has ? u : 0)) * p.dim, rj = (bt + (has ? v : 0)) * p.dim;
+			const float is = has ? p.inv_s[bs + u] : 0.0f, it = has ? p.inv_t[bt + v] : 0.0f;
+			float dots = 0.0f, dott = 0.0f;
+			if (has) {
+				for (int t = 0; t < chunks; t++) {
+					const int e = 4 * ql + 32 * t;
+					const float4 es = *reinterpret_cast<const float4 *>(p.Es + ri + e);
+					const float4 et = *reinterpret_cast<const float4 *>(p.Et + rj + e);
+					const float4 tb = bf16x4(p.Etb + rj + e), sb = bf16x4(p.Esb + ri + e);
+					dots += g * tb.x * es.x * is + g * tb.y * es.y * is + g * tb.z * es.z * is + g * tb.w * es.w * is;
+					dott += g * sb.x * et.x * it + g * sb.y * et.y * it + g * sb.z * et.z * it + g * sb.w * et.w * it;
+				}
+			}
+			if (p.normalize) {
+				dots = quarter_sum(dots);
+				dott = quarter_sum(dott);
+			}
+			if (has) {
+				for (int t = 0; t < chunks; t++) {
+					const int e = 4 * ql + 32 * t;
+					const float4 tb = bf16x4(p.Etb + rj + e), sb = bf16x4(p.Esb + ri + e);
+					float4 os, ot;
+					if (p.normalize) {
+						const float4 es = *reinterpret_cast<const float4 *>(p.Es + ri + e);
+						const float4 et = *reinterpret_cast<const float4 *>(p.Et + rj + e);
+						os = make_float4((g * tb.x - dots * es.x * is) * is, (g * tb.y - dots * es.y * is) * is,
+						                 (g * tb.z - dots * es.z * is) * is, (g * tb.w - dots * es.w * is) * is);
+						ot = make_float4((g * sb.x - dott * et.x * it) * it, (g * sb.y - dott * et.y * it) * it,
+						                 (g * sb.z - dott * et.z * it) * it, (g * sb.w - dott * et.w * it) * it);
+					} else {
+						os = make_float4(g * tb.x, g * tb.y, g * tb.z, g * tb.w);
+						ot = make_float4(g * sb.x, g * sb.y, g * sb.z, g * sb.w);
+					}
+					*reinterpret_cast<float4 *>(p.dEs + ri + e) = os;
+					*reinterpret_cast<float4 *>(p.dEt + rj + e) = ot;
+				}
+			}
+		}
+		if (negm) break;
+	}
+}
+
 // DTW on two series with d(u, v) = |x_u - y_v|: every visited cell adds
 // g * sign(x_u - y_v) to dx_u and subtracts it from dy_v (one thread per pair).
 struct SeriesGradParams {
@@ -239,7 +331,15 @@ extern "C" pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int
 	                reinterpret_cast<const __nv_bfloat16 *>(Es_bf16), reinterpret_cast<const __nv_bfloat16 *>(Et_bf16),
 	                inv_s, inv_t, dEs, dEt, n_s, n_t};
 	const int64_t threads = batch * 32;
-	path_embedding_grad_kernel<<<int((threads + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+	// 16-byte rows (the vector kernel) when the width is a multiple of 32 and the rows aligned
+	const bool vec = dim % 32 == 0 &&
+	                 ((reinterpret_cast<uintptr_t>(Es) | reinterpret_cast<uintptr_t>(Et) | reinterpret_cast<uintptr_t>(dEs) |
+	                   reinterpret_cast<uintptr_t>(dEt)) & 15) == 0 &&
+	                 ((reinterpret_cast<uintptr_t>(Es_bf16) | reinterpret_cast<uintptr_t>(Et_bf16)) & 7) == 0;
+	if (vec)
+		path_embedding_grad_vec_kernel<<<int((threads + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+	else
+		path_embedding_grad_kernel<<<int((threads + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
 }
 
