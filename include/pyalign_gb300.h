@@ -285,6 +285,13 @@ pa_status pa_path_gradients(int32_t type, int32_t locality, int32_t direction, i
  * inverse norms.  Device memory; allocates nothing. */
 pa_status pa_normalize_rows_bf16(const float *E, int64_t rows, int32_t dim, int32_t normalize, void *out_bf16,
                                  float *inv_norm, void *stream);
+
+/* pa_normalize_rows_bf16 for batch x n rows of a (batch, n, dim) tensor with each pair's
+ * length (lengths: device, batch int32): rows i >= lengths[k] of pair k get a zero BF16 row
+ * and 1/|E| = 0 without reading E (the padding rows of the product are zero).  E must be
+ * 16-byte aligned when dim is a multiple of 4 (its rows are then read as 16-byte words). */
+pa_status pa_normalize_rows_bf16_lengths(const float *E, int64_t batch, int64_t n, int32_t dim, int32_t normalize,
+                                         const int32_t *lengths, void *out_bf16, float *inv_norm, void *stream);
 pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
                                       const int64_t *path_offsets, const int32_t *path_len,
                                       const float *grad_scores, const float *Es, const float *Et,

@@ -73,6 +73,8 @@ def _lib():
                                                   vp, vp, vp]
         L.pa_normalize_rows_bf16.restype = i32
         L.pa_normalize_rows_bf16.argtypes = [vp, i64, i32, i32, vp, vp, vp]
+        L.pa_normalize_rows_bf16_lengths.restype = i32
+        L.pa_normalize_rows_bf16_lengths.argtypes = [vp, i64, i64, i32, i32, vp, vp, vp, vp]
         L.pa_path_series_gradients.restype = i32
         L.pa_path_series_gradients.argtypes = [i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp]
         L.pa_similarity_bf16.restype = i32
@@ -102,6 +104,38 @@ def tensor_core_status(device=None):
     v = int(st.item())
     st.zero_()
     return v
+
+
+_small_cache = {}   # (device, dtype, bytes) -> device tensor: index arrays seen before
+_staging = {}       # (device, dtype) -> (pinned buffer, event of its last copy)
+
+
+def _to_device(arr, device):
+    """A small host index array (lengths, offsets) on the device without blocking the host: a
+    content-keyed cache (a training loop passes the same lengths every step) and, for new
+    contents, a non-blocking copy out of a reused pinned buffer."""
+    arr = np.ascontiguousarray(arr)
+    device = torch.device(device)
+    key = (str(device), arr.dtype.str, arr.shape, arr.tobytes())
+    hit = _small_cache.get(key)
+    if hit is not None:
+        return hit
+    dtype = torch.from_numpy(arr[:0]).dtype
+    buf, ev = _staging.get((str(device), arr.dtype.str), (None, None))
+    if buf is None or buf.numel() < arr.size:
+        buf, ev = torch.empty(max(arr.size, 1 << 14), dtype=dtype, pin_memory=True), None
+    if ev is not None:
+        ev.synchronize()  # the previous copy out of the buffer has finished
+    flat = buf[:arr.size]
+    flat.copy_(torch.from_numpy(arr.reshape(-1)))
+    out = flat.to(device, non_blocking=True).reshape(arr.shape)
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream(device))
+    _staging[(str(device), arr.dtype.str)] = (buf, ev)
+    if len(_small_cache) >= 32:
+        _small_cache.pop(next(iter(_small_cache)))
+    _small_cache[key] = out
+    return out
 
 
 def _lengths(lengths, B):
@@ -210,7 +244,7 @@ def _forward_paths(S, lengths, gap, locality, direction, dtw):
     _alg.check(L.pa_solve_dense_paths(
         solver.handle, base, offsets.ctypes.data, ss, st_, B, n_s, n_t, ln.ctypes.data,
         scores.data_ptr(), paths.data_ptr(), poff.ctypes.data, plen.data_ptr()))
-    return scores, paths, plen, torch.from_numpy(poff).to(S.device, non_blocking=False), ss == 1
+    return scores, paths, plen, _to_device(poff, S.device), ss == 1
 
 
 def _gap_grads(dtw, linear, locality, direction, B, paths, plen, poff, grad):
@@ -284,16 +318,23 @@ def alignment_score(S, lengths, gap_open=None, gap_extend=None, locality="global
     return AlignmentScore.apply(S, lengths, go, ge, locality, direction, dtw, linear)
 
 
-def normalized_bf16(E, normalize=True):
+def normalized_bf16(E, normalize=True, lengths=None):
     """The BF16 factor of E (batch, n, d) for the similarity product -- E / |E| per row when
     normalising -- and 1 / |E| per row, in one pass (pa_normalize_rows_bf16).  d is padded
-    with zeros to a multiple of 16 (the tensor-core K step)."""
+    with zeros to a multiple of 16 (the tensor-core K step).  With ``lengths`` (batch,) the
+    rows past each pair's length are zero and not read (pa_normalize_rows_bf16_lengths)."""
     E = _pad16(E.contiguous().float())
     B, n, dim = E.shape
     Eb = torch.empty(E.shape, dtype=torch.bfloat16, device=E.device)
     inv = torch.empty(B * n, dtype=torch.float32, device=E.device)
-    _alg.check(_lib().pa_normalize_rows_bf16(E.data_ptr(), B * n, dim, int(normalize), Eb.data_ptr(),
-                                             inv.data_ptr(), torch.cuda.current_stream().cuda_stream))
+    stream = torch.cuda.current_stream().cuda_stream
+    if lengths is None:
+        _alg.check(_lib().pa_normalize_rows_bf16(E.data_ptr(), B * n, dim, int(normalize), Eb.data_ptr(),
+                                                 inv.data_ptr(), stream))
+    else:
+        ln = _to_device(np.minimum(np.asarray(lengths).reshape(B), n).astype(np.int32), E.device)
+        _alg.check(_lib().pa_normalize_rows_bf16_lengths(E.data_ptr(), B, n, dim, int(normalize), ln.data_ptr(),
+                                                         Eb.data_ptr(), inv.data_ptr(), stream))
     return Eb, inv
 
 
@@ -306,8 +347,9 @@ class CosineSimilarity(torch.autograd.Function):
     def forward(ctx, Es, Et, lengths):
         B, n_s, d = Es.shape
         n_t = Et.shape[1]
-        Esb, inv_s = normalized_bf16(Es)
-        Etb, inv_t = normalized_bf16(Et)
+        ln = None if lengths is None else np.asarray(lengths).reshape(B, 2)
+        Esb, inv_s = normalized_bf16(Es, True, None if ln is None else ln[:, 0])  # padding rows: zero
+        Etb, inv_t = normalized_bf16(Et, True, None if ln is None else ln[:, 1])
         if lengths is None:
             lengths = np.tile(np.array([[n_s, n_t]], np.int32), (B, 1))
             out = None
@@ -355,8 +397,9 @@ class EmbeddingAlignmentScore(torch.autograd.Function):
         dim_in = Es.shape[-1]
         Es = _pad16(Es.contiguous().float())
         Et = _pad16(Et.contiguous().float())
-        Esb, inv_s = normalized_bf16(Es, normalize)
-        Etb, inv_t = normalized_bf16(Et, normalize)
+        ln = np.asarray(lengths).reshape(Es.shape[0], 2)
+        Esb, inv_s = normalized_bf16(Es, normalize, ln[:, 0])  # rows past a pair's length: zero, not read
+        Etb, inv_t = normalized_bf16(Et, normalize, ln[:, 1])
         # S^T = en_t en_s^T on the tensor cores, only the cells inside the lengths; its
         # transposed view is S with stride 1 along s
         S = similarity_bf16(Esb, Etb, lengths)

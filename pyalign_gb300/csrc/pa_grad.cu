@@ -124,6 +124,47 @@ __global__ void normalize_rows_bf16_kernel(const float *E, int64_t rows, int32_t
 	if (lane == 0) inv_norm[r] = inv;
 }
 
+// The same with each pair's length: rows past it get a zero factor and 1/|E| = 0 without
+// reading E (the product's padding rows must be zero, and their values are never used);
+// rows of a width that is a multiple of 4 are read as 16-byte words.
+__global__ void normalize_rows_bf16_len_kernel(const float *E, int64_t batch, int64_t n, int32_t dim,
+                                               int32_t normalize, const int32_t *len, __nv_bfloat16 *out,
+                                               float *inv_norm) {
+	const int64_t r = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (r >= batch * n) return;
+	const int64_t k = r / n, i = r - k * n;
+	__nv_bfloat16 *o = out + r * dim;
+	if (i >= len[k]) {
+		for (int c = lane; c < dim; c += 32) o[c] = __float2bfloat16_rn(0.0f);
+		if (lane == 0) inv_norm[r] = 0.0f;
+		return;
+	}
+	const float *x = E + r * dim;
+	const bool vec = (dim & 3) == 0;
+	float ss = 0.0f;
+	if (vec) {
+		for (int c = 4 * lane; c < dim; c += 128) {
+			const float4 v = *reinterpret_cast<const float4 *>(x + c);
+			ss += v.x * v.x + v.y * v.y + v.z * v.z + v.w * v.w;
+		}
+	} else {
+		for (int c = lane; c < dim; c += 32) ss += x[c] * x[c];
+	}
+	for (int o2 = 16; o2 > 0; o2 >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o2);
+	const float inv = normalize ? 1.0f / fmaxf(sqrtf(ss), 1e-12f) : 1.0f;
+	if (vec) {
+		for (int c = 4 * lane; c < dim; c += 128) {
+			const float4 v = *reinterpret_cast<const float4 *>(x + c);
+			__nv_bfloat162 w[2] = {__floats2bfloat162_rn(v.x * inv, v.y * inv), __floats2bfloat162_rn(v.z * inv, v.w * inv)};
+			*reinterpret_cast<uint2 *>(o + c) = *reinterpret_cast<const uint2 *>(w);  // 8-byte store
+		}
+	} else {
+		for (int c = lane; c < dim; c += 32) o[c] = __float2bfloat16_rn(x[c] * inv);
+	}
+	if (lane == 0) inv_norm[r] = inv;
+}
+
 struct EmbGradParams {
 	int64_t batch;
 	int32_t dim, normalize;
@@ -314,6 +355,18 @@ extern "C" pa_status pa_normalize_rows_bf16(const float *E, int64_t rows, int32_
 	if (rows == 0) return PA_OK;
 	normalize_rows_bf16_kernel<<<int((rows * 32 + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
 	    E, rows, dim, normalize, reinterpret_cast<__nv_bfloat16 *>(out_bf16), inv_norm);
+	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}
+
+extern "C" pa_status pa_normalize_rows_bf16_lengths(const float *E, int64_t batch, int64_t n, int32_t dim,
+                                                    int32_t normalize, const int32_t *lengths, void *out_bf16,
+                                                    float *inv_norm, void *stream) {
+	if (batch < 0 || n < 0 || dim <= 0 || !E || !lengths || !out_bf16 || !inv_norm) return PA_ERR_INVALID_ARGUMENT;
+	if (batch * n == 0) return PA_OK;
+	const bool aligned = ((reinterpret_cast<uintptr_t>(E)) & 15) == 0 && ((reinterpret_cast<uintptr_t>(out_bf16)) & 7) == 0;
+	if (!aligned && (dim & 3) == 0) return PA_ERR_INVALID_ARGUMENT;  // 16-byte rows need aligned bases
+	normalize_rows_bf16_len_kernel<<<int((batch * n * 32 + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+	    E, batch, n, dim, normalize, lengths, reinterpret_cast<__nv_bfloat16 *>(out_bf16), inv_norm);
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
 }
 
