@@ -263,6 +263,15 @@ pa_status pa_solve_dense_paths(pa_solver *s, const float *sim, const int64_t *of
                                int64_t stride_t, int64_t batch, int64_t n_s, int64_t n_t, const int32_t *length,
                                float *scores, int32_t *paths, const int64_t *path_offsets, int32_t *path_len);
 
+/* The same for two float32 series per pair (device memory): S(i, j) = |x[k * x_stride + i] -
+ * y[k * y_stride + j]| computed in the DP kernel, never stored -- the cost matrix of DTW on
+ * series (pyalign/problems/factory.py's distance-based problems with the absolute difference).
+ * Replaces materialising the batch * n_s * n_t matrix for pa_solve_dense_paths; results are
+ * identical (the kernel computes the same float32 difference).  Linear, affine or DTW solvers. */
+pa_status pa_solve_series_paths(pa_solver *s, const float *x, int64_t x_stride, const float *y, int64_t y_stride,
+                                int64_t batch, int64_t n_s, int64_t n_t, const int32_t *length, float *scores,
+                                int32_t *paths, const int64_t *path_offsets, int32_t *path_len);
+
 /* Backward: the max-plus subgradient of the optimal score.  Adds grad_scores[k] to dS at
  * every aligned (diagonal-step) cell of pair k's path -- every visited cell for DTW -- and
  * writes dgap[4k..4k+3] = d score / d (open_s, extend_s, open_t, extend_t) times
@@ -301,7 +310,8 @@ pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normal
 
 /* Fused backward of DTW on two series with d(u, v) = |x_u - y_v| (x: (batch, n_s),
  * y: (batch, n_t) float32): every visited cell adds grad * sign(x_u - y_v) to dx_u and
- * subtracts it from dy_v.  Device memory; allocates nothing. */
+ * subtracts it from dy_v (per row and column: grad times the exact count of signs, adding to
+ * dx and dy, which the caller zeroes).  Device memory; allocates nothing. */
 pa_status pa_path_series_gradients(int64_t batch, const int32_t *paths, const int64_t *path_offsets,
                                    const int32_t *path_len, const float *grad_scores, const float *x,
                                    const float *y, int64_t n_s, int64_t n_t, float *dx, float *dy, void *stream);

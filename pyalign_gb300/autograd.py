@@ -66,6 +66,8 @@ def _lib():
         vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
         L.pa_solve_dense_paths.restype = i32
         L.pa_solve_dense_paths.argtypes = [vp, vp, vp, i64, i64, i64, i64, i64, vp, vp, vp, vp, vp]
+        L.pa_solve_series_paths.restype = i32
+        L.pa_solve_series_paths.argtypes = [vp, vp, i64, vp, i64, i64, i64, i64, vp, vp, vp, vp, vp]
         L.pa_path_gradients.restype = i32
         L.pa_path_gradients.argtypes = [i32, i32, i32, i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp]
         L.pa_path_embedding_gradients.restype = i32
@@ -226,25 +228,46 @@ def _forward_paths(S, lengths, gap, locality, direction, dtw):
         S = S.contiguous()
     B, n_s, n_t = S.shape
     ss, st_ = S.stride(1), S.stride(2)
-    ln = np.ascontiguousarray(np.asarray(lengths).reshape(B, 2).T, dtype=np.int32)
-    if (ln[0] > n_s).any() or (ln[1] > n_t).any() or (ln < 0).any():
-        raise ValueError("lengths exceed the similarity tensor")
-    solver = _solver(B, n_s, n_t, locality, direction, dtw, gap)
-    L = _lib()
-    stream = torch.cuda.current_stream()
-    _alg.check(L.pa_solver_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
+    solver, ln, scores, paths, plen, poff = _path_buffers(B, n_s, n_t, lengths, locality, direction, dtw, gap,
+                                                          S.device, "the similarity tensor")
     offsets = S.storage_offset() + np.arange(B, dtype=np.int64) * S.stride(0)
-    sizes = 2 * (ln[0].astype(np.int64) + ln[1] + 2)
-    poff = np.zeros(B, np.int64)
-    poff[1:] = np.cumsum(sizes)[:-1]
-    paths = torch.empty(int(sizes.sum()), dtype=torch.int32, device=S.device)
-    plen = torch.zeros(B, dtype=torch.int32, device=S.device)
-    scores = torch.empty(B, dtype=torch.float32, device=S.device)
     base = S.data_ptr() - S.storage_offset() * S.element_size()
-    _alg.check(L.pa_solve_dense_paths(
+    _alg.check(_lib().pa_solve_dense_paths(
         solver.handle, base, offsets.ctypes.data, ss, st_, B, n_s, n_t, ln.ctypes.data,
         scores.data_ptr(), paths.data_ptr(), poff.ctypes.data, plen.data_ptr()))
     return scores, paths, plen, _to_device(poff, S.device), ss == 1
+
+
+def _path_buffers(B, n_s, n_t, lengths, locality, direction, dtw, gap, device, what):
+    """The solver on the current stream, the (2, B) int32 lengths and the output buffers of a
+    paths solve: scores, packed paths (2 (|s| + |t| + 2) entries per pair), path lengths and
+    the host path offsets."""
+    ln = np.ascontiguousarray(np.asarray(lengths).reshape(B, 2).T, dtype=np.int32)
+    if (ln[0] > n_s).any() or (ln[1] > n_t).any() or (ln < 0).any():
+        raise ValueError("lengths exceed " + what)
+    solver = _solver(B, n_s, n_t, locality, direction, dtw, gap)
+    stream = torch.cuda.current_stream()
+    _alg.check(_lib().pa_solver_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
+    sizes = 2 * (ln[0].astype(np.int64) + ln[1] + 2)
+    poff = np.zeros(B, np.int64)
+    poff[1:] = np.cumsum(sizes)[:-1]
+    paths = torch.empty(int(sizes.sum()), dtype=torch.int32, device=device)
+    plen = torch.zeros(B, dtype=torch.int32, device=device)
+    scores = torch.empty(B, dtype=torch.float32, device=device)
+    return solver, ln, scores, paths, plen, poff
+
+
+def _series_paths(x, y, lengths, gap, locality, direction, dtw):
+    """_forward_paths for S(u, v) = |x_u - y_v| of the series rows of x and y (contiguous
+    float32 CUDA tensors): the kernel computes each cell, no matrix is formed."""
+    B, n_s = x.shape
+    n_t = y.shape[1]
+    solver, ln, scores, paths, plen, poff = _path_buffers(B, n_s, n_t, lengths, locality, direction, dtw, gap,
+                                                          x.device, "the series")
+    _alg.check(_lib().pa_solve_series_paths(
+        solver.handle, x.data_ptr(), x.stride(0), y.data_ptr(), y.stride(0), B, n_s, n_t, ln.ctypes.data,
+        scores.data_ptr(), paths.data_ptr(), poff.ctypes.data, plen.data_ptr()))
+    return scores, paths, plen, _to_device(poff, x.device)
 
 
 def _gap_grads(dtw, linear, locality, direction, B, paths, plen, poff, grad):
@@ -446,8 +469,9 @@ class SeriesDTW(torch.autograd.Function):
     def forward(ctx, x, y, lengths):
         x = x.contiguous().float()
         y = y.contiguous().float()
-        D = (y[:, :, None] - x[:, None, :]).abs().transpose(1, 2)  # stride 1 along u
-        scores, paths, plen, poff, _ = _forward_paths(D, lengths, None, "global", "minimize", True)
+        if x.dim() != 2 or y.dim() != 2 or x.shape[0] != y.shape[0] or not x.is_cuda or y.device != x.device:
+            raise ValueError("x, y must be (batch, len) CUDA tensors on one device")
+        scores, paths, plen, poff = _series_paths(x, y, lengths, None, "global", "minimize", True)
         ctx.save_for_backward(x, y, paths, plen, poff)
         return scores
 

@@ -37,7 +37,9 @@ namespace pa {
 enum GapKind { GAP_LINEAR = 0, GAP_AFFINE = 1, GAP_DTW = 2, GAP_GENERAL = 3 };
 enum LocKind { LOC_LOCAL = 0, LOC_GLOBAL = 1, LOC_SEMI = 2 };
 enum TbKind { TB_NONE = 0, TB_ONE = 1, TB_ALL = 2 };
-enum SubKind { SUB_TABLE = 0, SUB_BINARY = 1, SUB_DENSE = 2, SUB_PROFILE = 3, SUB_COLPROF = 4 };
+enum SubKind { SUB_TABLE = 0, SUB_BINARY = 1, SUB_DENSE = 2, SUB_PROFILE = 3, SUB_COLPROF = 4, SUB_SERIES = 5 };
+// SUB_SERIES: S(i, j) = |x_i - y_j| of two float32 series, computed per cell; the series travel
+// in the code registers as raw 32-bit words (a = x, b = y), scaled by dense_sign.
 
 // SUB_COLPROF: per thread and letter c, the int8 scores of the thread's R rows against c,
 // kept in shared memory after the table as colprof[c * BLOCK + thread] (8 bytes): one
@@ -625,6 +627,10 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 					} else if (sub_kind == SUB_TABLE) {
 #pragma unroll
 						for (int r = 0; r < R; r++) S[r] = tab[qa[r] * p.table_cols + tcode];
+					} else if (sub_kind == SUB_SERIES) {
+						const float yj = __int_as_float(int(tcode));
+#pragma unroll
+						for (int r = 0; r < R; r++) S[r] = V(fabsf(__int_as_float(int(qa[r])) - yj) * p.dense_sign);
 					} else if (dvec) {
 						// column j's group is complete once at most DENSE_RING - 2 newer ones remain;
 						// the refill goes to the slot read in the previous step

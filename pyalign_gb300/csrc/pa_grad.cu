@@ -315,7 +315,14 @@ __global__ void path_embedding_grad_vec_kernel(EmbGradParams p) {
 }
 
 // DTW on two series with d(u, v) = |x_u - y_v|: every visited cell adds
-// g * sign(x_u - y_v) to dx_u and subtracts it from dy_v (one thread per pair).
+// g * sign(x_u - y_v) to dx_u and subtracts it from dy_v.
+//
+// One warp per pair, 32 path points per step.  A DTW path is monotone (every step lowers u,
+// v or both), so the points of one row u -- and those of one column v -- are consecutive: a
+// segmented warp scan of the signs gives each run's count, and the run's last lane adds
+// g * count to dx[u] (dy[v]).  A run that reaches the end of a step is carried into the next
+// one.  Each dx[u], dy[v] thus has one writer, and the sum is g times an exact integer
+// count, independent of the order of the points.
 struct SeriesGradParams {
 	int64_t batch;
 	const int32_t *paths;
@@ -327,9 +334,21 @@ struct SeriesGradParams {
 	int64_t n_s, n_t;
 };
 
+// inclusive scan of a over the lanes' runs of equal key (runs are contiguous)
+__device__ __forceinline__ int run_scan(int a, int key, int lane) {
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const int t = __shfl_up_sync(0xffffffffu, a, o);
+		const int tk = __shfl_up_sync(0xffffffffu, key, o);
+		if (lane >= o && tk == key) a += t;
+	}
+	return a;
+}
+
 __global__ void path_series_grad_kernel(SeriesGradParams p) {
-	const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (k >= p.batch) return;
+	const int64_t k = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (k >= p.batch) return;  // whole warps
 	const float g = p.grad[k];
 	const int n = p.path_len[k];
 	const int32_t *P = p.paths + p.path_off[k];
@@ -337,13 +356,38 @@ __global__ void path_series_grad_kernel(SeriesGradParams p) {
 	const float *y = p.y + k * p.n_t;
 	float *dx = p.dx + k * p.n_s;
 	float *dy = p.dy + k * p.n_t;
-	for (int q = 0; q < n; q++) {
-		const int u = P[2 * q], v = P[2 * q + 1];
-		if (u < 0 || v < 0) break;
-		const float diff = x[u] - y[v];
-		const float sg = diff > 0.0f ? g : (diff < 0.0f ? -g : 0.0f);
-		dx[u] += sg;
-		dy[v] -= sg;
+	int cu = -1, cv = -1, cx = 0, cy = 0;  // the runs carried from the last step (warp-uniform)
+	for (int q0 = 0; q0 < n; q0 += 32) {
+		const int q = q0 + lane;
+		int u = -1, v = -1, sg = 0;
+		if (q < n) {
+			u = P[2 * q];
+			v = P[2 * q + 1];
+		}
+		if (u >= 0 && v >= 0 && u < p.n_s && v < p.n_t) {  // a walk's final point may be (-1, -1)
+			const float d = x[u] - y[v];
+			sg = d > 0.0f ? 1 : (d < 0.0f ? -1 : 0);
+		} else {
+			u = v = -1;
+		}
+		// the carried runs: continued by lane 0, else complete
+		if (lane == 0) {
+			if (cu >= 0 && u != cu) dx[cu] += g * float(cx);
+			if (cv >= 0 && v != cv) dy[cv] -= g * float(cy);
+		}
+		const int ax = run_scan(sg + ((lane == 0 && u == cu) ? cx : 0), u, lane);
+		const int ay = run_scan(sg + ((lane == 0 && v == cv) ? cy : 0), v, lane);
+		const int nu = __shfl_down_sync(0xffffffffu, u, 1), nv = __shfl_down_sync(0xffffffffu, v, 1);
+		if (lane < 31 && u >= 0 && nu != u) dx[u] += g * float(ax);
+		if (lane < 31 && v >= 0 && nv != v) dy[v] -= g * float(ay);
+		cu = __shfl_sync(0xffffffffu, u, 31);
+		cv = __shfl_sync(0xffffffffu, v, 31);
+		cx = __shfl_sync(0xffffffffu, ax, 31);
+		cy = __shfl_sync(0xffffffffu, ay, 31);
+	}
+	if (lane == 0) {
+		if (cu >= 0) dx[cu] += g * float(cx);
+		if (cv >= 0) dy[cv] -= g * float(cy);
 	}
 }
 
@@ -404,7 +448,7 @@ extern "C" pa_status pa_path_series_gradients(int64_t batch, const int32_t *path
 		return PA_ERR_INVALID_ARGUMENT;
 	if (batch == 0) return PA_OK;
 	SeriesGradParams p{batch, paths, path_offsets, path_len, grad_scores, x, y, dx, dy, n_s, n_t};
-	path_series_grad_kernel<<<int((batch + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+	path_series_grad_kernel<<<int((batch + 7) / 8), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
 }
 

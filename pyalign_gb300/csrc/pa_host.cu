@@ -92,7 +92,7 @@ struct PinBuf {
 enum Goal { GOAL_SCORE = 0, GOAL_ONE = 1, GOAL_ALL = 2 };
 // Output shapes of the 15 solve methods (factory.h:699-808).
 enum Method { M_SCORE = 0, M_ALIGNMENT = 1, M_ALIGNMENT_ITER = 2, M_SOLUTION = 3, M_SOLUTION_ITER = 4, M_PATHS = 5 };
-enum Form { F_DENSE = 0, F_INDEXED = 1, F_BINARY = 2 };
+enum Form { F_DENSE = 0, F_INDEXED = 1, F_BINARY = 2, F_SERIES = 3 };  // F_SERIES: S = |x_i - y_j| of two series
 
 struct Input {
 	int form;
@@ -107,6 +107,9 @@ struct Input {
 	// dense form with explicit layout: S(k, i, j) = sim[dense_off[k] + i * dense_si + j * dense_sj]
 	const int64_t *dense_off_host = nullptr;
 	int64_t dense_si = 0, dense_sj = 0;
+	// series form: S(k, i, j) = |x[k * x_stride + i] - y[k * y_stride + j]| (device)
+	const float *sx = nullptr, *sy = nullptr;
+	int64_t sx_stride = 0, sy_stride = 0;
 };
 
 // Device buffers of the caller that receive the one-optimal paths (M_PATHS).
@@ -364,7 +367,8 @@ struct pa_solver {
 		bool valid = false;
 		int method = -1, form = -1;
 		int64_t B = 0, n_s = 0, n_t = 0, trows = 0, tcols = 0, dsi = 0, dsj = 0;
-		const void *a = nullptr, *b = nullptr, *sim = nullptr, *table = nullptr;
+		const void *a = nullptr, *b = nullptr, *sim = nullptr, *table = nullptr, *sx = nullptr, *sy = nullptr;
+		int64_t sxs = 0, sys = 0;
 		float eq = 0, ne = 0;
 		int32_t *maps_out = nullptr, *paths = nullptr, *path_len = nullptr;
 		float *scores = nullptr;
@@ -679,7 +683,9 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.order = s->m.order + first;  // a pipeline chunk: its pairs occupy order[first, first + npairs)
 	p.len_s = s->m.ls;
 	p.len_t = s->m.lt;
-	p.sub_kind = in.form == F_DENSE ? SUB_DENSE : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
+	p.sub_kind = in.form == F_DENSE ? SUB_DENSE
+	             : in.form == F_SERIES ? SUB_SERIES
+	             : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
 	p.neg_inf = ISINT ? V(-(1 << 29)) : V(-INFINITY);
 	p.G = plan.G;
 	p.key_shift = plan.key_shift;
@@ -694,13 +700,22 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	const bool h16 = ISINT && plan.h16;
 
 	// ---- sequences and substitution
-	if (in.form != F_DENSE) {
+	if (in.form == F_SERIES) {
+		// the series travel through the code paths as raw 32-bit words
+		p.a = reinterpret_cast<const uint32_t *>(in.sx);
+		p.b = reinterpret_cast<const uint32_t *>(in.sy);
+		p.a_stride = in.sx_stride;
+		p.b_stride = in.sy_stride;
+		p.dense_sign = s->sign;
+	} else if (in.form != F_DENSE) {
 		p.a = in.location == PA_DEVICE ? in.a : s->d_a.as<uint32_t>();
 		p.b = in.location == PA_DEVICE ? in.b : s->d_b.as<uint32_t>();
 		p.a_stride = in.n_s;
 		p.b_stride = in.n_t;
 	}
-	if (in.form == F_INDEXED) {
+	if (in.form == F_SERIES) {
+		// nothing more: S is computed in the kernel
+	} else if (in.form == F_INDEXED) {
 		p.table_rows = int32_t(in.table_rows);
 		p.table_cols = int32_t(in.table_cols);
 		p.table = s->d_tab.as<V>();
@@ -911,7 +926,7 @@ pa_status validate(pa_solver *s, const Input &in) {
 // 2^23 in magnitude, which also means the reference's float32 arithmetic is exact.
 bool int_mode_ok(const pa_solver *s, const Input &in, const float *host_table, int64_t max_ls, int64_t max_lt,
                  double *bound_out) {
-	if (in.form == F_DENSE) return false;
+	if (in.form == F_DENSE || in.form == F_SERIES) return false;
 	if (s->gap == GAP_GENERAL) return false;
 	double m = 0;
 	auto chk = [&](float x) {
@@ -1243,6 +1258,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		const pa_solver::Repeat &r = s->rep;
 		if (!r.valid || r.method != method || r.form != in.form || r.B != B || r.n_s != in.n_s || r.n_t != in.n_t)
 			return false;
+		if (r.sx != in.sx || r.sy != in.sy || r.sxs != in.sx_stride || r.sys != in.sy_stride) return false;
 		if (r.a != in.a || r.b != in.b || r.sim != in.sim || r.table != in.table || r.trows != in.table_rows ||
 		    r.tcols != in.table_cols || r.dsi != in.dense_si || r.dsj != in.dense_sj || r.stream != st)
 			return false;
@@ -1722,6 +1738,10 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		r.a = in.a;
 		r.b = in.b;
 		r.sim = in.sim;
+		r.sx = in.sx;
+		r.sy = in.sy;
+		r.sxs = in.sx_stride;
+		r.sys = in.sy_stride;
 		r.table = in.table;
 		r.eq = in.eq;
 		r.ne = in.ne;
@@ -2179,6 +2199,35 @@ pa_status pa_solve_dense_paths(pa_solver *s, const float *sim, const int64_t *of
 	in.dense_off_host = offsets;
 	in.dense_si = stride_s;
 	in.dense_sj = stride_t;
+	UserPaths up_{};
+	up_.paths = paths;
+	up_.path_off = path_offsets;
+	up_.path_len = path_len;
+	up_.scores = scores;
+	pa_result *r = nullptr;
+	pa_status st = solve_impl(s, in, M_PATHS, nullptr, &r, nullptr, nullptr, &up_);
+	if (r) pa_result_destroy(r);
+	return st;
+}
+
+pa_status pa_solve_series_paths(pa_solver *s, const float *x, int64_t x_stride, const float *y, int64_t y_stride,
+                                int64_t batch, int64_t n_s, int64_t n_t, const int32_t *length, float *scores,
+                                int32_t *paths, const int64_t *path_offsets, int32_t *path_len) {
+	if (!s || !x || !y || !length || !paths || !path_offsets || !path_len)
+		return fail(PA_ERR_INVALID_ARGUMENT, "null argument");
+	if (x_stride < n_s || y_stride < n_t) return fail(PA_ERR_INVALID_ARGUMENT, "series stride below its length");
+	if (s->gap == GAP_GENERAL) return fail(PA_ERR_UNSUPPORTED, "series form: linear, affine or DTW gap costs only");
+	Input in{};
+	in.form = F_SERIES;
+	in.location = PA_DEVICE;
+	in.batch = batch;
+	in.n_s = n_s;
+	in.n_t = n_t;
+	in.sx = x;
+	in.sy = y;
+	in.sx_stride = x_stride;
+	in.sy_stride = y_stride;
+	in.length = length;
 	UserPaths up_{};
 	up_.paths = paths;
 	up_.path_off = path_offsets;

@@ -273,3 +273,66 @@ def test_fused_cosine_gradients_match_torch_normalize(torch_ag):
     assert torch.allclose(sc, sc2, atol=1e-4)
     assert torch.allclose(a.grad, a2.grad, atol=2e-3, rtol=1e-2)
     assert torch.allclose(b.grad, b2.grad, atol=2e-3, rtol=1e-2)
+
+
+@pytest.mark.parametrize("case", [("dtw", "global", "minimize"), ("affine", "global", "minimize"),
+                                  ("linear", "local", "maximize")])
+def test_series_paths_equal_dense_paths(torch_ag, case):
+    """The series form (S = |x_u - y_v| computed in the kernel) gives the scores and paths of
+    the dense form on the materialised matrix, bit for bit; the series rows are strided views
+    of wider buffers, the lengths ragged down to one cell."""
+    torch, ag = torch_ag
+    kind, locality, direction = case
+    g = torch.Generator(device="cuda").manual_seed(41)
+    B, ns, nt = 40, 300, 257
+    xb = torch.cumsum(torch.randn(B, ns + 20, device="cuda", generator=g), 1)
+    yb = torch.cumsum(torch.randn(B, nt + 7, device="cuda", generator=g), 1)
+    x, y = xb[:, 3:3 + ns], yb[:, 5:5 + nt]
+    rng = np.random.default_rng(12)
+    lengths = np.stack([rng.integers(1, ns + 1, B), rng.integers(1, nt + 1, B)], axis=1)
+    lengths[0] = (1, 1)
+    lengths[1] = (ns, nt)
+    lengths[2] = (1, nt)
+    dtw = kind == "dtw"
+    gap = None if dtw else ((0.7, None) if kind == "linear" else (1.5, 0.4))
+    s1, p1, l1, o1 = ag._series_paths(x, y, lengths, gap, locality, direction, dtw)
+    D = (x[:, :, None] - y[:, None, :]).abs()
+    s2, p2, l2, o2, _ = ag._forward_paths(D, lengths, gap, locality, direction, dtw)
+    assert torch.equal(s1, s2)
+    assert torch.equal(l1, l2) and torch.equal(o1, o2)
+    o = o1.cpu().numpy()
+    n = l1.cpu().numpy()
+    P1, P2 = p1.cpu().numpy(), p2.cpu().numpy()
+    for k in range(B):
+        assert np.array_equal(P1[o[k]:o[k] + 2 * n[k]], P2[o[k]:o[k] + 2 * n[k]]), k
+
+
+def test_series_dtw_weighted_gradients_match_path_counts(torch_ag):
+    """The series backward with per-pair weights: dx_u = w_k * (number of the path's cells in
+    row u with x_u > y_v minus those with x_u < y_v), dy likewise with the sign reversed --
+    recomputed on the host from the forward's own paths (long paths: several warp steps)."""
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(9)
+    B, ns, nt = 24, 400, 333
+    x0 = torch.cumsum(torch.randn(B, ns, device="cuda", generator=g), 1)
+    y0 = torch.cumsum(torch.randn(B, nt, device="cuda", generator=g), 1)
+    rng = np.random.default_rng(4)
+    lengths = np.stack([rng.integers(1, ns + 1, B), rng.integers(1, nt + 1, B)], axis=1)
+    w = torch.randn(B, device="cuda", generator=g)
+    x = x0.clone().requires_grad_(True)
+    y = y0.clone().requires_grad_(True)
+    (ag.dtw_series_score(x, y, lengths) * w).sum().backward()
+    _, paths, plen, poff = ag._series_paths(x0, y0, lengths, None, "global", "minimize", True)
+    P, n, o = paths.cpu().numpy(), plen.cpu().numpy(), poff.cpu().numpy()
+    xs, ys, wk = x0.cpu().numpy(), y0.cpu().numpy(), w.cpu().numpy().astype(np.float64)
+    dx = np.zeros((B, ns))
+    dy = np.zeros((B, nt))
+    for k in range(B):
+        pts = P[o[k]:o[k] + 2 * n[k]].reshape(-1, 2)
+        pts = pts[(pts[:, 0] >= 0) & (pts[:, 1] >= 0)]
+        assert pts[0].tolist() == [lengths[k, 0] - 1, lengths[k, 1] - 1] and pts[-1].tolist() == [0, 0]
+        sg = np.sign(xs[k, pts[:, 0]] - ys[k, pts[:, 1]]).astype(np.float64)
+        np.add.at(dx[k], pts[:, 0], wk[k] * sg)
+        np.add.at(dy[k], pts[:, 1], -wk[k] * sg)
+    assert np.allclose(x.grad.cpu().numpy(), dx, rtol=1e-6, atol=1e-6)
+    assert np.allclose(y.grad.cpu().numpy(), dy, rtol=1e-6, atol=1e-6)
