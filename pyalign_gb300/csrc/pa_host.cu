@@ -568,9 +568,11 @@ int choose_G(const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, int
 			cells += double(npass * rpp) * double(lt[k] + G - 1);
 		}
 		cells *= 1.0 + 0.06 * c;
-		// keep at least 16 warps per SM busy: narrower groups pack more pairs per warp
+		// keep at least 4 warps per SM busy: narrower groups pack more pairs per warp (below
+		// that the launch is latency-bound; at 4096 pairs of 64 x 64 one 64-row stripe per
+		// pair, G = 8 with 7 warps per SM, beats G = 32 with 27 per SM, 3 of 4 lanes idle, 3x)
 		const int64_t warps = (pairs + 32 / G - 1) / (32 / G);
-		if (c > 0 && warps < int64_t(sm_count) * 16) break;
+		if (c > 0 && warps < int64_t(sm_count) * 4) break;
 		if (c == 0 || cells < best) {
 			best = cells;
 			bestG = G;
@@ -1078,7 +1080,7 @@ struct TuneEntry {
 };
 std::mutex g_tune_mu;
 std::vector<TuneEntry> g_tune;
-constexpr double TUNE_MIN_CELLS = 2e7;  // smaller launches keep the analytic choice
+constexpr double TUNE_MIN_CELLS = 4e6;  // smaller launches keep the analytic choice
 
 uint64_t tune_key(const pa_solver *s, const Input &in, const Plan &plan, const std::vector<int32_t> &ls,
                   const std::vector<int32_t> &lt, double *cells) {
@@ -1784,15 +1786,18 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		return PA_OK;
 	}
 
-	// ---- download
-	res.scores.resize(size_t(B));
-	res.has.resize(size_t(B));
-	res.seeds.resize(size_t(2 * B));
-	int32_t status = 0;
-	PA_CUDA(pa_copy(s, res.scores.data(), s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
-	PA_CUDA(pa_copy(s, res.has.data(), s->d_has.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
-	PA_CUDA(pa_copy(s, res.seeds.data(), s->d_seed.p, size_t(B) * 8, cudaMemcpyDeviceToHost, st));
-	PA_CUDA(pa_copy(s, &status, s->d_status.p, 4, cudaMemcpyDeviceToHost, st));
+	// ---- download: the status word, and the per-pair scores and seeds where the host needs
+	// them (a result object, or host scores), through the solver's pinned block
+	const bool host_scores = out != nullptr || scores_out != nullptr || (goal == GOAL_ALL && method == M_SCORE);
+	const size_t hb = 16 + (host_scores ? size_t(B) * 4 : 0) + (out ? size_t(B) * 12 : 0);
+	PA_CUDA(s->h_out.ensure(hb));
+	unsigned char *hp = s->h_out.as<unsigned char>();
+	PA_CUDA(pa_copy(s, hp, s->d_status.p, 4, cudaMemcpyDeviceToHost, st));
+	if (host_scores) PA_CUDA(pa_copy(s, hp + 16, s->d_score.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+	if (out) {
+		PA_CUDA(pa_copy(s, hp + 16 + size_t(B) * 4, s->d_has.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
+		PA_CUDA(pa_copy(s, hp + 16 + size_t(B) * 8, s->d_seed.p, size_t(B) * 8, cudaMemcpyDeviceToHost, st));
+	}
 	res.map_off = map_off;
 	res.mask_off = mask_off;
 	if (need_walk) {
@@ -1835,6 +1840,18 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	PA_CUDA(cudaStreamSynchronize(st));
 	for (int k = 0; k < 4; k++) cudaEventElapsedTime(&s->last_ms[k], s->ev[k], s->ev[k + 1]);
 	s->last_launches = launches;
+	int32_t status = 0;
+	std::memcpy(&status, hp, 4);
+	if (host_scores) {
+		res.scores.resize(size_t(B));
+		std::memcpy(res.scores.data(), hp + 16, size_t(B) * 4);
+	}
+	if (out) {
+		res.has.resize(size_t(B));
+		res.seeds.resize(size_t(2 * B));
+		std::memcpy(res.has.data(), hp + 16 + size_t(B) * 4, size_t(B) * 4);
+		std::memcpy(res.seeds.data(), hp + 16 + size_t(B) * 8, size_t(B) * 8);
+	}
 	if ((status & ST_BAD_CODE) && in.form == F_INDEXED && s->gap != GAP_GENERAL) {
 		uint32_t mx[2] = {0, 0};
 		PA_CUDA(cudaMemcpy(mx, s->d_codes_max.p, 8, cudaMemcpyDeviceToHost));
@@ -2168,18 +2185,14 @@ pa_status pa_solve_batch(pa_solver *s, const pa_batch *b, float *scores, int32_t
 	in.ne = b->ne;
 	in.length = b->length;
 	if (s->goal == GOAL_ALL) return fail(PA_ERR_UNSUPPORTED, "pa_solve_batch returns one alignment per pair");
-	pa_result *r = nullptr;
 	const bool dev = b->location == PA_DEVICE;
-	pa_status st = solve_impl(s, in, maps ? M_ALIGNMENT : M_SCORE, dev ? nullptr : scores, &r, maps, map_offsets);
+	// no result object: only the scores (and the maps, written in place) leave the call
+	pa_status st = solve_impl(s, in, maps ? M_ALIGNMENT : M_SCORE, dev ? nullptr : scores, nullptr, maps, map_offsets);
 	if (st) return st;
 	if (dev && scores) {
 		cudaError_t e = pa_copy(s, scores, s->d_score.p, size_t(b->batch) * 4, cudaMemcpyDeviceToDevice, s->stream);
-		if (e != cudaSuccess) {
-			pa_result_destroy(r);
-			return fail(PA_ERR_CUDA, cudaGetErrorString(e));
-		}
+		if (e != cudaSuccess) return fail(PA_ERR_CUDA, cudaGetErrorString(e));
 	}
-	pa_result_destroy(r);
 	return PA_OK;
 }
 
