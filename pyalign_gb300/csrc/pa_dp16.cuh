@@ -45,6 +45,13 @@
 
 #include "pa_dp.cuh"
 
+#ifndef PA_DP16_SKEW
+#define PA_DP16_SKEW 1     // two columns: row r + 1's first column before row r's second
+#endif
+#ifndef PA_DP16_IMADNIB
+#define PA_DP16_IMADNIB 1  // traceback nibbles accumulated by IMAD (FMA pipe)
+#endif
+
 namespace pa {
 
 __device__ __forceinline__ uint32_t h_add(uint32_t a, uint32_t b) {
@@ -314,50 +321,71 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 					uint32_t mlo0 = 0, mhi0 = 0, mlo1 = 0, mhi1 = 0;
 					uint32_t smax0 = HMIN, smax1 = HMIN, even0 = HMIN, even1 = HMIN;
 					uint32_t x0 = 0, x1 = 0;  // global: column j0's D of this lane's rows (C = 2)
-#pragma unroll
-					for (int r = 0; r < R; r++) {
+					// the traceback nibble of a cell into the row's word (rows 0-3: lo, 4-7: hi)
+					auto put_nib = [&](uint32_t &lo, uint32_t &hi, int r, uint32_t n) {
+						uint32_t &w = r < 4 ? lo : hi;
+						w = PA_DP16_IMADNIB ? uint32_t(imad(int32_t(w), p.sixteen, int32_t(n))) : w * 16u + n;
+					};
+					// local seeds: the row's key (D | row tag) into the step's best, two rows per max3
+					auto put_seed = [&](uint32_t &best, uint32_t &even, int r, uint32_t D, uint32_t t) {
+						const uint32_t k = TB == TB_ONE ? h_addk(D, p.one, t) : D;  // D | t
+						if ((r & 1) == 0) even = k;
+						else best = h_max3(best, even, k);
+					};
+					// column j0 of row r: its D and Q feed column j1 of the same row
+					uint32_t c0D[R], c0Q[R];
+					auto col0 = [&](int r) {
 						const uint32_t old = Dl[r];
 						uint32_t D0, P0, Q0;
 						const uint32_t S0 = uint32_t(prmt(prA[r], prB[r], sel0));  // sign-replicating prmt
 						const uint32_t key0 = cell16<GAP, LOC>(p, S0, dsave0, old, Ql[r], uD0, uP0, fl[r], D0, P0, Q0);
-						uint32_t D1 = D0, P1 = P0, Q1 = Q0, key1 = key0;
-						if (C == 2) {
-							const uint32_t S1 = uint32_t(prmt(prA[r], prB[r], sel1));
-							key1 = cell16<GAP, LOC>(p, S1, dsave1, D0, Q0, uD1, uP1, fl[r], D1, P1, Q1);
-						}
-						if (TB == TB_ONE) {
-							const uint32_t n0 = nib16<GAP>(key0, P0, Q0);
-							if (r < 4) mlo0 = mlo0 * 16u + n0;
-							else mhi0 = mhi0 * 16u + n0;
-							if (C == 2) {
-								const uint32_t n1 = nib16<GAP>(key1, P1, Q1);
-								if (r < 4) mlo1 = mlo1 * 16u + n1;
-								else mhi1 = mhi1 * 16u + n1;
-							}
-						}
-						if (SEED) {
-							const uint32_t t0 = TB == TB_ONE ? uint32_t(r * C) * 0x10001u : 0u;
-							const uint32_t k0 = TB == TB_ONE ? h_addk(D0, p.one, t0) : D0;  // D0 | t0
-							if ((r & 1) == 0) even0 = k0;
-							else smax0 = h_max3(smax0, even0, k0);
-							if (C == 2) {
-								const uint32_t k1 = TB == TB_ONE ? h_addk(D1, p.one, t0 + 0x10001u) : D1;
-								if ((r & 1) == 0) even1 = k1;
-								else smax1 = h_max3(smax1, even1, k1);
-							}
-						}
+						if (TB == TB_ONE) put_nib(mlo0, mhi0, r, nib16<GAP>(key0, P0, Q0));
+						if (SEED) put_seed(smax0, even0, r, D0, TB == TB_ONE ? uint32_t(r * C) * 0x10001u : 0u);
 						if (LOC == LOC_GLOBAL && C == 2) {
 							if (r == nvA - 1) x0 = (x0 & 0xFFFF0000u) | (D0 & 0x0000FFFFu);
 							if (r == nvB - 1) x0 = (x0 & 0x0000FFFFu) | (D0 & 0xFFFF0000u);
 						}
 						dsave0 = old;
-						dsave1 = D0;
-						Dl[r] = C == 2 ? D1 : D0;
-						if (GAP == GAP_AFFINE) Ql[r] = C == 2 ? Q1 : Q0;
 						uD0 = D0;
 						uP0 = P0;
+						c0D[r] = D0;
+						c0Q[r] = Q0;
+						if (C == 1) {
+							Dl[r] = D0;
+							if (GAP == GAP_AFFINE) Ql[r] = Q0;
+						}
+					};
+					// column j1 of row r (C = 2)
+					auto col1 = [&](int r) {
+						uint32_t D1, P1, Q1;
+						const uint32_t S1 = uint32_t(prmt(prA[r], prB[r], sel1));
+						const uint32_t key1 = cell16<GAP, LOC>(p, S1, dsave1, c0D[r], c0Q[r], uD1, uP1, fl[r], D1, P1, Q1);
+						if (TB == TB_ONE) put_nib(mlo1, mhi1, r, nib16<GAP>(key1, P1, Q1));
+						if (SEED) put_seed(smax1, even1, r, D1, TB == TB_ONE ? uint32_t(r * C + 1) * 0x10001u : 0u);
+						dsave1 = c0D[r];
+						Dl[r] = D1;
+						if (GAP == GAP_AFFINE) Ql[r] = Q1;
 						uD1 = D1;
 						uP1 = P1;
+					};
+					if (C == 1) {
+#pragma unroll
+						for (int r = 0; r < R; r++) col0(r);
+					} else if (PA_DP16_SKEW) {
+						// column j0 of row r + 1 before column j1 of row r: row r's old D (the
+						// diagonal of row r + 1, column j0) is dead before column j1 of row r
+						// replaces it, so the new values take the old ones' registers
+#pragma unroll
+						for (int r = 0; r <= R; r++) {
+							if (r < R) col0(r);
+							if (r >= 1) col1(r - 1);
+						}
+					} else {
+#pragma unroll
+						for (int r = 0; r < R; r++) {
+							col0(r);
+							col1(r);
+						}
 					}
 					outD0 = uD0;
 					outP0 = uP0;

@@ -525,9 +525,27 @@ bool h16_plan(const pa_solver *s, const Input &in, const float *host_table, cons
 // 1 : 2 : 4 : ..., so each chunk's upload (about 4x faster per pair than its DP) is hidden
 // behind the previous chunk's DP and only the small first chunk's upload is exposed.
 void chunk_range(int64_t B, int K, int c, int64_t &k0, int64_t &k1) {
-	const int64_t den = (int64_t(1) << K) - 1;
-	k0 = B * ((int64_t(1) << c) - 1) / den;
-	k1 = B * ((int64_t(1) << (c + 1)) - 1) / den;
+	// PA_CHUNK_SHAPE=sym (experiments): sizes 1 : 2 : 4 ... 4 : 2 : 1, so the last chunk's
+	// walk and download, exposed after the DP, are small too
+	static const bool sym = [] {
+		const char *e = std::getenv("PA_CHUNK_SHAPE");
+		return e && std::strcmp(e, "sym") == 0;
+	}();
+	if (!sym) {
+		const int64_t den = (int64_t(1) << K) - 1;
+		k0 = B * ((int64_t(1) << c) - 1) / den;
+		k1 = B * ((int64_t(1) << (c + 1)) - 1) / den;
+		return;
+	}
+	int64_t den = 0, before = 0;
+	for (int i = 0; i < K; i++) {
+		const int64_t w = int64_t(1) << std::min(i, K - 1 - i);
+		den += w;
+		if (i < c) before += w;
+	}
+	const int64_t w = int64_t(1) << std::min(c, K - 1 - c);
+	k0 = B * before / den;
+	k1 = B * (before + w) / den;
 }
 
 // a 16-bit addend in both halves
@@ -1202,9 +1220,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 
 	auto R_ = std::make_shared<ResultData>();
 	ResultData &res = *R_;
-	res.batch = B;
-	res.ls = ls;
-	res.lt = lt;
+	res.batch = B;  // (the lengths join the result at the end, when a result is returned)
 	res.goal = s->goal;
 	res.gap = s->gap;
 	res.loc = s->loc;
@@ -1345,6 +1361,17 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	}
 	std::vector<int32_t> order, level_start;
 	std::vector<int64_t> mask_off, map_off, path_off, val_off, dense_off;
+	struct Lend {  // a repeat's offsets lent to this call, returned however the call ends
+		pa_solver::Repeat *r = nullptr;
+		std::vector<int64_t> *mo, *mp, *po, *vo;
+		~Lend() {
+			if (!r) return;
+			r->mask_off.swap(*mo);
+			r->map_off.swap(*mp);
+			r->path_off.swap(*po);
+			r->val_off.swap(*vo);
+		}
+	} lend{nullptr, &mask_off, &map_off, &path_off, &val_off};
 	// per-pair metadata of a plan: processing order, stripe tickets, output offsets, staged
 	// to the device; output buffers sized
 	auto stage = [&](Plan &plan) -> pa_status {
@@ -1654,10 +1681,12 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		plan.key_shift = r.key_shift;
 		plan.ntickets = r.ntickets;
 		plan.nlevels = r.nlevels;
-		mask_off = r.mask_off;
-		map_off = r.map_off;
-		path_off = r.path_off;
-		val_off = r.val_off;
+		// the staged offsets of the last call, lent to this one (swapped back on every return)
+		mask_off.swap(r.mask_off);
+		map_off.swap(r.map_off);
+		path_off.swap(r.path_off);
+		val_off.swap(r.val_off);
+		lend.r = &r;
 		if (chunked) {
 			if (pa_status e = pipeline()) return e;
 		} else if (in.location == PA_HOST) {
@@ -1798,8 +1827,10 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		PA_CUDA(pa_copy(s, hp + 16 + size_t(B) * 4, s->d_has.p, size_t(B) * 4, cudaMemcpyDeviceToHost, st));
 		PA_CUDA(pa_copy(s, hp + 16 + size_t(B) * 8, s->d_seed.p, size_t(B) * 8, cudaMemcpyDeviceToHost, st));
 	}
-	res.map_off = map_off;
-	res.mask_off = mask_off;
+	if (out) {
+		res.map_off = map_off;
+		res.mask_off = mask_off;
+	}
 	if (need_walk) {
 		if ((maps_out && in.location == PA_DEVICE) || paths_to_user || chunked) {
 			// results stay on the device, or the pipeline downloaded them chunk by chunk
@@ -1874,6 +1905,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	}
 	if (scores_out) std::memcpy(scores_out, res.scores.data(), size_t(B) * 4);
 	if (out) {
+		res.ls = std::move(ls);
+		res.lt = std::move(lt);
 		*out = new pa_result{R_};
 	}
 	return PA_OK;
