@@ -1218,6 +1218,16 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		max_lt = std::max<int64_t>(max_lt, lt[size_t(k)]);
 	}
 
+	if (maps_out && map_offsets && in.location == PA_HOST) {
+		// host maps are staged in a packed device buffer: the offsets must be the packed ones
+		int64_t o = 0;
+		for (int64_t k = 0; k < B; k++) {
+			if (map_offsets[k] != o)
+				return fail(PA_ERR_INVALID_ARGUMENT, "map_offsets must be the prefix sums of min(|s|, |t|)");
+			o += std::min(ls[size_t(k)], lt[size_t(k)]);
+		}
+	}
+
 	auto R_ = std::make_shared<ResultData>();
 	ResultData &res = *R_;
 	res.batch = B;  // (the lengths join the result at the end, when a result is returned)
@@ -1727,22 +1737,14 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			if (pa_status e = tune_plan(s, ls, lt, in, plan, stage, dp)) return e;
 		}
 		// host buffers and many pairs: the repeats of this solve run as a pipeline of chunks
-		// (3 chunks from 32K pairs, 2 from 8K; PA_CHUNKS overrides, up to 12) when the
-		// alignment maps go to the packed offsets (the caller's offsets, if given, equal them)
+		// (3 chunks from 32K pairs, 2 from 8K; PA_CHUNKS overrides, up to 12); host maps use
+		// the packed offsets (checked above)
 		plan.nchunks = 1;
 		if (repeatable && in.location == PA_HOST && in.form != F_DENSE && !plan.units && !want_paths) {
 			int K = B >= 32768 ? 3 : B >= 8192 ? 2 : 1;
 			if (const char *e = std::getenv("PA_CHUNKS")) K = std::atoi(e);
-			bool packed = true;
-			if (maps_out && map_offsets) {
-				int64_t o = 0;
-				for (int64_t k = 0; k < B && packed; k++) {
-					packed = map_offsets[k] == o;
-					o += std::min(ls[size_t(k)], lt[size_t(k)]);
-				}
-			}
 			K = std::min(K, 12);
-			if (K > 1 && packed && B >= (int64_t(1) << K)) plan.nchunks = K;
+			if (K > 1 && B >= (int64_t(1) << K)) plan.nchunks = K;
 		}
 		if (pa_status e = stage(plan)) return e;
 		if (pa_status e = device_work(st, true)) return e;

@@ -140,12 +140,13 @@ def test_repeated_dense_paths_and_gradients(env, monkeypatch):
     assert not torch.equal(got, want)
 
 
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("chunks", [None, "3"])
-def test_repeated_host_batch_solves(env, monkeypatch, chunks):
+def test_repeated_host_batch_solves(env, monkeypatch, chunks, pinned):
     """pa_solve_batch with host buffers: a repeat reuses the plan and staged metadata (no
     graph) -- with PA_CHUNKS=3 as a pipeline of three pair ranges whose uploads, DPs, walks and
     map downloads overlap; new contents and new lengths are solved exactly as by a solver that
-    never caches."""
+    never caches; maps in pageable or pinned host memory."""
     torch, alg, ag = env
     if chunks:
         monkeypatch.setenv("PA_CHUNKS", chunks)
@@ -158,12 +159,15 @@ def test_repeated_host_batch_solves(env, monkeypatch, chunks):
     table = np.full((4, 4), -3.0, np.float32)
     np.fill_diagonal(table, 2.0)
 
-    def solve(solver, a, b, ln):
+    def solve(solver, a, b, ln, pin=False):
         sizes = np.minimum(ln[0], ln[1]).astype(np.int64)
         offs = np.zeros(n, np.int64)
         offs[1:] = np.cumsum(sizes)[:-1]
         sc = np.full(n, np.nan, np.float32)
-        mp = np.full(max(1, int(sizes.sum())), -7, np.int32)
+        if pin:
+            mp = torch.full((max(1, int(sizes.sum())),), -7, dtype=torch.int32).pin_memory().numpy()
+        else:
+            mp = np.full(max(1, int(sizes.sum())), -7, np.int32)
         length = np.ascontiguousarray(ln, dtype=np.int32)
         bt = alg.Batch(form=1, location=0, batch=n, n_s=n_s, n_t=n_t,
                        a=a.ctypes.data_as(P(ctypes.c_uint32)), b=b.ctypes.data_as(P(ctypes.c_uint32)),
@@ -179,21 +183,44 @@ def test_repeated_host_batch_solves(env, monkeypatch, chunks):
     monkeypatch.delenv("PA_GRAPHS")
     solver = _batch_solver(alg, torch, n, n_s, n_t)
     for rep in range(3):
-        got = solve(solver, a, b, ln)
+        got = solve(solver, a, b, ln, pinned)
         assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), rep
         assert not solver.last_plan()["graph"]
     a[:, :] = rng.integers(0, 4, size=(n, n_s))              # new contents, same host buffer
-    got = solve(solver, a, b, ln)
+    got = solve(solver, a, b, ln, pinned)
     monkeypatch.setenv("PA_GRAPHS", "0")
     want2 = solve(ref, a, b, ln)
     monkeypatch.delenv("PA_GRAPHS")
     assert np.array_equal(got[0], want2[0]) and np.array_equal(got[1], want2[1])
     ln2 = ln.copy()
     ln2[1, :11] = 3                                           # new lengths: planned anew
-    got = solve(solver, a, b, ln2)
+    got = solve(solver, a, b, ln2, pinned)
     monkeypatch.setenv("PA_GRAPHS", "0")
     want3 = solve(ref, a, b, ln2)
     assert np.array_equal(got[0], want3[0]) and np.array_equal(got[1], want3[1])
+
+
+def test_host_maps_need_packed_offsets(env):
+    """Host maps are staged at the packed offsets: other offsets are refused before any work."""
+    torch, alg, ag = env
+    P = ctypes.POINTER
+    n, n_s, n_t = 8, 20, 20
+    rng = np.random.default_rng(3)
+    a = rng.integers(0, 4, size=(n, n_s)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, n_t)).astype(np.uint32)
+    table = np.eye(4, dtype=np.float32)
+    length = np.full((2, n), 20, np.int32)
+    offs = np.arange(n, dtype=np.int64) * 25                 # gaps between the maps
+    sc = np.zeros(n, np.float32)
+    mp = np.zeros(n * 25, np.int32)
+    bt = alg.Batch(form=1, location=0, batch=n, n_s=n_s, n_t=n_t,
+                   a=a.ctypes.data_as(P(ctypes.c_uint32)), b=b.ctypes.data_as(P(ctypes.c_uint32)),
+                   table=table.ctypes.data_as(P(ctypes.c_float)), table_rows=4, table_cols=4,
+                   length=length.ctypes.data_as(P(ctypes.c_int32)))
+    solver = _batch_solver(alg, torch, n, n_s, n_t)
+    with pytest.raises(ValueError, match="prefix sums"):
+        alg.check(alg.lib().pa_solve_batch(solver.handle, ctypes.byref(bt), sc.ctypes.data_as(ctypes.c_void_p),
+                                           mp.ctypes.data_as(ctypes.c_void_p), offs.ctypes.data_as(P(ctypes.c_int64))))
 
 
 def test_pipelined_python_api_repeats(env, monkeypatch, oracle_alg):
