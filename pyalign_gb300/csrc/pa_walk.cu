@@ -11,18 +11,22 @@ namespace pa {
 // solver.h:2995-3016).  Diagonal steps are the alignment edges (solver.h:809-847).
 //
 // The walk is a chain of dependent mask reads, so its speed is the latency of one read.
-// The warp therefore caches a window of the masks: lane l holds the word of the 8-row block
-// (u >> 3) - (l >> 4) at column v - (l & 15), i.e. 16 rows x 16 columns up-left of the cell
-// where the window was placed, loaded in one round trip; a cell outside the window
-// re-places it there.  Runs are resolved 16 cells at a time: for a run of diagonal steps
-// lane k decodes cell (u - k, v - k) and one ballot gives the run's length (lanes then write
-// their map entries and path points in parallel), and the start of an affine gap -- the
-// first cell up or left whose extend bit is clear -- is found the same way.  A diagonal or
-// gap run thus costs one memory round trip per 8-16 cells and a few instructions per 16
-// cells instead of per cell.
-__global__ void walk_kernel(WalkParams p) {
+// The warp therefore caches a window of the masks in shared memory: lane l loads the words
+// of the 8-row blocks (u >> 3) - r, r = 0..3, at column v - l -- 32 columns and the 25-32
+// rows up-left of the cell where the window was placed, four independent loads in one round
+// trip; a cell outside the window re-places it there.  Runs are resolved 32 cells at a time:
+// for a run of diagonal steps lane k decodes cell (u - k, v - k) and one ballot gives the
+// run's length (lanes then write their map entries and path points in parallel), and the
+// start of an affine gap -- the first cell up or left whose extend bit is clear -- is found
+// the same way.  A diagonal or gap run thus costs one memory round trip per 25-32 cells and a
+// few instructions per 32 cells instead of per cell.
+constexpr int WALK_WARPS = 4;  // warps per block of walk_kernel (128 threads)
+constexpr int WIN_BLOCKS = 4;  // 8-row blocks per window
+__global__ void __launch_bounds__(WALK_WARPS * 32) walk_kernel(WalkParams p) {
+	__shared__ uint32_t wins[WALK_WARPS][WIN_BLOCKS][32];
 	const int wid = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
 	const int lane = threadIdx.x & 31;
+	uint32_t(*const win)[32] = wins[threadIdx.x >> 5];  // [row block ub - r][column vb - c]
 	if (wid >= p.npairs) return;  // whole warps
 	const int pair = p.pair0 + wid;
 	if (p.status && (*p.status & ST_BAD_CODE)) return;  // the DP did not run: no seeds, no masks
@@ -47,48 +51,56 @@ __global__ void walk_kernel(WalkParams p) {
 	const int S = two ? ((lt + 1) >> 1) + G - 1 : lt + G - 1;
 	const bool s2t = ls <= lt;
 	const bool affine = p.gap == GAP_AFFINE;
-	int ub = -1000000, vb = -1000000;  // window: row blocks ub-1..ub, columns vb-15..vb
-	uint32_t win = 0;
+	int ub = -1000000, vb = -1000000;  // window: row blocks ub-3..ub, columns vb-31..vb
 	// place the window with cell (i, j) at its bottom-right corner (warp-uniform i, j)
 	auto place = [&](int i, int j) {
 		ub = i >> 3;
 		vb = j;
-		const int rb = ub - (lane >> 4), col = vb - (lane & 15);
-		win = 0u;
-		if (rb >= 0 && col >= 0) {
-			const int q = rb / G, sb = rb - q * G;
-			win = two ? W[((int64_t(q) * S + ((col >> 1) + sb)) * G + sb) * 2 + (col & 1)]
-			          : W[(int64_t(q) * S + (col + sb)) * G + sb];
+		const int col = vb - lane;
+		uint32_t w[WIN_BLOCKS];
+#pragma unroll
+		for (int r = 0; r < WIN_BLOCKS; r++) {
+			const int rb = ub - r;
+			w[r] = 0u;
+			if (rb >= 0 && col >= 0) {
+				const int q = rb / G, sb = rb - q * G;
+				w[r] = two ? W[((int64_t(q) * S + ((col >> 1) + sb)) * G + sb) * 2 + (col & 1)]
+				           : W[(int64_t(q) * S + (col + sb)) * G + sb];
+			}
 		}
+		__syncwarp();  // every lane is done reading the previous window
+#pragma unroll
+		for (int r = 0; r < WIN_BLOCKS; r++) win[r][lane] = w[r];
+		__syncwarp();
 	};
 	auto inwin = [&](int i, int j) {
 		const int dr = ub - (i >> 3), dc = vb - j;
-		return i >= 0 && j >= 0 && dr >= 0 && dr <= 1 && dc >= 0 && dc <= 15;
+		return i >= 0 && j >= 0 && dr >= 0 && dr < WIN_BLOCKS && dc >= 0 && dc <= 31;
 	};
-	// nibble of this lane's cell (i, j), valid where ok (the cell lies in the window): every
-	// lane reads its own cell with one shuffle.  Row r's nibble (D source code | P-extend << 2
-	// | Q-extend << 3) sits at bits 4(R-1-r); the 16-bit kernel's nibbles hold the code in
-	// bits 2-3 and the open bits in 0-1.
+	// nibble of this lane's cell (i, j), valid where ok (the cell lies in the window).  Row
+	// r's nibble (D source code | P-extend << 2 | Q-extend << 3) sits at bits 4(R-1-r); the
+	// 16-bit kernel's nibbles hold the code in bits 2-3 and the open bits in 0-1.
 	auto nib_at = [&](int i, int j, bool ok) -> uint32_t {
-		const int src = ok ? (ub - (i >> 3)) * 16 + (vb - j) : 0;
-		const uint32_t w = __shfl_sync(0xffffffffu, win, src);
+		const uint32_t w = ok ? win[ub - (i >> 3)][vb - j] : 0u;
 		const uint32_t n = (w >> (4 * (R - 1 - (i & (R - 1))))) & 15u;
 		return fmt16 ? ((n >> 2) | ((~n & 3u) << 2)) : n;
 	};
+	// index of the lowest clear bit of a ballot (32 when all are set)
+	auto first_clear = [](uint32_t b) { return b == 0xffffffffu ? 32 : __ffs(int(~b)) - 1; };
 	// first cell of a gap run: from (i, j) up (di = 1) or left (dj = 1) while the cell's
 	// extend bit (mask) is set and the index is positive; lane m looks m cells ahead, one
-	// ballot resolves up to 16 cells (the scalar loop: k = i; while (k > 0 && ext(k)) k--)
+	// ballot resolves up to 32 cells (the scalar loop: k = i; while (k > 0 && ext(k)) k--)
 	auto gap_start = [&](int i, int j, int di, int dj, uint32_t mask) -> int {
 		for (;;) {
 			if (!inwin(i, j)) place(i, j);
 			const int r = i - di * lane, c = j - dj * lane;
-			const bool ok = lane < 16 && inwin(r, c);
+			const bool ok = inwin(r, c);
 			const uint32_t n = nib_at(r, c, ok);
 			const bool stop = ok && ((di ? r : c) == 0 || !(n & mask));
 			const uint32_t bs = __ballot_sync(0xffffffffu, stop);
 			const uint32_t bo = __ballot_sync(0xffffffffu, ok);
 			const int first_stop = bs ? __ffs(int(bs)) - 1 : 32;
-			const int first_out = __ffs(int(~bo)) - 1;
+			const int first_out = first_clear(bo);  // >= 1: lane 0's cell (i, j) is in the window
 			if (first_stop < first_out) return (di ? i : j) - first_stop;
 			i -= di * first_out;
 			j -= dj * first_out;
@@ -96,13 +108,13 @@ __global__ void walk_kernel(WalkParams p) {
 	};
 	while (u >= 0 && v >= 0) {
 		if (!inwin(u, v)) place(u, v);
-		// a run of diagonal steps: lane k < 16 looks at (u - k, v - k), one ballot finds how
-		// many consecutive cells from (u, v) have the diagonal code
+		// a run of diagonal steps: lane k looks at (u - k, v - k), one ballot finds how many
+		// consecutive cells from (u, v) have the diagonal code
 		const int iu = u - lane, iv = v - lane;
-		const bool ok = lane < 16 && inwin(iu, iv);
+		const bool ok = inwin(iu, iv);
 		const uint32_t n = nib_at(iu, iv, ok);
 		const uint32_t bal = __ballot_sync(0xffffffffu, ok && (n & 3u) == 2u);
-		const int run = __ffs(int(~bal)) - 1;
+		const int run = first_clear(bal);
 		if (run > 0) {
 			if (lane < run) {
 				if (map) {
