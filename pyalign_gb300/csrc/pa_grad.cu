@@ -165,6 +165,65 @@ __global__ void normalize_rows_bf16_len_kernel(const float *E, int64_t batch, in
 	if (lane == 0) inv_norm[r] = inv;
 }
 
+// The same for widths that are a multiple of 4 up to 512, the common case: a warp takes RPW
+// rows at once -- every lane issues its NV 16-byte loads of all RPW rows before any sum is
+// reduced, so a warp keeps RPW * NV loads in flight instead of one row's -- holds the rows
+// in registers (one read of E), and writes each lane's four BF16 values as one 8-byte store,
+// zeros included.  The sums run in the order of the kernel above, so the factors and 1/|E|
+// are the same bit for bit.
+template <int NV, int RPW>
+__global__ void __launch_bounds__(256) normalize_rows_bf16_rows_kernel(const float *E, int64_t batch, int64_t n,
+                                                                      int32_t dim, int32_t normalize,
+                                                                      const int32_t *len, __nv_bfloat16 *out,
+                                                                      float *inv_norm) {
+	const int lane = threadIdx.x & 31;
+	const int64_t rows = batch * n;
+	const int64_t r0 = ((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * RPW;
+	if (r0 >= rows) return;  // whole warps
+	float4 v[RPW][NV];
+	bool has[RPW];
+#pragma unroll
+	for (int q = 0; q < RPW; q++) {
+		const int64_t r = r0 + q;
+		bool h = r < rows;
+		if (h) {
+			const int64_t k = r / n, i = r - k * n;
+			h = i < len[k];
+		}
+		has[q] = h;
+#pragma unroll
+		for (int j = 0; j < NV; j++) {
+			const int c = 4 * lane + 128 * j;
+			v[q][j] = (h && c < dim) ? *reinterpret_cast<const float4 *>(E + r * dim + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+	}
+#pragma unroll
+	for (int q = 0; q < RPW; q++) {
+		const int64_t r = r0 + q;
+		float ss = 0.0f;
+#pragma unroll
+		for (int j = 0; j < NV; j++)
+			if (4 * lane + 128 * j < dim) {
+				const float4 x = v[q][j];
+				ss += x.x * x.x + x.y * x.y + x.z * x.z + x.w * x.w;
+			}
+		for (int o2 = 16; o2 > 0; o2 >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o2);
+		const float inv = has[q] ? (normalize ? 1.0f / fmaxf(sqrtf(ss), 1e-12f) : 1.0f) : 0.0f;
+		if (r < rows) {
+#pragma unroll
+			for (int j = 0; j < NV; j++) {
+				const int c = 4 * lane + 128 * j;
+				if (c < dim) {
+					const float4 x = v[q][j];
+					__nv_bfloat162 w[2] = {__floats2bfloat162_rn(x.x * inv, x.y * inv), __floats2bfloat162_rn(x.z * inv, x.w * inv)};
+					*reinterpret_cast<uint2 *>(out + r * dim + c) = *reinterpret_cast<const uint2 *>(w);
+				}
+			}
+			if (lane == 0) inv_norm[r] = inv;
+		}
+	}
+}
+
 struct EmbGradParams {
 	int64_t batch;
 	int32_t dim, normalize;
@@ -409,8 +468,20 @@ extern "C" pa_status pa_normalize_rows_bf16_lengths(const float *E, int64_t batc
 	if (batch * n == 0) return PA_OK;
 	const bool aligned = ((reinterpret_cast<uintptr_t>(E)) & 15) == 0 && ((reinterpret_cast<uintptr_t>(out_bf16)) & 7) == 0;
 	if (!aligned && (dim & 3) == 0) return PA_ERR_INVALID_ARGUMENT;  // 16-byte rows need aligned bases
-	normalize_rows_bf16_len_kernel<<<int((batch * n * 32 + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-	    E, batch, n, dim, normalize, lengths, reinterpret_cast<__nv_bfloat16 *>(out_bf16), inv_norm);
+	cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+	__nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out_bf16);
+	constexpr int RPW = 4;
+	const int64_t blocks = (batch * n + 8 * RPW - 1) / (8 * RPW);  // 8 warps of RPW rows per block
+	if ((dim & 3) == 0 && dim <= 512) {
+		const int nv = (dim + 127) / 128;
+		if (nv == 1) normalize_rows_bf16_rows_kernel<1, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
+		else if (nv == 2) normalize_rows_bf16_rows_kernel<2, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
+		else if (nv == 3) normalize_rows_bf16_rows_kernel<3, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
+		else normalize_rows_bf16_rows_kernel<4, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
+	} else {
+		normalize_rows_bf16_len_kernel<<<int((batch * n * 32 + 255) / 256), 256, 0, st>>>(E, batch, n, dim, normalize,
+		                                                                              lengths, o, inv_norm);
+	}
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
 }
 

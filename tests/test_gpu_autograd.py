@@ -336,3 +336,31 @@ def test_series_dtw_weighted_gradients_match_path_counts(torch_ag):
         np.add.at(dy[k], pts[:, 1], -wk[k] * sg)
     assert np.allclose(x.grad.cpu().numpy(), dx, rtol=1e-6, atol=1e-6)
     assert np.allclose(y.grad.cpu().numpy(), dy, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("dim", [16, 100, 128, 256, 384, 512, 520])
+def test_normalized_bf16_rows_with_lengths(torch_ag, dim):
+    """The length-aware BF16 factor: rows inside each pair's length are E / |E| rounded to
+    BF16 (the row-wise kernel for widths that are multiples of 4 up to 512, the one-row kernel
+    otherwise) and agree with the plain kernel's rows to one BF16 rounding step (it sums the
+    squares in another order); rows past the length are zero with 1/|E| = 0; a row count that
+    is not a multiple of the rows a warp takes."""
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(dim)
+    B, n = 7, 37
+    E = torch.randn(B, n, dim, device="cuda", generator=g)
+    ln = np.array([0, 1, 5, 36, 37, 20, 3])
+    Eb, inv = ag.normalized_bf16(E, True, ln)
+    Eb0, inv0 = ag.normalized_bf16(E, True, None)
+    d = Eb.shape[-1]
+    Eb, Eb0 = Eb.view(B, n, d), Eb0.view(B, n, d)
+    inv, inv0 = inv.view(B, n), inv0.view(B, n)
+    ref = torch.nn.functional.normalize(E, dim=-1)
+    for k in range(B):
+        m = int(ln[k])
+        assert torch.equal(Eb[k, m:], torch.zeros_like(Eb[k, m:])) and torch.equal(inv[k, m:], torch.zeros_like(inv[k, m:]))
+        if m:
+            # the same rounding of the same values; the plain kernel sums in another order
+            assert torch.allclose(inv[k, :m], inv0[k, :m], rtol=1e-6)
+            assert torch.allclose(Eb[k, :m, :dim].float(), ref[k, :m], atol=1e-2, rtol=1e-2)
+            assert (Eb[k, :m].float() - Eb0[k, :m].float()).abs().max().item() <= 2 ** -8
