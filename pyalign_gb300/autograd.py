@@ -275,16 +275,17 @@ def _gap_grads(dtw, linear, locality, direction, B, paths, plen, poff, grad):
     if dtw:
         return None, None
     A = _alg
-    dgap = torch.zeros((B, 4), dtype=torch.float32, device=grad.device)
+    dgap = torch.empty((B, 4), dtype=torch.float32, device=grad.device)  # every pair writes its 4
     _alg.check(_lib().pa_path_gradients(
         int(A.Type.ALIGNMENT), int(A.Locality.__members__[locality.upper()]),
         int(A.Direction.__members__[direction.upper()]), B, paths.data_ptr(), poff.data_ptr(),
         plen.data_ptr(), grad.data_ptr(), None, None, 0, 0, dgap.data_ptr(),
         torch.cuda.current_stream().cuda_stream))
-    tot = dgap.sum(dim=0)
+    # one reduction: (open_s + open_t, extend_s + extend_t) summed over pairs
     if linear:
-        return tot[0] + tot[1] + tot[2] + tot[3], None
-    return tot[0] + tot[2], tot[1] + tot[3]
+        return dgap.sum(), None
+    tot = dgap.view(B, 2, 2).sum(dim=(0, 1))
+    return tot[0], tot[1]
 
 
 class AlignmentScore(torch.autograd.Function):

@@ -1167,19 +1167,27 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 	float best = INFINITY;
 	int bestG = plan.G, bestC = plan.C;
 	bool bestU = plan.units, bestH = plan.h16;
-	for (const auto &c : cand) {
+	// one untimed run first (clocks and caches leave their idle state), then each candidate
+	// timed twice, keeping its faster run: a single cold timing could misplace a candidate
+	for (size_t ci = 0; ci <= cand.size(); ci++) {
+		const Cand &c = cand[ci == 0 ? 0 : ci - 1];
 		Plan pl = plan;
 		pl.G = c.G;
 		pl.units = c.units;
 		pl.h16 = c.h16;
 		pl.C = c.C;
 		if (pa_status e = stage(pl)) return e;
-		PA_CUDA(cudaEventRecord(s->ev[1], st));
-		if (pa_status e = dp(pl, pl.tb, false, nullptr)) return e;
-		PA_CUDA(cudaEventRecord(s->ev[2], st));
-		PA_CUDA(cudaEventSynchronize(s->ev[2]));
-		float ms = 0;
-		PA_CUDA(cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]));
+		float ms = INFINITY;
+		for (int rep = 0; rep < (ci == 0 ? 1 : 2); rep++) {
+			PA_CUDA(cudaEventRecord(s->ev[1], st));
+			if (pa_status e = dp(pl, pl.tb, false, nullptr)) return e;
+			PA_CUDA(cudaEventRecord(s->ev[2], st));
+			PA_CUDA(cudaEventSynchronize(s->ev[2]));
+			float t = 0;
+			PA_CUDA(cudaEventElapsedTime(&t, s->ev[1], s->ev[2]));
+			ms = std::min(ms, t);
+		}
+		if (ci == 0) continue;  // the warm-up
 		if (ms < best) {
 			best = ms;
 			bestG = pl.G;
