@@ -525,8 +525,9 @@ def precision_config(torch, pairs, seed, steps=3):
     stream = torch.cuda.current_stream()
 
     def product(alpha=1.0, beta=0.0):
-        Esb, _ = ag.normalized_bf16(Es, True, ls)  # rows past each length: zero, not read
-        Etb, _ = ag.normalized_bf16(Et, True, lt)
+        # rows past each length: zero up to the product's tile, not read; not written beyond
+        Esb, _ = ag.normalized_bf16(Es, True, ls, tiled=True)
+        Etb, _ = ag.normalized_bf16(Et, True, lt, tiled=True)
         return ag.similarity_bf16(Esb, Etb, lengths, out=St, alpha=alpha, beta=beta), Esb, Etb
 
     S, Esb, Etb = product()

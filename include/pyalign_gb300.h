@@ -301,6 +301,14 @@ pa_status pa_normalize_rows_bf16(const float *E, int64_t rows, int32_t dim, int3
  * 16-byte aligned when dim is a multiple of 4 (its rows are then read as 16-byte words). */
 pa_status pa_normalize_rows_bf16_lengths(const float *E, int64_t batch, int64_t n, int32_t dim, int32_t normalize,
                                          const int32_t *lengths, void *out_bf16, float *inv_norm, void *stream);
+
+/* pa_normalize_rows_bf16_lengths writing only the rows a product of `tile`-row tiles reads:
+ * rows below each length as above, the rows from the length up to the next multiple of
+ * `tile` zero, and the rows (and 1/|E| entries) beyond left unwritten. */
+pa_status pa_normalize_rows_bf16_tiled(const float *E, int64_t batch, int64_t n, int32_t dim, int32_t normalize,
+                                       const int32_t *lengths, int32_t tile, void *out_bf16, float *inv_norm,
+                                       void *stream);
+
 pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
                                       const int64_t *path_offsets, const int32_t *path_len,
                                       const float *grad_scores, const float *Es, const float *Et,

@@ -77,6 +77,8 @@ def _lib():
         L.pa_normalize_rows_bf16.argtypes = [vp, i64, i32, i32, vp, vp, vp]
         L.pa_normalize_rows_bf16_lengths.restype = i32
         L.pa_normalize_rows_bf16_lengths.argtypes = [vp, i64, i64, i32, i32, vp, vp, vp, vp]
+        L.pa_normalize_rows_bf16_tiled.restype = i32
+        L.pa_normalize_rows_bf16_tiled.argtypes = [vp, i64, i64, i32, i32, vp, i32, vp, vp, vp]
         L.pa_path_series_gradients.restype = i32
         L.pa_path_series_gradients.argtypes = [i64, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp, vp]
         L.pa_similarity_bf16.restype = i32
@@ -167,7 +169,7 @@ def similarity_bf16(Esb, Etb, lengths, out=None, alpha=1.0, beta=0.0):
     meta[B:2 * B] = ln[1]
     meta[2 * B + 1:] = np.cumsum(tiles)
     total = int(meta[-1])
-    dmeta = torch.from_numpy(meta).to(Esb.device, non_blocking=False)
+    dmeta = _to_device(meta, Esb.device)  # no host wait for the queued work
     if out is None:
         out = torch.empty((B, n_t, n_s), dtype=torch.float32, device=Esb.device)
     elif out.shape != (B, n_t, n_s) or out.dtype != torch.float32 or out.stride(2) != 1 or not out.is_cuda:
@@ -342,11 +344,17 @@ def alignment_score(S, lengths, gap_open=None, gap_extend=None, locality="global
     return AlignmentScore.apply(S, lengths, go, ge, locality, direction, dtw, linear)
 
 
-def normalized_bf16(E, normalize=True, lengths=None):
+SIM_TILE = 128  # rows of a tile of the tensor-core product (pa_simgemm.cu TM, TN)
+
+
+def normalized_bf16(E, normalize=True, lengths=None, tiled=False):
     """The BF16 factor of E (batch, n, d) for the similarity product -- E / |E| per row when
     normalising -- and 1 / |E| per row, in one pass (pa_normalize_rows_bf16).  d is padded
     with zeros to a multiple of 16 (the tensor-core K step).  With ``lengths`` (batch,) the
-    rows past each pair's length are zero and not read (pa_normalize_rows_bf16_lengths)."""
+    rows past each pair's length are zero and not read (pa_normalize_rows_bf16_lengths);
+    with ``tiled`` only the rows the product's tiles read are written (up to each length
+    rounded up to SIM_TILE; the rows beyond keep whatever the fresh tensor held), for a factor
+    that only similarity_bf16 and the aligned rows of the backward read."""
     E = _pad16(E.contiguous().float())
     B, n, dim = E.shape
     Eb = torch.empty(E.shape, dtype=torch.bfloat16, device=E.device)
@@ -357,8 +365,12 @@ def normalized_bf16(E, normalize=True, lengths=None):
                                                  inv.data_ptr(), stream))
     else:
         ln = _to_device(np.minimum(np.asarray(lengths).reshape(B), n).astype(np.int32), E.device)
-        _alg.check(_lib().pa_normalize_rows_bf16_lengths(E.data_ptr(), B, n, dim, int(normalize), ln.data_ptr(),
-                                                         Eb.data_ptr(), inv.data_ptr(), stream))
+        if tiled:
+            _alg.check(_lib().pa_normalize_rows_bf16_tiled(E.data_ptr(), B, n, dim, int(normalize), ln.data_ptr(),
+                                                           SIM_TILE, Eb.data_ptr(), inv.data_ptr(), stream))
+        else:
+            _alg.check(_lib().pa_normalize_rows_bf16_lengths(E.data_ptr(), B, n, dim, int(normalize),
+                                                             ln.data_ptr(), Eb.data_ptr(), inv.data_ptr(), stream))
     return Eb, inv
 
 
@@ -422,8 +434,9 @@ class EmbeddingAlignmentScore(torch.autograd.Function):
         Es = _pad16(Es.contiguous().float())
         Et = _pad16(Et.contiguous().float())
         ln = np.asarray(lengths).reshape(Es.shape[0], 2)
-        Esb, inv_s = normalized_bf16(Es, normalize, ln[:, 0])  # rows past a pair's length: zero, not read
-        Etb, inv_t = normalized_bf16(Et, normalize, ln[:, 1])
+        # rows past a pair's length: zero up to the product's tile, not read, not written beyond
+        Esb, inv_s = normalized_bf16(Es, normalize, ln[:, 0], tiled=True)
+        Etb, inv_t = normalized_bf16(Et, normalize, ln[:, 1], tiled=True)
         # S^T = en_t en_s^T on the tensor cores, only the cells inside the lengths; its
         # transposed view is S with stride 1 along s
         S = similarity_bf16(Esb, Etb, lengths)

@@ -128,13 +128,14 @@ __global__ void normalize_rows_bf16_kernel(const float *E, int64_t rows, int32_t
 // reading E (the product's padding rows must be zero, and their values are never used);
 // rows of a width that is a multiple of 4 are read as 16-byte words.
 __global__ void normalize_rows_bf16_len_kernel(const float *E, int64_t batch, int64_t n, int32_t dim,
-                                               int32_t normalize, const int32_t *len, __nv_bfloat16 *out,
-                                               float *inv_norm) {
+                                               int32_t normalize, const int32_t *len, int32_t tile,
+                                               __nv_bfloat16 *out, float *inv_norm) {
 	const int64_t r = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
 	const int lane = threadIdx.x & 31;
 	if (r >= batch * n) return;
 	const int64_t k = r / n, i = r - k * n;
 	__nv_bfloat16 *o = out + r * dim;
+	if (tile > 0 && i >= (int64_t(len[k]) + tile - 1) / tile * tile) return;  // past the last tile: not written
 	if (i >= len[k]) {
 		for (int c = lane; c < dim; c += 32) o[c] = __float2bfloat16_rn(0.0f);
 		if (lane == 0) inv_norm[r] = 0.0f;
@@ -171,26 +172,30 @@ __global__ void normalize_rows_bf16_len_kernel(const float *E, int64_t batch, in
 // in registers (one read of E), and writes each lane's four BF16 values as one 8-byte store,
 // zeros included.  The sums run in the order of the kernel above, so the factors and 1/|E|
 // are the same bit for bit.
+// tile > 0: rows from each length rounded up to a multiple of tile on are not written.
 template <int NV, int RPW>
 __global__ void __launch_bounds__(256) normalize_rows_bf16_rows_kernel(const float *E, int64_t batch, int64_t n,
                                                                       int32_t dim, int32_t normalize,
-                                                                      const int32_t *len, __nv_bfloat16 *out,
-                                                                      float *inv_norm) {
+                                                                      const int32_t *len, int32_t tile,
+                                                                      __nv_bfloat16 *out, float *inv_norm) {
 	const int lane = threadIdx.x & 31;
 	const int64_t rows = batch * n;
 	const int64_t r0 = ((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * RPW;
 	if (r0 >= rows) return;  // whole warps
 	float4 v[RPW][NV];
-	bool has[RPW];
+	bool has[RPW], put[RPW];
 #pragma unroll
 	for (int q = 0; q < RPW; q++) {
 		const int64_t r = r0 + q;
-		bool h = r < rows;
+		bool h = r < rows, w = h;
 		if (h) {
 			const int64_t k = r / n, i = r - k * n;
-			h = i < len[k];
+			const int32_t m = len[k];
+			h = i < m;
+			w = tile <= 0 || i < (int64_t(m) + tile - 1) / tile * tile;
 		}
 		has[q] = h;
+		put[q] = w;
 #pragma unroll
 		for (int j = 0; j < NV; j++) {
 			const int c = 4 * lane + 128 * j;
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(256) normalize_rows_bf16_rows_kernel(const flo
 			}
 		for (int o2 = 16; o2 > 0; o2 >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o2);
 		const float inv = has[q] ? (normalize ? 1.0f / fmaxf(sqrtf(ss), 1e-12f) : 1.0f) : 0.0f;
-		if (r < rows) {
+		if (r < rows && put[q]) {
 #pragma unroll
 			for (int j = 0; j < NV; j++) {
 				const int c = 4 * lane + 128 * j;
@@ -461,10 +466,12 @@ extern "C" pa_status pa_normalize_rows_bf16(const float *E, int64_t rows, int32_
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
 }
 
-extern "C" pa_status pa_normalize_rows_bf16_lengths(const float *E, int64_t batch, int64_t n, int32_t dim,
-                                                    int32_t normalize, const int32_t *lengths, void *out_bf16,
-                                                    float *inv_norm, void *stream) {
-	if (batch < 0 || n < 0 || dim <= 0 || !E || !lengths || !out_bf16 || !inv_norm) return PA_ERR_INVALID_ARGUMENT;
+namespace {
+
+pa_status normalize_lengths(const float *E, int64_t batch, int64_t n, int32_t dim, int32_t normalize,
+                            const int32_t *lengths, int32_t tile, void *out_bf16, float *inv_norm, void *stream) {
+	if (batch < 0 || n < 0 || dim <= 0 || tile < 0 || !E || !lengths || !out_bf16 || !inv_norm)
+		return PA_ERR_INVALID_ARGUMENT;
 	if (batch * n == 0) return PA_OK;
 	const bool aligned = ((reinterpret_cast<uintptr_t>(E)) & 15) == 0 && ((reinterpret_cast<uintptr_t>(out_bf16)) & 7) == 0;
 	if (!aligned && (dim & 3) == 0) return PA_ERR_INVALID_ARGUMENT;  // 16-byte rows need aligned bases
@@ -474,15 +481,30 @@ extern "C" pa_status pa_normalize_rows_bf16_lengths(const float *E, int64_t batc
 	const int64_t blocks = (batch * n + 8 * RPW - 1) / (8 * RPW);  // 8 warps of RPW rows per block
 	if ((dim & 3) == 0 && dim <= 512) {
 		const int nv = (dim + 127) / 128;
-		if (nv == 1) normalize_rows_bf16_rows_kernel<1, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
-		else if (nv == 2) normalize_rows_bf16_rows_kernel<2, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
-		else if (nv == 3) normalize_rows_bf16_rows_kernel<3, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
-		else normalize_rows_bf16_rows_kernel<4, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, o, inv_norm);
+		if (nv == 1) normalize_rows_bf16_rows_kernel<1, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, tile, o, inv_norm);
+		else if (nv == 2) normalize_rows_bf16_rows_kernel<2, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, tile, o, inv_norm);
+		else if (nv == 3) normalize_rows_bf16_rows_kernel<3, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, tile, o, inv_norm);
+		else normalize_rows_bf16_rows_kernel<4, RPW><<<int(blocks), 256, 0, st>>>(E, batch, n, dim, normalize, lengths, tile, o, inv_norm);
 	} else {
 		normalize_rows_bf16_len_kernel<<<int((batch * n * 32 + 255) / 256), 256, 0, st>>>(E, batch, n, dim, normalize,
-		                                                                              lengths, o, inv_norm);
+		                                                                              lengths, tile, o, inv_norm);
 	}
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" pa_status pa_normalize_rows_bf16_lengths(const float *E, int64_t batch, int64_t n, int32_t dim,
+                                                    int32_t normalize, const int32_t *lengths, void *out_bf16,
+                                                    float *inv_norm, void *stream) {
+	return normalize_lengths(E, batch, n, dim, normalize, lengths, 0, out_bf16, inv_norm, stream);
+}
+
+extern "C" pa_status pa_normalize_rows_bf16_tiled(const float *E, int64_t batch, int64_t n, int32_t dim,
+                                                  int32_t normalize, const int32_t *lengths, int32_t tile,
+                                                  void *out_bf16, float *inv_norm, void *stream) {
+	if (tile <= 0) return PA_ERR_INVALID_ARGUMENT;
+	return normalize_lengths(E, batch, n, dim, normalize, lengths, tile, out_bf16, inv_norm, stream);
 }
 
 extern "C" pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,

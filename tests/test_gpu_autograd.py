@@ -364,3 +364,29 @@ def test_normalized_bf16_rows_with_lengths(torch_ag, dim):
             assert torch.allclose(inv[k, :m], inv0[k, :m], rtol=1e-6)
             assert torch.allclose(Eb[k, :m, :dim].float(), ref[k, :m], atol=1e-2, rtol=1e-2)
             assert (Eb[k, :m].float() - Eb0[k, :m].float()).abs().max().item() <= 2 ** -8
+
+
+def test_normalized_bf16_tiled_writes_only_the_product_tiles(torch_ag):
+    """The tiled factor equals the length-aware one on every row below each length rounded up
+    to the product's tile and leaves the rows beyond untouched; the product and the scores of
+    the embedding form are unchanged."""
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(77)
+    B, n, d = 6, 300, 128
+    E = torch.randn(B, n, d, device="cuda", generator=g)
+    ln = np.array([0, 1, 127, 128, 129, 300])
+    full, inv_full = ag.normalized_bf16(E, True, ln)
+    tiled, inv_t = ag.normalized_bf16(E, True, ln, tiled=True)
+    for k in range(B):
+        top = min(n, -(-int(ln[k]) // ag.SIM_TILE) * ag.SIM_TILE)
+        assert torch.equal(tiled[k, :top], full[k, :top])
+        assert torch.equal(inv_t.view(B, n)[k, :top], inv_full.view(B, n)[k, :top])
+    lengths = np.stack([np.array([5, 64, 128, 200, 256, 256]), np.array([7, 100, 130, 256, 1, 256])], axis=1)
+    Es = torch.randn(B, 256, d, device="cuda", generator=g)
+    Et = torch.randn(B, 256, d, device="cuda", generator=g)
+    a = ag.embedding_alignment_score(Es, Et, lengths, 0.5, 0.1, "global")
+    Esb, _ = ag.normalized_bf16(Es, True, lengths[:, 0])
+    Etb, _ = ag.normalized_bf16(Et, True, lengths[:, 1])
+    S = ag.similarity_bf16(Esb, Etb, lengths)
+    b = ag.alignment_score(S, lengths, 0.5, 0.1, "global")
+    assert torch.equal(a, b)
