@@ -45,13 +45,6 @@
 
 #include "pa_dp.cuh"
 
-#ifndef PA_DP16_SKEW
-#define PA_DP16_SKEW 1     // two columns: row r + 1's first column before row r's second
-#endif
-#ifndef PA_DP16_IMADNIB
-#define PA_DP16_IMADNIB 1  // traceback nibbles accumulated by IMAD (FMA pipe)
-#endif
-
 namespace pa {
 
 __device__ __forceinline__ uint32_t h_add(uint32_t a, uint32_t b) {
@@ -324,7 +317,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 					// the traceback nibble of a cell into the row's word (rows 0-3: lo, 4-7: hi)
 					auto put_nib = [&](uint32_t &lo, uint32_t &hi, int r, uint32_t n) {
 						uint32_t &w = r < 4 ? lo : hi;
-						w = PA_DP16_IMADNIB ? uint32_t(imad(int32_t(w), p.sixteen, int32_t(n))) : w * 16u + n;
+						w = uint32_t(imad(int32_t(w), p.sixteen, int32_t(n)));  // on the FMA pipe
 					};
 					// local seeds: the row's key (D | row tag) into the step's best, two rows per max3
 					auto put_seed = [&](uint32_t &best, uint32_t &even, int r, uint32_t D, uint32_t t) {
@@ -371,20 +364,14 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 					if (C == 1) {
 #pragma unroll
 						for (int r = 0; r < R; r++) col0(r);
-					} else if (PA_DP16_SKEW) {
+					} else {
 						// column j0 of row r + 1 before column j1 of row r: row r's old D (the
 						// diagonal of row r + 1, column j0) is dead before column j1 of row r
-						// replaces it, so the new values take the old ones' registers
+						// replaces it, so the new values can take the old ones' registers
 #pragma unroll
 						for (int r = 0; r <= R; r++) {
 							if (r < R) col0(r);
 							if (r >= 1) col1(r - 1);
-						}
-					} else {
-#pragma unroll
-						for (int r = 0; r < R; r++) {
-							col0(r);
-							col1(r);
 						}
 					}
 					outD0 = uD0;

@@ -525,27 +525,9 @@ bool h16_plan(const pa_solver *s, const Input &in, const float *host_table, cons
 // 1 : 2 : 4 : ..., so each chunk's upload (about 4x faster per pair than its DP) is hidden
 // behind the previous chunk's DP and only the small first chunk's upload is exposed.
 void chunk_range(int64_t B, int K, int c, int64_t &k0, int64_t &k1) {
-	// PA_CHUNK_SHAPE=sym (experiments): sizes 1 : 2 : 4 ... 4 : 2 : 1, so the last chunk's
-	// walk and download, exposed after the DP, are small too
-	static const bool sym = [] {
-		const char *e = std::getenv("PA_CHUNK_SHAPE");
-		return e && std::strcmp(e, "sym") == 0;
-	}();
-	if (!sym) {
-		const int64_t den = (int64_t(1) << K) - 1;
-		k0 = B * ((int64_t(1) << c) - 1) / den;
-		k1 = B * ((int64_t(1) << (c + 1)) - 1) / den;
-		return;
-	}
-	int64_t den = 0, before = 0;
-	for (int i = 0; i < K; i++) {
-		const int64_t w = int64_t(1) << std::min(i, K - 1 - i);
-		den += w;
-		if (i < c) before += w;
-	}
-	const int64_t w = int64_t(1) << std::min(c, K - 1 - c);
-	k0 = B * before / den;
-	k1 = B * (before + w) / den;
+	const int64_t den = (int64_t(1) << K) - 1;
+	k0 = B * ((int64_t(1) << c) - 1) / den;
+	k1 = B * ((int64_t(1) << (c + 1)) - 1) / den;
 }
 
 // a 16-bit addend in both halves
