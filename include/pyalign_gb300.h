@@ -316,6 +316,15 @@ pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normal
                                       const float *inv_t, int64_t n_s, int64_t n_t, float *dEs, float *dEt,
                                       void *stream);
 
+/* pa_path_embedding_gradients writing every row of dEs and dEt: the rows without an aligned
+ * cell (padding rows included) are set to zero, so the caller need not zero them first. */
+pa_status pa_path_embedding_gradients_full(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
+                                           const int64_t *path_offsets, const int32_t *path_len,
+                                           const float *grad_scores, const float *Es, const float *Et,
+                                           const void *Es_bf16, const void *Et_bf16, const float *inv_s,
+                                           const float *inv_t, int64_t n_s, int64_t n_t, float *dEs, float *dEt,
+                                           void *stream);
+
 /* Fused backward of DTW on two series with d(u, v) = |x_u - y_v| (x: (batch, n_s),
  * y: (batch, n_t) float32): every visited cell adds grad * sign(x_u - y_v) to dx_u and
  * subtracts it from dy_v (per row and column: grad times the exact count of signs, adding to

@@ -73,6 +73,8 @@ def _lib():
         L.pa_path_embedding_gradients.restype = i32
         L.pa_path_embedding_gradients.argtypes = [i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, i64,
                                                   vp, vp, vp]
+        L.pa_path_embedding_gradients_full.restype = i32
+        L.pa_path_embedding_gradients_full.argtypes = L.pa_path_embedding_gradients.argtypes
         L.pa_normalize_rows_bf16.restype = i32
         L.pa_normalize_rows_bf16.argtypes = [vp, i64, i32, i32, vp, vp, vp]
         L.pa_normalize_rows_bf16_lengths.restype = i32
@@ -455,9 +457,9 @@ class EmbeddingAlignmentScore(torch.autograd.Function):
         B, n_s, dim = Es.shape
         n_t = Et.shape[1]
         d_in = ctx.dim_in
-        dEs = torch.zeros_like(Es)
-        dEt = torch.zeros_like(Et)
-        _alg.check(_lib().pa_path_embedding_gradients(
+        dEs = torch.empty_like(Es)  # every row is written: the aligned ones, zeros elsewhere
+        dEt = torch.empty_like(Et)
+        _alg.check(_lib().pa_path_embedding_gradients_full(
             B, dim, int(normalize), paths.data_ptr(), poff.data_ptr(), plen.data_ptr(), grad.data_ptr(),
             Es.data_ptr(), Et.data_ptr(), Esb.data_ptr(), Etb.data_ptr(), inv_s.data_ptr(), inv_t.data_ptr(),
             n_s, n_t, dEs.data_ptr(), dEt.data_ptr(), torch.cuda.current_stream().cuda_stream))

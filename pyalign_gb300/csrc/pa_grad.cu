@@ -241,6 +241,7 @@ struct EmbGradParams {
 	const float *inv_s, *inv_t;           // 1/|E| per row (1 when not normalising)
 	float *dEs, *dEt;                     // zero except on aligned rows
 	int64_t n_s, n_t;
+	int32_t zero_rest;                    // vector kernel: also write the zero rows (see there)
 };
 
 __device__ __forceinline__ float warp_sum(float x) {
@@ -303,6 +304,11 @@ __device__ __forceinline__ float4 bf16x4(const __nv_bfloat16 *p4) {
 	                   __uint_as_float(w.y & 0xffff0000u));
 }
 
+// With zero_rest the kernel writes every row of the pair's dE itself, so dE needs no
+// zeroing beforehand (which would write the aligned rows twice): the warp first marks the
+// rows of its aligned cells in a bitmap in shared memory (ceil(n_s / 32) + ceil(n_t / 32)
+// words per warp, dynamic), stores zeros to the unmarked rows -- padding rows included --
+// and then writes the aligned rows below.
 __global__ void path_embedding_grad_vec_kernel(EmbGradParams p) {
 	const int64_t k = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
 	const int lane = threadIdx.x & 31;
@@ -311,6 +317,39 @@ __global__ void path_embedding_grad_vec_kernel(EmbGradParams p) {
 	const int n = p.path_len[k];
 	const int32_t *P = p.paths + p.path_off[k];
 	const int64_t bs = k * p.n_s, bt = k * p.n_t;
+	if (p.zero_rest) {
+		extern __shared__ uint32_t row_marks[];
+		const int ws = int((p.n_s + 31) >> 5), wt = int((p.n_t + 31) >> 5);
+		uint32_t *ms = row_marks + (threadIdx.x >> 5) * (ws + wt), *mt = ms + ws;
+		for (int w = lane; w < ws + wt; w += 32) ms[w] = 0u;
+		__syncwarp();
+		for (int q0 = 0; q0 + 1 < n; q0 += 32) {
+			const int q = q0 + lane;
+			int u0 = -1, v0 = -1;
+			bool neg = false, al = false;
+			if (q + 1 < n) {
+				u0 = P[2 * q];
+				v0 = P[2 * q + 1];
+				neg = u0 < 0 || v0 < 0;
+				al = !neg && P[2 * q + 2] == u0 - 1 && P[2 * q + 3] == v0 - 1;
+			}
+			const uint32_t negm = __ballot_sync(0xffffffffu, neg);
+			const int stop = negm ? __ffs(int(negm)) - 1 : 32;
+			if (al && lane < stop && u0 < p.n_s && v0 < p.n_t) {
+				atomicOr(ms + (u0 >> 5), 1u << (u0 & 31));
+				atomicOr(mt + (v0 >> 5), 1u << (v0 & 31));
+			}
+			if (negm) break;
+		}
+		__syncwarp();
+		const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+		for (int64_t i = 0; i < p.n_s; i++)
+			if (!((ms[i >> 5] >> (i & 31)) & 1u))
+				for (int c = 4 * lane; c < p.dim; c += 128) *reinterpret_cast<float4 *>(p.dEs + (bs + i) * p.dim + c) = z;
+		for (int64_t j = 0; j < p.n_t; j++)
+			if (!((mt[j >> 5] >> (j & 31)) & 1u))
+				for (int c = 4 * lane; c < p.dim; c += 128) *reinterpret_cast<float4 *>(p.dEt + (bt + j) * p.dim + c) = z;
+	}
 	const int quarter = lane >> 3, ql = lane & 7;
 	const int chunks = p.dim >> 5;
 	for (int q0 = 0; q0 + 1 < n; q0 += 32) {
@@ -507,30 +546,66 @@ extern "C" pa_status pa_normalize_rows_bf16_tiled(const float *E, int64_t batch,
 	return normalize_lengths(E, batch, n, dim, normalize, lengths, tile, out_bf16, inv_norm, stream);
 }
 
-extern "C" pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
-                                                 const int64_t *path_offsets, const int32_t *path_len,
-                                                 const float *grad_scores, const float *Es, const float *Et,
-                                                 const void *Es_bf16, const void *Et_bf16, const float *inv_s,
-                                                 const float *inv_t, int64_t n_s, int64_t n_t, float *dEs, float *dEt,
-                                                 void *stream) {
-	if (batch < 0 || dim <= 0 || !paths || !path_offsets || !path_len || !grad_scores || !Es || !Et || !Es_bf16 ||
-	    !Et_bf16 || !inv_s || !inv_t || !dEs || !dEt)
+namespace {
+
+pa_status embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
+                              const int64_t *path_offsets, const int32_t *path_len, const float *grad_scores,
+                              const float *Es, const float *Et, const void *Es_bf16, const void *Et_bf16,
+                              const float *inv_s, const float *inv_t, int64_t n_s, int64_t n_t, float *dEs,
+                              float *dEt, bool full, void *stream) {
+	if (batch < 0 || dim <= 0 || n_s < 0 || n_t < 0 || !paths || !path_offsets || !path_len || !grad_scores || !Es ||
+	    !Et || !Es_bf16 || !Et_bf16 || !inv_s || !inv_t || !dEs || !dEt)
 		return PA_ERR_INVALID_ARGUMENT;
 	if (batch == 0) return PA_OK;
+	cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 	EmbGradParams p{batch, dim, normalize, paths, path_offsets, path_len, grad_scores, Es, Et,
 	                reinterpret_cast<const __nv_bfloat16 *>(Es_bf16), reinterpret_cast<const __nv_bfloat16 *>(Et_bf16),
-	                inv_s, inv_t, dEs, dEt, n_s, n_t};
+	                inv_s, inv_t, dEs, dEt, n_s, n_t, 0};
 	const int64_t threads = batch * 32;
 	// 16-byte rows (the vector kernel) when the width is a multiple of 32 and the rows aligned
 	const bool vec = dim % 32 == 0 &&
 	                 ((reinterpret_cast<uintptr_t>(Es) | reinterpret_cast<uintptr_t>(Et) | reinterpret_cast<uintptr_t>(dEs) |
 	                   reinterpret_cast<uintptr_t>(dEt)) & 15) == 0 &&
 	                 ((reinterpret_cast<uintptr_t>(Es_bf16) | reinterpret_cast<uintptr_t>(Et_bf16)) & 7) == 0;
+	// the row marks of the 8 warps of a block in shared memory
+	const size_t marks = size_t(8) * size_t((n_s + 31) / 32 + (n_t + 31) / 32) * 4;
+	if (full && vec && marks <= 48 * 1024) {
+		p.zero_rest = 1;
+		path_embedding_grad_vec_kernel<<<int((threads + 255) / 256), 256, marks, st>>>(p);
+		return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+	}
+	if (full) {
+		if (cudaMemsetAsync(dEs, 0, size_t(batch * n_s * dim) * 4, st) != cudaSuccess ||
+		    cudaMemsetAsync(dEt, 0, size_t(batch * n_t * dim) * 4, st) != cudaSuccess)
+			return PA_ERR_CUDA;
+	}
 	if (vec)
-		path_embedding_grad_vec_kernel<<<int((threads + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+		path_embedding_grad_vec_kernel<<<int((threads + 255) / 256), 256, 0, st>>>(p);
 	else
-		path_embedding_grad_kernel<<<int((threads + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+		path_embedding_grad_kernel<<<int((threads + 255) / 256), 256, 0, st>>>(p);
 	return cudaGetLastError() == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" pa_status pa_path_embedding_gradients(int64_t batch, int32_t dim, int32_t normalize, const int32_t *paths,
+                                                 const int64_t *path_offsets, const int32_t *path_len,
+                                                 const float *grad_scores, const float *Es, const float *Et,
+                                                 const void *Es_bf16, const void *Et_bf16, const float *inv_s,
+                                                 const float *inv_t, int64_t n_s, int64_t n_t, float *dEs, float *dEt,
+                                                 void *stream) {
+	return embedding_gradients(batch, dim, normalize, paths, path_offsets, path_len, grad_scores, Es, Et, Es_bf16,
+	                           Et_bf16, inv_s, inv_t, n_s, n_t, dEs, dEt, false, stream);
+}
+
+extern "C" pa_status pa_path_embedding_gradients_full(int64_t batch, int32_t dim, int32_t normalize,
+                                                      const int32_t *paths, const int64_t *path_offsets,
+                                                      const int32_t *path_len, const float *grad_scores,
+                                                      const float *Es, const float *Et, const void *Es_bf16,
+                                                      const void *Et_bf16, const float *inv_s, const float *inv_t,
+                                                      int64_t n_s, int64_t n_t, float *dEs, float *dEt, void *stream) {
+	return embedding_gradients(batch, dim, normalize, paths, path_offsets, path_len, grad_scores, Es, Et, Es_bf16,
+	                           Et_bf16, inv_s, inv_t, n_s, n_t, dEs, dEt, true, stream);
 }
 
 extern "C" pa_status pa_path_series_gradients(int64_t batch, const int32_t *paths, const int64_t *path_offsets,

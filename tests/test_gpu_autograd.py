@@ -390,3 +390,35 @@ def test_normalized_bf16_tiled_writes_only_the_product_tiles(torch_ag):
     S = ag.similarity_bf16(Esb, Etb, lengths)
     b = ag.alignment_score(S, lengths, 0.5, 0.1, "global")
     assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("dim", [128, 48])
+def test_embedding_gradients_full_writes_every_row(torch_ag, dim):
+    """pa_path_embedding_gradients_full on NaN-filled outputs equals the accumulate-into-zeros
+    entry bit for bit: every row is written (aligned rows with their gradient, the others --
+    gap and padding rows -- with zeros).  dim 48: the one-row kernel after a memset."""
+    torch, ag = torch_ag
+    g = torch.Generator(device="cuda").manual_seed(dim + 1)
+    B, n = 12, 90
+    Es = torch.randn(B, n, dim, device="cuda", generator=g)
+    Et = torch.randn(B, n, dim, device="cuda", generator=g)
+    rng = np.random.default_rng(dim)
+    lengths = np.stack([rng.integers(1, n + 1, B), rng.integers(1, n + 1, B)], axis=1)
+    lengths[0] = (n, n)
+    Esb, inv_s = ag.normalized_bf16(Es, True, lengths[:, 0])
+    Etb, inv_t = ag.normalized_bf16(Et, True, lengths[:, 1])
+    S = ag.similarity_bf16(Esb, Etb, lengths)
+    _, paths, plen, poff, _ = ag._forward_paths(S, lengths, (0.5, 0.1), "global", "maximize", False)
+    grad = torch.randn(B, device="cuda", generator=g)
+    Es16, Et16 = ag._pad16(Es), ag._pad16(Et)
+    d = Es16.shape[-1]
+    out = {}
+    for name, fill in (("pa_path_embedding_gradients", 0.0), ("pa_path_embedding_gradients_full", float("nan"))):
+        dEs = torch.full_like(Es16, fill)
+        dEt = torch.full_like(Et16, fill)
+        ag._alg.check(getattr(ag._lib(), name)(
+            B, d, 1, paths.data_ptr(), poff.data_ptr(), plen.data_ptr(), grad.data_ptr(), Es16.data_ptr(),
+            Et16.data_ptr(), Esb.data_ptr(), Etb.data_ptr(), inv_s.data_ptr(), inv_t.data_ptr(), n, n,
+            dEs.data_ptr(), dEt.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        out[fill == 0.0] = (dEs, dEt)
+    assert torch.equal(out[True][0], out[False][0]) and torch.equal(out[True][1], out[False][1])
