@@ -360,6 +360,9 @@ struct pa_solver {
 	DevBuf d_border_mode[4];          // borders per arithmetic mode: float, int tagged, int plain, packed 16-bit
 	bool border_ready[4] = {false, false, false, false};
 	std::vector<unsigned char> h_tab;  // staging of the converted similarity table
+	// the per-pair lengths of the current call, kept across calls: a fresh vector of that size
+	// per call would be new pages (allocator mmap) faulted in on every call
+	std::vector<int32_t> h_ls, h_lt;
 
 	// Repeated solves: the signature of the last device-resident solve and, once the same
 	// solve came twice in a row, a CUDA graph of its device work (see solve_impl).
@@ -1199,13 +1202,25 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	// per-lane lengths, clamped to the batch arrays (stale lanes of a partial batch carry
 	// lengths beyond the master shape; the reference computes them from padding and the
 	// Python layer discards them, solve.py:382-396, 554-560)
-	std::vector<int32_t> ls(static_cast<size_t>(B)), lt(static_cast<size_t>(B));
+	std::vector<int32_t> &ls = s->h_ls, &lt = s->h_lt;
+	ls.resize(size_t(B));  // every entry is written below
+	lt.resize(size_t(B));
 	int64_t max_ls = 0, max_lt = 0;
-	for (int64_t k = 0; k < B; k++) {
-		ls[size_t(k)] = int32_t(std::min<int64_t>(std::max(in.length[k], 0), in.n_s));
-		lt[size_t(k)] = int32_t(std::min<int64_t>(std::max(in.length[B + k], 0), in.n_t));
-		max_ls = std::max<int64_t>(max_ls, ls[size_t(k)]);
-		max_lt = std::max<int64_t>(max_lt, lt[size_t(k)]);
+	{
+		// int32 throughout, so the compiler vectorises the clamp and the maxima
+		const int32_t cs = int32_t(std::min<int64_t>(in.n_s, INT32_MAX)), ct = int32_t(std::min<int64_t>(in.n_t, INT32_MAX));
+		const int32_t *l0 = in.length, *l1 = in.length + B;
+		int32_t *ps = ls.data(), *pt = lt.data();
+		int32_t ms = 0, mt = 0;
+		for (int64_t k = 0; k < B; k++) {
+			const int32_t a = std::min(std::max(l0[k], 0), cs), b = std::min(std::max(l1[k], 0), ct);
+			ps[k] = a;
+			pt[k] = b;
+			ms = std::max(ms, a);
+			mt = std::max(mt, b);
+		}
+		max_ls = ms;
+		max_lt = mt;
 	}
 
 	if (maps_out && map_offsets && in.location == PA_HOST) {
@@ -1254,7 +1269,12 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	if (in.form == F_INDEXED) {
 		host_table.resize(size_t(in.table_rows * in.table_cols));
 		if (in.location == PA_DEVICE) {
-			PA_CUDA(pa_copy(s, host_table.data(), in.table, host_table.size() * 4, cudaMemcpyDeviceToHost, st));
+			// through the solver's pinned block (a pageable destination makes the driver stage it)
+			const size_t nb = host_table.size() * 4;
+			PA_CUDA(s->h_out.ensure(nb + 16));
+			PA_CUDA(pa_copy(s, s->h_out.p, in.table, nb, cudaMemcpyDeviceToHost, st));
+			PA_CUDA(cudaStreamSynchronize(st));
+			std::memcpy(host_table.data(), s->h_out.p, nb);
 		} else if (!host_table.empty()) {
 			std::memcpy(host_table.data(), in.table, host_table.size() * 4);
 		}
@@ -1897,8 +1917,8 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	}
 	if (scores_out) std::memcpy(scores_out, res.scores.data(), size_t(B) * 4);
 	if (out) {
-		res.ls = std::move(ls);
-		res.lt = std::move(lt);
+		res.ls = ls;
+		res.lt = lt;
 		*out = new pa_result{R_};
 	}
 	return PA_OK;
