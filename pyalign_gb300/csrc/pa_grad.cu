@@ -184,12 +184,20 @@ __global__ void __launch_bounds__(256) normalize_rows_bf16_rows_kernel(const flo
 	if (r0 >= rows) return;  // whole warps
 	float4 v[RPW][NV];
 	bool has[RPW], put[RPW];
+	// (pair, row) of the warp's first row by one division, then stepped (a 64-bit division
+	// per row would dominate this kernel's instructions)
+	int64_t k = r0 / n, i = r0 - k * n;
 #pragma unroll
 	for (int q = 0; q < RPW; q++) {
 		const int64_t r = r0 + q;
+		if (q > 0) {
+			if (++i == n) {
+				i = 0;
+				k++;
+			}
+		}
 		bool h = r < rows, w = h;
 		if (h) {
-			const int64_t k = r / n, i = r - k * n;
 			const int32_t m = len[k];
 			h = i < m;
 			w = tile <= 0 || i < (int64_t(m) + tile - 1) / tile * tile;
