@@ -381,7 +381,7 @@ __global__ void path_embedding_grad_vec_kernel(EmbGradParams p) {
 			const int src = m ? __ffs(int(m)) - 1 : 32;
 			const int u = __shfl_sync(0xffffffffu, u0, src < 32 ? src : 0);
 			const int v = __shfl_sync(0xffffffffu, v0, src < 32 ? src : 0);
-			for (int c = 0; c < 4 && am; c++) am &= am - 1;  // the four cells of this round
+			for (int c = 0; c < 4 && am; c++) am &= am - 1;  // the four cells of this pass
 			const bool has = src < 32 && u >= 0 && u < p.n_s && v >= 0 && v < p.n_t;
 			const int64_t ri = (bs + (has ? u : 0)) * p.dim, rj = (bt + (has ? v : 0)) * p.dim;
 			const float is = has ? p.inv_s[bs + u] : 0.0f, it = has ? p.inv_t[bt + v] : 0.0f;

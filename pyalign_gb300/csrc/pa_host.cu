@@ -1269,7 +1269,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	if (in.form == F_INDEXED) {
 		host_table.resize(size_t(in.table_rows * in.table_cols));
 		if (in.location == PA_DEVICE) {
-			// through the solver's pinned block (a pageable destination makes the driver stage it)
+			// through the solver's pinned block (a pageable destination makes CUDA stage the copy)
 			const size_t nb = host_table.size() * 4;
 			PA_CUDA(s->h_out.ensure(nb + 16));
 			PA_CUDA(pa_copy(s, s->h_out.p, in.table, nb, cudaMemcpyDeviceToHost, st));
