@@ -66,3 +66,16 @@ def test_length_limits_and_options(libpath):
     assert s.batch_size == alg.DEFAULT_BATCH_SIZE
     d["batch"] = False
     assert alg.m16.create_solver(10, 10, alg.m16.create_options(d)).batch_size == 1
+
+
+def test_differentiable_forms_refuse_host_tensors(libpath):
+    """The autograd forms run on the GPU only: host tensors are refused with a ValueError
+    before any work (no CPU fallback)."""
+    torch = pytest.importorskip("torch")
+    import numpy as np
+    from pyalign_gb300 import autograd as ag
+    lengths = np.array([[4, 5]])
+    with pytest.raises(ValueError, match="CUDA"):
+        ag.alignment_score(torch.zeros(1, 4, 5), lengths, 1.0, 0.5, "global")
+    with pytest.raises(ValueError, match="CUDA"):
+        ag.dtw_series_score(torch.zeros(1, 4), torch.zeros(1, 5), lengths)
