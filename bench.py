@@ -209,49 +209,47 @@ class ClockSampler:
 
 # --------------------------------------------------------------------------- CPU baseline
 
-def cpu_baseline(a, b, ls, lt, table, seconds):
-    """The oracle (CPU restatement of the reference's solver) on a bounded sample, all host
-    threads.  Returns (GCUPS, threads, sample description)."""
+def oracle_solver(oalg, locality, detail, gap, cap_s, cap_t):
+    """An oracle solver (CPU restatement of the reference's solver) with the options the
+    native module would receive for this workload."""
+    import types
+    return oalg.m16.create_solver(cap_s, cap_t, oalg.m16.create_options({
+        "solver": oalg.Type.ALIGNMENT, "direction": oalg.Direction.MAXIMIZE, "batch": True, "batch_size": 1,
+        "return_dup": False, "locality": oalg.Locality.__members__[locality],
+        "codomain": types.SimpleNamespace(detail=oalg.Detail.__members__[detail], count=oalg.Count.ONE),
+        "gap_cost": gap}))
+
+
+def cpu_baseline(a, b, ls, lt, table, seconds, threads=None):
+    """The oracle (CPU restatement of the reference's solver) on a bounded prefix of the
+    workload: score + one alignment per pair, `threads` host threads (default: all).
+    Returns (GCUPS, threads, sample description, pairs, scores, maps) -- the scores and the
+    concatenated alignment maps of those pairs are the parity check of the GPU arm."""
     import oracle.algorithm as oalg
-    L = ctypes.CDLL(oalg.build())
-    L.pao_batch_alignments.restype = ctypes.c_int64
-    vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
-    L.pao_batch_alignments.argtypes = [vp, i32, vp, vp, vp, i64, vp, i64, vp, i32, i32, vp, vp, vp]
-    threads = os.cpu_count() or 1
-    opts = oalg._Options()
-    opts.type, opts.direction, opts.detail, opts.count, opts.locality = 0, 1, 1, 0, 0
-    opts.remove_dup, opts.gap_kind = 1, 1
-    opts.affine_u_s = opts.affine_u_t = 2.0   # Gotoh u = extend
-    opts.affine_v_s = opts.affine_v_t = 3.0   # Gotoh v = open - extend
-    opts.cap_s = opts.cap_t = 1000
+    threads = threads or os.cpu_count() or 1
+    solver = oracle_solver(oalg, "LOCAL", "ALIGNMENT", AffineGap(5.0, 2.0), a.shape[1], b.shape[1])
 
-    def run(idx):
-        n = len(idx)
-        sa = np.ascontiguousarray(a[idx])
-        sb = np.ascontiguousarray(b[idx])
-        sls = np.ascontiguousarray(ls[idx])
-        slt = np.ascontiguousarray(lt[idx])
-        sizes = np.minimum(sls, slt).astype(np.int64)
-        offs = np.zeros(n, np.int64)
-        offs[1:] = np.cumsum(sizes)[:-1]
-        maps = np.zeros(int(sizes.sum()) + 1, np.int32)
-        scores = np.zeros(n, np.float32)
+    def run(n):
         t0 = time.perf_counter()
-        cells = L.pao_batch_alignments(
-            ctypes.addressof(opts), n, sls.ctypes.data, slt.ctypes.data, sa.ctypes.data, sa.shape[1],
-            sb.ctypes.data, sb.shape[1], table.ctypes.data, 4, threads, scores.ctypes.data,
-            maps.ctypes.data, offs.ctypes.data)
-        return cells, time.perf_counter() - t0
+        sc, mp, _, cells = oalg.batch_alignments(solver, a[:n], b[:n], table, ls[:n], lt[:n], threads)
+        return cells, time.perf_counter() - t0, sc, mp
 
-    probe = np.arange(0, min(len(ls), threads * 2))
-    cells, dt = run(probe)
-    rate = cells / max(dt, 1e-6)
-    target = rate * seconds
+    cells, dt, _, _ = run(min(len(ls), threads * 2))
+    target = cells / max(dt, 1e-6) * seconds
     cum = np.cumsum(ls.astype(np.int64) * lt.astype(np.int64))
     n = int(np.searchsorted(cum, target)) + 1
     n = max(threads, min(n, len(ls)))
-    cells, dt = run(np.arange(n))
-    return cells / dt / 1e9, threads, f"first {n} pairs of the workload ({cells:.3e} cells, {dt:.1f} s)"
+    cells, dt, sc, mp = run(n)
+    return (cells / dt / 1e9, threads, f"first {n} pairs of the workload ({cells:.3e} cells, {dt:.1f} s)",
+            n, sc, mp)
+
+
+def parity_of(n, sc_ref, mp_ref, sc, mp):
+    """Bit-exact comparison of the first n pairs' scores and concatenated alignment maps."""
+    bad = int(np.count_nonzero(np.asarray(sc[:n]) != sc_ref[:n]))
+    maps_equal = mp_ref is None or np.array_equal(np.asarray(mp[:len(mp_ref)]), mp_ref)
+    return {"pairs": int(n), "score_mismatches": bad, "maps_equal": bool(maps_equal),
+            "mismatches": bad + (0 if maps_equal else 1)}
 
 
 # --------------------------------------------------------------------------- other workloads
@@ -269,6 +267,40 @@ def _time_device(torch, fn, steps=3, warmup=1):
     return e0.elapsed_time(e1) / 1000.0 / steps
 
 
+def make_global_linear_64(seed, pairs=4096):
+    """4096 pairs of 64 x 64 letters i.i.d. uniform over 20: global alignment, linear gap 1,
+    eq +1 / ne -1 (pyalign's binary form)."""
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, 20, size=(pairs, 64)).astype(np.uint32)
+    b = rng.integers(0, 20, size=(pairs, 64)).astype(np.uint32)
+    ln = np.full(pairs, 64, np.int32)
+    return a, b, ln, ln.copy()
+
+
+def make_semiglobal_long(seed, pairs=256, ls=5000, lt=10000):
+    """256 pairs of 5000 x 10000 residues of a 20-letter alphabet with per-batch letter
+    frequencies ~ Dirichlet(1) and a seeded symmetric integer substitution matrix (diagonal
+    U[4, 11], off-diagonal U[-4, 2]): semiglobal alignment, affine gap open 10 / extend 1."""
+    rng = np.random.default_rng(seed)
+    freq = rng.dirichlet(np.ones(20))
+    a = rng.choice(20, size=(pairs, ls), p=freq).astype(np.uint32)
+    b = rng.choice(20, size=(pairs, lt), p=freq).astype(np.uint32)
+    m = rng.integers(-4, 3, size=(20, 20))
+    m = np.triu(m, 1) + np.triu(m, 1).T
+    np.fill_diagonal(m, rng.integers(4, 12, size=20))
+    return a, b, np.full(pairs, ls, np.int32), np.full(pairs, lt, np.int32), m.astype(np.float32)
+
+
+class LinearGap:
+    """pyalign.gaps.LinearGapCost(g) as seen by the native module (gaps.py:120-160)."""
+
+    def __init__(self, g):
+        self.g = g
+
+    def to_special_case(self):
+        return {"linear": self.g}
+
+
 def other_configs(torch, alg, L, seed):
     """The other synthetic workloads of the solve, through pa_solve_batch / the native
     module with device-resident codes: (1) global linear gap 1, eq +1 / ne -1, 4096 pairs
@@ -279,7 +311,6 @@ def other_configs(torch, alg, L, seed):
     import types
     out = {}
     P = ctypes.POINTER
-    rng = np.random.default_rng(seed)
 
     def run_batch(opts, a, b, ls, lt, table=None, eq=None, ne=None, maps=True):
         B = a.shape[0]
@@ -312,7 +343,7 @@ def other_configs(torch, alg, L, seed):
         L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
         cells = float((ls.astype(np.int64) * lt).sum())
         return {"value": cells / t / 1e9, "unit": "GCUPS", "ms": t * 1000, "dp_ms": ms4[1], "traceback_ms": ms4[2],
-                "plan": solver.last_plan()}
+                "plan": solver.last_plan()}, sc.cpu().numpy(), mp.cpu().numpy()
 
     def opts(alg_, locality, detail, gap, batch, count="ONE"):
         return {"solver": alg_.Type.ALIGNMENT, "direction": alg_.Direction.MAXIMIZE, "batch": True,
@@ -320,34 +351,28 @@ def other_configs(torch, alg, L, seed):
                 "codomain": types.SimpleNamespace(detail=alg_.Detail.__members__[detail], count=alg_.Count.__members__[count]),
                 "gap_cost": gap}
 
-    class Lin:
-        def __init__(self, g):
-            self.g = g
+    import oracle.algorithm as oalg   # the checker of the sampled pairs' results
 
-        def to_special_case(self):
-            return {"linear": self.g}
-
-    # config 1
-    B1 = 4096
-    a1 = rng.integers(0, 20, size=(B1, 64)).astype(np.uint32)
-    b1 = rng.integers(0, 20, size=(B1, 64)).astype(np.uint32)
-    l1 = np.full(B1, 64, np.int32)
-    out["global_linear_64x64"] = dict(run_batch(opts(alg, "GLOBAL", "ALIGNMENT", Lin(1.0), B1), a1, b1, l1, l1,
-                                                eq=1.0, ne=-1.0),
-                                      workload="4096 pairs of 64 x 64, 20 letters, global linear gap 1, eq +1 / ne -1, score + one traceback")
-    # config 3
-    B3 = 256
-    freq = rng.dirichlet(np.ones(20))
-    a3 = rng.choice(20, size=(B3, 5000), p=freq).astype(np.uint32)
-    b3 = rng.choice(20, size=(B3, 10000), p=freq).astype(np.uint32)
-    m = rng.integers(-4, 3, size=(20, 20))
-    m = np.triu(m, 1) + np.triu(m, 1).T
-    np.fill_diagonal(m, rng.integers(4, 12, size=20))
-    t3 = m.astype(np.float32)
-    ls3 = np.full(B3, 5000, np.int32)
-    lt3 = np.full(B3, 10000, np.int32)
+    # config 1: every pair against the oracle (eq/ne as a 20 x 20 table of the indexed form)
+    a1, b1, l1, _ = make_global_linear_64(seed)
+    B1 = a1.shape[0]
+    r1, sc1, mp1 = run_batch(opts(alg, "GLOBAL", "ALIGNMENT", LinearGap(1.0), B1), a1, b1, l1, l1, eq=1.0, ne=-1.0)
+    eqne = np.where(np.eye(20, dtype=bool), 1.0, -1.0).astype(np.float32)
+    osol = oracle_solver(oalg, "GLOBAL", "ALIGNMENT", LinearGap(1.0), 64, 64)
+    osc, omp, _, _ = oalg.batch_alignments(osol, a1, b1, eqne, l1, l1)
+    out["global_linear_64x64"] = dict(
+        r1, parity=parity_of(B1, osc, omp, sc1, mp1),
+        workload="4096 pairs of 64 x 64, 20 letters, global linear gap 1, eq +1 / ne -1, score + one traceback")
+    # config 3: score only; the first pairs of the bag against the oracle's two-row score
+    a3, b3, ls3, lt3, t3 = make_semiglobal_long(seed + 1)
+    B3 = a3.shape[0]
+    r3, sc3, _ = run_batch(opts(alg, "SEMIGLOBAL", "SCORE", AffineGap(10.0, 1.0), B3), a3, b3, ls3, lt3, table=t3,
+                           maps=False)
+    n3 = 4
+    osol = oracle_solver(oalg, "SEMIGLOBAL", "SCORE", AffineGap(10.0, 1.0), 5000, 10000)
+    osc3, _ = oalg.batch_scores_lean(osol, a3[:n3], b3[:n3], t3, ls3[:n3], lt3[:n3])
     out["semiglobal_affine_5000x10000_score"] = dict(
-        run_batch(opts(alg, "SEMIGLOBAL", "SCORE", AffineGap(10.0, 1.0), B3), a3, b3, ls3, lt3, table=t3, maps=False),
+        r3, parity=parity_of(n3, osc3, None, sc3, None),
         workload="256 pairs of 5000 x 10000, 20 letters, semiglobal affine 10/1, score only")
     # all optimal alignments (first 20 of 2 pairs), through the native module's iterator
     mod = alg.m16
@@ -502,6 +527,28 @@ def fwd_bwd(torch, pairs, seed, steps=3):
                                 "(series form: |x-y| computed in the DP kernel)"}}
 
 
+def error_report(sc32, rep, scale, bound=1e-5):
+    """Error of the float32 scores against the FP64 replay of each pair's recovered path:
+    the largest error relative to |score|, how many pairs (and which fraction) exceed `bound`
+    relative to |score| and the range of |score| among them, and -- where the magnitude of
+    the summed terms is given (sum |S| over the aligned cells plus the gap costs) -- the
+    largest error relative to it and how many pairs exceed `bound` that way."""
+    err = (sc32.double() - rep).abs().cpu().numpy()
+    mag = rep.abs().cpu().numpy()
+    rel = err / np.maximum(mag, 1e-300)
+    over = rel > bound
+    out = {"pairs": int(len(rel)), "max_rel_score": float(rel.max()), "bound": bound,
+           "over_bound_rel_score": int(over.sum()), "over_bound_fraction": float(over.mean()),
+           "abs_score_of_those": [float(mag[over].min()), float(mag[over].max())] if over.any() else None,
+           "median_abs_score": float(np.median(mag))}
+    if scale is not None:
+        rt = err / scale.cpu().numpy()
+        out.update({"max_rel_terms": float(rt.max()), "over_bound_rel_terms": int((rt > bound).sum())})
+        if over.any():
+            out["score_over_terms_of_those_max"] = float((mag / scale.cpu().numpy())[over].max())
+    return out
+
+
 def precision_config(torch, pairs, seed, steps=3):
     """The precision form: global Gotoh (open 0.5, extend 0.1, maximize) on S = cos of
     per-token embeddings (d = 256, N(0, 1) then L2-normalised, lengths U[32, 512]) with the
@@ -549,8 +596,7 @@ def precision_config(torch, pairs, seed, steps=3):
     t_dp = ev[1].elapsed_time(ev[2]) / 1000 / steps
     t_all = ev[2].elapsed_time(ev[3]) / 1000 / steps
     sc32, rep, scale = ag.path_scores_f64(S, lengths, 0.5, 0.1, "global", "maximize", with_scale=True)
-    err_score = float(((sc32.double() - rep).abs() / rep.abs()).max())
-    err_scale = float(((sc32.double() - rep).abs() / scale).max())
+    gotoh_err = error_report(sc32, rep, scale)
 
     D, _, _ = product(-1.0, 1.0)
     ag._forward_paths(D, lengths, None, "global", "minimize", True)
@@ -563,7 +609,7 @@ def precision_config(torch, pairs, seed, steps=3):
     torch.cuda.synchronize()
     t_dtw = ev[4].elapsed_time(ev[5]) / 1000 / steps
     dsc, drep = ag.path_scores_f64(D, lengths, locality="global", direction="minimize", dtw=True)
-    derr = float(((dsc.double() - drep).abs() / drep.abs()).max())
+    dtw_err = error_report(dsc, drep, None)
     status = ag.tensor_core_status()
     tiles = float((((lt + 127) // 128) * ((ls + 127) // 128)).sum())
     return {
@@ -573,9 +619,9 @@ def precision_config(torch, pairs, seed, steps=3):
                     "tile_tflops": 2.0 * d * tiles * 128 * 128 / t_gemm / 1e12,
                     "out_gbs": 4.0 * cells / t_gemm / 1e9, "status": status},
         "dp_gcups": cells / t_dp / 1e9, "dp_ms": t_dp * 1e3, "total_ms": t_all * 1e3,
-        "error_vs_fp64_replay": {"max_rel_score": err_score, "max_rel_terms": err_scale},
+        "error_vs_fp64_replay": gotoh_err,
         "dtw": {"value": cells / t_dtw / 1e9, "unit": "GCUPS", "ms": t_dtw * 1e3,
-                "error_vs_fp64_replay": {"max_rel_score": derr},
+                "error_vs_fp64_replay": dtw_err,
                 "workload": "DTW (minimize) on 1 - cos of the same pairs, distance from the product's epilogue"},
     }
 
@@ -592,7 +638,7 @@ def run_reference(args):
     desc = None
     threads = os.cpu_count() or 1
     for k in range(args.warmup + args.steps):
-        g, threads, desc = cpu_baseline(a, b, ls, lt, table, per_step if k >= args.warmup else 1.0)
+        g, threads, desc, _, _, _ = cpu_baseline(a, b, ls, lt, table, per_step if k >= args.warmup else 1.0)
         if k >= args.warmup:
             vals.append(g)
     value = statistics.median(vals)
@@ -823,20 +869,29 @@ def run_ours(args):
     prec = precision_config(torch, args.precision_pairs, args.seed + 2) if args.precision_pairs > 0 else None
     prepd = prepare_config(torch, a, b, ls, lt) if args.prepare else None
 
-    cpu = None
+    # CPU baseline on all host threads and on one core; the oracle's scores and alignment
+    # maps of the sampled pairs are compared bit for bit with the GPU arm's (exit 1 on any
+    # difference, after the line is printed)
+    cpu, parity = None, None
     if not args.no_cpu_baseline and world == 1:
-        g, threads, desc = cpu_baseline(a, b, ls, lt, table, args.cpu_seconds)
-        cpu = {"value": g, "unit": "GCUPS", "cores": threads, "kind": "port", "sample": desc}
+        g, threads, desc, n_par, sc_ref, mp_ref = cpu_baseline(a, b, ls, lt, table, args.cpu_seconds)
+        g1, _, desc1, _, _, _ = cpu_baseline(a, b, ls, lt, table, args.cpu_seconds / 2, threads=1)
+        cpu = {"value": g, "unit": "GCUPS", "cores": threads, "kind": "port", "sample": desc,
+               "one_core": {"value": g1, "unit": "GCUPS", "cores": 1, "sample": desc1}}
+        parity = dict(parity_of(n_par, sc_ref, mp_ref, sc_h.numpy(), mp_h.numpy()),
+                      against="oracle (CPU restatement of the reference's solver)",
+                      arm="e2e (host buffers); the device-resident run's scores equal it")
 
     if plain is not None:
         plain["batched_over_plain"] = value / plain["value"]
     line = {
         "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed * 1000.0 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "int16x2" if packed else "int32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "pairs": B, "cells_per_step": cells, "form": "indexed (a, b uint32 codes)",
                    "l2": "inputs larger than L2: 524 MB of codes and ~14 GB of traceback masks per step",
                    "parallelism": f"dp{world} (independent pairs per GPU)"},
+        "parity": parity,
         "roofline": roof_alu,
         "roofline_hbm": roof_hbm,
         "cpu_baseline": cpu,
@@ -856,6 +911,11 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+    bad = [k for k, v in (("bench", parity), *((k, v.get("parity")) for k, v in (others or {}).items()))
+           if v is not None and v["mismatches"]]
+    if bad:
+        print(f"parity failure against the oracle: {bad}", file=sys.stderr)
+        sys.exit(1)
 
 
 def main():

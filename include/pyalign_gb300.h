@@ -413,7 +413,10 @@ pa_status pa_measure_int16x2_peak(float *gops, float *ms);
  * capacity n_s x n_t).  Inputs a (batch x n_s), b (batch x n_t), table, len_s, len_t
  * (batch int32 each) and the output scores (batch float32) are device memory of the
  * caller; the work runs on `stream` (a cudaStream_t, NULL = default stream) and is
- * complete when the stream is.
+ * complete when the stream is.  The call blocks the calling thread until `stream` has run
+ * the check that every code indexes the table (it synchronises `stream` once, after the
+ * two index-range kernels, and then queues the DP without waiting for it), so an out-of-
+ * range code is reported by the call itself (PA_ERR_INVALID_ARGUMENT).
  * All scratch lives in one static device array of PA_NOALLOC_SCRATCH_BYTES per device
  * (held until the process exits): batch <= PA_NOALLOC_MAX_BATCH, n_s, n_t <=
  * PA_NOALLOC_MAX_LEN and a table of at most 64 x 64; larger sizes are rejected with

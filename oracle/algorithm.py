@@ -546,3 +546,87 @@ class _IndexModule:
 
 m16 = _IndexModule(16)
 m32 = _IndexModule(32)
+
+
+# --- threaded batch helpers of the checker (indexed form) ---
+
+def _batch_args(a, b, ls, lt, table):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    b = np.ascontiguousarray(b, dtype=np.uint32)
+    ls = np.ascontiguousarray(ls, dtype=np.int32)
+    lt = np.ascontiguousarray(lt, dtype=np.int32)
+    table = np.ascontiguousarray(table, dtype=np.float32)
+    return a, b, ls, lt, table
+
+
+def batch_alignments(solver, a, b, table, ls, lt, threads=None):
+    """Score and one alignment map per pair of the indexed form on `threads` host threads,
+    each pair as one lane of Solver::alignment (solver.h:2610-2630), with the options of an
+    oracle `solver`.  Returns (scores f32[n], maps i32 concatenated at offsets, offsets
+    i64[n + 1] = prefix sums of min(|s|, |t|), cells)."""
+    lib = _load()
+    a, b, ls, lt, table = _batch_args(a, b, ls, lt, table)
+    n = len(ls)
+    sizes = np.minimum(ls, lt).astype(np.int64)
+    offs = np.zeros(n + 1, np.int64)
+    offs[1:] = np.cumsum(sizes)
+    maps = np.zeros(int(offs[-1]) + 1, np.int32)
+    scores = np.zeros(n, np.float32)
+    vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+    lib.pao_batch_alignments.restype = i64
+    lib.pao_batch_alignments.argtypes = [vp, i32, vp, vp, vp, i64, vp, i64, vp, i32, i32, vp, vp, vp]
+    cells = lib.pao_batch_alignments(
+        ctypes.addressof(solver._copts), n, ls.ctypes.data, lt.ctypes.data, a.ctypes.data, a.shape[1],
+        b.ctypes.data, b.shape[1], table.ctypes.data, table.shape[1], int(threads or os.cpu_count() or 1),
+        scores.ctypes.data, maps.ctypes.data, offs.ctypes.data)
+    return scores, maps[:int(offs[-1])], offs, int(cells)
+
+
+def batch_scores_lean(solver, a, b, table, ls, lt, threads=None):
+    """Scores of the indexed form with two rows per layer (memory O(|t|) per pair, for pairs
+    of 5000 x 10000 cells), linear or affine gaps, with the options of an oracle `solver`.
+    Returns (scores f32[n], cells)."""
+    lib = _load()
+    a, b, ls, lt, table = _batch_args(a, b, ls, lt, table)
+    n = len(ls)
+    scores = np.zeros(n, np.float32)
+    vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+    lib.pao_batch_scores_lean.restype = i64
+    lib.pao_batch_scores_lean.argtypes = [vp, i32, vp, vp, vp, i64, vp, i64, vp, i32, i32, vp]
+    cells = lib.pao_batch_scores_lean(
+        ctypes.addressof(solver._copts), n, ls.ctypes.data, lt.ctypes.data, a.ctypes.data, a.shape[1],
+        b.ctypes.data, b.shape[1], table.ctypes.data, table.shape[1], int(threads or os.cpu_count() or 1),
+        scores.ctypes.data)
+    return scores, int(cells)
+
+
+def batch_f64(S, ls, lt, *, dtw=False, locality="global", direction="maximize", open_=0.5, extend=0.1,
+              threads=None):
+    """The FP64 twin on a batch of float32 matrices S (B, n, m) (converted to double): global
+    (or `locality`) affine Gotoh with open/extend, or DTW.  Returns (scores f64[B], scales
+    f64[B]) where scale = sum |S| over the cells the optimal path adds + the path's gap cost."""
+    lib = _load()
+    S = np.ascontiguousarray(S, dtype=np.float32)
+    ls = np.ascontiguousarray(ls, dtype=np.int32)
+    lt = np.ascontiguousarray(lt, dtype=np.int32)
+    B = len(ls)
+    o = _Options()
+    o.type = int(Type.DTW if dtw else Type.ALIGNMENT)
+    o.direction = int(Direction.__members__[direction.upper()])
+    o.detail, o.count, o.remove_dup = 1, 0, 1
+    o.locality = int(Locality.__members__[locality.upper()])
+    o.gap_kind = 0 if dtw else 1
+    o.cap_s, o.cap_t = int(ls.max(initial=0)), int(lt.max(initial=0))
+    gaps = np.zeros(6, np.float64)
+    if not dtw:
+        gaps[2] = gaps[4] = extend
+        gaps[3] = gaps[5] = open_ - extend
+    scores = np.zeros(B, np.float64)
+    scales = np.zeros(B, np.float64)
+    vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+    lib.pao_batch_f64.restype = None
+    lib.pao_batch_f64.argtypes = [vp, vp, i32, vp, vp, vp, i64, i64, i32, vp, vp]
+    lib.pao_batch_f64(ctypes.addressof(o), gaps.ctypes.data, B, ls.ctypes.data, lt.ctypes.data, S.ctypes.data,
+                      S.shape[1] * S.shape[2], S.shape[2], int(threads or os.cpu_count() or 1),
+                      scores.ctypes.data, scales.ctypes.data)
+    return scores, scales

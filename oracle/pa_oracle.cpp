@@ -668,3 +668,177 @@ int32_t pao_solve_f64(const pao_options *o, const double *gaps, const double *ge
 }
 
 }  // extern "C"
+
+namespace {
+
+// Score only, two rows per layer: the recurrences of LinearGapCostSolver::solve
+// (solver.h:2825-2855) and AffineGapCostSolver::solve (solver.h:2970-3036) with the same
+// float operations in the same order as Problem::solve above, the borders of build_layers
+// (solver.h:2806-2814, 2918-2967), and the score of Solver::score (solver.h:2593-2608): the
+// value at the seed -- global (ls-1, lt-1) (solver.h:2174-2188), semiglobal the optimum of
+// the last row then the last column (solver.h:2266-2294), local the optimum over every cell
+// (solver.h:2035-2056; only the value matters for a score, not which tied cell holds it).
+// Memory is O(lt), so pairs of 5000 x 10000 cells fit; pairs with an empty side go through
+// the full solver.
+float score_lean(const pao_options &o, int32_t ls, int32_t lt, const uint32_t *a, const uint32_t *b,
+                 const float *table, int32_t A) {
+	typedef float T;
+	const Dir<T> dir{o.direction == DIR_MAX};
+	const T sgn = dir.sgn();
+	const T worst = dir.worst();
+	const bool local = o.locality == LOC_LOCAL, global = o.locality == LOC_GLOBAL;
+	const bool affine = o.gap_kind == GAP_AFFINE;
+	std::vector<T> ws, wt;
+	if (affine) {
+		ws = affine_vector<T>(o.affine_u_s, o.affine_v_s, size_t(o.cap_s) + 1);
+		wt = affine_vector<T>(o.affine_u_t, o.affine_v_t, size_t(o.cap_t) + 1);
+	}
+	const T w1s = T(o.affine_u_s) + T(o.affine_v_s), w1t = T(o.affine_u_t) + T(o.affine_v_t);
+	// row u - 1 and row u of D and P, index j + 1 (column -1 at index 0)
+	std::vector<T> Dp(size_t(lt) + 1), Dc(size_t(lt) + 1), Pp(size_t(lt) + 1), Pc(size_t(lt) + 1);
+	for (int32_t j = -1; j < lt; j++) {
+		T x;
+		if (affine) x = global ? wt[size_t(j + 1)] * sgn : T(0);
+		else x = global ? (T(j + 1) * o.linear_t) * sgn : T(0);
+		Dp[size_t(j + 1)] = x;
+		Pp[size_t(j + 1)] = worst;  // P(-1, j)
+	}
+	T best = worst;  // local: optimum over all cells; semiglobal: over the last column
+	std::vector<T> last_row;
+	for (int32_t u = 0; u < ls; u++) {
+		T left;
+		if (affine) left = global ? ws[size_t(u + 1)] * sgn : T(0);
+		else left = global ? (T(u + 1) * o.linear_s) * sgn : T(0);
+		Dc[0] = left;
+		Pc[0] = left;     // P(u, -1) = D(u, -1)
+		T Q = worst;      // Q(u, -1)
+		const float *trow = table + size_t(a[u]) * size_t(A);
+		for (int32_t v = 0; v < lt; v++) {
+			const T s = trow[b[v]];
+			T d;
+			if (affine) {
+				T P = Dp[size_t(v + 1)] + w1s * sgn;
+				P = dir.opt(Pp[size_t(v + 1)] + T(o.affine_u_s) * sgn, P);
+				T Qn = Dc[size_t(v)] + w1t * sgn;
+				Qn = dir.opt(Q + T(o.affine_u_t) * sgn, Qn);
+				Q = Qn;
+				Pc[size_t(v + 1)] = P;
+				const T dg = Dp[size_t(v)] + s;
+				d = local ? dir.opt(dg, T(0)) : dg;
+				d = dir.opt(P, d);
+				d = dir.opt(Q, d);
+			} else {
+				const T dg = Dp[size_t(v)] + s;
+				d = local ? dir.opt(dg, T(0)) : dg;
+				d = dir.opt(Dp[size_t(v + 1)] + T(o.linear_s) * sgn, d);
+				d = dir.opt(Dc[size_t(v)] + T(o.linear_t) * sgn, d);
+			}
+			Dc[size_t(v + 1)] = d;
+			if (local) best = dir.opt(d, best);
+		}
+		if (o.locality == LOC_SEMIGLOBAL) best = dir.opt(Dc[size_t(lt)], best);
+		std::swap(Dp, Dc);
+		std::swap(Pp, Pc);
+	}
+	// Dp now holds row ls - 1
+	if (global) return Dp[size_t(lt)];
+	if (o.locality == LOC_SEMIGLOBAL) {
+		// last row first (j ascending), then the last column: the optimum's value is the same
+		// whichever cell of a tie the scan keeps
+		T r = worst;
+		for (int32_t j = 0; j < lt; j++) r = dir.opt(Dp[size_t(j + 1)], r);
+		return dir.opt(best, r);
+	}
+	return best;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Scores of `npairs` problems of the indexed form on `nthreads` threads with the memory-lean
+// score_lean above (linear or affine gaps, any locality, either direction, alignment type).
+// Pairs with an empty side are solved by the full solver.  Returns the cell count.
+int64_t pao_batch_scores_lean(const pao_options *o, int32_t npairs, const int32_t *ls, const int32_t *lt,
+                              const uint32_t *a, int64_t a_stride, const uint32_t *b, int64_t b_stride,
+                              const float *table, int32_t A, int32_t nthreads, float *scores) {
+	std::atomic<int32_t> next{0};
+	auto work = [&]() {
+		for (;;) {
+			const int32_t k = next.fetch_add(1);
+			if (k >= npairs) break;
+			const uint32_t *ak = a + int64_t(k) * a_stride, *bk = b + int64_t(k) * b_stride;
+			if (ls[k] > 0 && lt[k] > 0 && o->gap_kind != GAP_GENERAL && o->type == TYPE_ALIGNMENT) {
+				scores[k] = score_lean(*o, ls[k], lt[k], ak, bk, table, A);
+				continue;
+			}
+			std::vector<float> sim(static_cast<size_t>(ls[k]) * static_cast<size_t>(lt[k]));
+			for (int32_t i = 0; i < ls[k]; i++)
+				for (int32_t j = 0; j < lt[k]; j++) sim[size_t(i) * size_t(lt[k]) + size_t(j)] = table[size_t(ak[i]) * size_t(A) + bk[j]];
+			pao_result *r = pao_solve(o, ls[k], lt[k], sim.data());
+			float sc = 0;
+			if (!pao_next(r, &sc, nullptr, nullptr, nullptr)) sc = pao_worst(r);
+			scores[k] = sc;
+			pao_free(r);
+		}
+	};
+	std::vector<std::thread> th;
+	for (int32_t t = 0; t < std::max(1, nthreads); t++) th.emplace_back(work);
+	for (auto &t : th) t.join();
+	int64_t cells = 0;
+	for (int32_t k = 0; k < npairs; k++) cells += int64_t(ls[k]) * lt[k];
+	return cells;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// FP64 twin on a batch of float32 similarity (or distance) matrices, `nthreads` host
+// threads: pair k reads S + k * pair_stride, row i at + i * row_stride, converted to double.
+// Writes the FP64 score of each pair and the magnitude of the terms it sums along its
+// optimal path -- sum |S| over the cells the score adds (aligned cells; every visited cell
+// for DTW) plus |score - sum S| (the gap costs) -- the denominator for scores near zero.
+void pao_batch_f64(const pao_options *o, const double *gaps, int32_t npairs, const int32_t *ls, const int32_t *lt,
+                   const float *S, int64_t pair_stride, int64_t row_stride, int32_t nthreads, double *scores,
+                   double *scales) {
+	std::atomic<int32_t> next{0};
+	auto work = [&]() {
+		std::vector<double> sim;
+		std::vector<int32_t> path;
+		for (;;) {
+			const int32_t k = next.fetch_add(1);
+			if (k >= npairs) break;
+			const int32_t n_s = ls[k], n_t = lt[k];
+			sim.resize(size_t(n_s) * size_t(n_t));
+			const float *Sk = S + int64_t(k) * pair_stride;
+			for (int32_t i = 0; i < n_s; i++)
+				for (int32_t j = 0; j < n_t; j++) sim[size_t(i) * size_t(n_t) + size_t(j)] = double(Sk[int64_t(i) * row_stride + j]);
+			path.assign(2 * (size_t(n_s) + size_t(n_t) + 4), 0);
+			double sc = 0;
+			int32_t np = 0;
+			if (!pao_solve_f64(o, gaps, nullptr, nullptr, n_s, n_t, sim.data(), &sc, path.data(), &np)) {
+				scores[k] = std::nan("");
+				scales[k] = std::nan("");
+				continue;
+			}
+			double tot = 0, mag = 0;
+			for (int32_t q = 0; q + 1 < np; q++) {
+				const int32_t u0 = path[2 * q], v0 = path[2 * q + 1], u1 = path[2 * q + 2], v1 = path[2 * q + 3];
+				if (u0 < 0 || v0 < 0) break;
+				if (o->type == TYPE_DTW || (u1 == u0 - 1 && v1 == v0 - 1)) {
+					const double x = sim[size_t(u0) * size_t(n_t) + size_t(v0)];
+					tot += x;
+					mag += std::fabs(x);
+				}
+			}
+			scores[k] = sc;
+			scales[k] = mag + std::fabs(tot - sc);
+		}
+	};
+	std::vector<std::thread> th;
+	for (int32_t t = 0; t < std::max(1, nthreads); t++) th.emplace_back(work);
+	for (auto &t : th) t.join();
+}
+
+}  // extern "C"

@@ -12,7 +12,10 @@
 // error text (read with pa_last_error) in host memory.
 //
 // The array is shared by every call on a device and keeps the last call's contents; the
-// parts that must start at zero (the work counter) are cleared by each call.  Calls whose
+// parts that must start at zero (the work counter, the kernel's status word, the code
+// maxima) are cleared by each call.  Each call waits on `stream` for the check that every
+// code indexes the table (the host reads the maxima back), so the call returns only after
+// the work queued on `stream` before it has finished; the DP itself is left running.  Calls whose
 // GPU work overlaps (two streams, or two threads on one stream without ordering) race on
 // the array and give wrong results.  The first call on a device looks up the array's device
 // address with cudaGetSymbolAddress, once per device, with that device current; make that
@@ -52,6 +55,7 @@ struct Prep {
 	float *left_D, *top_D;
 	int32_t *order;
 	int32_t *counter;
+	int32_t *status;     // the DP kernel's status word (progress timeouts, bad codes)
 	const int32_t *len_s_in, *len_t_in;  // caller's lengths
 	int32_t *len_s, *len_t;              // clamped to [0, n_s] x [0, n_t]
 	int32_t global;      // 1: global borders -w(k), else 0
@@ -72,7 +76,10 @@ __device__ float affine_w(float u, float v, int64_t n, int64_t k) {
 __global__ void noalloc_prep_kernel(Prep p) {
 	const int64_t stride = int64_t(gridDim.x) * blockDim.x;
 	const int64_t t0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (t0 == 0) *p.counter = 0;
+	if (t0 == 0) {
+		*p.counter = 0;
+		*p.status = 0;
+	}
 	for (int64_t k = t0; k < p.batch; k += stride) {
 		p.order[k] = int32_t(k);
 		p.len_s[k] = int32_t(min(max(int64_t(p.len_s_in[k]), int64_t(0)), p.n_s));
@@ -160,6 +167,7 @@ extern "C" pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, con
 		return x;
 	};
 	int32_t *counter = reinterpret_cast<int32_t *>(take(8));
+	int32_t *status = reinterpret_cast<int32_t *>(take(8));
 	uint32_t *codes_max = reinterpret_cast<uint32_t *>(take(8));
 	int32_t *order = reinterpret_cast<int32_t *>(take(size_t(batch) * 4));
 	int32_t *seeds = reinterpret_cast<int32_t *>(take(size_t(batch) * 8));
@@ -174,7 +182,10 @@ extern "C" pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, con
 	const int G = 32;
 	const int64_t slots_fit = int64_t((SCRATCH_BYTES - used) / row_bytes);
 	int sms = 0;
-	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+		cudaGetLastError();
+		return reject(PA_ERR_CUDA, "pa_solve_indexed_for_score_noalloc: cannot read the SM count of the device");
+	}
 	int64_t blocks = std::min<int64_t>(int64_t(sms) * 4, slots_fit / WARPS);
 	blocks = std::min<int64_t>(blocks, (batch + WARPS - 1) / WARPS);
 	if (blocks < 1) return reject(PA_ERR_LENGTH, "pa_solve_indexed_for_score_noalloc: scratch too small for this length");
@@ -207,6 +218,7 @@ extern "C" pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, con
 	pr.top_D = top_D;
 	pr.order = order;
 	pr.counter = counter;
+	pr.status = status;
 	pr.len_s_in = len_s;
 	pr.len_t_in = len_t;
 	pr.len_s = cls;
@@ -263,7 +275,7 @@ extern "C" pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, con
 	p.scratch = rows;
 	p.scratch_stride = 2 * std::max<int64_t>(n_t, 1);
 	p.work_counter = counter;
-	p.status = reinterpret_cast<int32_t *>(codes_max);
+	p.status = status;
 	const int loc = o->locality == PA_LOCAL ? LOC_LOCAL : o->locality == PA_GLOBAL ? LOC_GLOBAL : LOC_SEMI;
 	const size_t smem = size_t(table_rows * table_cols) * sizeof(float);
 	cudaError_t e = o->gap_kind == PA_GAP_LINEAR ? launch_dp_f_linear(loc, TB_NONE, false, p, int(blocks), smem, st)

@@ -2,7 +2,9 @@
 
 Run in the build container (where the reference checkout exists):
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <path of the pyalign checkout>
+
+(or with PYALIGN_REFERENCE set to that path)
 
 What it does:
 1. Imports the reference's *Python* package (pyalign 0.4.4) from the checkout, with two
@@ -163,7 +165,9 @@ class Recorder:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("PYALIGN_REFERENCE"),
+                    required=not os.environ.get("PYALIGN_REFERENCE"),
+                    help="root of the pyalign 0.4.4 checkout (default: $PYALIGN_REFERENCE)")
     ap.add_argument("--out", default=os.path.join(HERE, "reference_tests.json"))
     args = ap.parse_args()
 

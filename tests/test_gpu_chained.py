@@ -161,3 +161,23 @@ def test_autotuned_plan_matches_analytic_plan(gpu_alg, monkeypatch):
         res = solver.solve_indexed_for_alignment(a, b, table, ln)
         out[tune] = [(r.score, r.s_to_t.tolist()) for r in res]
     assert out["0"] == out["1"]
+
+
+def test_chained_matches_oracle_at_bench_size(gpu_alg, oracle_alg):
+    """The long-pair workload at its full size: 256 pairs of 5000 x 10000 residues, 20
+    letters with Dirichlet(1) frequencies, a seeded symmetric integer matrix, semiglobal
+    affine 10/1, score only -- the solver's own plan (stripe-chained) over the whole bag, and
+    the first pairs' scores against the oracle's two-row score (same float32 operations),
+    bit for bit."""
+    import bench
+    a, b, ls, lt, table = bench.make_semiglobal_long(2024)
+    n = a.shape[0]
+    opts = dict(options(gpu_alg, locality="semiglobal", detail="score", gap=Gap("affine", 10.0, 1.0)),
+                batch_size=n, batch=True)
+    solver = gpu_alg.m16.create_solver(a.shape[1], b.shape[1], gpu_alg.m16.create_options(opts))
+    g = np.asarray(solver.solve_indexed_for_score(a, b, table, np.stack([ls, lt]).astype(np.uint16)))
+    assert solver.last_plan()["kernel"] == "stripe-chained", solver.last_plan()
+    k = 6
+    osol = oracle_alg.m16.create_solver(a.shape[1], b.shape[1], oracle_alg.m16.create_options(opts))
+    r, _ = oracle_alg.batch_scores_lean(osol, a[:k], b[:k], table, ls[:k], lt[:k])
+    assert np.array_equal(g[:k], r), (g[:k], r)

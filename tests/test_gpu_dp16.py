@@ -185,3 +185,25 @@ def test_dp16_bad_codes_then_valid(analytic, gpu_alg, oracle_alg):
     _, r = call(oracle_alg, opts, (a.shape[1], b.shape[1]), "alignment", "indexed", a, b, ln, table=table)
     d = compare("alignment", g, r, n)
     assert d is None, d
+
+
+def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg):
+    """4,096 pairs drawn like the batched workload (DNA, |s|, |t| ~ U[100, 1000], half of them
+    a query and a 10%-mutated copy; local affine 5/2, +2/-3; score + one traceback) through
+    the solver's own plan -- the 16-bit twin kernel -- against the oracle, every score and
+    every alignment map bit for bit."""
+    import bench
+    a, b, ls, lt, table = bench.make_workload(4096, 4242)
+    n = a.shape[0]
+    opts = dict(options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"]), batch_size=n, batch=True)
+    solver = gpu_alg.m16.create_solver(a.shape[1], b.shape[1], gpu_alg.m16.create_options(opts))
+    res = solver.solve_indexed_for_alignment(a, b, table, np.stack([ls, lt]).astype(np.uint16))
+    assert solver.last_plan()["kernel"].startswith("16-bit"), solver.last_plan()
+    osol = oracle_alg.m16.create_solver(a.shape[1], b.shape[1], oracle_alg.m16.create_options(opts))
+    osc, omp, offs, _ = oracle_alg.batch_alignments(osol, a, b, table, ls, lt)
+    bad = []
+    for k in range(n):
+        m = res[k].s_to_t if ls[k] <= lt[k] else res[k].t_to_s
+        if res[k].score != osc[k] or not np.array_equal(np.asarray(m), omp[offs[k]:offs[k + 1]]):
+            bad.append(k)
+    assert not bad, (len(bad), bad[:10])

@@ -141,3 +141,46 @@ def test_embedding_alignment_error_vs_fp64_oracle(env):
         assert max(e_gemm) <= 1e-5, (name, max(e_gemm))
         assert same >= B - 2, (name, same)   # optimal paths coincide but for near-ties
     print("relative score error (max over pairs):", report)
+
+
+def test_precision_report_at_size(env):
+    """1,024 pairs of the precision workload (L ~ U[32, 512], d = 256, cos on the tensor
+    cores, global Gotoh 0.5/0.1 and DTW on 1 - cos): the float32 DP against the FP64 oracle
+    DP on the same S, for every pair.  Bound: the error relative to the magnitude of the
+    terms the score sums is <= 1e-5 for every pair.  Relative to |score| the pairs above 1e-5
+    are reported with their |score| and summed-terms magnitude: global scores of random
+    embeddings can nearly cancel, and there the float32 rounding of the terms, not of the
+    score, sets the error.  DTW scores are sums of positive distances: bounded by 1e-5 of
+    |score| for every pair."""
+    torch, ag, oalg, _ = env
+    rng = np.random.default_rng(1044)
+    B, n, d = 1024, 512, 256
+    lengths = rng.integers(32, n + 1, size=(B, 2))
+    g = torch.Generator(device="cuda").manual_seed(1044)
+    Es = torch.randn(B, n, d, device="cuda", generator=g)
+    Et = torch.randn(B, n, d, device="cuda", generator=g)
+    S = ag.cosine_similarity_batch(Es, Et, lengths)
+    assert ag.tensor_core_status() == 0
+    sc32, rep64 = ag.path_scores_f64(S, lengths, OPEN, EXT, "global", "maximize")
+    Sh = S.cpu().numpy()
+    o64, scale = oalg.batch_f64(Sh, lengths[:, 0], lengths[:, 1], open_=OPEN, extend=EXT)
+    sc = sc32.double().cpu().numpy()
+    err = np.abs(sc - o64)
+    rel_s = err / np.abs(o64)
+    rel_t = err / scale
+    over = rel_s > 1e-5
+    print(f"gotoh: max rel |score| {rel_s.max():.3e}, over 1e-5: {int(over.sum())}/{B}, "
+          f"max rel terms {rel_t.max():.3e}")
+    assert rel_t.max() <= 1e-5, rel_t.max()
+    print("  (|score|, summed terms) of those:", list(zip(np.abs(o64[over]).round(4), scale[over].round(2))))
+    rep = np.abs(sc - rep64.cpu().numpy()) / scale
+    assert rep.max() <= 1e-5, rep.max()
+
+    Esb, _ = ag.normalized_bf16(Es)
+    Etb, _ = ag.normalized_bf16(Et)
+    D = ag.similarity_bf16(Esb, Etb, lengths, out=torch.ones((B, n, n), device="cuda"), alpha=-1.0, beta=1.0)
+    dsc, _ = ag.path_scores_f64(D, lengths, locality="global", direction="minimize", dtw=True)
+    d64, _ = oalg.batch_f64(D.cpu().numpy(), lengths[:, 0], lengths[:, 1], dtw=True, direction="minimize")
+    drel = np.abs(dsc.double().cpu().numpy() - d64) / np.abs(d64)
+    print(f"dtw: max rel |score| {drel.max():.3e}")
+    assert drel.max() <= 1e-5, drel.max()

@@ -107,6 +107,28 @@ def test_noalloc_matches_regular_entry_two_calls(env):
     assert np.array_equal(want3, got3)
 
 
+def test_noalloc_global_affine_fractional_costs(env, oracle_alg):
+    """Global affine borders with fractional costs (open 2.7, extend 0.3) and a capacity with
+    n_s != n_t: the border vector the entry point builds on the device must equal the
+    regular entry's and the oracle's, bit for bit, on two calls in a row."""
+    rng = np.random.default_rng(2025)
+    ftab = rng.normal(size=(5, 5)).astype(np.float32)
+    for k, direction in enumerate(("maximize", "minimize")):
+        hi = 300 + 200 * k
+        pairs = random_pairs(rng, 90 + 40 * k, 0, hi, alphabet=5, related=0.5)
+        pairs.append((rng.integers(0, 5, size=7).astype(np.uint32), rng.integers(0, 5, size=hi + 41).astype(np.uint32)))
+        gap = Gap("affine", 2.7, 0.3)
+        want, got = _both(env, pairs, ftab, "global", direction, gap)
+        assert np.array_equal(want, got), np.nonzero(want != got)[0][:10]
+        n = len(pairs)
+        a, b, ln = pack(pairs, n)
+        assert a.shape[1] != b.shape[1]
+        osol = oracle_alg.m16.create_solver(a.shape[1], b.shape[1], oracle_alg.m16.create_options(
+            _options_dict(oracle_alg, "global", direction, gap, n)))
+        ref = np.asarray(osol.solve_indexed_for_score(a, b, ftab, ln))
+        assert np.array_equal(ref, got), np.nonzero(ref != got)[0][:10]
+
+
 def test_noalloc_rejects_sizes_beyond_maximum(env):
     torch, alg, L = env
     o = _c_options(alg, "local", "maximize", Gap("linear", 1.0))
