@@ -53,8 +53,8 @@ def parse():
     ap.add_argument("--other-configs", type=int, default=1, help="also measure the other workloads (0: skip)")
     ap.add_argument("--precision-pairs", type=int, default=8192, help="pairs of the precision measurement (0: skip)")
     ap.add_argument("--prepare", type=int, default=1, help="also time problem preparation from strings (0: skip)")
-    ap.add_argument("--plain-pairs", type=int, default=2048,
-                    help="pairs timed on the plain path (one launch per 4-pair batch)")
+    ap.add_argument("--plain", type=int, default=1,
+                    help="also time the plain GPU path: one launch per 100-wide length bucket (0: skip)")
     return ap.parse_args()
 
 
@@ -374,22 +374,40 @@ def other_configs(torch, alg, L, seed):
     out["semiglobal_affine_5000x10000_score"] = dict(
         r3, parity=parity_of(n3, osc3, None, sc3, None),
         workload="256 pairs of 5000 x 10000, 20 letters, semiglobal affine 10/1, score only")
-    # all optimal alignments (first 20 of 2 pairs), through the native module's iterator
+    # all-optimal codomain on the whole bag through the native module's iterator form:
+    # one solve writes the 16-bit all-optimal masks of all 256 pairs (25.6 GB, left on the
+    # device), the co-optimal path counts of every pair are computed on the device, and the
+    # host enumerates the first 20 alignments of two pairs in the reference's order
     mod = alg.m16
-    solver = mod.create_solver(5000, 10000, mod.create_options(
-        opts(alg, "SEMIGLOBAL", "ALIGNMENT", AffineGap(10.0, 1.0), 2, count="ALL")))
+    o3 = opts(alg, "SEMIGLOBAL", "ALIGNMENT", AffineGap(10.0, 1.0), B3, count="ALL")
+    solver = mod.create_solver(5000, 10000, mod.create_options(o3))
+    ln3 = np.stack([ls3, lt3]).astype(np.uint16)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = solver.solve_indexed_for_alignment_iterator(a3[:2], b3[:2], t3, np.stack([ls3[:2], lt3[:2]]).astype(np.uint16))
+    res = solver.solve_indexed_for_alignment_iterator(a3, b3, t3, ln3)
+    t_solve = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    counts = alg.path_counts(res[0]._res)
+    t_count = time.perf_counter() - t0
+    t0 = time.perf_counter()
     n_items = 0
-    for it in res:
+    for it in res[:2]:
         for _ in range(20):
             if it.next() is None:
                 break
             n_items += 1
-    dt = time.perf_counter() - t0
+    t_enum = time.perf_counter() - t0
+    del res
+    cells3 = float((ls3.astype(np.int64) * lt3).sum())
     out["semiglobal_affine_5000x10000_all_optimal"] = {
-        "value": 2 * 5000 * 10000 / dt / 1e9, "unit": "GCUPS", "ms": dt * 1000, "alignments": n_items,
-        "workload": "2 pairs of 5000 x 10000, all-optimal masks on the GPU, first 20 alignments each (host DFS)"}
+        "value": cells3 / t_solve / 1e9, "unit": "GCUPS", "ms": t_solve * 1000, "pairs": B3,
+        "mask_bytes": int(2 * cells3), "plan": solver.last_plan(),
+        "path_counts": {"ms": t_count * 1000, "gcups": cells3 / t_count / 1e9,
+                        "min": int(counts.min()), "median": float(np.median(counts.astype(np.float64))),
+                        "max": int(counts.max()), "saturated": int((counts == np.iinfo(np.uint64).max).sum())},
+        "first_alignments": {"pairs": 2, "alignments": n_items, "ms": t_enum * 1000},
+        "workload": "256 pairs of 5000 x 10000, all-optimal masks of every pair on the GPU (host-timed solve "
+                    "call), co-optimal path counts on the GPU, first 20 alignments of 2 pairs (host DFS)"}
     return out
 
 
@@ -626,6 +644,84 @@ def precision_config(torch, pairs, seed, steps=3):
     }
 
 
+# --------------------------------------------------------------------------- plain path
+
+PLAIN_ENV = {"PA_TUNE": "0", "PA_GRAPHS": "0", "PA_GRID": "exact"}
+
+
+def plain_gpu(torch, alg, L, a, b, ls, lt, t_d, stream, plan, width=100, steps=3):
+    """The plain GPU path of the batched workload: the bag split into length buckets
+    (|s| and |t| in 100-wide bins, each bucket padded to its own longest pair), one
+    pa_solve_batch call (one DP launch and one walk launch, synchronised) per bucket, the
+    plan fixed (no autotuner), no graph replay, a non-persistent grid (one warp per work
+    unit).  Two kernels: the int32 one-column kernel at G = 8 (the analytic plan without the
+    16-bit and two-column forms) and the kernel and G the batched form chose."""
+    P = ctypes.POINTER
+    lo = int(min(ls.min(), lt.min()))
+    top = max(0, (int(max(ls.max(), lt.max())) - lo) // width - 1)   # the longest length joins the last bin
+    key = np.minimum((ls - lo) // width, top) * 1000 + np.minimum((lt - lo) // width, top)
+    buckets = []
+    for kv in np.unique(key):
+        idx = np.nonzero(key == kv)[0]
+        n_s, n_t = int(ls[idx].max()), int(lt[idx].max())
+        a_b = torch.from_numpy(np.ascontiguousarray(a[idx, :n_s]).view(np.int32)).cuda()
+        b_b = torch.from_numpy(np.ascontiguousarray(b[idx, :n_t]).view(np.int32)).cuda()
+        length = np.ascontiguousarray(np.stack([ls[idx], lt[idx]]), dtype=np.int32)
+        sizes = np.minimum(ls[idx], lt[idx]).astype(np.int64)
+        offs = np.zeros(len(idx), np.int64)
+        offs[1:] = np.cumsum(sizes)[:-1]
+        buckets.append(dict(n=len(idx), n_s=n_s, n_t=n_t, a=a_b, b=b_b, length=length, offs=offs,
+                            sc=torch.empty(len(idx), dtype=torch.float32, device="cuda"),
+                            mp=torch.empty(max(1, int(sizes.sum())), dtype=torch.int32, device="cuda")))
+    cells = float((ls.astype(np.int64) * lt).sum())
+
+    def run(env):
+        saved = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        try:
+            for bk in buckets:   # solvers and batch structs, outside the timed region
+                mod = alg.m16
+                bk["solver"] = mod.create_solver(bk["n_s"], bk["n_t"], mod.create_options(options_dict(alg, bk["n"])))
+                alg.check(L.pa_solver_set_stream(bk["solver"].handle, ctypes.c_void_p(stream.cuda_stream)))
+                bk["batch"] = alg.Batch(form=1, location=1, batch=bk["n"], n_s=bk["n_s"], n_t=bk["n_t"],
+                                        a=ctypes.cast(bk["a"].data_ptr(), P(ctypes.c_uint32)),
+                                        b=ctypes.cast(bk["b"].data_ptr(), P(ctypes.c_uint32)),
+                                        table=ctypes.cast(t_d.data_ptr(), P(ctypes.c_float)), table_rows=4,
+                                        table_cols=4, length=bk["length"].ctypes.data_as(P(ctypes.c_int32)))
+
+            def one_pass():
+                for bk in buckets:
+                    alg.check(L.pa_solve_batch(bk["solver"].handle, ctypes.byref(bk["batch"]),
+                                               ctypes.c_void_p(bk["sc"].data_ptr()), ctypes.c_void_p(bk["mp"].data_ptr()),
+                                               bk["offs"].ctypes.data_as(P(ctypes.c_int64))))
+            one_pass()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                one_pass()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            plans = {str(bk["solver"].last_plan()) for bk in buckets}
+            return cells * steps / (e0.elapsed_time(e1) / 1000.0) / 1e9, sorted(plans)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+
+    v_int32, plans_int32 = run(dict(PLAIN_ENV, PA_GROUP_WIDTH="8", PA_DP16="0", PA_DP_COLS="1"))
+    same = dict(PLAIN_ENV, PA_GROUP_WIDTH=str(plan["G"]))
+    if plan["arithmetic"] != "int16x2":
+        same["PA_DP16"] = "0"
+    v_same, plans_same = run(same)
+    return {"value": v_int32, "unit": "GCUPS", "pairs": len(ls), "buckets": len(buckets),
+            "bucket_width": width, "plans": plans_int32, "batched_over_plain": None,
+            "workload": "the whole bag, one synchronous solve call per length bucket, device-resident codes",
+            "same_kernel": {"value": v_same, "unit": "GCUPS", "plans": plans_same}}
+
+
 # --------------------------------------------------------------------------- arms
 
 def run_reference(args):
@@ -762,50 +858,13 @@ def run_ours(args):
     # correctness spot check of the device results against the host path below
     sc_dev = sc_d.cpu().numpy().copy()
 
-    # ---- the plain GPU path: pyalign's ProblemBatch shape, one native call (one DP launch)
-    # per batch of 4 pairs -- the SIMD width of the reference on the aarch64 host -- with the
-    # batch padded to its master shape, on a sample of the workload (device-resident codes)
+    # ---- the plain GPU path: one launch per length bucket (100-wide bins of |s| and |t|)
+    # over the whole bag, device-resident codes, one synchronous solve call per bucket, fixed
+    # plan (no tuner), no graphs, a non-persistent grid; "plain" runs the int32 one-column
+    # kernel at G = 8, "plain_same_kernel" the batched form's kernel and width per bucket
     plain = None
-    if args.plain_pairs > 0:
-        lanes = 4
-        npl = min(args.plain_pairs, B) // lanes * lanes
-        psolver = mod.create_solver(1000, 1000, mod.create_options(options_dict(alg, lanes)))
-        alg.check(L.pa_solver_set_stream(psolver.handle, ctypes.c_void_p(stream.cuda_stream)))
-        order = np.argsort(ls[:npl].astype(np.int64) * lt[:npl], kind="stable")
-        batches = []
-        for k0 in range(0, npl, lanes):
-            idx = order[k0:k0 + lanes]
-            n_s, n_t = int(ls[idx].max()), int(lt[idx].max())
-            pa_ = torch.from_numpy(np.ascontiguousarray(a[idx, :n_s]).view(np.int32)).cuda()
-            pb_ = torch.from_numpy(np.ascontiguousarray(b[idx, :n_t]).view(np.int32)).cuda()
-            plen = np.ascontiguousarray(np.stack([ls[idx], lt[idx]]), dtype=np.int32)
-            psz = np.minimum(ls[idx], lt[idx]).astype(np.int64)
-            poff = np.zeros(lanes, np.int64)
-            poff[1:] = np.cumsum(psz)[:-1]
-            pmaps = torch.empty(int(psz.sum()), dtype=torch.int32, device="cuda")
-            psc = torch.empty(lanes, dtype=torch.float32, device="cuda")
-            P = ctypes.POINTER
-            bt = alg.Batch(form=1, location=1, batch=lanes, n_s=n_s, n_t=n_t,
-                           a=ctypes.cast(pa_.data_ptr(), P(ctypes.c_uint32)),
-                           b=ctypes.cast(pb_.data_ptr(), P(ctypes.c_uint32)),
-                           table=ctypes.cast(t_d.data_ptr(), P(ctypes.c_float)), table_rows=4, table_cols=4,
-                           length=plen.ctypes.data_as(P(ctypes.c_int32)))
-            batches.append((bt, psc, pmaps, poff, plen, pa_, pb_))
-        pcells = int((ls[:npl].astype(np.int64) * lt[:npl]).sum())
-
-        def plain_pass():
-            for bt, psc, pmaps, poff, _, _, _ in batches:
-                alg.check(L.pa_solve_batch(psolver.handle, ctypes.byref(bt), ctypes.c_void_p(psc.data_ptr()),
-                                           ctypes.c_void_p(pmaps.data_ptr()),
-                                           poff.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
-        plain_pass()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        plain_pass()
-        torch.cuda.synchronize()
-        pt = time.perf_counter() - t0
-        plain = {"value": pcells / pt / 1e9, "unit": "GCUPS", "pairs": npl, "pairs_per_launch": lanes,
-                 "batched_over_plain": None}
+    if args.plain:
+        plain = plain_gpu(torch, alg, L, a, b, ls, lt, t_d, stream, plan)
 
     # ---- end-to-end timing through the C ABI with host buffers
     for _ in range(max(1, args.warmup)):
@@ -884,6 +943,7 @@ def run_ours(args):
 
     if plain is not None:
         plain["batched_over_plain"] = value / plain["value"]
+        plain["same_kernel"]["batched_over_plain_same_kernel"] = value / plain["same_kernel"]["value"]
     line = {
         "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed * 1000.0 / args.steps, "higher_is_better": True,

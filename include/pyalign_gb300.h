@@ -229,6 +229,14 @@ int32_t pa_iterator_next(pa_iterator *it, float *score, int32_t *map, int32_t *p
                          int64_t *path_len);
 void pa_iterator_destroy(pa_iterator *it);
 
+/* Number of co-optimal traceback paths of every lane of an all-optimal result (count ALL,
+ * linear or affine gaps): how many alignments the reference's depth-first enumeration
+ * (TracebackIterators<true>::Iterator::next, solver.h:1647-1716) yields with return_dup set,
+ * i.e. before de-duplication of identical alignments.  Computed on the device from the
+ * result's masks in one wavefront pass; `counts` (batch uint64, host) saturate at
+ * 2^64 - 1.  The reference has no counterpart: its enumeration is the only way to count. */
+pa_status pa_result_path_counts(const pa_result *r, uint64_t *counts);
+
 /* ---- batched form: the whole bag in one call (no per-lane objects) ----
  * Score plus one optimal traceback for `batch` pairs of uneven lengths, the throughput
  * path behind ProblemBatch.  Inputs and outputs are host or device memory

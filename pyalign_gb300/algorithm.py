@@ -121,6 +121,7 @@ def lib():
         L.pa_iterator_next.restype = _c_i32
         L.pa_iterator_next.argtypes = [_P, _PF, _PI, _PI, _PL]
         L.pa_iterator_destroy.argtypes = [_P]
+        L.pa_result_path_counts.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64)]
         _lib = L
     return _lib
 
@@ -253,10 +254,11 @@ def _general_costs(spec, n):
 class _Result:
     """Owner of a pa_result handle (one solve call)."""
 
-    __slots__ = ("ptr",)
+    __slots__ = ("ptr", "_path_counts")
 
     def __init__(self, ptr):
         self.ptr = ptr
+        self._path_counts = None
 
     def __del__(self):
         if self.ptr and _lib is not None:
@@ -461,6 +463,13 @@ class _Iter:
             _lib.pa_iterator_destroy(self._it)
             self._it = None
 
+    def path_count(self):
+        """Number of co-optimal traceback paths of this lane -- the number of results this
+        iterator yields when the solver's options keep duplicates (return_dup), computed on
+        the GPU for every lane of the solve at once (pa_result_path_counts); uint64,
+        saturating at 2**64 - 1.  All-optimal results with linear or affine gaps only."""
+        return int(path_counts(self._res)[self._lane])
+
     def _next(self):
         sc = ctypes.c_float(0)
         mp = np.zeros((min(self._ls, self._lt),), dtype=np.int32)
@@ -469,6 +478,16 @@ class _Iter:
         if not lib().pa_iterator_next(self._it, ctypes.byref(sc), _ip(mp), _ip(path), ctypes.byref(n)):
             return None
         return float(sc.value), mp, path[:n.value].copy()
+
+
+def path_counts(res):
+    """Co-optimal traceback path count per lane of an all-optimal result (uint64 array)."""
+    cached = res._path_counts
+    if cached is None:
+        cached = np.zeros(lib().pa_result_size(res.ptr), dtype=np.uint64)
+        check(lib().pa_result_path_counts(res.ptr, cached.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+        res._path_counts = cached
+    return cached
 
 
 class AlignmentIterator(_Iter):

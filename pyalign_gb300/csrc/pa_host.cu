@@ -192,6 +192,7 @@ struct ResultData {
 	}
 	std::vector<int64_t> val_off;
 	std::vector<float> values;
+	mutable std::vector<uint64_t> path_counts;  // all-optimal: co-optimal path count per lane, once computed
 	// general (WSB) gap: traceback codes and values per lane
 	std::vector<int64_t> wsb_off;
 	std::vector<int32_t> wsb_tb;
@@ -878,10 +879,15 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	const int64_t groups_needed = plan.units ? plan.ntickets : (units_needed + gpw - 1) / gpw;  // warps needed
 	int64_t grid = int64_t(s->sm_count) * bps;
 	grid = std::min<int64_t>(grid, (groups_needed + WARPS - 1) / WARPS);
+	// PA_GRID=exact: one block per WARPS work units, each warp takes one unit and exits -- the
+	// non-persistent launch of a plain per-bucket solve, kept for that comparison
+	if (const char *ge = std::getenv("PA_GRID"))
+		if (std::strcmp(ge, "exact") == 0) grid = (groups_needed + WARPS - 1) / WARPS;
 	grid = std::max<int64_t>(grid, 1);
 	// scratch rows: per group slot, or per pair in the stripe-chained mode
 	const int64_t slots = plan.units ? std::max<int64_t>(npairs, 1) : grid * WARPS * gpw;
-	p.scratch_stride = 2 * std::max<int64_t>(plan.max_lt, 1);
+	// two boundary rows per slot (double-buffered by pass), one for the 16-bit kernel
+	p.scratch_stride = (h16 ? 1 : 2) * std::max<int64_t>(plan.max_lt, 1);
 	PA_CUDA(scratch.ensure(size_t(slots * p.scratch_stride) * 2 * sizeof(V)));
 	p.scratch = scratch.p;
 	if (plan.units) {
@@ -2582,5 +2588,80 @@ int32_t pa_iterator_next(pa_iterator *it, float *score, int32_t *map, int32_t *p
 }
 
 void pa_iterator_destroy(pa_iterator *it) { delete it; }
+
+}  // extern "C"
+
+namespace pa {
+cudaError_t path_count_solve(int32_t npairs, int32_t G, int32_t local, int32_t affine, const int32_t *len_s,
+                             const int32_t *len_t, const int64_t *mask_off, const void *masks, const int32_t *seed,
+                             unsigned long long *counts, unsigned long long *scratch, int64_t scratch_stride,
+                             int32_t *work_counter, int grid, cudaStream_t st);
+}  // namespace pa
+
+extern "C" {
+
+// Number of co-optimal traceback paths per lane of an all-optimal result: the count of
+// results the reference's depth-first enumeration (solver.h:1647-1716) produces without
+// de-duplication, computed on the device over the result's masks (path_count_kernel,
+// pa_count.cu), uint64 saturating at 2^64 - 1.  Blocks until the counts are on the host.
+pa_status pa_result_path_counts(const pa_result *r, uint64_t *counts) {
+	if (!r || !counts) return fail(PA_ERR_INVALID_ARGUMENT, "pa_result_path_counts: null argument");
+	const ResultData &d = *r->d;
+	if (d.goal != GOAL_ALL || !d.dev_masks_all || d.gap == GAP_GENERAL)
+		return fail(PA_ERR_UNSUPPORTED, "path counts need an all-optimal result with linear or affine gap costs");
+	const int64_t B = d.batch;
+	if (d.path_counts.size() != size_t(B)) {
+		const bool local = d.loc == LOC_LOCAL;
+		std::vector<int32_t> seed(size_t(2 * B), -1);
+		int64_t max_lt = 1;
+		for (int64_t k = 0; k < B; k++) {
+			max_lt = std::max<int64_t>(max_lt, d.lt[size_t(k)]);
+			if (!local && d.has[size_t(k)]) {
+				seed[size_t(2 * k)] = d.seeds[size_t(2 * k)];
+				seed[size_t(2 * k + 1)] = d.seeds[size_t(2 * k + 1)];
+			}
+		}
+		int dev = 0, sms = 1;
+		PA_CUDA(cudaGetDevice(&dev));
+		PA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+		const int gpw = 32 / d.G;
+		const int64_t warps = (B + gpw - 1) / gpw;
+		const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(int64_t(sms) * 8, (warps + WARPS - 1) / WARPS));
+		const int64_t slots = grid * WARPS * gpw;
+		const int64_t stride = 4 * max_lt;
+		DevBuf dl, dm, dseed, dcnt, dscr, dctr;
+		PA_CUDA(dl.ensure(size_t(2 * B) * 4));
+		PA_CUDA(dm.ensure(size_t(B) * 8));
+		PA_CUDA(dseed.ensure(size_t(2 * B) * 4));
+		PA_CUDA(dcnt.ensure(size_t(B) * 8));
+		PA_CUDA(dscr.ensure(size_t(slots * stride) * 8));
+		PA_CUDA(dctr.ensure(4));
+		PA_CUDA(cudaMemcpy(dl.p, d.ls.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemcpy(dl.as<int32_t>() + B, d.lt.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemcpy(dm.p, d.mask_off.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemcpy(dseed.p, seed.data(), size_t(2 * B) * 4, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemset(dctr.p, 0, 4));
+		PA_CUDA(pa::path_count_solve(int32_t(B), d.G, local ? 1 : 0, d.gap == GAP_AFFINE ? 1 : 0, dl.as<int32_t>(),
+		                             dl.as<int32_t>() + B, dm.as<int64_t>(), d.dev_masks_all, dseed.as<int32_t>(),
+		                             dcnt.as<unsigned long long>(), dscr.as<unsigned long long>(), stride,
+		                             dctr.as<int32_t>(), int(grid), nullptr));
+		std::vector<uint64_t> c(static_cast<size_t>(B), 0);
+		PA_CUDA(cudaMemcpy(c.data(), dcnt.p, size_t(B) * 8, cudaMemcpyDeviceToHost));
+		for (int64_t k = 0; k < B; k++) {
+			const int ls = d.ls[size_t(k)], lt = d.lt[size_t(k)];
+			if (local) {
+				// seeds exist only for a strictly positive optimum (solver.h:2060-2091)
+				if (!(d.scores[size_t(k)] * d.sign > 0.0f) || ls == 0 || lt == 0) c[size_t(k)] = 0;
+			} else if (ls == 0 || lt == 0) {
+				c[size_t(k)] = d.has[size_t(k)] ? 1 : 0;  // the seed itself has a negative coordinate
+			} else if (!d.has[size_t(k)]) {
+				c[size_t(k)] = 0;
+			}
+		}
+		d.path_counts.swap(c);
+	}
+	std::memcpy(counts, d.path_counts.data(), size_t(B) * 8);
+	return PA_OK;
+}
 
 }  // extern "C"

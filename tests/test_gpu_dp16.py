@@ -187,18 +187,23 @@ def test_dp16_bad_codes_then_valid(analytic, gpu_alg, oracle_alg):
     assert d is None, d
 
 
-def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg):
+@pytest.mark.parametrize("plan", ["twins-G16", "own"])
+def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg, monkeypatch, plan):
     """4,096 pairs drawn like the batched workload (DNA, |s|, |t| ~ U[100, 1000], half of them
-    a query and a 10%-mutated copy; local affine 5/2, +2/-3; score + one traceback) through
-    the solver's own plan -- the 16-bit twin kernel -- against the oracle, every score and
-    every alignment map bit for bit."""
+    a query and a 10%-mutated copy; local affine 5/2, +2/-3; score + one traceback) against
+    the oracle, every score and every alignment map bit for bit: with the batched
+    workload's plan (the 16-bit twin kernel, two columns per step, G = 16) and with the
+    plan the solver picks for this bag on its own."""
     import bench
+    if plan == "twins-G16":
+        monkeypatch.setenv("PA_GROUP_WIDTH", "16")
     a, b, ls, lt, table = bench.make_workload(4096, 4242)
     n = a.shape[0]
     opts = dict(options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"]), batch_size=n, batch=True)
     solver = gpu_alg.m16.create_solver(a.shape[1], b.shape[1], gpu_alg.m16.create_options(opts))
     res = solver.solve_indexed_for_alignment(a, b, table, np.stack([ls, lt]).astype(np.uint16))
-    assert solver.last_plan()["kernel"].startswith("16-bit"), solver.last_plan()
+    if plan == "twins-G16":
+        assert solver.last_plan()["kernel"] == TWINS["2"] and solver.last_plan()["G"] == 16, solver.last_plan()
     osol = oracle_alg.m16.create_solver(a.shape[1], b.shape[1], oracle_alg.m16.create_options(opts))
     osc, omp, offs, _ = oracle_alg.batch_alignments(osol, a, b, table, ls, lt)
     bad = []
