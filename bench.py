@@ -508,7 +508,7 @@ def fwd_bwd(torch, pairs, seed, steps=3):
     fb = cells * steps / (ev[1].elapsed_time(ev[2]) / 1000) / 1e9
 
     # DTW on random walks
-    nd = max(1, pairs // 4)
+    nd = pairs
     dl = rng.integers(128, 1025, size=(nd, 2))
     dcells = float((dl[:, 0].astype(np.int64) * dl[:, 1]).sum())
     x0 = torch.cumsum(torch.randn(nd, 1024, device="cuda", generator=g), dim=1)
@@ -884,6 +884,30 @@ def run_ours(args):
     if not np.array_equal(sc_dev, sc_h.numpy()):
         raise SystemExit("device-resident and host-buffer runs disagree")
 
+    # ---- the reference-facing module call: Solver.solve_indexed_for_alignment, the native
+    # method pyalign's indexed form calls for a batch (solve.py:399-432), with host numpy
+    # arrays in the layouts pyalign builds (codes uint32 (batch, n), lengths uint16 (2, batch))
+    # and its result as a tuple of Alignment objects
+    ln16 = np.stack([ls, lt]).astype(np.uint16)
+    api_solver = mod.create_solver(1000, 1000, mod.create_options(options_dict(alg, B)))
+    alg.check(L.pa_solver_set_stream(api_solver.handle, ctypes.c_void_p(stream.cuda_stream)))
+    api_res = api_solver.solve_indexed_for_alignment(a, b, table, ln16)
+    barrier()
+    api_steps = max(3, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(api_steps):
+        api_res = api_solver.solve_indexed_for_alignment(a, b, table, ln16)
+    barrier()
+    api_s = max_over_ranks(time.perf_counter() - t0)
+    if float(api_res[0].score) != float(sc_h[0]) or not np.array_equal(
+            np.asarray(api_res[B - 1].s_to_t if ls[B - 1] <= lt[B - 1] else api_res[B - 1].t_to_s),
+            mp_h.numpy()[offs[B - 1]:offs[B - 1] + sizes[B - 1]]):
+        raise SystemExit("module call and pa_solve_batch disagree")
+    e2e_api = {"value": cells * world * api_steps / api_s / 1e9, "unit": "GCUPS", "steps": api_steps,
+               "call": "Solver.solve_indexed_for_alignment of the native module (one call for the whole bag), "
+                       "host numpy arrays, a tuple of Alignment objects returned"}
+    del api_res
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -957,6 +981,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "GCUPS", "h2d_bytes_per_step": int(h2d.value),
                 "d2h_bytes_per_step": int(d2h.value)},
+        "e2e_api": e2e_api,
         "gpu_launches": launches,
         "plain_gpu": plain,
         "fwd_bwd": fb,

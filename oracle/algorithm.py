@@ -412,9 +412,20 @@ class Solver:
         self._check_batch(sim.shape[2])
         length = self._check_len(length)
         self._check_cap(sim.shape[0], sim.shape[1])
-        return [_Pair(self, int(length[0, k]), int(length[1, k]),
-                      sim[:int(length[0, k]), :int(length[1, k]), k])
-                for k in range(self._batch_size)]
+        out = []
+        for k in range(self._batch_size):
+            ls, lt = self._lane_lengths(length, k, sim.shape[0], sim.shape[1])
+            out.append(_Pair(self, ls, lt, sim[:ls, :lt, k]))
+        return out
+
+    @staticmethod
+    def _lane_lengths(length, k, n_s, n_t):
+        """Lane k's lengths, clamped to the batch arrays: a partial batch's trailing lanes keep
+        the lengths of an earlier, larger batch (solve.py:382-396 rewrites only the lanes it
+        fills); the reference computes them over stale array contents and pyalign discards
+        their results (solve.py:554-560), so any value serves -- clamping keeps them in the
+        arrays."""
+        return min(int(length[0, k]), n_s), min(int(length[1, k]), n_t)
 
     def _pairs_indexed(self, a, b, sim, length):
         a, b = np.asarray(a), np.asarray(b)
@@ -429,7 +440,7 @@ class Solver:
         self._check_cap(a.shape[1], b.shape[1])
         out = []
         for k in range(self._batch_size):
-            ls, lt = int(length[0, k]), int(length[1, k])
+            ls, lt = self._lane_lengths(length, k, a.shape[1], b.shape[1])
             out.append(_Pair(self, ls, lt, sim[np.ix_(a[k, :ls], b[k, :lt])]))
         return out
 
@@ -442,7 +453,7 @@ class Solver:
         eq, ne = np.float32(eq), np.float32(ne)
         out = []
         for k in range(self._batch_size):
-            ls, lt = int(length[0, k]), int(length[1, k])
+            ls, lt = self._lane_lengths(length, k, a.shape[1], b.shape[1])
             m = a[k, :ls][:, None] == b[k, :lt][None, :]
             out.append(_Pair(self, ls, lt, np.where(m, eq, ne).astype(np.float32)))
         return out

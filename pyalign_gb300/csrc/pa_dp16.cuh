@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 	const int gpw = 32 / G;
 	const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const int slot = warp_global * gpw + grp;
+	const int64_t half = p.scratch_stride / 2;
 	const int rpp = G * R;
 	const int ntwins = (p.npairs + 1) >> 1;
 	const uint32_t NEG = p.h_neg;
@@ -212,13 +213,8 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 		for (int q = 0; q < wpass; q++) {
 			const bool pass_active = q < npass;
 			const int row0 = q * rpp + sub * R;
-			// one boundary row per group slot: the pass reads the row the previous pass wrote
-			// and overwrites it behind itself -- lane 0 reads column c (two steps ahead) in step
-			// c / C - 2 and uses it in step c / C, the last lane writes column c in step
-			// c / C + G - 1, and every step starts with a full-warp shuffle, so each column is
-			// read before it is overwritten
-			int2 *bout = reinterpret_cast<int2 *>(p.scratch) + int64_t(slot) * p.scratch_stride;
-			const int2 *bin = bout;
+			const int2 *bin = reinterpret_cast<const int2 *>(p.scratch) + int64_t(slot) * p.scratch_stride + (q & 1) * half;
+			int2 *bout = reinterpret_cast<int2 *>(p.scratch) + int64_t(slot) * p.scratch_stride + ((q + 1) & 1) * half;
 			const bool write_boundary = sub == G - 1 && q + 1 < npass;
 
 			// int8 score profiles of this lane's rows (bytes = letters of t), the zero floor of
@@ -263,24 +259,22 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 				if (pass_active && q < npA) mA = m + p.mask_off[pa] + (int64_t(q) * sA * G + sub) * C;
 				if (pass_active && q < npB) mB = m + p.mask_off[pb] + (int64_t(q) * sB * G + sub) * C;
 			}
-			// lane 0: the (D, P) above this pass's first row in the columns of the next two steps
-			// (bn: the next step, bm: the one after), read two steps ahead -- the border row, or
-			// the boundary row the group's last lane wrote in the previous pass (complete before
-			// this pass: same warp, __syncwarp between passes)
-			const int2 none = make_int2(int32_t(NEG), int32_t(NEG));
-			auto fetch = [&](int col) -> int2 {
-				return q == 0 ? make_int2(int32_t(__ldg(p.top16 + col + 1)), int32_t(NEG)) : bin[col];
-			};
-			int2 bn0 = none, bn1 = none, bm0 = none, bm1 = none;
+			// lane 0: the (D, P) above this pass's first row in the next step's columns, read one
+			// step ahead -- the border row, or the boundary row the group's last lane wrote in the
+			// previous pass (complete before this pass: same warp, __syncwarp between passes)
+			int2 bn0 = make_int2(int32_t(NEG), int32_t(NEG)), bn1 = bn0;
 			if (sub == 0 && pass_active) {
-				bn0 = fetch(0);
-				if (C == 2 && lt > 1) bn1 = fetch(1);
-				if (C < lt) bm0 = fetch(C);
-				if (C == 2 && C + 1 < lt) bm1 = fetch(C + 1);
+				if (q == 0) {
+					bn0.x = int32_t(p.top16[1]);
+					if (C == 2 && lt > 1) bn1.x = int32_t(p.top16[2]);
+				} else {
+					bn0 = bin[0];
+					if (C == 2 && lt > 1) bn1 = bin[1];
+				}
 			}
-			uint32_t tnA0 = pass_active ? __ldg(browA) : 0u, tnB0 = pass_active ? __ldg(browB) : 0u;
-			uint32_t tnA1 = (C == 2 && pass_active && lt > 1) ? __ldg(browA + 1) : 0u;
-			uint32_t tnB1 = (C == 2 && pass_active && lt > 1) ? __ldg(browB + 1) : 0u;
+			uint32_t tnA0 = pass_active ? browA[0] : 0u, tnB0 = pass_active ? browB[0] : 0u;
+			uint32_t tnA1 = (C == 2 && pass_active && lt > 1) ? browA[1] : 0u;
+			uint32_t tnB1 = (C == 2 && pass_active && lt > 1) ? browB[1] : 0u;
 
 			for (int s = 0; s < wsteps; s++) {
 				const int j0 = C * (s - sub), j1 = j0 + 1;
@@ -295,23 +289,21 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 				const bool act1 = C == 2 && act && j1 < lt;
 				const uint32_t tcA0 = tnA0, tcB0 = tnB0, tcA1 = tnA1, tcB1 = tnB1;
 				if (act && j0 + C < lt) {
-					tnA0 = __ldg(browA + j0 + C);
-					tnB0 = __ldg(browB + j0 + C);
+					tnA0 = browA[j0 + C];
+					tnB0 = browB[j0 + C];
 				}
 				if (C == 2 && act && j0 + 3 < lt) {
-					tnA1 = __ldg(browA + j0 + 3);
-					tnB1 = __ldg(browB + j0 + 3);
+					tnA1 = browA[j0 + 3];
+					tnB1 = browB[j0 + 3];
 				}
 				if (sub == 0 && act) {
 					upD0 = uint32_t(bn0.x);
 					upP0 = uint32_t(bn0.y);
 					upD1 = uint32_t(bn1.x);
 					upP1 = uint32_t(bn1.y);
-					bn0 = bm0;
-					bn1 = bm1;
-					const int n0 = j0 + 2 * C, n1 = n0 + 1;  // the columns of the step after next
-					if (n0 < lt) bm0 = fetch(n0);
-					if (C == 2 && n1 < lt) bm1 = fetch(n1);
+					const int n0 = j0 + C, n1 = j0 + 3;  // the next step's columns
+					if (n0 < lt) bn0 = q == 0 ? make_int2(int32_t(p.top16[n0 + 1]), int32_t(NEG)) : bin[n0];
+					if (C == 2 && n1 < lt) bn1 = q == 0 ? make_int2(int32_t(p.top16[n1 + 1]), int32_t(NEG)) : bin[n1];
 				}
 				if (act) {
 					// prmt selectors: half A = byte tcA of prA sign-extended, half B = byte tcB of prB
@@ -392,18 +384,16 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 					}
 					if (TB == TB_ONE) {
 						// rows 0-3 of each half in mlo, 4-7 in mhi, row r at bits 4 (R - 1 - r) of the word
-						// (streaming stores: the words are read back only along the optimal paths,
-						// and must not evict the boundary rows and codes from L2)
 						if (C == 2) {
 							if (mA && j0 < ctA)
-								__stcs(reinterpret_cast<uint2 *>(mA) + int64_t(s) * G,
-								       make_uint2(__byte_perm(mhi0, mlo0, 0x5410), __byte_perm(mhi1, mlo1, 0x5410)));
+								reinterpret_cast<uint2 *>(mA)[int64_t(s) * G] =
+								    make_uint2(__byte_perm(mhi0, mlo0, 0x5410), __byte_perm(mhi1, mlo1, 0x5410));
 							if (mB && j0 < ctB)
-								__stcs(reinterpret_cast<uint2 *>(mB) + int64_t(s) * G,
-								       make_uint2(__byte_perm(mhi0, mlo0, 0x7632), __byte_perm(mhi1, mlo1, 0x7632)));
+								reinterpret_cast<uint2 *>(mB)[int64_t(s) * G] =
+								    make_uint2(__byte_perm(mhi0, mlo0, 0x7632), __byte_perm(mhi1, mlo1, 0x7632));
 						} else {
-							if (mA && j0 < ctA) __stcs(mA + int64_t(s) * G, __byte_perm(mhi0, mlo0, 0x5410));
-							if (mB && j0 < ctB) __stcs(mB + int64_t(s) * G, __byte_perm(mhi0, mlo0, 0x7632));
+							if (mA && j0 < ctA) mA[int64_t(s) * G] = __byte_perm(mhi0, mlo0, 0x5410);
+							if (mB && j0 < ctB) mB[int64_t(s) * G] = __byte_perm(mhi0, mlo0, 0x7632);
 						}
 					}
 					if (SEED) {

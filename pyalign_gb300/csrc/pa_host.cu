@@ -886,8 +886,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	grid = std::max<int64_t>(grid, 1);
 	// scratch rows: per group slot, or per pair in the stripe-chained mode
 	const int64_t slots = plan.units ? std::max<int64_t>(npairs, 1) : grid * WARPS * gpw;
-	// two boundary rows per slot (double-buffered by pass), one for the 16-bit kernel
-	p.scratch_stride = (h16 ? 1 : 2) * std::max<int64_t>(plan.max_lt, 1);
+	p.scratch_stride = 2 * std::max<int64_t>(plan.max_lt, 1);
 	PA_CUDA(scratch.ensure(size_t(slots * p.scratch_stride) * 2 * sizeof(V)));
 	p.scratch = scratch.p;
 	if (plan.units) {

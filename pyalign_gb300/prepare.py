@@ -138,3 +138,45 @@ def patch_prepare(solve_module=None):
     prepare._pa_original = original
     cls.prepare = prepare
     return original
+
+
+def bag_batches(bag, batch_size):
+    """The batches of a ProblemBag for this library, in O(B log B): the problems sorted by
+    shape (|s| then |t|, largest first) and cut into runs of ``batch_size``, each with its
+    own largest shape as master shape.  pyalign's ProblemBag.batches (instance.py:230-275)
+    groups by Morton order with a rescan of the remaining problems per batch, which at
+    65,536 problems costs seconds of Python; the grouping only decides which lanes share a
+    native call, and each lane's result depends on its own lengths alone, so any grouping
+    whose master shape covers every member gives the same results.  Yields the same
+    ProblemBatch objects (problems, indices, master_shape)."""
+    from pyalign.problems.instance import ProblemBatch
+    problems = bag.problems
+    if batch_size == 1:
+        for i, p in enumerate(problems):
+            yield ProblemBatch([p], [i], p.shape)
+        return
+    shapes = np.array([p.shape for p in problems], dtype=np.int64).reshape(-1, 2)
+    order = np.lexsort((-shapes[:, 1], -shapes[:, 0]))
+    for k0 in range(0, len(order), batch_size):
+        idx = order[k0:k0 + batch_size].tolist()
+        master = (int(shapes[idx, 0].max()), int(shapes[idx, 1].max()))
+        yield ProblemBatch([problems[i] for i in idx], idx, master)
+
+
+def patch_batches(instance_module=None):
+    """Install ``bag_batches`` as ``ProblemBag.batches`` of pyalign.problems.instance (call
+    after ``import pyalign``; opt-in); returns the original method."""
+    if instance_module is None:
+        import pyalign.problems.instance as instance_module
+    cls = instance_module.ProblemBag
+    original = cls.batches
+    if getattr(original, "_pa_bag_batches", False):
+        return original._pa_original
+
+    def batches(self, batch_size):
+        return bag_batches(self, batch_size)
+
+    batches._pa_bag_batches = True
+    batches._pa_original = original
+    cls.batches = batches
+    return original
