@@ -613,8 +613,39 @@ def precision_config(torch, pairs, seed, steps=3):
     t_gemm = ev[0].elapsed_time(ev[1]) / 1000 / steps
     t_dp = ev[1].elapsed_time(ev[2]) / 1000 / steps
     t_all = ev[2].elapsed_time(ev[3]) / 1000 / steps
+    # the float DP kernel alone (the solver's phase events of its last solve) against the
+    # measured float32 add/add/max peak: global Gotoh 9 ops + one-optimal traceback 4 per cell
+    dp_solver = ag._solver(pairs, n, n, "global", "maximize", False, (0.5, 0.1))
+    ag._forward_paths(S, lengths, (0.5, 0.1), "global", "maximize", False)
+    torch.cuda.synchronize()
+    ms4, _ = dp_solver.last_timings()
+    from pyalign_gb300 import algorithm as alg
+    f32_peak, pms = ctypes.c_float(0), ctypes.c_float(0)
+    alg.check(alg.lib().pa_measure_f32_peak(ctypes.byref(f32_peak), ctypes.byref(pms)))
+    dp_kernel_s = ms4[1] / 1000.0
+    f_ops = 13.0 * cells / dp_kernel_s / 1e9
+    dp_roof = {"bound": "alu", "achieved": f_ops, "peak": float(f32_peak.value), "unit": "Gop/s",
+               "frac": f_ops / float(f32_peak.value), "ops_per_cell": 13, "kernel_ms": ms4[1],
+               "plan": dp_solver.last_plan(), "peak_source": "measured in-run (pa_measure_f32_peak)",
+               "hbm": {"bytes_per_cell": 4.5, "achieved_gbs": 4.5 * cells / dp_kernel_s / 1e9,
+                       "note": "S read (4 B) + traceback nibble (0.5 B) per cell"}}
     sc32, rep, scale = ag.path_scores_f64(S, lengths, 0.5, 0.1, "global", "maximize", with_scale=True)
     gotoh_err = error_report(sc32, rep, scale)
+
+    # the same forward with the pairs in ranges: the product of range c + 1 overlaps the DP
+    # of range c on a second stream
+    piped = {}
+    for chunks in (4, 8):
+        ag.similarity_alignment_scores(Es, Et, lengths, 0.5, 0.1, "global", "maximize", chunks=chunks)
+        torch.cuda.synchronize()
+        ev[6].record(stream)
+        for _ in range(steps):
+            sc_p = ag.similarity_alignment_scores(Es, Et, lengths, 0.5, 0.1, "global", "maximize", chunks=chunks)
+        ev[7].record(stream)
+        torch.cuda.synchronize()
+        piped[chunks] = ev[6].elapsed_time(ev[7]) / steps
+    if not torch.equal(sc_p, sc32):
+        raise SystemExit("chunked similarity scores differ from the unchunked ones")
 
     D, _, _ = product(-1.0, 1.0)
     ag._forward_paths(D, lengths, None, "global", "minimize", True)
@@ -637,6 +668,11 @@ def precision_config(torch, pairs, seed, steps=3):
                     "tile_tflops": 2.0 * d * tiles * 128 * 128 / t_gemm / 1e12,
                     "out_gbs": 4.0 * cells / t_gemm / 1e9, "status": status},
         "dp_gcups": cells / t_dp / 1e9, "dp_ms": t_dp * 1e3, "total_ms": t_all * 1e3,
+        "dp_roofline": dp_roof,
+        "chunked": {"total_ms": {str(k): v for k, v in piped.items()},
+                    "gcups": {str(k): cells / (v / 1e3) / 1e9 for k, v in piped.items()},
+                    "how": "similarity_alignment_scores: the product of one range of pairs overlaps the DP "
+                           "of the previous range on a second stream"},
         "error_vs_fp64_replay": gotoh_err,
         "dtw": {"value": cells / t_dtw / 1e9, "unit": "GCUPS", "ms": t_dtw * 1e3,
                 "error_vs_fp64_replay": dtw_err,
@@ -858,14 +894,6 @@ def run_ours(args):
     # correctness spot check of the device results against the host path below
     sc_dev = sc_d.cpu().numpy().copy()
 
-    # ---- the plain GPU path: one launch per length bucket (100-wide bins of |s| and |t|)
-    # over the whole bag, device-resident codes, one synchronous solve call per bucket, fixed
-    # plan (no tuner), no graphs, a non-persistent grid; "plain" runs the int32 one-column
-    # kernel at G = 8, "plain_same_kernel" the batched form's kernel and width per bucket
-    plain = None
-    if args.plain:
-        plain = plain_gpu(torch, alg, L, a, b, ls, lt, t_d, stream, plan)
-
     # ---- end-to-end timing through the C ABI with host buffers
     for _ in range(max(1, args.warmup)):
         step_host()
@@ -907,6 +935,15 @@ def run_ours(args):
                "call": "Solver.solve_indexed_for_alignment of the native module (one call for the whole bag), "
                        "host numpy arrays, a tuple of Alignment objects returned"}
     del api_res
+
+    # ---- the plain GPU path: one launch per length bucket (100-wide bins of |s| and |t|)
+    # over the whole bag, device-resident codes, one synchronous solve call per bucket, fixed
+    # plan (no tuner), no graphs, a non-persistent grid; "plain" runs the int32 one-column
+    # kernel at G = 8, "plain_same_kernel" the batched form's kernel and width per bucket
+    # (measured after the end-to-end runs: its many short-lived solvers are not in their way)
+    plain = None
+    if args.plain:
+        plain = plain_gpu(torch, alg, L, a, b, ls, lt, t_d, stream, plan)
 
     if rank != 0:
         if dist is not None:

@@ -411,6 +411,10 @@ pa_status pa_measure_int32_peak(float *gops, float *ms);
  * operations per instruction: the roofline denominator of the packed 16-bit twin kernel. */
 pa_status pa_measure_int16x2_peak(float *gops, float *ms);
 
+/* Diagnostic: the same mix in float32 (FADD, FADD, FMNMX): the roofline denominator of the
+ * float DP kernels of the similarity-matrix and DTW forms. */
+pa_status pa_measure_f32_peak(float *gops, float *ms);
+
 /* ---- allocation-free score solve ----
  * No counterpart in the reference (its solver allocates its matrices on the host).
  * For callers that cannot allocate device memory while they run -- a process that owns

@@ -95,22 +95,39 @@ __global__ void __launch_bounds__(BLOCK) path_count_kernel(CountParams p) {
 			}
 			unsigned long long outN = 1ull, outP = 0ull;  // this lane's last row, previous column
 			unsigned long long prev_up = 1ull;            // N(row0 - 1, j - 1); column -1 is a leaf
+			// the mask words of the next four steps and (lane 0) the boundary row of the next two
+			// columns, loaded ahead: one pair's steps are a chain of dependent cells, so a load
+			// used in its own step would cost a memory round trip per step
+			const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
+			auto load = [&](int st) -> uint4 {
+				const int jj = st - sub;
+				return (pass_active && jj >= 0 && jj < lt) ? __ldg(M + (int64_t(q) * S + st) * G + sub) : zero4;
+			};
+			auto load_row = [&](int col) -> ulonglong2 {
+				if (sub != 0 || !pass_active || col >= lt) return make_ulonglong2(1ull, 0ull);
+				if (q == 0) return make_ulonglong2(1ull, 0ull);  // N(-1, j): a leaf; no P list above
+				return make_ulonglong2(bin[2 * col], bin[2 * col + 1]);
+			};
+			uint4 w0 = load(0), w1 = load(1), w2 = load(2), w3 = load(3);
+			ulonglong2 b0 = load_row(0), b1 = load_row(1);
 			for (int s = 0; s < wsteps; s++) {
+				const uint4 w = w0;
+				w0 = w1;
+				w1 = w2;
+				w2 = w3;
+				w3 = load(s + 4);
+				const ulonglong2 bcur = b0;  // lane 0: (N, Pc) above row 0 in column s
+				b0 = b1;
+				b1 = load_row(s + 2);
 				const int j = s - sub;
 				unsigned long long upN = shfl_up64(outN, G);
 				unsigned long long upP = shfl_up64(outP, G);
 				const bool act = pass_active && j >= 0 && j < lt;
 				if (act) {
 					if (sub == 0) {
-						if (q == 0) {
-							upN = 1ull;  // N(-1, j): a leaf
-							upP = 0ull;
-						} else {
-							upN = bin[2 * j];
-							upP = bin[2 * j + 1];
-						}
+						upN = bcur.x;
+						upP = bcur.y;
 					}
-					const uint4 w = M[(int64_t(q) * S + s) * G + sub];
 					const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
 					unsigned long long dN = prev_up, uN = upN, uP = upP;
 #pragma unroll

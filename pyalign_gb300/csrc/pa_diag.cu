@@ -1,6 +1,6 @@
-// Measured integer ALU peaks of this GPU for the operation mix of the DP cell update
-// (add, add, max): on int32 lanes, the roofline denominator of the int32 DP kernels, and on
-// packed 16-bit pairs, that of the 16-bit twin kernel.
+// Measured ALU peaks of this GPU for the operation mix of the DP cell update (add, add,
+// max): on int32 lanes, the roofline denominator of the int32 DP kernels; on packed 16-bit
+// pairs, that of the 16-bit twin kernel; on float32, that of the float DP kernels.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "../../include/pyalign_gb300.h"
@@ -56,6 +56,29 @@ __global__ void __launch_bounds__(256) int16x2_peak_kernel(int iters, uint32_t c
 	out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// The same mix in float32 (two adds, one max per chain step), the arithmetic of the float
+// DP kernels (similarity-matrix and DTW forms).
+__global__ void __launch_bounds__(256) f32_peak_kernel(int iters, float c1, float c2, float *out) {
+	float x[CHAINS], y[CHAINS];
+#pragma unroll
+	for (int k = 0; k < CHAINS; k++) {
+		x[k] = float(threadIdx.x + k);
+		y[k] = float(blockIdx.x) - float(k);
+	}
+	for (int i = 0; i < iters; i++) {
+#pragma unroll
+		for (int k = 0; k < CHAINS; k++) {
+			const float t = fmaxf(x[k] + c1, y[k] + c2);  // 3 float ops
+			y[k] = x[k];
+			x[k] = t;
+		}
+	}
+	float s = 0.0f;
+#pragma unroll
+	for (int k = 0; k < CHAINS; k++) s += x[k] - y[k];
+	out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 template <typename K, typename C>
 pa_status time_peak(K kernel, C c1, C c2, double ops_per_chain_step, float *gops, float *ms_out) {
 	int dev = 0, sms = 0;
@@ -93,6 +116,10 @@ pa_status time_peak(K kernel, C c1, C c2, double ops_per_chain_step, float *gops
 
 extern "C" pa_status pa_measure_int16x2_peak(float *gops, float *ms_out) {
 	return time_peak(int16x2_peak_kernel, 0x00030003u, 0xFFFBFFFBu, 6.0, gops, ms_out);
+}
+
+extern "C" pa_status pa_measure_f32_peak(float *gops, float *ms_out) {
+	return time_peak(f32_peak_kernel, 0.5f, -0.25f, 3.0, gops, ms_out);
 }
 
 extern "C" pa_status pa_measure_int32_peak(float *gops, float *ms_out) {
