@@ -373,7 +373,9 @@ pa_status pa_path_scores_f64(int32_t type, int32_t locality, int32_t direction, 
 
 /* Device time of the phases of the last solve on this solver, in milliseconds
  * (0: upload, 1: DP kernels, 2: traceback kernels, 3: download), and the number of
- * kernels launched.  Measured with CUDA events on the solver's stream. */
+ * kernels launched.  Measured with CUDA events on the solver's stream.  After a
+ * device-resident paths solve (pa_solve_dense_paths, pa_solve_series_paths), which returns
+ * without waiting, only the DP time is reported, and this call waits for the DP to end. */
 pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel_launches);
 
 /* The DP plan of the last solve on this solver (diagnostic): plan4[0] = kernel family

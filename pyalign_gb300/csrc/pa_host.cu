@@ -339,6 +339,7 @@ struct pa_solver {
 	bool stream_set = false;  // pa_solver_set_stream was called (stream may be NULL then)
 	cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 	float last_ms[4] = {0, 0, 0, 0};
+	bool dp_timing_pending = false;  // a device-resident paths solve: read ev[1] -> ev[2] on demand
 	int32_t last_launches = 0;
 	int32_t last_plan[4] = {0, 0, 0, 0};  // kernel family, G, arithmetic, graph replay
 	int64_t bytes_h2d = 0, bytes_d2h = 0;
@@ -1828,6 +1829,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		// device-resident form: results stay on the device, nothing to wait for here
 		s->last_launches = launches;
 		for (auto &ms : s->last_ms) ms = 0.0f;
+		s->dp_timing_pending = true;  // the DP's phase events, read without a wait here
 		if (out) *out = nullptr;
 		return PA_OK;
 	}
@@ -1887,6 +1889,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	PA_CUDA(cudaEventRecord(s->ev[4], st));
 	PA_CUDA(cudaStreamSynchronize(st));
 	for (int k = 0; k < 4; k++) cudaEventElapsedTime(&s->last_ms[k], s->ev[k], s->ev[k + 1]);
+	s->dp_timing_pending = false;
 	s->last_launches = launches;
 	int32_t status = 0;
 	std::memcpy(&status, hp, 4);
@@ -2141,6 +2144,17 @@ pa_status pa_solver_last_plan(const pa_solver *s, int32_t *plan4) {
 
 pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel_launches) {
 	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
+	if (s->dp_timing_pending) {
+		// a device-resident paths solve returned without waiting: its DP time is read here,
+		// once the DP's end event has completed (the other phases stay 0)
+		pa_solver *m = const_cast<pa_solver *>(s);
+		m->dp_timing_pending = false;
+		if (cudaEventSynchronize(m->ev[2]) != cudaSuccess ||
+		    cudaEventElapsedTime(&m->last_ms[1], m->ev[1], m->ev[2]) != cudaSuccess) {
+			cudaGetLastError();
+			m->last_ms[1] = 0.0f;
+		}
+	}
 	if (ms4)
 		for (int k = 0; k < 4; k++) ms4[k] = s->last_ms[k];
 	if (kernel_launches) *kernel_launches = s->last_launches;
