@@ -632,21 +632,6 @@ def precision_config(torch, pairs, seed, steps=3):
     sc32, rep, scale = ag.path_scores_f64(S, lengths, 0.5, 0.1, "global", "maximize", with_scale=True)
     gotoh_err = error_report(sc32, rep, scale)
 
-    # the same forward with the pairs in ranges: the product of range c + 1 overlaps the DP
-    # of range c on a second stream
-    piped = {}
-    for chunks in (4, 8):
-        ag.similarity_alignment_scores(Es, Et, lengths, 0.5, 0.1, "global", "maximize", chunks=chunks)
-        torch.cuda.synchronize()
-        ev[6].record(stream)
-        for _ in range(steps):
-            sc_p = ag.similarity_alignment_scores(Es, Et, lengths, 0.5, 0.1, "global", "maximize", chunks=chunks)
-        ev[7].record(stream)
-        torch.cuda.synchronize()
-        piped[chunks] = ev[6].elapsed_time(ev[7]) / steps
-    if not torch.equal(sc_p, sc32):
-        raise SystemExit("chunked similarity scores differ from the unchunked ones")
-
     D, _, _ = product(-1.0, 1.0)
     ag._forward_paths(D, lengths, None, "global", "minimize", True)
     torch.cuda.synchronize()
@@ -669,10 +654,6 @@ def precision_config(torch, pairs, seed, steps=3):
                     "out_gbs": 4.0 * cells / t_gemm / 1e9, "status": status},
         "dp_gcups": cells / t_dp / 1e9, "dp_ms": t_dp * 1e3, "total_ms": t_all * 1e3,
         "dp_roofline": dp_roof,
-        "chunked": {"total_ms": {str(k): v for k, v in piped.items()},
-                    "gcups": {str(k): cells / (v / 1e3) / 1e9 for k, v in piped.items()},
-                    "how": "similarity_alignment_scores: the product of one range of pairs overlaps the DP "
-                           "of the previous range on a second stream"},
         "error_vs_fp64_replay": gotoh_err,
         "dtw": {"value": cells / t_dtw / 1e9, "unit": "GCUPS", "ms": t_dtw * 1e3,
                 "error_vs_fp64_replay": dtw_err,

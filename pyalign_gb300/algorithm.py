@@ -567,7 +567,8 @@ class Solver:
         lib().pa_solver_last_timings(self._h, ms, ctypes.byref(n))
         return list(ms), n.value
 
-    KERNELS = ("one-column", "two-column", "stripe-chained", "16-bit twins", "general gaps", "16-bit twins, two-column")
+    KERNELS = ("one-column", "two-column", "stripe-chained", "16-bit twins", "general gaps", "16-bit twins, two-column",
+               "16-bit twins, 4x4 blocks")
 
     def last_plan(self):
         """(kernel family, lanes per pair group, arithmetic, graph replay) of the last solve."""

@@ -185,54 +185,6 @@ def similarity_bf16(Esb, Etb, lengths, out=None, alpha=1.0, beta=0.0):
     return out.transpose(1, 2)
 
 
-_SIDE_STREAMS = {}
-
-
-def similarity_alignment_scores(Es, Et, lengths, gap_open=None, gap_extend=None, locality="global",
-                                direction="maximize", dtw=False, chunks=4):
-    """Forward-only scores of the similarity-matrix form -- S = cos(E_s, E_t) of per-token
-    embeddings on the tensor cores (BF16 factors, FP32 accumulation; DTW: the distance
-    1 - cos from the same epilogue), then the float32 DP -- with the work cut into `chunks`
-    ranges of pairs: the product of range c + 1 runs on the caller's stream while the DP of
-    range c runs on a second stream.  The DP of these short pairs holds only a few warps per
-    SM, so the two kernels share the SMs instead of running one after the other.  Every
-    pair's S and score are those of the unchunked form, bit for bit (each pair's tiles and
-    DP are independent of the others).  Es: (batch, len_s, d), Et: (batch, len_t, d),
-    lengths (batch, 2).  Returns the float32 scores (batch,)."""
-    B, n_s, _ = Es.shape
-    n_t = Et.shape[1]
-    ln = np.asarray(lengths).reshape(B, 2)
-    dev = Es.device
-    main = torch.cuda.current_stream(dev)
-    side = _SIDE_STREAMS.get(dev.index)
-    if side is None:
-        side = _SIDE_STREAMS[dev.index] = torch.cuda.Stream(device=dev)
-    linear = gap_extend is None
-    gap = None if dtw else ((float(gap_open), None) if linear else (float(gap_open), float(gap_extend)))
-    Esb, _ = normalized_bf16(Es, True, ln[:, 0], tiled=True)
-    Etb, _ = normalized_bf16(Et, True, ln[:, 1], tiled=True)
-    St = torch.empty((B, n_t, n_s), dtype=torch.float32, device=dev)
-    scores = torch.empty(B, dtype=torch.float32, device=dev)
-    side.wait_stream(main)
-    chunks = max(1, min(int(chunks), B))
-    for c in range(chunks):
-        k0, k1 = B * c // chunks, B * (c + 1) // chunks
-        if k1 == k0:
-            continue
-        S = similarity_bf16(Esb[k0:k1], Etb[k0:k1], ln[k0:k1], out=St[k0:k1],
-                            alpha=-1.0 if dtw else 1.0, beta=1.0 if dtw else 0.0)
-        ready = torch.cuda.Event()
-        ready.record(main)
-        with torch.cuda.stream(side):
-            side.wait_event(ready)
-            sc, _, _, _, _ = _forward_paths(S, ln[k0:k1], gap, locality, direction, dtw)
-            scores[k0:k1].copy_(sc)
-    main.wait_stream(side)
-    for t in (St, scores, Esb, Etb):
-        t.record_stream(side)
-    return scores
-
-
 def _pad16(E):
     d = E.shape[-1]
     return E if d % 16 == 0 else torch.nn.functional.pad(E, (0, 16 - d % 16))

@@ -870,6 +870,7 @@ struct WalkParams {
 	int32_t G;
 	int32_t cols;   // columns per lane step of the DP that wrote the masks (1: dp_kernel, 2: dp2_kernel)
 	int32_t fmt16;  // 1: nibbles of dp16_kernel (code in bits 2-3, P-open bit 0, Q-open bit 1)
+	int32_t rows4;  // 1: records of dp16b_kernel (4 rows x 4 columns per lane step, cols = 4)
 	const int32_t *status;  // the DP's status: a launch that flagged ST_BAD_CODE has no masks
 	int32_t gap;    // GapKind
 	int32_t local;  // 1: stop at value-0 cells

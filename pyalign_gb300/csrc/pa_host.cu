@@ -383,7 +383,7 @@ struct pa_solver {
 		std::vector<int64_t> user_map_off, user_path_off, dense_off;
 		// the plan and what the downloads need from it
 		int G = 0, C = 1, launches = 0, key_shift = 0, ntickets = 0, nlevels = 0;
-		bool units = false, use_int = false, h16 = false;
+		bool units = false, use_int = false, h16 = false, blk = false;
 		int32_t h_neg = 0;
 		int nchunks = 1;
 		std::vector<int64_t> mask_off, map_off, path_off, val_off;
@@ -453,6 +453,7 @@ struct Plan {
 	int32_t ntickets = 0, nlevels = 0;
 	int C = 1;                 // columns per lane step: 2 = dp2_kernel (int32 tagged, no values)
 	bool h16 = false;          // packed 16-bit twin pairs (dp16_kernel); h_neg is its sentinel
+	bool blk = false;          // with h16: the 4 x 4 block kernel (dp16b_kernel: 4 rows per lane, C = 4)
 	int32_t h_neg = 0;
 	int C32 = 1;               // columns per lane step of the int32/float kernels for this launch
 	int nchunks = 1;           // repeated host-buffer solves: pipeline of this many pair ranges
@@ -542,6 +543,12 @@ uint32_t h16_value(int32_t v) { return uint32_t(uint16_t(v + 32768)) * 0x10001u;
 // a negative addend c as a 32-bit constant: adding it to a biased value always carries out
 // of the low half (the value exceeds -c), so the high half takes c - 1
 uint32_t h16_addk(int32_t c) { return (uint32_t(uint16_t(c - 1)) << 16) | uint32_t(uint16_t(c)); }
+
+// Rows per lane and traceback words per lane step of a plan's DP kernel: 8 rows and C
+// words (one per column) for dp_kernel / dp2_kernel / dp16_kernel, 4 rows and two words (a
+// 4 x 4 block) for dp16b_kernel.
+int plan_rows(const Plan &pl) { return pl.blk ? 4 : R; }
+int plan_words(const Plan &pl) { return pl.blk ? 2 : pl.C; }
 
 // Launches the two-column kernel can run: int32 tagged scoring without all-optimal masks
 // or Solution values.
@@ -864,12 +871,16 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	                      (uint64_t(tb) << 48) | (uint64_t(want_values) << 44) | uint64_t(smem);
 	const bool ch = plan.units;
 	const int cols = (ISINT && plan.C == 2 && tb != TB_ALL && !want_values) ? 2 : 1;
-	const uint64_t ckey = okey | (uint64_t(ch) << 40) | (uint64_t(cols == 2) << 41) | (uint64_t(h16) << 42);
+	const bool blk = h16 && plan.blk;
+	const uint64_t ckey = okey | (uint64_t(ch) << 40) | (uint64_t(cols == 2) << 41) | (uint64_t(h16) << 42) |
+	                      (uint64_t(blk) << 43);
 	for (const auto &kv : s->occ_cache)
 		if (kv.first == ckey) bps = kv.second;
 	if (bps == 0) {
-		if (h16) e = gk == GAP_LINEAR ? occupancy_dp16_linear(loc, tb, cols, smem, &bps)
-		                              : occupancy_dp16_affine(loc, tb, cols, smem, &bps);
+		if (blk) e = gk == GAP_LINEAR ? occupancy_dp16b_linear(loc, tb, smem, &bps)
+		                              : occupancy_dp16b_affine(loc, tb, smem, &bps);
+		else if (h16) e = gk == GAP_LINEAR ? occupancy_dp16_linear(loc, tb, cols, smem, &bps)
+		                                   : occupancy_dp16_affine(loc, tb, cols, smem, &bps);
 		else e = dp_occupancy<V>(gk, ch, loc, tb, want_values, smem, &bps, cols);
 	}
 	PA_CUDA(e);
@@ -904,8 +915,10 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 
 	PA_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(int32_t), st));
 	if constexpr (std::is_same<V, int32_t>::value) {
-		if (h16) e = gk == GAP_LINEAR ? launch_dp16_linear(loc, tb, cols, p, int(grid), smem, st)
-		                              : launch_dp16_affine(loc, tb, cols, p, int(grid), smem, st);
+		if (blk) e = gk == GAP_LINEAR ? launch_dp16b_linear(loc, tb, p, int(grid), smem, st)
+		                              : launch_dp16b_affine(loc, tb, p, int(grid), smem, st);
+		else if (h16) e = gk == GAP_LINEAR ? launch_dp16_linear(loc, tb, cols, p, int(grid), smem, st)
+		                                   : launch_dp16_affine(loc, tb, cols, p, int(grid), smem, st);
 		else e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st, cols);
 	} else {
 		e = dp_launch<V>(gk, ch, loc, tb, want_values, p, int(grid), smem, st, cols);
@@ -1086,6 +1099,7 @@ struct TuneEntry {
 	bool units;
 	bool h16;
 	int C;
+	bool blk;
 };
 std::mutex g_tune_mu;
 std::vector<TuneEntry> g_tune;
@@ -1128,6 +1142,7 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 				plan.G = t.G;
 				plan.units = t.units;
 				plan.h16 = plan.h16 && t.h16;  // the 16-bit kernel still needs this launch's bounds
+				plan.blk = plan.h16 && t.blk;
 				plan.C = plan.h16 ? t.C : plan.C32;
 				return PA_OK;
 			}
@@ -1142,22 +1157,27 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 		int G;
 		bool units, h16;
 		int C;
+		bool blk;
 	};
 	std::vector<Cand> cand;
 	for (int G : {32, 16, 8, 4, 2, 1})
 		if (G == 4 || (int64_t(G) * R <= 2 * plan.max_ls && (G >= 4 || plan.max_ls <= 256))) {
-			cand.push_back({G, false, false, C0});
+			cand.push_back({G, false, false, C0, false});
 			if (plan.h16) {
-				cand.push_back({G, false, true, 1});
-				if (C0 == 2) cand.push_back({G, false, true, 2});
+				cand.push_back({G, false, true, 1, false});
+				if (C0 == 2) cand.push_back({G, false, true, 2, false});
 			}
 		}
-	if (plan.max_ls > 2 * 32 * R) cand.push_back({32, true, false, C0});
+	// the 16-bit 4 x 4 block kernel (stripes of 4 G rows: the tile height 4 instead of 8)
+	if (plan.h16 && C0 == 2)
+		for (int G : {32, 16, 8})
+			if (int64_t(G) * 4 <= 2 * plan.max_ls) cand.push_back({G, false, true, 4, true});
+	if (plan.max_ls > 2 * 32 * R) cand.push_back({32, true, false, C0, false});
 	if (cand.size() < 2) return PA_OK;
 	cudaStream_t st = s->stream;
 	float best = INFINITY;
 	int bestG = plan.G, bestC = plan.C;
-	bool bestU = plan.units, bestH = plan.h16;
+	bool bestU = plan.units, bestH = plan.h16, bestB = plan.blk;
 	// one untimed run first (clocks and caches leave their idle state), then each candidate
 	// timed twice, keeping its faster run: a single cold timing could misplace a candidate
 	for (size_t ci = 0; ci <= cand.size(); ci++) {
@@ -1167,6 +1187,7 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 		pl.units = c.units;
 		pl.h16 = c.h16;
 		pl.C = c.C;
+		pl.blk = c.blk;
 		if (pa_status e = stage(pl)) return e;
 		float ms = INFINITY;
 		for (int rep = 0; rep < (ci == 0 ? 1 : 2); rep++) {
@@ -1185,14 +1206,16 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 			bestU = pl.units;
 			bestH = pl.h16;
 			bestC = pl.C;
+			bestB = pl.blk;
 		}
 	}
 	plan.G = bestG;
 	plan.units = bestU;
 	plan.h16 = bestH;
 	plan.C = bestC;
+	plan.blk = bestB;
 	std::lock_guard<std::mutex> lk(g_tune_mu);
-	if (g_tune.size() < 4096) g_tune.push_back({key, bestG, bestU, bestH, bestC});
+	if (g_tune.size() < 4096) g_tune.push_back({key, bestG, bestU, bestH, bestC, bestB});
 	return PA_OK;
 }
 
@@ -1384,6 +1407,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		plan.h16 = !plan.units && h16_plan(s, in, host_table.data(), ls, lt, tb, want_values, use_int, &hneg);
 		plan.h_neg = hneg;
 		if (plan.h16) plan.C = plan.C32;  // two columns per step unless PA_DP_COLS=1
+		if (const char *e = std::getenv("PA_DP_BLOCK"))  // experiments and tests: the 4 x 4 block kernel
+			if (plan.h16 && std::strcmp(e, "1") == 0) {
+				plan.blk = true;
+				plan.C = 4;
+			}
 	}
 	std::vector<int32_t> order, level_start;
 	std::vector<int64_t> mask_off, map_off, path_off, val_off, dense_off;
@@ -1407,7 +1435,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		// order[k0, k1) for its pair indices [k0, k1))
 		order.assign(size_t(B), 0);
 		{
-			const int64_t rpp = int64_t(plan.G) * R;
+			const int64_t rpp = int64_t(plan.G) * plan_rows(plan);
 			const int64_t kt = max_lt + 1;
 			const int64_t nkeys = ((max_ls + rpp - 1) / rpp + 1) * kt;
 			std::vector<int32_t> count(size_t(nkeys) + 1);
@@ -1453,12 +1481,12 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		path_off.assign(size_t(B) + 1, 0);
 		val_off.assign(size_t(B) + 1, 0);
 		dense_off.assign(size_t(B), 0);
-		const int rpp = plan.G * R;
+		const int rpp = plan.G * plan_rows(plan);
 		for (int64_t k = 0; k < B; k++) {
 			const int64_t a = ls[size_t(k)], b = lt[size_t(k)];
 			const int64_t npass = (a == 0 || b == 0) ? 0 : (a + rpp - 1) / rpp;
-			const int64_t steps = plan.C == 2 ? (b + 1) / 2 + plan.G - 1 : b + plan.G - 1;
-			mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * steps * plan.G * plan.C;
+			const int64_t steps = (b + plan.C - 1) / plan.C + plan.G - 1;
+			mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * steps * plan.G * plan_words(plan);
 			map_off[size_t(k) + 1] = map_off[size_t(k)] + std::min(a, b);
 			path_off[size_t(k) + 1] = path_off[size_t(k)] + 2 * (a + b + 2);
 			val_off[size_t(k) + 1] = val_off[size_t(k)] + int64_t(res.layers) * (a + 1) * (b + 1);
@@ -1542,6 +1570,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		w.G = plan.G;
 		w.cols = plan.C;
 		w.fmt16 = plan.h16 ? 1 : 0;
+		w.rows4 = plan.blk ? 1 : 0;
 		w.status = s->d_status.as<int32_t>();
 		w.gap = s->gap;
 		w.local = s->loc == LOC_LOCAL;
@@ -1700,6 +1729,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		plan.G = r.G;
 		plan.C = r.C;
 		plan.h16 = r.h16;
+		plan.blk = r.blk;
 		plan.h_neg = r.h_neg;
 		plan.nchunks = r.nchunks;
 		plan.units = r.units;
@@ -1766,7 +1796,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		if (pa_status e = device_work(st, true)) return e;
 	}
 	res.G = plan.G;
-	s->last_plan[0] = s->gap == GAP_GENERAL ? 4 : plan.h16 ? (plan.C == 2 ? 5 : 3) : plan.units ? 2 : plan.C == 2 ? 1 : 0;
+	s->last_plan[0] = s->gap == GAP_GENERAL ? 4
+	                  : plan.h16  ? (plan.blk ? 6 : plan.C == 2 ? 5 : 3)
+	                  : plan.units ? 2
+	                  : plan.C == 2 ? 1
+	                               : 0;
 	s->last_plan[1] = plan.G;
 	s->last_plan[2] = plan.h16 ? 2 : plan.use_int ? 1 : 0;
 	s->last_plan[3] = hit && s->rep.exec ? 1 : 0;
@@ -1811,6 +1845,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		r.G = plan.G;
 		r.C = plan.C;
 		r.h16 = plan.h16;
+		r.blk = plan.blk;
 		r.h_neg = plan.h_neg;
 		r.nchunks = plan.nchunks;
 		r.units = plan.units;

@@ -39,4 +39,12 @@ PA_DECL16(linear)
 PA_DECL16(affine)
 #undef PA_DECL16
 
+#define PA_DECL16B(GAP)                                                                                 \
+	cudaError_t launch_dp16b_##GAP(int loc, int tb, const DpParams<int32_t> &p, int grid, size_t smem,  \
+	                               cudaStream_t st);                                                 \
+	cudaError_t occupancy_dp16b_##GAP(int loc, int tb, size_t smem, int *blocks_per_sm);
+PA_DECL16B(linear)
+PA_DECL16B(affine)
+#undef PA_DECL16B
+
 }  // namespace pa

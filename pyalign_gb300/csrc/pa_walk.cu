@@ -48,7 +48,9 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) walk_kernel(WalkParams p) {
 	const int G = p.G;
 	const bool two = p.cols == 2;  // dp2_kernel layout: a uint2 per lane and step, columns j, j + 1
 	const bool fmt16 = p.fmt16 != 0;
-	const int S = two ? ((lt + 1) >> 1) + G - 1 : lt + G - 1;
+	const bool rows4 = p.rows4 != 0;  // dp16b_kernel records: 4-row lanes, 4 columns per step
+	const int S = rows4 ? ((lt + 3) >> 2) + G - 1 : two ? ((lt + 1) >> 1) + G - 1 : lt + G - 1;
+	const int npass4 = rows4 ? (ls + 4 * G - 1) / (4 * G) : 0;  // stripes of the 4-row layout
 	const bool s2t = ls <= lt;
 	const bool affine = p.gap == GAP_AFFINE;
 	int ub = -1000000, vb = -1000000;  // window: row blocks ub-3..ub, columns vb-31..vb
@@ -63,9 +65,24 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) walk_kernel(WalkParams p) {
 			const int rb = ub - r;
 			w[r] = 0u;
 			if (rb >= 0 && col >= 0) {
-				const int q = rb / G, sb = rb - q * G;
-				w[r] = two ? W[((int64_t(q) * S + ((col >> 1) + sb)) * G + sb) * 2 + (col & 1)]
-				           : W[(int64_t(q) * S + (col + sb)) * G + sb];
+				if (rows4) {
+					// the 8-row word of column col joins the 16-bit columns of the 4-row lanes
+					// 2 rb (rows 0-3: high half) and 2 rb + 1 (rows 4-7: low half)
+					uint32_t h[2] = {0u, 0u};
+#pragma unroll
+					for (int e = 0; e < 2; e++) {
+						const int b4 = 2 * rb + e, q = b4 / G, sb = b4 - q * G;
+						if (q < npass4) {
+							const uint32_t word = W[((int64_t(q) * S + ((col >> 2) + sb)) * G + sb) * 2 + ((col >> 1) & 1)];
+							h[e] = (word >> (16 * (col & 1))) & 0xffffu;
+						}
+					}
+					w[r] = (h[0] << 16) | h[1];
+				} else {
+					const int q = rb / G, sb = rb - q * G;
+					w[r] = two ? W[((int64_t(q) * S + ((col >> 1) + sb)) * G + sb) * 2 + (col & 1)]
+					           : W[(int64_t(q) * S + (col + sb)) * G + sb];
+				}
 			}
 		}
 		__syncwarp();  // every lane is done reading the previous window

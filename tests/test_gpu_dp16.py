@@ -21,7 +21,7 @@ from _cases import Gap, call, compare, options, pack, random_pairs
 pytestmark = pytest.mark.gpu
 
 GAPS = {"linear": Gap("linear", 2.0), "affine": Gap("affine", 5.0, 2.0)}
-TWINS = {"1": "16-bit twins", "2": "16-bit twins, two-column"}
+TWINS = {"1": "16-bit twins", "2": "16-bit twins, two-column", "blk": "16-bit twins, 4x4 blocks"}
 
 
 @pytest.fixture(scope="module")
@@ -41,11 +41,13 @@ def analytic(monkeypatch):
     monkeypatch.setenv("PA_DP_MODE", "groups")
 
 
-@pytest.fixture(params=["1", "2"])
+@pytest.fixture(params=["1", "2", "blk"])
 def cols(request, monkeypatch):
-    """One or two columns per lane step."""
+    """One or two columns per lane step of 8 rows, or 4 x 4 blocks (4 rows, 4 columns)."""
     if request.param == "1":
         monkeypatch.setenv("PA_DP_COLS", "1")
+    if request.param == "blk":
+        monkeypatch.setenv("PA_DP_BLOCK", "1")
     return request.param
 
 
@@ -187,7 +189,7 @@ def test_dp16_bad_codes_then_valid(analytic, gpu_alg, oracle_alg):
     assert d is None, d
 
 
-@pytest.mark.parametrize("plan", ["twins-G16", "own"])
+@pytest.mark.parametrize("plan", ["twins-G16", "blocks-G8", "blocks-G16", "own"])
 def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg, monkeypatch, plan):
     """4,096 pairs drawn like the batched workload (DNA, |s|, |t| ~ U[100, 1000], half of them
     a query and a 10%-mutated copy; local affine 5/2, +2/-3; score + one traceback) against
@@ -195,15 +197,19 @@ def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg, monkeypatch, p
     workload's plan (the 16-bit twin kernel, two columns per step, G = 16) and with the
     plan the solver picks for this bag on its own."""
     import bench
-    if plan == "twins-G16":
-        monkeypatch.setenv("PA_GROUP_WIDTH", "16")
+    if plan != "own":
+        monkeypatch.setenv("PA_GROUP_WIDTH", plan.split("-G")[1])
+    if plan.startswith("blocks"):
+        monkeypatch.setenv("PA_DP_BLOCK", "1")
     a, b, ls, lt, table = bench.make_workload(4096, 4242)
     n = a.shape[0]
     opts = dict(options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"]), batch_size=n, batch=True)
     solver = gpu_alg.m16.create_solver(a.shape[1], b.shape[1], gpu_alg.m16.create_options(opts))
     res = solver.solve_indexed_for_alignment(a, b, table, np.stack([ls, lt]).astype(np.uint16))
-    if plan == "twins-G16":
-        assert solver.last_plan()["kernel"] == TWINS["2"] and solver.last_plan()["G"] == 16, solver.last_plan()
+    if plan != "own":
+        want = TWINS["blk"] if plan.startswith("blocks") else TWINS["2"]
+        assert solver.last_plan()["kernel"] == want and solver.last_plan()["G"] == int(plan.split("-G")[1]), \
+            solver.last_plan()
     osol = oracle_alg.m16.create_solver(a.shape[1], b.shape[1], oracle_alg.m16.create_options(opts))
     osc, omp, offs, _ = oracle_alg.batch_alignments(osol, a, b, table, ls, lt)
     bad = []

@@ -115,6 +115,39 @@ def test_repeated_batch_solves(env, monkeypatch):
     assert np.array_equal(got[0], want3[0]) and np.array_equal(got[1], want3[1])
 
 
+@pytest.mark.parametrize("G", ["1", "8", "16"])
+def test_repeated_block_kernel_solves(env, monkeypatch, G):
+    """Repeats and graph replays of a plan on the 4 x 4 block kernel keep that kernel (and its
+    traceback layout) on every repetition, with the results of an uncached solve."""
+    torch, alg, ag = env
+    monkeypatch.setenv("PA_DP_BLOCK", "1")
+    monkeypatch.setenv("PA_GROUP_WIDTH", G)
+    rng = np.random.default_rng(50 + int(G))
+    n, n_s, n_t = 301, 260, 270
+    ln = np.stack([rng.integers(1, n_s + 1, n), rng.integers(1, n_t + 1, n)]).astype(np.int32)
+    a = rng.integers(0, 4, size=(n, n_s)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, n_t)).astype(np.uint32)
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    a_d = torch.from_numpy(a.view(np.int32)).cuda()
+    b_d = torch.from_numpy(b.view(np.int32)).cuda()
+    t_d = torch.from_numpy(table).cuda()
+    sc = torch.empty(n, device="cuda")
+    mp = torch.empty(int(np.minimum(ln[0], ln[1]).sum()), dtype=torch.int32, device="cuda")
+    sc_r, mp_r = torch.empty_like(sc), torch.empty_like(mp)
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    ref_solver = _batch_solver(alg, torch, n, n_s, n_t)
+    want = _solve_batch(alg, torch, ref_solver, a_d, b_d, t_d, ln, sc_r, mp_r)
+    assert ref_solver.last_plan()["kernel"] == "16-bit twins, 4x4 blocks", ref_solver.last_plan()
+    monkeypatch.delenv("PA_GRAPHS")
+    solver = _batch_solver(alg, torch, n, n_s, n_t)
+    for rep in range(4):  # planned, cached plan + captured graph, graph, graph
+        got = _solve_batch(alg, torch, solver, a_d, b_d, t_d, ln, sc, mp)
+        plan = solver.last_plan()
+        assert plan["kernel"] == "16-bit twins, 4x4 blocks" and plan["G"] == int(G), (rep, plan)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), rep
+
+
 def test_repeated_dense_paths_and_gradients(env, monkeypatch):
     """The autograd front end (pa_solve_dense_paths): repeated forward + backward on one
     similarity buffer whose contents change in place."""

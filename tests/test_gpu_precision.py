@@ -185,31 +185,3 @@ def test_precision_report_at_size(env):
     print(f"dtw: max rel |score| {drel.max():.3e}")
     assert drel.max() <= 1e-5, drel.max()
 
-
-@pytest.mark.parametrize("dtw", [False, True])
-def test_chunked_similarity_scores_equal_unchunked(env, dtw):
-    """similarity_alignment_scores (product of one range of pairs overlapping the DP of the
-    previous range on a second stream) gives the unchunked scores bit for bit, for any
-    number of ranges."""
-    torch, ag, _, _ = env
-    rng = np.random.default_rng(1046)
-    B, n, d = 300, 320, 256
-    lengths = rng.integers(1, n + 1, size=(B, 2))
-    g = torch.Generator(device="cuda").manual_seed(1046)
-    Es = torch.randn(B, n, d, device="cuda", generator=g)
-    Et = torch.randn(B, n, d, device="cuda", generator=g)
-    Esb, _ = ag.normalized_bf16(Es, True, lengths[:, 0], tiled=True)
-    Etb, _ = ag.normalized_bf16(Et, True, lengths[:, 1], tiled=True)
-    S = ag.similarity_bf16(Esb, Etb, lengths, alpha=-1.0 if dtw else 1.0, beta=1.0 if dtw else 0.0)
-    if dtw:
-        want, _, _, _, _ = ag._forward_paths(S, lengths, None, "global", "minimize", True)
-    else:
-        want, _, _, _, _ = ag._forward_paths(S, lengths, (OPEN, EXT), "global", "maximize", False)
-    for chunks in (1, 3, 7):
-        if dtw:
-            got = ag.similarity_alignment_scores(Es, Et, lengths, locality="global", direction="minimize", dtw=True,
-                                                 chunks=chunks)
-        else:
-            got = ag.similarity_alignment_scores(Es, Et, lengths, OPEN, EXT, "global", "maximize", chunks=chunks)
-        torch.cuda.synchronize()
-        assert torch.equal(got, want), (chunks, (got != want).nonzero()[:5])
