@@ -2643,7 +2643,9 @@ namespace pa {
 cudaError_t path_count_solve(int32_t npairs, int32_t G, int32_t local, int32_t affine, const int32_t *len_s,
                              const int32_t *len_t, const int64_t *mask_off, const void *masks, const int32_t *seed,
                              unsigned long long *counts, unsigned long long *scratch, int64_t scratch_stride,
-                             int32_t *work_counter, int grid, cudaStream_t st);
+                             int32_t *work_counter, int grid, cudaStream_t st, int32_t ntickets,
+                             int32_t nlevels, const int32_t *level_start, const int32_t *order, int32_t *progress,
+                             int32_t *status, unsigned long long *partial);
 }  // namespace pa
 
 extern "C" {
@@ -2672,29 +2674,90 @@ pa_status pa_result_path_counts(const pa_result *r, uint64_t *counts) {
 		int dev = 0, sms = 1;
 		PA_CUDA(cudaGetDevice(&dev));
 		PA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-		const int gpw = 32 / d.G;
-		const int64_t warps = (B + gpw - 1) / gpw;
-		const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(int64_t(sms) * 8, (warps + WARPS - 1) / WARPS));
-		const int64_t slots = grid * WARPS * gpw;
-		const int64_t stride = 4 * max_lt;
-		DevBuf dl, dm, dseed, dcnt, dscr, dctr;
+		DevBuf dl, dm, dseed, dcnt, dscr, dctr, dord, dlev, dprog, dpart, dstat;
 		PA_CUDA(dl.ensure(size_t(2 * B) * 4));
 		PA_CUDA(dm.ensure(size_t(B) * 8));
 		PA_CUDA(dseed.ensure(size_t(2 * B) * 4));
 		PA_CUDA(dcnt.ensure(size_t(B) * 8));
-		PA_CUDA(dscr.ensure(size_t(slots * stride) * 8));
 		PA_CUDA(dctr.ensure(4));
 		PA_CUDA(cudaMemcpy(dl.p, d.ls.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
 		PA_CUDA(cudaMemcpy(dl.as<int32_t>() + B, d.lt.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
 		PA_CUDA(cudaMemcpy(dm.p, d.mask_off.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
 		PA_CUDA(cudaMemcpy(dseed.p, seed.data(), size_t(2 * B) * 4, cudaMemcpyHostToDevice));
 		PA_CUDA(cudaMemset(dctr.p, 0, 4));
-		PA_CUDA(pa::path_count_solve(int32_t(B), d.G, local ? 1 : 0, d.gap == GAP_AFFINE ? 1 : 0, dl.as<int32_t>(),
-		                             dl.as<int32_t>() + B, dm.as<int64_t>(), d.dev_masks_all, dseed.as<int32_t>(),
-		                             dcnt.as<unsigned long long>(), dscr.as<unsigned long long>(), stride,
-		                             dctr.as<int32_t>(), int(grid), nullptr));
+		// few long pairs written with G = 32: a warp per 256-row stripe, stripes chained
+		const int64_t rpp32 = 32 * R;
+		int64_t max_np = 0;
+		for (int64_t k = 0; k < B; k++)
+			if (d.ls[size_t(k)] > 0 && d.lt[size_t(k)] > 0)
+				max_np = std::max<int64_t>(max_np, (d.ls[size_t(k)] + rpp32 - 1) / rpp32);
+		bool chain = d.G == 32 && max_np >= 3;
+		if (const char *e = std::getenv("PA_COUNT_MODE"))  // tests: "group" or "chain" (G = 32 only)
+			chain = std::strcmp(e, "chain") == 0 ? d.G == 32 : std::strcmp(e, "group") == 0 ? false : chain;
 		std::vector<uint64_t> c(static_cast<size_t>(B), 0);
-		PA_CUDA(cudaMemcpy(c.data(), dcnt.p, size_t(B) * 8, cudaMemcpyDeviceToHost));
+		if (chain) {
+			// tickets stripe-major: level q holds stripe q of every pair with more than q stripes
+			// (an empty pair counts as one), the pairs with the most stripes first
+			std::vector<int32_t> np(static_cast<size_t>(B)), order(static_cast<size_t>(B)), rank(static_cast<size_t>(B));
+			for (int64_t k = 0; k < B; k++) {
+				const int64_t a = d.ls[size_t(k)], b = d.lt[size_t(k)];
+				np[size_t(k)] = int32_t(std::max<int64_t>(1, (a == 0 || b == 0) ? 1 : (a + rpp32 - 1) / rpp32));
+				order[size_t(k)] = int32_t(k);
+			}
+			std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return np[size_t(x)] > np[size_t(y)]; });
+			for (int64_t w = 0; w < B; w++) rank[size_t(order[size_t(w)])] = int32_t(w);
+			const int64_t nlev = np[size_t(order[0])];
+			std::vector<int32_t> level_start(static_cast<size_t>(nlev) + 1, 0);
+			for (int64_t q = 0; q < nlev; q++) {
+				int64_t above = 0;  // pairs with more than q stripes
+				for (int64_t k = 0; k < B; k++) above += np[size_t(k)] > q;
+				level_start[size_t(q) + 1] = int32_t(level_start[size_t(q)] + above);
+			}
+			const int64_t nt = level_start.back();
+			const int64_t stride = 4 * max_lt;
+			PA_CUDA(dord.ensure(size_t(B) * 4));
+			PA_CUDA(dlev.ensure(level_start.size() * 4));
+			PA_CUDA(dprog.ensure(size_t(nt) * 4));
+			PA_CUDA(dpart.ensure(size_t(nt) * 8));
+			PA_CUDA(dstat.ensure(4));
+			PA_CUDA(dscr.ensure(size_t(B * stride) * 8));
+			PA_CUDA(cudaMemcpy(dord.p, order.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+			PA_CUDA(cudaMemcpy(dlev.p, level_start.data(), level_start.size() * 4, cudaMemcpyHostToDevice));
+			PA_CUDA(cudaMemset(dprog.p, 0, size_t(nt) * 4));
+			PA_CUDA(cudaMemset(dstat.p, 0, 4));
+			const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(int64_t(sms) * 4, (nt + WARPS - 1) / WARPS));
+			PA_CUDA(pa::path_count_solve(int32_t(B), 32, local ? 1 : 0, d.gap == GAP_AFFINE ? 1 : 0, dl.as<int32_t>(),
+			                             dl.as<int32_t>() + B, dm.as<int64_t>(), d.dev_masks_all, dseed.as<int32_t>(),
+			                             dcnt.as<unsigned long long>(), dscr.as<unsigned long long>(), stride,
+			                             dctr.as<int32_t>(), int(grid), nullptr, int32_t(nt), int32_t(nlev),
+			                             dlev.as<int32_t>(), dord.as<int32_t>(), dprog.as<int32_t>(),
+			                             dstat.as<int32_t>(), dpart.as<unsigned long long>()));
+			std::vector<uint64_t> part(static_cast<size_t>(nt));
+			int32_t status = 0;
+			PA_CUDA(cudaMemcpy(part.data(), dpart.p, size_t(nt) * 8, cudaMemcpyDeviceToHost));
+			PA_CUDA(cudaMemcpy(&status, dstat.p, 4, cudaMemcpyDeviceToHost));
+			if (status & ST_TIMEOUT)
+				return fail(PA_ERR_TIMEOUT, "a chained stripe of the path count timed out waiting for the stripe above it");
+			for (int64_t k = 0; k < B; k++)
+				for (int32_t q = 0; q < np[size_t(k)]; q++) {
+					const uint64_t x = part[size_t(level_start[size_t(q)] + rank[size_t(k)])];
+					const uint64_t y = c[size_t(k)] + x;
+					c[size_t(k)] = y < x ? ~uint64_t(0) : y;
+				}
+		} else {
+			const int gpw = 32 / d.G;
+			const int64_t warps = (B + gpw - 1) / gpw;
+			const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(int64_t(sms) * 8, (warps + WARPS - 1) / WARPS));
+			const int64_t slots = grid * WARPS * gpw;
+			const int64_t stride = 4 * max_lt;
+			PA_CUDA(dscr.ensure(size_t(slots * stride) * 8));
+			PA_CUDA(pa::path_count_solve(int32_t(B), d.G, local ? 1 : 0, d.gap == GAP_AFFINE ? 1 : 0, dl.as<int32_t>(),
+			                             dl.as<int32_t>() + B, dm.as<int64_t>(), d.dev_masks_all, dseed.as<int32_t>(),
+			                             dcnt.as<unsigned long long>(), dscr.as<unsigned long long>(), stride,
+			                             dctr.as<int32_t>(), int(grid), nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr,
+			                             nullptr));
+			PA_CUDA(cudaMemcpy(c.data(), dcnt.p, size_t(B) * 8, cudaMemcpyDeviceToHost));
+		}
 		for (int64_t k = 0; k < B; k++) {
 			const int ls = d.ls[size_t(k)], lt = d.lt[size_t(k)];
 			if (local) {

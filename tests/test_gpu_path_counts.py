@@ -84,3 +84,36 @@ def test_path_counts_equal_enumeration(monkeypatch, gpu_alg, oracle_alg, localit
     assert compared >= n // 2
     if locality == "local":
         assert counts[2] == 0  # optimum 0: no seed
+
+
+@pytest.mark.parametrize("count_mode", ["chain", "group"])
+def test_path_counts_of_multi_stripe_pairs(monkeypatch, gpu_alg, oracle_alg, count_mode):
+    """Pairs of 513-800 rows (three or four 256-row stripes of the stripe-chained layout): the
+    count with a warp per stripe, stripes chained (and, for comparison, a group per pair)
+    equals the oracle's enumeration.  A continuous score table keeps ties -- and so the
+    enumerations -- small."""
+    monkeypatch.setenv("PA_DP_MODE", "units")
+    monkeypatch.setenv("PA_COUNT_MODE", count_mode)
+    rng = np.random.default_rng(6161)
+    n = 12
+    pairs = [(rng.integers(0, 3, size=int(rng.integers(513, 801))).astype(np.uint32),
+              rng.integers(0, 3, size=int(rng.integers(20, 61))).astype(np.uint32)) for _ in range(n)]
+    pairs[0] = (pairs[0][0], pairs[0][1][:0])   # empty t
+    a, b, ln = pack(pairs, n)
+    table = np.round(rng.normal(size=(3, 3)), 1).astype(np.float32)
+    for locality, gap in (("global", Gap("affine", 2.0, 0.5)), ("local", Gap("affine", 2.0, 0.5)),
+                          ("semiglobal", Gap("linear", 1.0))):
+        o = dict(options(gpu_alg, locality=locality, count="all", gap=gap, return_dup=True), batch_size=n, batch=True)
+        cap = (a.shape[1], b.shape[1])
+        gs = gpu_alg.m16.create_solver(*cap, gpu_alg.m16.create_options(o))
+        its = gs.solve_indexed_for_alignment_iterator(a, b, table, ln)
+        assert gs.last_plan()["kernel"] == "stripe-chained", gs.last_plan()
+        counts = [it.path_count() for it in its]
+        os_ = oracle_alg.m16.create_solver(*cap, oracle_alg.m16.create_options(o))
+        oits = os_.solve_indexed_for_alignment_iterator(a, b, table, ln)
+        for k in range(n):
+            want = _count(oits[k])
+            if want > CAP:
+                assert counts[k] > CAP, (locality, k, counts[k])
+            else:
+                assert counts[k] == want, (locality, k, counts[k], want)
