@@ -291,6 +291,23 @@ def make_semiglobal_long(seed, pairs=256, ls=5000, lt=10000):
     return a, b, np.full(pairs, ls, np.int32), np.full(pairs, lt, np.int32), m.astype(np.float32)
 
 
+class LogGap:
+    """pyalign.gaps.LogarithmicGapCost(u, v) (w(k) = u + v ln k, gaps.py:195-225) as seen by the
+    native module: a general cost vector."""
+
+    def __init__(self, u, v):
+        self.u, self.v = u, v
+
+    def to_special_case(self):
+        return {}
+
+    def costs(self, n):
+        w = np.full((n,), self.u, dtype=np.float32)
+        w[1:] += self.v * np.log(np.arange(1, n), dtype=np.float32)
+        w[0] = 0
+        return w
+
+
 class LinearGap:
     """pyalign.gaps.LinearGapCost(g) as seen by the native module (gaps.py:120-160)."""
 
@@ -374,6 +391,37 @@ def other_configs(torch, alg, L, seed):
     out["semiglobal_affine_5000x10000_score"] = dict(
         r3, parity=parity_of(n3, osc3, None, sc3, None),
         workload="256 pairs of 5000 x 10000, 20 letters, semiglobal affine 10/1, score only")
+    # general (logarithmic) gap costs, O(|s| |t| (|s| + |t|)): 64 pairs of 300 x 300 DNA, local,
+    # score + one alignment through the native module; the first pairs against the oracle
+    rw = np.random.default_rng(seed + 3)
+    Bw, Lw = 64, 300
+    aw = rw.integers(0, 4, size=(Bw, Lw)).astype(np.uint32)
+    bw = aw.copy()
+    mut = rw.random(size=(Bw, Lw)) < 0.15
+    bw[mut] = rw.integers(0, 4, size=int(mut.sum()))
+    tw = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(tw, 2.0)
+    lnw = np.full((2, Bw), Lw, np.uint16)
+    ow = opts(alg, "LOCAL", "ALIGNMENT", LogGap(3.0, 1.0), Bw)
+    sw = alg.m16.create_solver(Lw, Lw, alg.m16.create_options(ow))
+    resw = sw.solve_indexed_for_alignment(aw, bw, tw, lnw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    resw = sw.solve_indexed_for_alignment(aw, bw, tw, lnw)
+    t_w = time.perf_counter() - t0
+    kw = 4
+    osw = oracle_solver(oalg, "LOCAL", "ALIGNMENT", LogGap(3.0, 1.0), Lw, Lw)
+    osc_w, omp_w, offs_w, _ = oalg.batch_alignments(osw, aw[:kw], bw[:kw], tw, np.full(kw, Lw), np.full(kw, Lw))
+    gsc_w = np.array([resw[k].score for k in range(kw)], np.float32)
+    gmp_w = np.concatenate([np.asarray(resw[k].s_to_t, np.int32) for k in range(kw)])
+    cells_w = float(Bw * Lw * Lw)
+    out["local_log_gap_300x300"] = {
+        "value": cells_w / t_w / 1e9, "unit": "GCUPS", "ms": t_w * 1000,
+        "candidates_per_s": cells_w * (2 * Lw) / t_w, "plan": sw.last_plan(),
+        "parity": parity_of(kw, osc_w, omp_w, gsc_w, gmp_w),
+        "workload": "64 pairs of 300 x 300 DNA (a query and a 15%-substituted copy), local, general gap "
+                    "3 + ln k, score + one alignment, host arrays through the native module"}
+
     # all-optimal codomain on the whole bag through the native module's iterator form:
     # one solve writes the 16-bit all-optimal masks of all 256 pairs (25.6 GB, left on the
     # device), the co-optimal path counts of every pair are computed on the device, and the

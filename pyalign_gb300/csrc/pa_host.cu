@@ -346,7 +346,7 @@ struct pa_solver {
 
 	DevBuf d_a, d_b, d_tab, d_dense, d_dense_off, d_ls, d_lt, d_order, d_mask_off, d_score, d_seed, d_has,
 	    d_masks, d_scratch, d_counter, d_status, d_border, d_maps, d_map_off, d_paths, d_path_off,
-	    d_path_len, d_vals, d_val_off, d_best, d_gen, d_wsb_off, d_wsb_tb, d_wsb_vals, d_wsb_sub,
+	    d_path_len, d_vals, d_val_off, d_best, d_gen, d_wsb_off, d_wsb_tb, d_wsb_vals, d_wsb_vals_t, d_wsb_sub,
 	    d_wsb_sub_off, d_codes_max, d_progress, d_chain;
 	PinBuf h_stage, h_out;
 	// per-call pair metadata, staged in one pinned buffer and sent with one copy
@@ -1015,6 +1015,7 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	PA_CUDA(s->d_wsb_sub_off.ensure(toff.size() * 8));
 	PA_CUDA(pa_copy(s, s->d_wsb_sub_off.p, toff.data(), toff.size() * 8, cudaMemcpyHostToDevice, st));
 	PA_CUDA(s->d_wsb_vals.ensure(size_t(voff[size_t(B)]) * 4));
+	PA_CUDA(s->d_wsb_vals_t.ensure(size_t(voff[size_t(B)]) * 4));
 	PA_CUDA(s->d_wsb_tb.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
 	PA_CUDA(s->d_wsb_sub.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
 	std::vector<float> tab;
@@ -1052,6 +1053,7 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	w.gap_s = g + ns + nt;
 	w.gap_t = g + 2 * ns + nt;
 	w.vals = s->d_wsb_vals.as<float>();
+	w.vals_t = s->d_wsb_vals_t.as<float>();
 	w.vals_off = s->d_wsb_off.as<int64_t>();
 	w.tb = s->d_wsb_tb.as<int32_t>();
 	w.tb_off = s->d_wsb_sub_off.as<int64_t>();

@@ -25,6 +25,7 @@ struct WsbParams {
 	const float *left_D;   // normalised borders, index i+1 for row i
 	const float *top_D;
 	float *vals;           // normalised D, (ls+1) x (lt+1) per pair at vals_off
+	float *vals_t;         // the same values transposed, (lt+1) x (ls+1): the row scans read it
 	const int64_t *vals_off;
 	int32_t *tb;           // ls x lt traceback codes per pair at tb_off: kind | (k+1) << 2
 	const int64_t *tb_off;
