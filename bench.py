@@ -57,7 +57,12 @@ def parse():
                     help="pairs of 5000 x 10000 in the all-optimal measurement of the long-pair workload")
     ap.add_argument("--plain", type=int, default=1,
                     help="also time the plain GPU path: one launch per 100-wide length bucket (0: skip)")
-    return ap.parse_args()
+    ap.add_argument("--plain-pairs", type=int, default=None,
+                    help="earlier spelling of --plain (0 skips the plain path)")
+    args = ap.parse_args()
+    if args.plain_pairs is not None:
+        args.plain = int(args.plain_pairs != 0)
+    return args
 
 
 # --------------------------------------------------------------------------- workload

@@ -381,10 +381,16 @@ pa_status pa_solver_last_timings(const pa_solver *s, float *ms4, int32_t *kernel
 /* The DP plan of the last solve on this solver (diagnostic): plan4[0] = kernel family
  * (0: one column per lane step, 1: two columns per lane step, 2: stripe-chained, 3: packed
  * 16-bit twin pairs, one column per step, 4: general gap costs, 5: packed 16-bit twin pairs,
- * two columns per step), plan4[1] = lanes per pair group G, plan4[2] =
- * arithmetic (0: float32, 1: int32, 2: packed int16), plan4[3] = 1 when the solve ran as a
- * replayed CUDA graph.  No counterpart in the reference. */
+ * two columns per step, 6: packed 16-bit twin pairs on 4 x 4 blocks), plan4[1] = lanes per
+ * pair group G, plan4[2] = arithmetic (0: float32, 1: int32, 2: packed int16), plan4[3] = 1
+ * when the solve ran as a replayed CUDA graph.  No counterpart in the reference. */
 pa_status pa_solver_last_plan(const pa_solver *s, int32_t *plan4);
+
+/* The group width per length bucket of |s| (widths4[0..3] for |s| <= 128, <= 256, <= 512 and
+ * longer) of the last solve on this solver, when its 16-bit twin launch gave each bucket a
+ * width of its own; all four 0 when one width G (pa_solver_last_plan) served every pair.
+ * Diagnostic; no counterpart in the reference. */
+pa_status pa_solver_last_bucket_widths(const pa_solver *s, int32_t *widths4);
 
 /* Bytes copied host->device and device->host by the last solve call of this solver
  * (inputs, per-pair metadata, results). */

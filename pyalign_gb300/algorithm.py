@@ -79,6 +79,7 @@ def lib():
         L.pa_solver_set_stream.argtypes = [_P, _P]
         L.pa_solver_last_timings.argtypes = [_P, _PF, _PI]
         L.pa_solver_last_plan.argtypes = [_P, _PI]
+        L.pa_solver_last_bucket_widths.argtypes = [_P, _PI]
         dense = [_P, _PF, _c_i64, _c_i64, _c_i64, _PI]
         indexed = [_P, _PU, _PU, _c_i64, _c_i64, _c_i64, _PF, _c_i64, _c_i64, _PI]
         binary = [_P, _PU, _PU, _c_i64, _c_i64, _c_i64, _c_f32, _c_f32, _PI]
@@ -571,11 +572,15 @@ class Solver:
                "16-bit twins, 4x4 blocks")
 
     def last_plan(self):
-        """(kernel family, lanes per pair group, arithmetic, graph replay) of the last solve."""
+        """(kernel family, lanes per pair group, arithmetic, graph replay) of the last solve, and
+        the group width per length bucket of |s| (<= 128, <= 256, <= 512, longer) when the
+        launch gave each bucket its own (else None)."""
         v = (ctypes.c_int32 * 4)()
         lib().pa_solver_last_plan(self._h, v)
+        w = (ctypes.c_int32 * 4)()
+        lib().pa_solver_last_bucket_widths(self._h, w)
         return {"kernel": self.KERNELS[v[0]], "G": v[1], "arithmetic": ("float32", "int32", "int16x2")[v[2]],
-                "graph": bool(v[3])}
+                "graph": bool(v[3]), "bucket_widths": list(w) if any(w) else None}
 
     # --- argument marshalling (pytensor casts of factory.h:424-507)
     @staticmethod

@@ -59,6 +59,8 @@ constexpr int ST_TIMEOUT = 2;   // a chained stripe waited too long for the stri
 constexpr int PUB_CHUNK = 32;
 constexpr int WAIT_LIMIT = 1 << 23;
 
+constexpr int PA_MAX_SEG = 4;  // length buckets of one launch (|s| <= 128, 256, 512, more)
+
 template <typename V>
 struct DpParams {
 	int32_t npairs;
@@ -89,6 +91,15 @@ struct DpParams {
 	const V *top_Q;         // values output only: Q(-1,j)
 	V neg_inf;
 	int32_t G;              // lanes per pair group
+	// length buckets with their own group width (16-bit twin kernel): the processing order is
+	// cut into nseg segments, segment k holding units seg_unit[k] .. seg_unit[k + 1] - 1 and warp
+	// tasks seg_task[k] .. seg_task[k + 1] - 1 (one group of seg_G[k] lanes per unit, 32 /
+	// seg_G[k] units per task); nseg = 0: one width, G, for the whole launch
+	int32_t nseg;
+	int32_t seg_G[PA_MAX_SEG];
+	int32_t seg_unit[PA_MAX_SEG + 1];
+	int32_t seg_task[PA_MAX_SEG + 1];
+	int32_t slots_per_warp; // group slots of scratch per warp (32 / the narrowest width)
 	int32_t key_shift;      // local seeds: key = value * 2^key_shift + j
 	int32_t one, minus_one, minus_four, minus_eight, sixteen;  // IMAD multipliers (see imad)
 	// outputs
@@ -870,6 +881,7 @@ struct WalkParams {
 	int32_t G;
 	int32_t cols;   // columns per lane step of the DP that wrote the masks (1: dp_kernel, 2: dp2_kernel)
 	int32_t fmt16;  // 1: nibbles of dp16_kernel (code in bits 2-3, P-open bit 0, Q-open bit 1)
+	const int8_t *pair_G;  // per pair group width of a launch with length buckets (else G)
 	int32_t rows4;  // 1: records of dp16b_kernel (4 rows x 4 columns per lane step, cols = 4)
 	const int32_t *status;  // the DP's status: a launch that flagged ST_BAD_CODE has no masks
 	int32_t gap;    // GapKind

@@ -163,27 +163,39 @@ __global__ void __launch_bounds__(BLOCK, 4) dp16_kernel(DpParams<int32_t> p) {
 	for (int k = threadIdx.x; k < p.table_rows * cols; k += blockDim.x) stab[k] = p.table[k];
 	__syncthreads();
 
-	const int G = p.G;
 	const int lane = threadIdx.x & 31;
-	const int sub = lane % G;
-	const int grp = lane / G;
-	const int gpw = 32 / G;
 	const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const int slot = warp_global * gpw + grp;
 	const int64_t half = p.scratch_stride / 2;
-	const int rpp = G * R;
 	const int ntwins = (p.npairs + 1) >> 1;
 	const uint32_t NEG = p.h_neg;
 	const int32_t NEG32 = p.neg_inf;
 
 	for (;;) {
-		int base = 0;
-		if (lane == 0) base = atomicAdd(p.work_counter, gpw);
-		base = __shfl_sync(0xffffffffu, base, 0);
-		if (base >= ntwins) break;
+		// the next warp task: 32 / G twins of one width -- the launch's G, or with length
+		// buckets the width of the segment the task falls in
+		int G = p.G, base = 0, end = ntwins;
+		if (p.nseg > 0) {
+			int t = 0;
+			if (lane == 0) t = atomicAdd(p.work_counter, 1);
+			t = __shfl_sync(0xffffffffu, t, 0);
+			if (t >= p.seg_task[p.nseg]) break;
+			int k = 0;
+			while (k + 1 < p.nseg && p.seg_task[k + 1] <= t) k++;
+			G = p.seg_G[k];
+			base = p.seg_unit[k] + (t - p.seg_task[k]) * (32 / G);
+			end = p.seg_unit[k + 1];
+		} else {
+			if (lane == 0) base = atomicAdd(p.work_counter, 32 / G);
+			base = __shfl_sync(0xffffffffu, base, 0);
+			if (base >= ntwins) break;
+		}
+		const int sub = lane % G;
+		const int grp = lane / G;
+		const int slot = warp_global * p.slots_per_warp + grp;
+		const int rpp = G * R;
 		const int w = base + grp;
-		const int pa = w < ntwins ? p.order[2 * w] : -1;
-		const int pb = (w < ntwins && 2 * w + 1 < p.npairs) ? p.order[2 * w + 1] : -1;
+		const int pa = w < end ? p.order[2 * w] : -1;
+		const int pb = (w < end && 2 * w + 1 < p.npairs) ? p.order[2 * w + 1] : -1;
 		const int lsA = pa >= 0 ? p.len_s[pa] : 0, ltA = pa >= 0 ? p.len_t[pa] : 0;
 		const int lsB = pb >= 0 ? p.len_s[pb] : 0, ltB = pb >= 0 ? p.len_t[pb] : 0;
 		const bool emptyA = lsA == 0 || ltA == 0, emptyB = lsB == 0 || ltB == 0;

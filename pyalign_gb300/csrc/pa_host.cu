@@ -316,6 +316,37 @@ struct pa_iterator {
 	std::vector<std::pair<int, int>> scratch;
 };
 
+// Length buckets of |s| that can get a group width of their own (Plan::bucket_G): rows up to
+// 128, 256, 512 and more.
+constexpr int PA_BUCKETS = PA_MAX_SEG;
+constexpr int PA_MAX_CHUNKS = 12;  // pipeline chunks of a repeated host-buffer solve
+inline int bucket_of(int64_t ls) { return ls <= 128 ? 0 : ls <= 256 ? 1 : ls <= 512 ? 2 : 3; }
+// "g0,g1,g2,g3": a group width (1, 2, 4, 8, 16 or 32) per length bucket
+bool parse_bucket_widths(const char *e, int *g) {
+	int v[PA_BUCKETS];
+	for (int k = 0; k < PA_BUCKETS; k++) {
+		char *end = nullptr;
+		const long x = std::strtol(e, &end, 10);
+		if (end == e || x < 1 || x > 32 || (x & (x - 1))) return false;
+		v[k] = int(x);
+		e = end;
+		if (k + 1 < PA_BUCKETS) {
+			if (*e != ',') return false;
+			e++;
+		}
+	}
+	if (*e) return false;
+	for (int k = 0; k < PA_BUCKETS; k++) g[k] = v[k];
+	return true;
+}
+
+// The segments of one DP launch's order with length buckets: segment k has group width G[k],
+// units (twins) unit[k] .. unit[k + 1] - 1 and warp tasks task[k] .. task[k + 1] - 1.
+struct SegInfo {
+	int nseg = 0, Gmin = 32;
+	int G[PA_MAX_SEG] = {}, unit[PA_MAX_SEG + 1] = {}, task[PA_MAX_SEG + 1] = {};
+};
+
 // ---------------------------------------------------------------------------------------
 // Solver
 
@@ -342,6 +373,7 @@ struct pa_solver {
 	bool dp_timing_pending = false;  // a device-resident paths solve: read ev[1] -> ev[2] on demand
 	int32_t last_launches = 0;
 	int32_t last_plan[4] = {0, 0, 0, 0};  // kernel family, G, arithmetic, graph replay
+	int32_t last_widths[4] = {0, 0, 0, 0};  // group width per length bucket (0: one width)
 	int64_t bytes_h2d = 0, bytes_d2h = 0;
 
 	DevBuf d_a, d_b, d_tab, d_dense, d_dense_off, d_ls, d_lt, d_order, d_mask_off, d_score, d_seed, d_has,
@@ -357,6 +389,7 @@ struct pa_solver {
 	struct {
 		int32_t *ls, *lt, *order, *level_start;
 		int64_t *mask_off, *map_off, *path_off, *val_off, *dense_off;
+		int8_t *pair_G;  // per pair group width (length buckets)
 	} m{};
 	std::vector<std::pair<uint64_t, int>> occ_cache;  // (kernel variant, smem) -> blocks per SM
 	DevBuf d_border_mode[4];          // borders per arithmetic mode: float, int tagged, int plain, packed 16-bit
@@ -383,7 +416,9 @@ struct pa_solver {
 		std::vector<int64_t> user_map_off, user_path_off, dense_off;
 		// the plan and what the downloads need from it
 		int G = 0, C = 1, launches = 0, key_shift = 0, ntickets = 0, nlevels = 0;
-		bool units = false, use_int = false, h16 = false, blk = false;
+		bool units = false, use_int = false, h16 = false, blk = false, seg = false;
+		int bucket_G[PA_BUCKETS] = {};
+		SegInfo segs[PA_MAX_CHUNKS];
 		int32_t h_neg = 0;
 		int nchunks = 1;
 		std::vector<int64_t> mask_off, map_off, path_off, val_off;
@@ -454,6 +489,12 @@ struct Plan {
 	int C = 1;                 // columns per lane step: 2 = dp2_kernel (int32 tagged, no values)
 	bool h16 = false;          // packed 16-bit twin pairs (dp16_kernel); h_neg is its sentinel
 	bool blk = false;          // with h16: the 4 x 4 block kernel (dp16b_kernel: 4 rows per lane, C = 4)
+	// with h16 (dp16_kernel): a group width per length bucket of |s| (bucket_of), the pairs of
+	// one launch ordered bucket by bucket; stage() cuts each pipeline chunk's order into
+	// segments of one width (segs[chunk])
+	bool seg = false;
+	int bucket_G[PA_BUCKETS] = {16, 16, 16, 16};
+	SegInfo segs[PA_MAX_CHUNKS];
 	int32_t h_neg = 0;
 	int C32 = 1;               // columns per lane step of the int32/float kernels for this launch
 	int nchunks = 1;           // repeated host-buffer solves: pipeline of this many pair ranges
@@ -684,7 +725,8 @@ cudaError_t dp_occupancy(int gk, bool chain, int loc, int tb, bool vals, size_t 
 template <typename V>
 pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const float *host_table,
                  int64_t npairs, bool want_values, const float *best_in_dev, int *launches, int64_t first = 0,
-                 int codes_slot = 0, int side = 0) {
+                 int codes_slot = 0, int side = 0, int seg_slot = -1) {
+	if (seg_slot < 0) seg_slot = codes_slot;  // the pipeline chunk whose segments this launch runs
 	const bool ISINT = std::is_same<V, int32_t>::value;
 	const bool tag = ISINT && tb != TB_ALL;
 	const int scale = tag ? 4 : 1;
@@ -702,6 +744,19 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	             : (in.form == F_BINARY ? SUB_BINARY : SUB_TABLE);
 	p.neg_inf = ISINT ? V(-(1 << 29)) : V(-INFINITY);
 	p.G = plan.G;
+	p.slots_per_warp = 32 / plan.G;
+	// length buckets (16-bit two-column kernel): the segments of this chunk's order
+	const bool segd = ISINT && plan.h16 && !plan.blk && plan.seg && plan.segs[seg_slot].nseg > 0;
+	if (segd) {
+		const SegInfo &sg = plan.segs[seg_slot];
+		p.nseg = sg.nseg;
+		for (int k = 0; k < sg.nseg; k++) p.seg_G[k] = sg.G[k];
+		for (int k = 0; k <= sg.nseg; k++) {
+			p.seg_unit[k] = sg.unit[k];
+			p.seg_task[k] = sg.task[k];
+		}
+		p.slots_per_warp = 32 / sg.Gmin;
+	}
 	p.key_shift = plan.key_shift;
 	p.one = 1;
 	p.minus_one = -1;
@@ -886,9 +941,11 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	PA_CUDA(e);
 	bps = std::max(bps, 1);
 	if (s->occ_cache.size() < 64) s->occ_cache.push_back({ckey, bps});
-	const int gpw = 32 / plan.G;
+	const int gpw = segd ? p.slots_per_warp : 32 / plan.G;
 	const int64_t units_needed = h16 ? (npairs + 1) / 2 : npairs;  // twins or pairs
-	const int64_t groups_needed = plan.units ? plan.ntickets : (units_needed + gpw - 1) / gpw;  // warps needed
+	const int64_t groups_needed = plan.units ? plan.ntickets
+	                              : segd     ? p.seg_task[p.nseg]  // warp tasks of the segments
+	                                         : (units_needed + gpw - 1) / gpw;  // warps needed
 	int64_t grid = int64_t(s->sm_count) * bps;
 	grid = std::min<int64_t>(grid, (groups_needed + WARPS - 1) / WARPS);
 	// PA_GRID=exact: one block per WARPS work units, each warp takes one unit and exits -- the
@@ -1094,7 +1151,14 @@ pa_status download_wsb(pa_solver *s, ResultData &res) {
 // keeps the fastest for every later call with that signature, process-wide.  Every plan
 // computes the same results (the order of pairs and the grouping never change a value).
 // PA_TUNE=0 turns the timing off (the analytic choice stands), as do the experiment
-// overrides PA_DP_MODE and PA_GROUP_WIDTH.
+// overrides PA_DP_MODE, PA_GROUP_WIDTH and PA_BUCKET_WIDTHS.
+//
+// When the 16-bit twin kernel wins and the pairs fall into more than one length bucket of
+// |s| (bucket_of), the tuner also tries a group width per bucket: from the timings of the
+// uniform widths it takes each width's time per computed cell (real cells plus stripe
+// padding and skew), gives every bucket the width with the lowest estimated time for its
+// own pairs, and times that plan too (one launch, the buckets in segments of one width
+// each); it is kept only when it is faster.
 struct TuneEntry {
 	uint64_t key;
 	int G;
@@ -1102,6 +1166,8 @@ struct TuneEntry {
 	bool h16;
 	int C;
 	bool blk;
+	bool seg;
+	int bucket_G[PA_BUCKETS];
 };
 std::mutex g_tune_mu;
 std::vector<TuneEntry> g_tune;
@@ -1134,7 +1200,9 @@ template <typename Stage, typename Dp>
 pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vector<int32_t> &lt, const Input &in,
                     Plan &plan, Stage &stage, Dp &dp) {
 	const char *te = std::getenv("PA_TUNE");
-	if ((te && std::strcmp(te, "0") == 0) || std::getenv("PA_DP_MODE") || std::getenv("PA_GROUP_WIDTH")) return PA_OK;
+	if ((te && std::strcmp(te, "0") == 0) || std::getenv("PA_DP_MODE") || std::getenv("PA_GROUP_WIDTH") ||
+	    std::getenv("PA_BUCKET_WIDTHS"))
+		return PA_OK;
 	double cells = 0;
 	const uint64_t key = tune_key(s, in, plan, ls, lt, &cells);
 	{
@@ -1146,6 +1214,8 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 				plan.h16 = plan.h16 && t.h16;  // the 16-bit kernel still needs this launch's bounds
 				plan.blk = plan.h16 && t.blk;
 				plan.C = plan.h16 ? t.C : plan.C32;
+				plan.seg = plan.h16 && !plan.blk && t.seg;
+				for (int k = 0; k < PA_BUCKETS; k++) plan.bucket_G[k] = t.bucket_G[k];
 				return PA_OK;
 			}
 	}
@@ -1180,6 +1250,21 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 	float best = INFINITY;
 	int bestG = plan.G, bestC = plan.C;
 	bool bestU = plan.units, bestH = plan.h16, bestB = plan.blk;
+	auto time_plan = [&](Plan &pl, int reps, float *ms) -> pa_status {
+		if (pa_status e = stage(pl)) return e;
+		*ms = INFINITY;
+		for (int rep = 0; rep < reps; rep++) {
+			PA_CUDA(cudaEventRecord(s->ev[1], st));
+			if (pa_status e = dp(pl, pl.tb, false, nullptr)) return e;
+			PA_CUDA(cudaEventRecord(s->ev[2], st));
+			PA_CUDA(cudaEventSynchronize(s->ev[2]));
+			float t = 0;
+			PA_CUDA(cudaEventElapsedTime(&t, s->ev[1], s->ev[2]));
+			*ms = std::min(*ms, t);
+		}
+		return PA_OK;
+	};
+	std::vector<float> cand_ms(cand.size(), INFINITY);
 	// one untimed run first (clocks and caches leave their idle state), then each candidate
 	// timed twice, keeping its faster run: a single cold timing could misplace a candidate
 	for (size_t ci = 0; ci <= cand.size(); ci++) {
@@ -1190,18 +1275,11 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 		pl.h16 = c.h16;
 		pl.C = c.C;
 		pl.blk = c.blk;
-		if (pa_status e = stage(pl)) return e;
+		pl.seg = false;
 		float ms = INFINITY;
-		for (int rep = 0; rep < (ci == 0 ? 1 : 2); rep++) {
-			PA_CUDA(cudaEventRecord(s->ev[1], st));
-			if (pa_status e = dp(pl, pl.tb, false, nullptr)) return e;
-			PA_CUDA(cudaEventRecord(s->ev[2], st));
-			PA_CUDA(cudaEventSynchronize(s->ev[2]));
-			float t = 0;
-			PA_CUDA(cudaEventElapsedTime(&t, s->ev[1], s->ev[2]));
-			ms = std::min(ms, t);
-		}
+		if (pa_status e = time_plan(pl, ci == 0 ? 1 : 2, &ms)) return e;
 		if (ci == 0) continue;  // the warm-up
+		cand_ms[ci - 1] = ms;
 		if (ms < best) {
 			best = ms;
 			bestG = pl.G;
@@ -1216,8 +1294,70 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 	plan.h16 = bestH;
 	plan.C = bestC;
 	plan.blk = bestB;
+	plan.seg = false;
+	if (bestH && !bestB && !bestU) {
+		// a width per length bucket, estimated from the uniform widths' time per computed cell
+		const int rows = R;
+		double pcells[6][PA_BUCKETS] = {};  // computed cells per (width index, bucket)
+		int bpop[PA_BUCKETS] = {};
+		static const int widths[6] = {32, 16, 8, 4, 2, 1};
+		for (size_t k = 0; k < ls.size(); k++) {
+			if (ls[k] == 0 || lt[k] == 0) continue;
+			const int b = bucket_of(ls[k]);
+			bpop[b]++;
+			for (int wi = 0; wi < 6; wi++) {
+				const int64_t rpp = int64_t(widths[wi]) * rows;
+				const int64_t np = (ls[k] + rpp - 1) / rpp;
+				const int64_t steps = (bestC == 2 ? (lt[k] + 1) / 2 : lt[k]) + widths[wi] - 1;
+				pcells[wi][b] += double(np * rpp) * double(steps);
+			}
+		}
+		double per_cell[6];
+		bool have[6] = {};
+		for (size_t ci = 0; ci < cand.size(); ci++) {
+			const Cand &c = cand[ci];
+			if (!c.h16 || c.blk || c.units || c.C != bestC || !std::isfinite(cand_ms[ci])) continue;
+			for (int wi = 0; wi < 6; wi++)
+				if (widths[wi] == c.G) {
+					const double tot = pcells[wi][0] + pcells[wi][1] + pcells[wi][2] + pcells[wi][3];
+					if (tot > 0) {
+						per_cell[wi] = double(cand_ms[ci]) / tot;
+						have[wi] = true;
+					}
+				}
+		}
+		int nb = 0;
+		bool differs = false;
+		Plan pl = plan;
+		for (int b = 0; b < PA_BUCKETS; b++) {
+			pl.bucket_G[b] = bestG;
+			if (!bpop[b]) continue;
+			nb++;
+			double bt = INFINITY;
+			for (int wi = 0; wi < 6; wi++)
+				if (have[wi] && per_cell[wi] * pcells[wi][b] < bt) {
+					bt = per_cell[wi] * pcells[wi][b];
+					pl.bucket_G[b] = widths[wi];
+				}
+			differs |= pl.bucket_G[b] != bestG;
+		}
+		if (nb > 1 && differs) {
+			pl.seg = true;
+			float ms = INFINITY;
+			if (pa_status e = time_plan(pl, 2, &ms)) return e;
+			if (ms < best) {
+				best = ms;
+				plan.seg = true;
+				for (int b = 0; b < PA_BUCKETS; b++) plan.bucket_G[b] = pl.bucket_G[b];
+			}
+		}
+	}
 	std::lock_guard<std::mutex> lk(g_tune_mu);
-	if (g_tune.size() < 4096) g_tune.push_back({key, bestG, bestU, bestH, bestC, bestB});
+	if (g_tune.size() < 4096) {
+		TuneEntry t{key, bestG, bestU, bestH, bestC, bestB, plan.seg, {}};
+		for (int b = 0; b < PA_BUCKETS; b++) t.bucket_G[b] = plan.bucket_G[b];
+		g_tune.push_back(t);
+	}
 	return PA_OK;
 }
 
@@ -1414,8 +1554,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 				plan.blk = true;
 				plan.C = 4;
 			}
+		if (const char *e = std::getenv("PA_BUCKET_WIDTHS"))  // experiments and tests: "g0,g1,g2,g3"
+			if (plan.h16 && !plan.blk && parse_bucket_widths(e, plan.bucket_G)) plan.seg = true;
 	}
 	std::vector<int32_t> order, level_start;
+	std::vector<int8_t> pair_g;  // group width per pair (length buckets)
 	std::vector<int64_t> mask_off, map_off, path_off, val_off, dense_off;
 	struct Lend {  // a repeat's offsets lent to this call, returned however the call ends
 		pa_solver::Repeat *r = nullptr;
@@ -1436,23 +1579,70 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		// (a pipelined solve sorts each chunk's pair range on its own: chunk c's pairs occupy
 		// order[k0, k1) for its pair indices [k0, k1))
 		order.assign(size_t(B), 0);
-		{
-			const int64_t rpp = int64_t(plan.G) * plan_rows(plan);
-			const int64_t kt = max_lt + 1;
-			const int64_t nkeys = ((max_ls + rpp - 1) / rpp + 1) * kt;
-			std::vector<int32_t> count(size_t(nkeys) + 1);
-			auto key = [&](int64_t k) {
-				const int64_t np = (ls[size_t(k)] + rpp - 1) / rpp;
-				return nkeys - 1 - (np * kt + lt[size_t(k)]);  // descending
-			};
+		pair_g.assign(size_t(B), int8_t(plan.G));
+		if (!plan.seg) {
+			{
+				const int64_t rpp = int64_t(plan.G) * plan_rows(plan);
+				const int64_t kt = max_lt + 1;
+				const int64_t nkeys = ((max_ls + rpp - 1) / rpp + 1) * kt;
+				std::vector<int32_t> count(size_t(nkeys) + 1);
+				auto key = [&](int64_t k) {
+					const int64_t np = (ls[size_t(k)] + rpp - 1) / rpp;
+					return nkeys - 1 - (np * kt + lt[size_t(k)]);  // descending
+				};
+				for (int c = 0; c < plan.nchunks; c++) {
+					int64_t k0, k1;
+					chunk_range(B, plan.nchunks, c, k0, k1);
+					std::fill(count.begin(), count.end(), 0);
+					for (int64_t k = k0; k < k1; k++) count[size_t(key(k)) + 1]++;
+					count[0] = int32_t(k0);
+					for (int64_t c2 = 0; c2 < nkeys; c2++) count[size_t(c2) + 1] += count[size_t(c2)];
+					for (int64_t k = k0; k < k1; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
+				}
+			}
+		} else {
+			// length buckets: within each chunk the pairs bucket by bucket (the longest first),
+			// each bucket by its stripe count at the bucket's width and |t|, largest first; a
+			// segment of one width per bucket, starting at an even position (a twin never
+			// straddles two widths: an odd bucket lends the next bucket's first pair)
+			std::vector<int32_t> idx;
 			for (int c = 0; c < plan.nchunks; c++) {
 				int64_t k0, k1;
 				chunk_range(B, plan.nchunks, c, k0, k1);
-				std::fill(count.begin(), count.end(), 0);
-				for (int64_t k = k0; k < k1; k++) count[size_t(key(k)) + 1]++;
-				count[0] = int32_t(k0);
-				for (int64_t c2 = 0; c2 < nkeys; c2++) count[size_t(c2) + 1] += count[size_t(c2)];
-				for (int64_t k = k0; k < k1; k++) order[size_t(count[size_t(key(k))]++)] = int32_t(k);
+				idx.resize(size_t(k1 - k0));
+				for (int64_t k = k0; k < k1; k++) idx[size_t(k - k0)] = int32_t(k);
+				auto np_of = [&](int32_t k) {
+					const int64_t g = plan.bucket_G[bucket_of(ls[size_t(k)])], rpp = g * plan_rows(plan);
+					return (ls[size_t(k)] + rpp - 1) / rpp;
+				};
+				std::stable_sort(idx.begin(), idx.end(), [&](int32_t x, int32_t y) {
+					const int bx = bucket_of(ls[size_t(x)]), by = bucket_of(ls[size_t(y)]);
+					if (bx != by) return bx > by;
+					const int64_t nx = np_of(x), ny = np_of(y);
+					if (nx != ny) return nx > ny;
+					return lt[size_t(x)] > lt[size_t(y)];
+				});
+				for (size_t i = 0; i < idx.size(); i++) order[size_t(k0) + i] = idx[i];
+				SegInfo &sg = plan.segs[c];
+				sg = SegInfo();
+				const int64_t n = k1 - k0;
+				int64_t pos = 0;
+				while (pos < n) {
+					const int bk = bucket_of(ls[size_t(idx[size_t(pos)])]);
+					const int g = plan.bucket_G[bk];
+					int64_t e = pos;
+					while (e < n && bucket_of(ls[size_t(idx[size_t(e)])]) == bk) e++;
+					if (e < n && (e & 1)) e++;
+					for (int64_t i = pos; i < e; i++) pair_g[size_t(idx[size_t(i)])] = int8_t(g);
+					const int64_t units = (e + 1) / 2 - pos / 2, per = 32 / g;
+					sg.G[sg.nseg] = g;
+					sg.unit[sg.nseg] = int(pos / 2);
+					sg.task[sg.nseg + 1] = sg.task[sg.nseg] + int((units + per - 1) / per);
+					sg.Gmin = std::min(sg.Gmin, g);
+					sg.nseg++;
+					pos = e;
+				}
+				sg.unit[sg.nseg] = int((n + 1) / 2);
 			}
 		}
 		// stripe-chained tickets: level q holds stripe q of every pair with more than q stripes
@@ -1483,12 +1673,12 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		path_off.assign(size_t(B) + 1, 0);
 		val_off.assign(size_t(B) + 1, 0);
 		dense_off.assign(size_t(B), 0);
-		const int rpp = plan.G * plan_rows(plan);
 		for (int64_t k = 0; k < B; k++) {
 			const int64_t a = ls[size_t(k)], b = lt[size_t(k)];
+			const int64_t gk = pair_g[size_t(k)], rpp = gk * plan_rows(plan);
 			const int64_t npass = (a == 0 || b == 0) ? 0 : (a + rpp - 1) / rpp;
-			const int64_t steps = (b + plan.C - 1) / plan.C + plan.G - 1;
-			mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * steps * plan.G * plan_words(plan);
+			const int64_t steps = (b + plan.C - 1) / plan.C + gk - 1;
+			mask_off[size_t(k) + 1] = mask_off[size_t(k)] + npass * steps * gk * plan_words(plan);
 			map_off[size_t(k) + 1] = map_off[size_t(k)] + std::min(a, b);
 			path_off[size_t(k) + 1] = path_off[size_t(k)] + 2 * (a + b + 2);
 			val_off[size_t(k) + 1] = val_off[size_t(k)] + int64_t(res.layers) * (a + 1) * (b + 1);
@@ -1497,7 +1687,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		// pair metadata: packed into one pinned staging buffer, one host-to-device copy
 		{
 			const size_t n32 = size_t(B), n64 = size_t(B) + 1;
-			const size_t bytes = ((3 * n32 * 4 + level_start.size() * 4 + 7) & ~size_t(7)) + 5 * n64 * 8 + 16;
+			const size_t bytes = ((3 * n32 * 4 + level_start.size() * 4 + 7) & ~size_t(7)) + 5 * n64 * 8 + 16 + n32 + 8;
 			if (s->meta_pending) {
 				PA_CUDA(cudaEventSynchronize(s->meta_ev));  // the previous call's copy has read it
 				s->meta_pending = false;
@@ -1529,6 +1719,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			s->m.val_off = reinterpret_cast<int64_t *>(put(val_off.data(), n64 * 8, 8));
 			s->m.dense_off = reinterpret_cast<int64_t *>(put(dense_off.data(), n32 * 8, 8));
 			o += 8;
+			s->m.pair_G = reinterpret_cast<int8_t *>(put(pair_g.data(), n32, 1));
 			PA_CUDA(pa_copy(s, d, h, o, cudaMemcpyHostToDevice, st));
 			PA_CUDA(cudaEventRecord(s->meta_ev, st));
 			s->meta_pending = true;
@@ -1545,6 +1736,19 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		return PA_OK;
 	};
 	auto dp = [&](const Plan &pl, int tbk, bool vals, const float *best_in) -> pa_status {
+		if (pl.seg && pl.h16 && !pl.blk && pl.nchunks > 1) {
+			// length buckets of a chunk-major order: one launch per chunk, each over its own
+			// segments (a whole-bag launch has none: segments do not cross chunks)
+			for (int c = 0; c < pl.nchunks; c++) {
+				int64_t k0, k1;
+				chunk_range(B, pl.nchunks, c, k0, k1);
+				if (k1 > k0)
+					if (pa_status e = run_dp<int32_t>(s, in, pl, tbk, host_table.data(), k1 - k0, vals, best_in,
+					                                  &launches, k0, 0, 0, c))
+						return e;
+			}
+			return PA_OK;
+		}
 		return pl.use_int ? run_dp<int32_t>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches)
 		                  : run_dp<float>(s, in, pl, tbk, host_table.data(), B, vals, best_in, &launches);
 	};
@@ -1573,6 +1777,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		w.cols = plan.C;
 		w.fmt16 = plan.h16 ? 1 : 0;
 		w.rows4 = plan.blk ? 1 : 0;
+		w.pair_G = plan.seg ? s->m.pair_G : nullptr;
 		w.status = s->d_status.as<int32_t>();
 		w.gap = s->gap;
 		w.local = s->loc == LOC_LOCAL;
@@ -1732,6 +1937,9 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		plan.C = r.C;
 		plan.h16 = r.h16;
 		plan.blk = r.blk;
+		plan.seg = r.seg;
+		for (int k = 0; k < PA_BUCKETS; k++) plan.bucket_G[k] = r.bucket_G[k];
+		for (int c = 0; c < PA_MAX_CHUNKS; c++) plan.segs[c] = r.segs[c];
 		plan.h_neg = r.h_neg;
 		plan.nchunks = r.nchunks;
 		plan.units = r.units;
@@ -1806,6 +2014,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	s->last_plan[1] = plan.G;
 	s->last_plan[2] = plan.h16 ? 2 : plan.use_int ? 1 : 0;
 	s->last_plan[3] = hit && s->rep.exec ? 1 : 0;
+	for (int k = 0; k < PA_BUCKETS; k++) s->last_widths[k] = plan.seg ? plan.bucket_G[k] : 0;
 	PA_CUDA(cudaEventRecord(s->ev[3], st));
 	if (repeatable && !hit) {
 		// remember this solve for the next call
@@ -1848,6 +2057,9 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		r.C = plan.C;
 		r.h16 = plan.h16;
 		r.blk = plan.blk;
+		r.seg = plan.seg;
+		for (int k = 0; k < PA_BUCKETS; k++) r.bucket_G[k] = plan.bucket_G[k];
+		for (int c = 0; c < PA_MAX_CHUNKS; c++) r.segs[c] = plan.segs[c];
 		r.h_neg = plan.h_neg;
 		r.nchunks = plan.nchunks;
 		r.units = plan.units;
@@ -2176,6 +2388,13 @@ pa_status pa_solver_last_plan(const pa_solver *s, int32_t *plan4) {
 	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
 	if (plan4)
 		for (int k = 0; k < 4; k++) plan4[k] = s->last_plan[k];
+	return PA_OK;
+}
+
+pa_status pa_solver_last_bucket_widths(const pa_solver *s, int32_t *widths4) {
+	if (!s) return fail(PA_ERR_INVALID_ARGUMENT, "null solver");
+	if (widths4)
+		for (int k = 0; k < PA_BUCKETS; k++) widths4[k] = s->last_widths[k];
 	return PA_OK;
 }
 

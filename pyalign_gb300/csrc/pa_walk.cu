@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(WALK_WARPS * 32) walk_kernel(WalkParams p) {
 	if (path && lane == 0) { path[0] = u; path[1] = v; }
 	int np = 1;
 	const uint32_t *W = p.masks + p.mask_off[pair];
-	const int G = p.G;
+	const int G = p.pair_G ? int(p.pair_G[pair]) : p.G;
 	const bool two = p.cols == 2;  // dp2_kernel layout: a uint2 per lane and step, columns j, j + 1
 	const bool fmt16 = p.fmt16 != 0;
 	const bool rows4 = p.rows4 != 0;  // dp16b_kernel records: 4-row lanes, 4 columns per step

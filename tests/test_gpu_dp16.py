@@ -106,6 +106,35 @@ def test_dp16_group_widths(monkeypatch, cols, gpu_alg, oracle_alg, G):
     assert d is None, d
 
 
+@pytest.mark.parametrize("widths", ["8,16,16,32", "1,4,16,2", "32,8,2,16"])
+@pytest.mark.parametrize("C", ["1", "2"])
+@pytest.mark.parametrize("method", ["score", "alignment"])
+def test_dp16_bucket_widths(analytic, monkeypatch, gpu_alg, oracle_alg, widths, C, method):
+    """A group width per length bucket of |s| (<= 128, <= 256, <= 512, longer) in one launch:
+    pairs of every bucket, odd bucket sizes (a twin that would straddle two buckets takes the
+    next bucket's first pair at the earlier bucket's width), empty pairs, an odd pair count."""
+    monkeypatch.setenv("PA_BUCKET_WIDTHS", widths)
+    if C == "1":
+        monkeypatch.setenv("PA_DP_COLS", "1")
+    rng = np.random.default_rng(zlib.crc32(f"buckets/{widths}/{C}/{method}".encode()))
+    pairs = _pairs(rng, 30) + random_pairs(rng, 17, 129, 256, alphabet=4, related=0.6) \
+        + random_pairs(rng, 9, 257, 512, alphabet=4, related=0.6) + random_pairs(rng, 7, 513, 700, alphabet=4,
+                                                                                  related=0.6)
+    pairs = [pairs[k] for k in rng.permutation(len(pairs))]
+    detail = "score" if method == "score" else "alignment"
+    opts = options(gpu_alg, locality="local", detail=detail, gap=GAPS["affine"])
+    table = rng.integers(-4, 0, size=(4, 4)).astype(np.float32)  # matches +2: 16-bit bounds at |s| = 700
+    np.fill_diagonal(table, 2.0)
+    plan, d = _run(gpu_alg, oracle_alg, opts, method, pairs, table)
+    assert plan["kernel"] == TWINS[C] and plan["bucket_widths"] == [int(g) for g in widths.split(",")], plan
+    assert d is None, d
+    # the 4 x 4 block kernel keeps one width
+    monkeypatch.setenv("PA_DP_BLOCK", "1")
+    plan, d = _run(gpu_alg, oracle_alg, opts, method, pairs, table)
+    assert plan["kernel"] == TWINS["blk"] and plan["bucket_widths"] is None, plan
+    assert d is None, d
+
+
 def test_dp16_bounds_fall_back(analytic, gpu_alg, oracle_alg):
     """Outside the 16-bit bounds the int32 kernels run, with the same results."""
     rng = np.random.default_rng(77)
@@ -189,15 +218,19 @@ def test_dp16_bad_codes_then_valid(analytic, gpu_alg, oracle_alg):
     assert d is None, d
 
 
-@pytest.mark.parametrize("plan", ["twins-G16", "blocks-G8", "blocks-G16", "own"])
+@pytest.mark.parametrize("plan", ["twins-G16", "blocks-G8", "blocks-G16", "buckets-8,16,16,32", "own"])
 def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg, monkeypatch, plan):
     """4,096 pairs drawn like the batched workload (DNA, |s|, |t| ~ U[100, 1000], half of them
     a query and a 10%-mutated copy; local affine 5/2, +2/-3; score + one traceback) against
     the oracle, every score and every alignment map bit for bit: with the batched
-    workload's plan (the 16-bit twin kernel, two columns per step, G = 16) and with the
-    plan the solver picks for this bag on its own."""
+    workload's plan (the 16-bit twin kernel, two columns per step, G = 16), with the block
+    kernel, with a group width per length bucket, and with the plan the solver picks for
+    this bag on its own."""
     import bench
-    if plan != "own":
+    if plan.startswith("buckets"):
+        monkeypatch.setenv("PA_BUCKET_WIDTHS", plan.split("-")[1])
+        monkeypatch.setenv("PA_DP_MODE", "groups")          # 4,096 such pairs would run stripe-chained
+    elif plan != "own":
         monkeypatch.setenv("PA_GROUP_WIDTH", plan.split("-G")[1])
     if plan.startswith("blocks"):
         monkeypatch.setenv("PA_DP_BLOCK", "1")
@@ -206,7 +239,9 @@ def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg, monkeypatch, p
     opts = dict(options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"]), batch_size=n, batch=True)
     solver = gpu_alg.m16.create_solver(a.shape[1], b.shape[1], gpu_alg.m16.create_options(opts))
     res = solver.solve_indexed_for_alignment(a, b, table, np.stack([ls, lt]).astype(np.uint16))
-    if plan != "own":
+    if plan.startswith("buckets"):
+        assert solver.last_plan()["bucket_widths"] == [8, 16, 16, 32], solver.last_plan()
+    elif plan != "own":
         want = TWINS["blk"] if plan.startswith("blocks") else TWINS["2"]
         assert solver.last_plan()["kernel"] == want and solver.last_plan()["G"] == int(plan.split("-G")[1]), \
             solver.last_plan()
@@ -218,3 +253,37 @@ def test_dp16_matches_oracle_at_bench_shapes(gpu_alg, oracle_alg, monkeypatch, p
         if res[k].score != osc[k] or not np.array_equal(np.asarray(m), omp[offs[k]:offs[k + 1]]):
             bad.append(k)
     assert not bad, (len(bad), bad[:10])
+
+
+def test_dp16_tuned_two_length_modes(gpu_alg, oracle_alg, monkeypatch):
+    """2,048 pairs in two length modes -- short queries (|s| ~ U[8, 64]) and long ones (|s| ~
+    U[600, 1000]), |t| ~ U[400, 1000] for both -- solved with the plan the tuner picks
+    (uniform widths, and a width per length bucket where that times faster), against the
+    oracle bit for bit; a second solve of the same signature takes the tuned plan."""
+    rng = np.random.default_rng(2222)
+    n, hi = 2048, 1000
+    ls = np.where(np.arange(n) % 2 == 0, rng.integers(8, 65, n), rng.integers(600, 1001, n))
+    lt = rng.integers(400, 1001, n)
+    a = rng.integers(0, 4, size=(n, hi)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, hi)).astype(np.uint32)
+    b[: n // 2, :hi] = a[: n // 2, :hi]
+    mut = rng.random(size=(n // 2, hi)) < 0.1
+    b[: n // 2][mut] = rng.integers(0, 4, size=int(mut.sum()))
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    monkeypatch.setenv("PA_DP_MODE", "groups")
+    opts = dict(options(gpu_alg, locality="local", detail="alignment", gap=GAPS["affine"]), batch_size=n, batch=True)
+    ln = np.stack([ls, lt]).astype(np.uint16)
+    osol = oracle_alg.m16.create_solver(hi, hi, oracle_alg.m16.create_options(opts))
+    osc, omp, offs, _ = oracle_alg.batch_alignments(osol, a, b, table, ls, lt)
+    plans = []
+    for rep in range(2):
+        solver = gpu_alg.m16.create_solver(hi, hi, gpu_alg.m16.create_options(opts))
+        res = solver.solve_indexed_for_alignment(a, b, table, ln)
+        plans.append(solver.last_plan())
+        bad = [k for k in range(n)
+               if res[k].score != osc[k] or not np.array_equal(
+                   np.asarray(res[k].s_to_t if ls[k] <= lt[k] else res[k].t_to_s), omp[offs[k]:offs[k + 1]])]
+        assert not bad, (rep, len(bad), bad[:10], plans[-1])
+    print("tuned plan:", plans[0])
+    assert plans[0]["kernel"].startswith("16-bit") and plans[0] == plans[1], plans

@@ -148,6 +148,43 @@ def test_repeated_block_kernel_solves(env, monkeypatch, G):
         assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), rep
 
 
+@pytest.mark.parametrize("widths", ["8,16,16,32", "1,4,32,2"])
+def test_repeated_bucket_width_solves(env, monkeypatch, widths):
+    """Repeats and graph replays of a plan with a group width per length bucket of |s| keep
+    the widths (the segments of the launch, each pair's traceback layout) on every
+    repetition, with the results of an uncached one-width solve."""
+    torch, alg, ag = env
+    rng = np.random.default_rng(sum(map(int, widths.split(","))))
+    n, n_s, n_t = 301, 700, 300
+    ln = np.stack([rng.integers(1, n_s + 1, n), rng.integers(1, n_t + 1, n)]).astype(np.int32)
+    a = rng.integers(0, 4, size=(n, n_s)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, n_t)).astype(np.uint32)
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    a_d = torch.from_numpy(a.view(np.int32)).cuda()
+    b_d = torch.from_numpy(b.view(np.int32)).cuda()
+    t_d = torch.from_numpy(table).cuda()
+    sc = torch.empty(n, device="cuda")
+    mp = torch.empty(int(np.minimum(ln[0], ln[1]).sum()), dtype=torch.int32, device="cuda")
+    sc_r, mp_r = torch.empty_like(sc), torch.empty_like(mp)
+    monkeypatch.setenv("PA_GRAPHS", "0")
+    monkeypatch.setenv("PA_TUNE", "0")
+    monkeypatch.setenv("PA_DP_MODE", "groups")
+    ref_solver = _batch_solver(alg, torch, n, n_s, n_t)
+    want = _solve_batch(alg, torch, ref_solver, a_d, b_d, t_d, ln, sc_r, mp_r)
+    assert ref_solver.last_plan()["bucket_widths"] is None, ref_solver.last_plan()
+    monkeypatch.delenv("PA_GRAPHS")
+    monkeypatch.setenv("PA_BUCKET_WIDTHS", widths)
+    solver = _batch_solver(alg, torch, n, n_s, n_t)
+    for rep in range(4):  # planned, cached plan + captured graph, graph, graph
+        got = _solve_batch(alg, torch, solver, a_d, b_d, t_d, ln, sc, mp)
+        plan = solver.last_plan()
+        assert plan["kernel"] == "16-bit twins, two-column", (rep, plan)
+        assert plan["bucket_widths"] == [int(g) for g in widths.split(",")], (rep, plan)
+        assert plan["graph"] == (rep >= 1), (rep, plan)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), rep
+
+
 def test_repeated_dense_paths_and_gradients(env, monkeypatch):
     """The autograd front end (pa_solve_dense_paths): repeated forward + backward on one
     similarity buffer whose contents change in place."""
@@ -174,12 +211,13 @@ def test_repeated_dense_paths_and_gradients(env, monkeypatch):
 
 
 @pytest.mark.parametrize("pinned", [False, True])
-@pytest.mark.parametrize("chunks", [None, "3"])
-def test_repeated_host_batch_solves(env, monkeypatch, chunks, pinned):
+@pytest.mark.parametrize("chunks,widths", [(None, None), ("3", None), ("3", "4,8,32,16"), ("5", "2,16,8,32")])
+def test_repeated_host_batch_solves(env, monkeypatch, chunks, widths, pinned):
     """pa_solve_batch with host buffers: a repeat reuses the plan and staged metadata (no
     graph) -- with PA_CHUNKS=3 as a pipeline of three pair ranges whose uploads, DPs, walks and
-    map downloads overlap; new contents and new lengths are solved exactly as by a solver that
-    never caches; maps in pageable or pinned host memory."""
+    map downloads overlap, also with a group width per length bucket (segments per chunk);
+    new contents and new lengths are solved exactly as by a one-width solver that never
+    caches; maps in pageable or pinned host memory."""
     torch, alg, ag = env
     if chunks:
         monkeypatch.setenv("PA_CHUNKS", chunks)
@@ -210,26 +248,34 @@ def test_repeated_host_batch_solves(env, monkeypatch, chunks, pinned):
                                            mp.ctypes.data_as(ctypes.c_void_p), offs.ctypes.data_as(P(ctypes.c_int64))))
         return sc, mp
 
-    monkeypatch.setenv("PA_GRAPHS", "0")
+    def ref_solve(a, b, ln):
+        with monkeypatch.context() as m:
+            m.setenv("PA_GRAPHS", "0")
+            if widths:
+                m.delenv("PA_BUCKET_WIDTHS")
+                m.setenv("PA_TUNE", "0")
+            return solve(ref, a, b, ln)
+
+    if widths:
+        monkeypatch.setenv("PA_BUCKET_WIDTHS", widths)
+        monkeypatch.setenv("PA_DP_MODE", "groups")
     ref = _batch_solver(alg, torch, n, n_s, n_t)
-    want = solve(ref, a, b, ln)
-    monkeypatch.delenv("PA_GRAPHS")
+    want = ref_solve(a, b, ln)
     solver = _batch_solver(alg, torch, n, n_s, n_t)
     for rep in range(3):
         got = solve(solver, a, b, ln, pinned)
         assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), rep
         assert not solver.last_plan()["graph"]
+        if widths:
+            assert solver.last_plan()["bucket_widths"] == [int(g) for g in widths.split(",")], solver.last_plan()
     a[:, :] = rng.integers(0, 4, size=(n, n_s))              # new contents, same host buffer
     got = solve(solver, a, b, ln, pinned)
-    monkeypatch.setenv("PA_GRAPHS", "0")
-    want2 = solve(ref, a, b, ln)
-    monkeypatch.delenv("PA_GRAPHS")
+    want2 = ref_solve(a, b, ln)
     assert np.array_equal(got[0], want2[0]) and np.array_equal(got[1], want2[1])
     ln2 = ln.copy()
     ln2[1, :11] = 3                                           # new lengths: planned anew
     got = solve(solver, a, b, ln2, pinned)
-    monkeypatch.setenv("PA_GRAPHS", "0")
-    want3 = solve(ref, a, b, ln2)
+    want3 = ref_solve(a, b, ln2)
     assert np.array_equal(got[0], want3[0]) and np.array_equal(got[1], want3[1])
 
 
