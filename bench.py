@@ -331,7 +331,8 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
     of 64 letters over 20, score + one traceback; (3) semiglobal affine open 10 / extend 1
     on 256 pairs of 5000 x 10000 residues of a 20-letter alphabet (per-batch Dirichlet(1)
     frequencies, symmetric integer matrix: diagonal U[4, 11], off-diagonal U[-4, 2]),
-    score only, and the first 20 all-optimal alignments of 2 pairs."""
+    score only, and all-optimal: masks, path counts and the first 20 alignments of every
+    pair on the device."""
     import types
     out = {}
     P = ctypes.POINTER
@@ -431,8 +432,10 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
 
     # all-optimal codomain on the whole bag through the native module's iterator form:
     # one solve writes the 16-bit all-optimal masks of all 256 pairs (25.6 GB, left on the
-    # device), the co-optimal path counts of every pair are computed on the device, and the
-    # host enumerates the first 20 alignments of two pairs in the reference's order
+    # device), the co-optimal path counts of every pair are computed on the device, the
+    # first 20 alignments of every pair are enumerated on the device in the reference's
+    # order, and the host search (pa_iterator_next) enumerates the first 20 of two pairs --
+    # the reference's way, one lane at a time -- which must equal the device's
     mod = alg.m16
     Ba = min(allopt_pairs, B3)
     o3 = opts(alg, "SEMIGLOBAL", "ALIGNMENT", AffineGap(10.0, 1.0), Ba, count="ALL")
@@ -446,13 +449,28 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
     counts = alg.path_counts(res[0]._res)
     t_count = time.perf_counter() - t0
     t0 = time.perf_counter()
-    n_items = 0
-    for it in res[:2]:
+    first = alg.FirstAlignments(res[0]._res, 20)
+    t_dev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    host_maps = []
+    for lane in range(min(2, Ba)):
+        h = ctypes.c_void_p()
+        alg.check(L.pa_result_iterator(res[0]._res.ptr, lane, ctypes.byref(h)))
         for _ in range(20):
-            if it.next() is None:
+            mp = np.zeros(min(int(ls3[lane]), int(lt3[lane])), np.int32)
+            if not L.pa_iterator_next(h, None, mp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), None, None):
                 break
-            n_items += 1
+            host_maps.append((lane, mp))
+        L.pa_iterator_destroy(h)
     t_enum = time.perf_counter() - t0
+    seen = {}
+    enum_bad = 0
+    for lane, mp in host_maps:
+        j = seen.get(lane, 0)
+        seen[lane] = j + 1
+        enum_bad += int(j >= first.counts[lane] or not np.array_equal(first.alignment(lane, j)[0], mp))
+    enum_bad += sum(int(first.counts[lane]) != seen.get(lane, 0) for lane in range(min(2, Ba)))
+    n_items = len(host_maps)
     del res
     cells3 = float((ls3[:Ba].astype(np.int64) * lt3[:Ba]).sum())
     out["semiglobal_affine_5000x10000_all_optimal"] = {
@@ -461,9 +479,15 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
         "path_counts": {"ms": t_count * 1000, "gcups": cells3 / t_count / 1e9,
                         "min": int(counts.min()), "median": float(np.median(counts.astype(np.float64))),
                         "max": int(counts.max()), "saturated": int((counts == np.iinfo(np.uint64).max).sum())},
-        "first_alignments": {"pairs": 2, "alignments": n_items, "ms": t_enum * 1000},
+        "first_alignments": {"pairs": Ba, "alignments": int(first.counts.sum()), "ms": t_dev * 1000,
+                             "alignments_per_s": float(first.counts.sum()) / t_dev,
+                             "host_search": {"pairs": min(2, Ba), "alignments": n_items, "ms": t_enum * 1000,
+                                             "alignments_per_s": n_items / t_enum if t_enum > 0 else None},
+                             "parity": {"compared": n_items, "mismatches": enum_bad,
+                                        "against": "the host search (pa_iterator_next) of the same lanes"}},
         "workload": f"{Ba} pairs of 5000 x 10000, all-optimal masks of every pair on the GPU (host-timed solve "
-                    "call), co-optimal path counts on the GPU, first 20 alignments of 2 pairs (host DFS)"}
+                    "call), co-optimal path counts on the GPU, first 20 alignments of every pair enumerated on "
+                    "the GPU (host-timed call, maps on the host), and of 2 pairs by the host search"}
     return out
 
 

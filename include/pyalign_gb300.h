@@ -237,6 +237,23 @@ void pa_iterator_destroy(pa_iterator *it);
  * 2^64 - 1.  The reference has no counterpart: its enumeration is the only way to count. */
 pa_status pa_result_path_counts(const pa_result *r, uint64_t *counts);
 
+/* The first k optimal alignments of every lane of an all-optimal result (count ALL, linear or
+ * affine gaps), enumerated on the device in the order and with the de-duplication of the
+ * reference's depth-first search (TracebackIterators<true>::Iterator::next,
+ * solver.h:1647-1716; remove_dup as the solver's options say): the same results, in the same
+ * order, as the first k calls of pa_iterator_next on each lane, for all lanes in one pass.
+ * Host outputs: counts (batch int32) = results of each lane, <= k (< k: the lane has no
+ * more); maps (may be NULL) = lane L's results at k * sum_{l < L} min(|s_l|, |t_l|), result j
+ * at + j * min(|s_L|, |t_L|), each an s_to_t map when |s| <= |t| and a t_to_s map otherwise,
+ * -1 where unaligned; paths and path_len (both or neither) = each result's walk, lane L's
+ * at k * sum_{l < L} (|s_l| + |t_l| + 2) points (x, y int32), result j at
+ * + j * (|s_L| + |t_L| + 2) points, path_len[L * k + j] points long; the slots past a lane's
+ * count hold -1 maps and 0 path lengths.  The scores are the
+ * lane's score (pa_result_score).  Blocks until the outputs are written.  No counterpart in
+ * the reference: it enumerates one lane at a time. */
+pa_status pa_result_first_alignments(const pa_result *r, int32_t k, int32_t *counts, int32_t *maps,
+                                     int32_t *paths, int32_t *path_len);
+
 /* ---- batched form: the whole bag in one call (no per-lane objects) ----
  * Score plus one optimal traceback for `batch` pairs of uneven lengths, the throughput
  * path behind ProblemBatch.  Inputs and outputs are host or device memory

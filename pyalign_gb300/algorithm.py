@@ -23,6 +23,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libpyalign_gb300.so")
 
 PA_OK, PA_ERR_INVALID_ARGUMENT, PA_ERR_LENGTH = 0, 1, 2
+PA_ERR_UNSUPPORTED = 7
 
 _c_i32, _c_i64, _c_f32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_float
 _P = ctypes.c_void_p
@@ -123,6 +124,7 @@ def lib():
         L.pa_iterator_next.argtypes = [_P, _PF, _PI, _PI, _PL]
         L.pa_iterator_destroy.argtypes = [_P]
         L.pa_result_path_counts.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64)]
+        L.pa_result_first_alignments.argtypes = [_P, _c_i32, _PI, _PI, _PI, _PI]
         _lib = L
     return _lib
 
@@ -255,11 +257,12 @@ def _general_costs(spec, n):
 class _Result:
     """Owner of a pa_result handle (one solve call)."""
 
-    __slots__ = ("ptr", "_path_counts")
+    __slots__ = ("ptr", "_path_counts", "_first")
 
     def __init__(self, ptr):
         self.ptr = ptr
         self._path_counts = None
+        self._first = {}
 
     def __del__(self):
         if self.ptr and _lib is not None:
@@ -452,12 +455,91 @@ class Solution:
         return Algorithm(*(L.pa_result_algorithm(self._res.ptr, k).decode() for k in range(3)))
 
 
+class FirstAlignments:
+    """The first k optimal alignments of every lane of an all-optimal result, enumerated on
+    the GPU in one pass (pa_result_first_alignments): what the first k next() calls of each
+    lane's iterator return.  `counts[lane]` results per lane (fewer than k: the lane has no
+    more); `alignment(lane, j)` -> the j-th map (s_to_t if |s| <= |t|, else t_to_s) and, when
+    enumerated with paths, the j-th walk ((n, 2) points)."""
+
+    __slots__ = ("k", "counts", "maps", "mstart", "msize", "paths", "plen", "pstart", "pstride")
+
+    def __init__(self, res, k, with_paths=False):
+        L = lib()
+        n = L.pa_result_size(res.ptr)
+        ls = np.zeros(n, np.int32)
+        lt = np.zeros(n, np.int32)
+        check(L.pa_result_lengths(res.ptr, _ip(ls), _ip(lt)))
+        self.k = int(k)
+        self.msize = np.minimum(ls, lt).astype(np.int64)
+        self.mstart = np.zeros(n, np.int64)
+        self.mstart[1:] = np.cumsum(self.msize)[:-1] * self.k
+        self.counts = np.zeros(n, np.int32)
+        self.maps = np.zeros(max(1, int(self.msize.sum()) * self.k), np.int32)
+        self.paths = self.plen = self.pstart = self.pstride = None
+        if with_paths:
+            self.pstride = (ls.astype(np.int64) + lt + 2)
+            self.pstart = np.zeros(n, np.int64)
+            self.pstart[1:] = np.cumsum(self.pstride)[:-1] * self.k
+            self.paths = np.zeros((max(1, int(self.pstride.sum()) * self.k), 2), np.int32)
+            self.plen = np.zeros(n * self.k, np.int32)
+        st = L.pa_result_first_alignments(res.ptr, self.k, _ip(self.counts), _ip(self.maps),
+                                          _ip(self.paths) if with_paths else None,
+                                          _ip(self.plen) if with_paths else None)
+        if st == PA_ERR_UNSUPPORTED:
+            raise NotImplementedError(L.pa_last_error().decode())
+        check(st)
+
+    def alignment(self, lane, j):
+        m = int(self.msize[lane])
+        a = int(self.mstart[lane]) + j * m
+        path = None
+        if self.paths is not None:
+            b = int(self.pstart[lane]) + j * int(self.pstride[lane])
+            path = self.paths[b:b + int(self.plen[lane * self.k + j])]
+        return self.maps[a:a + m], path
+
+
+_ENUM_BYTES = 1 << 30  # host memory the iterators' device enumeration may fill
+
+
+def _enumerated(res, with_paths):
+    """The device enumeration backing a result's all-optimal iterators, made at the first
+    next() of any of its lanes: the first k results of every lane, k = 101 (one more than
+    pyalign's List codomain takes, so its exhaustion test is served too; PA_ENUM_FIRST sets k,
+    0 turns this off), lowered so the results fit _ENUM_BYTES.  None when the result is not an
+    all-optimal one with linear or affine gaps (its iterators run on the host)."""
+    key = bool(with_paths)
+    if key in res._first:
+        return res._first[key]
+    k = int(os.environ.get("PA_ENUM_FIRST", "101"))
+    f = None
+    if k > 0:
+        L = lib()
+        n = L.pa_result_size(res.ptr)
+        ls = np.zeros(n, np.int32)
+        lt = np.zeros(n, np.int32)
+        check(L.pa_result_lengths(res.ptr, _ip(ls), _ip(lt)))
+        per = 4 * int(np.minimum(ls, lt).sum()) + 12 * n
+        if with_paths:
+            per += 8 * int((ls.astype(np.int64) + lt + 2).sum()) + 4 * n
+        k = min(k, _ENUM_BYTES // max(per, 1))
+        if k > 0:
+            try:
+                f = FirstAlignments(res, k, with_paths)
+            except NotImplementedError:
+                f = None
+    res._first[key] = f
+    return f
+
+
 class _Iter:
+    _with_paths = False
+
     def __init__(self, res, lane, ls, lt, dtype):
         self._res, self._lane, self._ls, self._lt, self._dtype = res, lane, ls, lt, dtype
-        h = _P()
-        check(lib().pa_result_iterator(res.ptr, lane, ctypes.byref(h)))
-        self._it = h
+        self._it = None      # the host search, made when the device results run out
+        self._served = 0     # results returned so far
 
     def __del__(self):
         if getattr(self, "_it", None) and _lib is not None:
@@ -472,12 +554,32 @@ class _Iter:
         return int(path_counts(self._res)[self._lane])
 
     def _next(self):
+        L = lib()
+        f = _enumerated(self._res, self._with_paths)
+        if f is not None:
+            c = int(f.counts[self._lane])
+            if self._served < c:
+                mp, path = f.alignment(self._lane, self._served)
+                self._served += 1
+                return float(L.pa_result_score(self._res.ptr, self._lane)), mp.copy(), \
+                    (path.copy() if path is not None else np.zeros((0, 2), np.int32))
+            if c < f.k:
+                return None
+        if self._it is None:
+            # the host search (pa_iterator_next), resumed after the results already served
+            h = _P()
+            check(L.pa_result_iterator(self._res.ptr, self._lane, ctypes.byref(h)))
+            self._it = h
+            for _ in range(self._served):
+                if not L.pa_iterator_next(h, None, None, None, None):
+                    return None
         sc = ctypes.c_float(0)
         mp = np.zeros((min(self._ls, self._lt),), dtype=np.int32)
         path = np.zeros((self._ls + self._lt + 4, 2), dtype=np.int32)
         n = ctypes.c_int64(0)
-        if not lib().pa_iterator_next(self._it, ctypes.byref(sc), _ip(mp), _ip(path), ctypes.byref(n)):
+        if not L.pa_iterator_next(self._it, ctypes.byref(sc), _ip(mp), _ip(path), ctypes.byref(n)):
             return None
+        self._served += 1
         return float(sc.value), mp, path[:n.value].copy()
 
 
@@ -503,6 +605,8 @@ class AlignmentIterator(_Iter):
 
 class SolutionIterator(_Iter):
     """SolutionIterator (factory.h:271-385): next() -> Solution or None."""
+
+    _with_paths = True
 
     def next(self):
         r = self._next()
@@ -544,6 +648,8 @@ class Solver:
         check(lib().pa_solver_create(ctypes.byref(c), int(max_len_s), int(max_len_t), ctypes.byref(h)))
         self._h = h
         self._batch_size = lib().pa_solver_batch_size(h)
+        # all-optimal iterators with linear or affine gaps enumerate on the device
+        self._enumerable = o.type != Type.DTW and int(o.count) == int(Count.ALL) and c.gap_kind != 2
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -666,6 +772,8 @@ class Solver:
 
     def _iterators(self, res, cls):
         n, ls, lt = self._lanes(res)
+        if not self._enumerable:
+            res._first = {False: None, True: None}  # one-optimal or general gaps: host iterators
         return tuple(cls(res, k, ls[k], lt[k], self._index_dtype) for k in range(n))
 
     def _solutions(self, res):

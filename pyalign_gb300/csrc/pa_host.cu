@@ -24,6 +24,7 @@
 
 #include "../../include/pyalign_gb300.h"
 #include "pa_dp.cuh"
+#include "pa_enum.h"
 #include "pa_launch.h"
 #include "pa_wsb.h"
 
@@ -2993,6 +2994,229 @@ pa_status pa_result_path_counts(const pa_result *r, uint64_t *counts) {
 		d.path_counts.swap(c);
 	}
 	std::memcpy(counts, d.path_counts.data(), size_t(B) * 8);
+	return PA_OK;
+}
+
+// The first k optimal alignments of every lane of an all-optimal result, enumerated on the
+// device (enum_kernel, pa_enum.cu) in the order and with the de-duplication of the
+// reference's depth-first search (solver.h:1647-1716).  Blocks until the results are in the
+// caller's host buffers.
+pa_status pa_result_first_alignments(const pa_result *r, int32_t k, int32_t *counts, int32_t *maps, int32_t *paths,
+                                     int32_t *path_len) {
+	if (!r || !counts || k < 1) return fail(PA_ERR_INVALID_ARGUMENT, "pa_result_first_alignments: bad argument");
+	if ((paths == nullptr) != (path_len == nullptr))
+		return fail(PA_ERR_INVALID_ARGUMENT, "pa_result_first_alignments: paths and path_len go together");
+	const ResultData &d = *r->d;
+	if (d.goal != GOAL_ALL || !d.dev_masks_all || d.gap == GAP_GENERAL)
+		return fail(PA_ERR_UNSUPPORTED, "device enumeration needs an all-optimal result with linear or affine gap costs");
+	const int64_t B = d.batch;
+	if (B == 0) return PA_OK;
+	const bool local = d.loc == LOC_LOCAL;
+	const int64_t K = k;
+	// per-lane regions: maps k x min(|s|, |t|), paths k x (|s| + |t| + 2), the search's path
+	std::vector<int64_t> moff(size_t(B) + 1, 0), poff(size_t(B) + 1, 0), woff(size_t(B) + 1, 0);
+	std::vector<int32_t> has(static_cast<size_t>(B), 0), seed(static_cast<size_t>(2 * B), 0);
+	std::vector<int32_t> all(static_cast<size_t>(B));
+	for (int64_t L = 0; L < B; L++) {
+		const int64_t ls = d.ls[size_t(L)], lt = d.lt[size_t(L)];
+		moff[size_t(L) + 1] = moff[size_t(L)] + K * std::min(ls, lt);
+		poff[size_t(L) + 1] = poff[size_t(L)] + (paths ? K * (ls + lt + 2) : 0);
+		woff[size_t(L) + 1] = woff[size_t(L)] + ls + lt + 2;
+		all[size_t(L)] = int32_t(L);
+		if (!local) {
+			has[size_t(L)] = d.has[size_t(L)];
+			seed[size_t(2 * L)] = d.seeds[size_t(2 * L)];
+			seed[size_t(2 * L + 1)] = d.seeds[size_t(2 * L + 1)];
+		}
+	}
+	DevBuf dl, dm, dhas, dseed, dwork, dpath, dmaps, dpaths, dplen, dhash, dnpts, dcnt, dstat;
+	PA_CUDA(dl.ensure(size_t(2 * B) * 4));
+	PA_CUDA(dm.ensure(size_t(B) * 8));
+	PA_CUDA(dhas.ensure(size_t(B) * 4));
+	PA_CUDA(dseed.ensure(size_t(2 * B) * 4));
+	PA_CUDA(dwork.ensure(size_t(B) * 4));
+	PA_CUDA(cudaMemcpy(dl.p, d.ls.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+	PA_CUDA(cudaMemcpy(dl.as<int32_t>() + B, d.lt.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+	PA_CUDA(cudaMemcpy(dm.p, d.mask_off.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+	PA_CUDA(cudaMemcpy(dhas.p, has.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+	PA_CUDA(cudaMemcpy(dseed.p, seed.data(), size_t(2 * B) * 4, cudaMemcpyHostToDevice));
+	int dev = 0, sms = 1;
+	PA_CUDA(cudaGetDevice(&dev));
+	PA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+
+	// ---- local seeds: every cell with the seed bit, in the stack's pop order (increasing row,
+	// then column: the reverse of the push order, solver.h:2066-2091); only lanes with a
+	// strictly positive optimum have any
+	DevBuf dsd, dsoff, dsn, dscap;
+	if (local) {
+		std::vector<int32_t> cand;
+		for (int64_t L = 0; L < B; L++)
+			if (d.ls[size_t(L)] > 0 && d.lt[size_t(L)] > 0 && d.scores[size_t(L)] * d.sign > 0.0f)
+				cand.push_back(int32_t(L));
+		std::vector<int32_t> cap(static_cast<size_t>(B), 0), n(static_cast<size_t>(B), 0);
+		int seed_cap0 = 16;
+		if (const char *e = std::getenv("PA_ENUM_SEEDS")) seed_cap0 = std::max(1, std::atoi(e));  // tests
+		for (int32_t L : cand) cap[size_t(L)] = seed_cap0;
+		std::vector<std::vector<std::pair<int32_t, int32_t>>> found(static_cast<size_t>(B));
+		std::vector<int32_t> work = cand;
+		for (int round = 0; !work.empty(); round++) {
+			if (round > 1) return fail(PA_ERR_INTERNAL, "local seed scan did not settle");
+			std::vector<int64_t> off(size_t(B) + 1, 0);
+			for (int64_t L = 0; L < B; L++) off[size_t(L) + 1] = off[size_t(L)] + cap[size_t(L)];
+			PA_CUDA(dsd.ensure(size_t(std::max<int64_t>(off[size_t(B)], 1)) * 8));
+			PA_CUDA(dsoff.ensure(size_t(B) * 8));
+			PA_CUDA(dscap.ensure(size_t(B) * 4));
+			PA_CUDA(dsn.ensure(size_t(B) * 4));
+			PA_CUDA(cudaMemcpy(dsoff.p, off.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+			PA_CUDA(cudaMemcpy(dscap.p, cap.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+			PA_CUDA(cudaMemset(dsn.p, 0, size_t(B) * 4));
+			PA_CUDA(cudaMemcpy(dwork.p, work.data(), work.size() * 4, cudaMemcpyHostToDevice));
+			pa::SeedScanParams sp{};
+			sp.nwork = int32_t(work.size());
+			sp.work = dwork.as<int32_t>();
+			sp.G = d.G;
+			sp.len_s = dl.as<int32_t>();
+			sp.len_t = dl.as<int32_t>() + B;
+			sp.mask_off = dm.as<int64_t>();
+			sp.masks = static_cast<const uint4 *>(d.dev_masks_all);
+			sp.seeds = dsd.as<int2>();
+			sp.seed_off = dsoff.as<int64_t>();
+			sp.seed_cap = dscap.as<int32_t>();
+			sp.seed_n = dsn.as<int32_t>();
+			const int grid = int(std::min<int64_t>(int64_t(work.size()), int64_t(sms) * 8));
+			PA_CUDA(pa::enum_seed_scan(sp, grid, nullptr));
+			std::vector<int32_t> got(static_cast<size_t>(B));
+			std::vector<int2> buf(size_t(std::max<int64_t>(off[size_t(B)], 1)));
+			PA_CUDA(cudaMemcpy(got.data(), dsn.p, size_t(B) * 4, cudaMemcpyDeviceToHost));
+			PA_CUDA(cudaMemcpy(buf.data(), dsd.p, size_t(off[size_t(B)]) * 8, cudaMemcpyDeviceToHost));
+			std::vector<int32_t> again;
+			for (int32_t L : work) {
+				if (got[size_t(L)] > cap[size_t(L)]) {  // more seeds than room: scan this lane again
+					again.push_back(L);
+					continue;
+				}
+				auto &f = found[size_t(L)];
+				f.clear();
+				for (int32_t x = 0; x < got[size_t(L)]; x++) {
+					const int2 c = buf[size_t(off[size_t(L)] + x)];
+					f.push_back({c.x, c.y});
+				}
+				std::sort(f.begin(), f.end());
+				n[size_t(L)] = got[size_t(L)];
+			}
+			std::fill(cap.begin(), cap.end(), 0);
+			for (int32_t L : again) cap[size_t(L)] = got[size_t(L)];
+			work.swap(again);
+		}
+		std::vector<int64_t> off(size_t(B) + 1, 0);
+		for (int64_t L = 0; L < B; L++) off[size_t(L) + 1] = off[size_t(L)] + n[size_t(L)];
+		std::vector<int2> flat(size_t(std::max<int64_t>(off[size_t(B)], 1)));
+		for (int64_t L = 0; L < B; L++)
+			for (size_t x = 0; x < found[size_t(L)].size(); x++)
+				flat[size_t(off[size_t(L)]) + x] = make_int2(found[size_t(L)][x].first, found[size_t(L)][x].second);
+		PA_CUDA(dsd.ensure(flat.size() * 8));
+		PA_CUDA(dsoff.ensure(size_t(B) * 8));
+		PA_CUDA(dsn.ensure(size_t(B) * 4));
+		PA_CUDA(cudaMemcpy(dsd.p, flat.data(), flat.size() * 8, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemcpy(dsoff.p, off.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemcpy(dsn.p, n.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+	}
+
+	// ---- the search
+	PA_CUDA(dpath.ensure(size_t(woff[size_t(B)]) * 8));
+	PA_CUDA(dmaps.ensure(size_t(std::max<int64_t>(moff[size_t(B)], 1)) * 4));
+	if (paths) {
+		PA_CUDA(dpaths.ensure(size_t(std::max<int64_t>(poff[size_t(B)], 1)) * 8));
+		PA_CUDA(dplen.ensure(size_t(B * K) * 4));
+	}
+	PA_CUDA(dhash.ensure(size_t(B * K) * 8));
+	PA_CUDA(dnpts.ensure(size_t(B * K) * 4));
+	PA_CUDA(dcnt.ensure(size_t(B) * 4));
+	PA_CUDA(dstat.ensure(size_t(B) * 4));
+	DevBuf dmo, dpo, dwo;
+	PA_CUDA(dmo.ensure(size_t(B) * 8));
+	PA_CUDA(dpo.ensure(size_t(B) * 8));
+	PA_CUDA(dwo.ensure(size_t(B) * 8));
+	PA_CUDA(cudaMemcpy(dmo.p, moff.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+	PA_CUDA(cudaMemcpy(dpo.p, poff.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+	PA_CUDA(cudaMemcpy(dwo.p, woff.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+	// stacks: |s| + |t| + 66 entries per lane at first; a lane that fills its stack is
+	// enumerated again with four times the room
+	std::vector<int32_t> scap(static_cast<size_t>(B), 0);
+	int64_t stack0 = -1;
+	if (const char *e = std::getenv("PA_ENUM_STACK")) stack0 = std::max(1, std::atoi(e));  // tests
+	for (int64_t L = 0; L < B; L++)
+		scap[size_t(L)] = int32_t(stack0 > 0 ? stack0 : d.ls[size_t(L)] + d.lt[size_t(L)] + 66);
+	std::vector<int32_t> work = all, status(static_cast<size_t>(B), 0);
+	DevBuf dstk, dsto, dscp;
+	PA_CUDA(dsto.ensure(size_t(B) * 8));
+	PA_CUDA(dscp.ensure(size_t(B) * 4));
+	for (int round = 0; !work.empty(); round++) {
+		std::vector<int64_t> so(static_cast<size_t>(B), 0);
+		int64_t tot = 0;
+		for (int32_t L : work) {
+			so[size_t(L)] = tot;
+			tot += scap[size_t(L)];
+		}
+		if (tot > (int64_t(1) << 31))
+			return fail(PA_ERR_INTERNAL, "device enumeration: the search stacks outgrow the device");
+		PA_CUDA(dstk.ensure(size_t(std::max<int64_t>(tot, 1)) * 16));
+		PA_CUDA(cudaMemcpy(dsto.p, so.data(), size_t(B) * 8, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemcpy(dscp.p, scap.data(), size_t(B) * 4, cudaMemcpyHostToDevice));
+		PA_CUDA(cudaMemcpy(dwork.p, work.data(), work.size() * 4, cudaMemcpyHostToDevice));
+		pa::EnumParams ep{};
+		ep.nwork = int32_t(work.size());
+		ep.work = dwork.as<int32_t>();
+		ep.G = d.G;
+		ep.local = local ? 1 : 0;
+		ep.affine = d.gap == GAP_AFFINE ? 1 : 0;
+		ep.remove_dup = d.remove_dup ? 1 : 0;
+		ep.k = k;
+		ep.len_s = dl.as<int32_t>();
+		ep.len_t = dl.as<int32_t>() + B;
+		ep.mask_off = dm.as<int64_t>();
+		ep.masks = static_cast<const uint4 *>(d.dev_masks_all);
+		ep.has = dhas.as<int32_t>();
+		ep.seed = dseed.as<int32_t>();
+		ep.seeds = local ? dsd.as<int2>() : nullptr;
+		ep.seed_off = local ? dsoff.as<int64_t>() : nullptr;
+		ep.seed_n = local ? dsn.as<int32_t>() : nullptr;
+		ep.stack = dstk.as<int4>();
+		ep.stack_off = dsto.as<int64_t>();
+		ep.stack_cap = dscp.as<int32_t>();
+		ep.path = dpath.as<int2>();
+		ep.path_off = dwo.as<int64_t>();
+		ep.maps = dmaps.as<int32_t>();
+		ep.map_off = dmo.as<int64_t>();
+		ep.paths = paths ? dpaths.as<int2>() : nullptr;
+		ep.paths_off = dpo.as<int64_t>();
+		ep.path_len = paths ? dplen.as<int32_t>() : nullptr;
+		ep.hash = dhash.as<unsigned long long>();
+		ep.npts = dnpts.as<int32_t>();
+		ep.count = dcnt.as<int32_t>();
+		ep.status = dstat.as<int32_t>();
+		PA_CUDA(pa::enum_solve(ep, nullptr));
+		PA_CUDA(cudaMemcpy(status.data(), dstat.p, size_t(B) * 4, cudaMemcpyDeviceToHost));
+		std::vector<int32_t> again;
+		for (int32_t L : work) {
+			if (status[size_t(L)] == pa::ENUM_BAD_PATH)
+				return fail(PA_ERR_INTERNAL, "device enumeration: a path outgrew |s| + |t| + 2 points");
+			if (status[size_t(L)] == pa::ENUM_OVERFLOW) {
+				if (scap[size_t(L)] > (1 << 28)) return fail(PA_ERR_INTERNAL, "device enumeration: stack limit");
+				scap[size_t(L)] *= 4;
+				again.push_back(L);
+			}
+		}
+		work.swap(again);
+	}
+	PA_CUDA(cudaMemcpy(counts, dcnt.p, size_t(B) * 4, cudaMemcpyDeviceToHost));
+	if (maps && moff[size_t(B)] > 0)
+		PA_CUDA(cudaMemcpy(maps, dmaps.p, size_t(moff[size_t(B)]) * 4, cudaMemcpyDeviceToHost));
+	if (paths) {
+		if (poff[size_t(B)] > 0)
+			PA_CUDA(cudaMemcpy(paths, dpaths.p, size_t(poff[size_t(B)]) * 8, cudaMemcpyDeviceToHost));
+		PA_CUDA(cudaMemcpy(path_len, dplen.p, size_t(B * K) * 4, cudaMemcpyDeviceToHost));
+	}
 	return PA_OK;
 }
 
