@@ -992,9 +992,16 @@ def run_ours(args):
             np.asarray(api_res[B - 1].s_to_t if ls[B - 1] <= lt[B - 1] else api_res[B - 1].t_to_s),
             mp_h.numpy()[offs[B - 1]:offs[B - 1] + sizes[B - 1]]):
         raise SystemExit("module call and pa_solve_batch disagree")
+    t0 = time.perf_counter()
+    n_obj = sum(1 for _ in api_res)
+    objects_ms = (time.perf_counter() - t0) * 1000
     e2e_api = {"value": cells * world * api_steps / api_s / 1e9, "unit": "GCUPS", "steps": api_steps,
                "call": "Solver.solve_indexed_for_alignment of the native module (one call for the whole bag), "
-                       "host numpy arrays, a tuple of Alignment objects returned"}
+                       "host numpy arrays; returns the per-lane sequence of Alignment objects, each made at its "
+                       "first access",
+               "objects_ms": objects_ms, "objects": n_obj,
+               "objects_note": "making all Alignment objects of one call by iterating the sequence (outside the "
+                               "timed calls; pyalign's own loop does this, solve.py:374-379)"}
     del api_res
 
     # ---- the plain GPU path: one launch per length bucket (100-wide bins of |s| and |t|)

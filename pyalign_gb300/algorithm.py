@@ -13,8 +13,11 @@ Every solve runs on the GPU.  If the library is not built or no CUDA device is p
 calls fail loudly; there is no CPU fallback.
 """
 
+import collections.abc
 import ctypes
 import enum
+import functools
+import operator
 import os
 
 import numpy as np
@@ -276,6 +279,45 @@ def _narrow(a, dtype):
         lo = np.iinfo(np.int16).min
         return np.where(a == np.iinfo(np.int32).min, lo, a).astype(np.int16)
     return a.astype(np.int32, copy=False)
+
+
+class _Lanes(collections.abc.Sequence):
+    """The per-lane results of one solve call -- the tuple the reference's methods return, one
+    entry per lane (factory.h:699-808) -- with each entry made at its first access and kept:
+    a call over 65,536 pairs returns without making 65,536 Python objects, and a consumer
+    that walks the results (pyalign zips them with its problems, solve.py:374-379) makes each
+    one once.  Indexing, negative indices, slices (as tuples), len() and iteration behave as
+    on a tuple."""
+
+    __slots__ = ("_make", "_items")
+
+    def __init__(self, make, n):
+        self._make = make
+        self._items = [None] * n
+
+    def __len__(self):
+        return len(self._items)
+
+    def __getitem__(self, k):
+        if isinstance(k, slice):
+            return tuple(self[i] for i in range(*k.indices(len(self._items))))
+        n = len(self._items)
+        k = operator.index(k)
+        if k < 0:
+            k += n
+        if not 0 <= k < n:
+            raise IndexError("result index out of range")
+        x = self._items[k]
+        if x is None:
+            x = self._items[k] = self._make(k)
+        return x
+
+    def __iter__(self):
+        for k in range(len(self._items)):
+            yield self[k]
+
+    def __repr__(self):
+        return f"({', '.join(repr(x) for x in self)})"
 
 
 class _AlignmentBatch:
@@ -767,18 +809,19 @@ class Solver:
         scores = np.zeros((n,), dtype=np.float32)
         check(lib().pa_result_export(res.ptr, _fp(scores), _ip(maps), offs.ctypes.data_as(_PL)))
         batch = _AlignmentBatch(scores, maps, offs, sizes, ls, lt, self._index_dtype)
-        lazy = Alignment._lazy
-        return tuple(lazy(batch, k) for k in range(n))
+        return _Lanes(functools.partial(Alignment._lazy, batch), n)
 
     def _iterators(self, res, cls):
         n, ls, lt = self._lanes(res)
         if not self._enumerable:
             res._first = {False: None, True: None}  # one-optimal or general gaps: host iterators
-        return tuple(cls(res, k, ls[k], lt[k], self._index_dtype) for k in range(n))
+        dt = self._index_dtype
+        return _Lanes(lambda k: cls(res, k, ls[k], lt[k], dt), n)
 
     def _solutions(self, res):
         n, ls, lt = self._lanes(res)
-        return tuple(Solution(res, k, ls[k], lt[k], self._index_dtype) for k in range(n))
+        dt = self._index_dtype
+        return _Lanes(lambda k: Solution(res, k, ls[k], lt[k], dt), n)
 
     def _dispatch(self, codomain, form, args):
         if codomain == "score":
