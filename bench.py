@@ -983,11 +983,16 @@ def run_ours(args):
     api_res = api_solver.solve_indexed_for_alignment(a, b, table, ln16)
     barrier()
     api_steps = max(3, args.steps // 4)
+    api_calls = []
     t0 = time.perf_counter()
     for _ in range(api_steps):
+        t1 = time.perf_counter()
         api_res = api_solver.solve_indexed_for_alignment(a, b, table, ln16)
+        api_calls.append((time.perf_counter() - t1) * 1000)
     barrier()
     api_s = max_over_ranks(time.perf_counter() - t0)
+    L.pa_solver_last_timings(api_solver.handle, ms4, ctypes.byref(nl))
+    api_phases = {"upload": ms4[0], "dp": ms4[1], "traceback": ms4[2], "download": ms4[3]}
     if float(api_res[0].score) != float(sc_h[0]) or not np.array_equal(
             np.asarray(api_res[B - 1].s_to_t if ls[B - 1] <= lt[B - 1] else api_res[B - 1].t_to_s),
             mp_h.numpy()[offs[B - 1]:offs[B - 1] + sizes[B - 1]]):
@@ -999,6 +1004,7 @@ def run_ours(args):
                "call": "Solver.solve_indexed_for_alignment of the native module (one call for the whole bag), "
                        "host numpy arrays; returns the per-lane sequence of Alignment objects, each made at its "
                        "first access",
+               "call_ms": api_calls, "phases_ms_last_call": api_phases,
                "objects_ms": objects_ms, "objects": n_obj,
                "objects_note": "making all Alignment objects of one call by iterating the sequence (outside the "
                                "timed calls; pyalign's own loop does this, solve.py:374-379)"}

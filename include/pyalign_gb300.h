@@ -276,6 +276,19 @@ typedef struct pa_batch {
 pa_status pa_solve_batch(pa_solver *s, const pa_batch *batch, float *scores, int32_t *maps,
                          const int64_t *map_offsets);
 
+/* The alignment codomain of the solve_*_for_alignment methods (factory.h:699-808) with the
+ * maps written straight into the caller's host buffer: host inputs (`location` PA_HOST), maps
+ * at map_offsets (host, batch entries, the prefix sums of min(|s|, |t|) of the lengths
+ * clamped to [0, n_s] and [0, n_t]), and a result object for the rest of each lane's
+ * Alignment (pa_result_score: the score, or the worst value where the lane has no
+ * alignment; pa_result_has_alignment).  pa_result_alignment / pa_result_export of maps refuse
+ * such a result (its maps are the caller's).  One-optimal solvers (count ONE, detail ALIGNMENT
+ * or SOLUTION, or DTW) with linear, affine or DTW costs; others get PA_ERR_UNSUPPORTED.  No
+ * counterpart in the reference: the module's solve_*_for_alignment methods use it to skip a
+ * copy of every map. */
+pa_status pa_solve_batch_result(pa_solver *s, const pa_batch *batch, int32_t *maps, const int64_t *map_offsets,
+                                pa_result **out);
+
 /* ---- differentiation (the fwd+bwd form) ----
  * Forward: score plus one optimal path per pair for a dense similarity held in device
  * memory with an explicit layout, S(k, i, j) = sim[offsets[k] + i*stride_s + j*stride_t]

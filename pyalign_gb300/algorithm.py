@@ -128,6 +128,7 @@ def lib():
         L.pa_iterator_destroy.argtypes = [_P]
         L.pa_result_path_counts.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64)]
         L.pa_result_first_alignments.argtypes = [_P, _c_i32, _PI, _PI, _PI, _PI]
+        L.pa_solve_batch_result.argtypes = [_P, ctypes.POINTER(Batch), _PI, _PL, ctypes.POINTER(_P)]
         _lib = L
     return _lib
 
@@ -692,6 +693,10 @@ class Solver:
         self._batch_size = lib().pa_solver_batch_size(h)
         # all-optimal iterators with linear or affine gaps enumerate on the device
         self._enumerable = o.type != Type.DTW and int(o.count) == int(Count.ALL) and c.gap_kind != 2
+        # one-optimal alignments with linear, affine or DTW costs: maps straight into the
+        # call's array (pa_solve_batch_result)
+        self._direct_maps = o.type == Type.DTW or (int(o.count) == int(Count.ONE) and
+                                                   int(o.detail) != int(Detail.SCORE) and c.gap_kind != 2)
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -739,8 +744,9 @@ class Solver:
     def _codes(x):
         return np.ascontiguousarray(x, dtype=np.uint32)
 
-    def _call(self, name, form, args):
-        L = lib()
+    def _inputs(self, form, args):
+        """Checked and converted arguments of a solve call (factory.h:424-507): the C
+        arguments before the outputs, the arrays they point into, and a pa_batch of them."""
         def batch_check(given):  # factory.h:387-394, checked before the lengths (526-533)
             if given != self._batch_size:
                 raise ValueError(f"problem of batch size {given} given to solver that was "
@@ -778,6 +784,20 @@ class Solver:
             lens = ln
         if lens.ndim != 2 or lens.shape[0] != 2 or lens.shape[1] != self._batch_size:
             raise ValueError(f"m_length has shape {tuple(lens.shape)}, expected (2, {self._batch_size})")
+        if form == "dense":
+            bt = Batch(form=0, location=0, batch=sim.shape[2], n_s=sim.shape[0], n_t=sim.shape[1], sim=_fp(sim),
+                       length=_ip(ln))
+        elif form == "indexed":
+            bt = Batch(form=1, location=0, batch=a.shape[0], n_s=a.shape[1], n_t=b.shape[1], a=_up(a), b=_up(b),
+                       table=_fp(sim), table_rows=sim.shape[0], table_cols=sim.shape[1], length=_ip(ln))
+        else:
+            bt = Batch(form=2, location=0, batch=a.shape[0], n_s=a.shape[1], n_t=b.shape[1], a=_up(a), b=_up(b),
+                       eq=float(eq), ne=float(ne), length=_ip(ln))
+        return head, keep, bt
+
+    def _call(self, name, form, args):
+        L = lib()
+        head, keep, _ = self._inputs(form, args)
         prefix = {"dense": "pa_solve_for_", "indexed": "pa_solve_indexed_for_", "binary": "pa_solve_binary_for_"}[form]
         fn = getattr(L, prefix + name)
         if name == "score":
@@ -823,9 +843,34 @@ class Solver:
         dt = self._index_dtype
         return _Lanes(lambda k: Solution(res, k, ls[k], lt[k], dt), n)
 
+    def _alignment_call(self, form, args):
+        """solve_*_for_alignment: the maps go straight into this call's array
+        (pa_solve_batch_result), the scores come from the result object."""
+        L = lib()
+        head, keep, bt = self._inputs(form, args)
+        n = int(bt.batch)
+        ln = keep[-1]
+        ls = np.clip(ln[0], 0, int(bt.n_s)).astype(np.int64)  # the lengths as the solve clamps them
+        lt = np.clip(ln[1], 0, int(bt.n_t)).astype(np.int64)
+        sizes = np.minimum(ls, lt)
+        offs = np.zeros((n,), dtype=np.int64)
+        if n > 1:
+            np.cumsum(sizes[:-1], out=offs[1:])
+        maps = np.empty((int(sizes.sum()),), dtype=np.int32)
+        h = _P()
+        check(L.pa_solve_batch_result(self._h, ctypes.byref(bt), _ip(maps), offs.ctypes.data_as(_PL), ctypes.byref(h)))
+        del keep
+        res = _Result(h)
+        scores = np.empty((n,), dtype=np.float32)
+        check(L.pa_result_export(res.ptr, _fp(scores), None, None))
+        batch = _AlignmentBatch(scores, maps, offs, sizes, ls, lt, self._index_dtype)
+        return _Lanes(functools.partial(Alignment._lazy, batch), n)
+
     def _dispatch(self, codomain, form, args):
         if codomain == "score":
             return self._call("score", form, args)
+        if codomain == "alignment" and self._direct_maps:
+            return self._alignment_call(form, args)
         res = self._call(codomain, form, args)
         if codomain == "alignment":
             return self._alignments(res)

@@ -154,6 +154,7 @@ struct ResultData {
 	std::vector<int32_t> seeds;   // 2 per lane
 	std::vector<int64_t> map_off;
 	std::vector<int32_t> maps;
+	bool maps_external = false;  // the maps went to the caller's buffer (pa_solve_batch_result)
 	std::vector<int64_t> path_off;
 	std::vector<int32_t> paths, path_len;
 	std::vector<int64_t> mask_off;
@@ -454,6 +455,17 @@ struct pa_solver {
 };
 
 namespace {
+
+// page-locked (pinned or registered) host memory: copies from or to it run asynchronously
+bool host_pinned(const void *p) {
+	if (!p) return true;
+	cudaPointerAttributes a{};
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeHost;
+}
 
 // every host<->device copy of a solve goes through here, so the solver can report bytes
 cudaError_t pa_copy(pa_solver *s, void *dst, const void *src, size_t n, cudaMemcpyKind kind, cudaStream_t st) {
@@ -1473,7 +1485,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		    r.tcols != in.table_cols || r.dsi != in.dense_si || r.dsj != in.dense_sj || r.stream != st)
 			return false;
 		if (std::memcmp(&r.eq, &in.eq, 4) || std::memcmp(&r.ne, &in.ne, 4)) return false;
-		if (r.maps_out != maps_out || r.ls != ls || r.lt != lt || r.table_host != host_table) return false;
+		// device maps are written by the captured graph, so the buffer must be the same one;
+		// host maps are copied out per call (any buffer with the same offsets will do)
+		if ((in.location == PA_DEVICE && r.maps_out != maps_out) || r.ls != ls || r.lt != lt ||
+		    r.table_host != host_table)
+			return false;
 		if (r.scores != (paths_to_user ? user_paths->scores : nullptr)) return false;
 		if (paths_to_user && (r.paths != user_paths->paths || r.path_len != user_paths->path_len ||
 		                      std::memcmp(r.user_path_off.data(), user_paths->path_off, size_t(B) * 8)))
@@ -1996,10 +2012,16 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		// host buffers and many pairs: the repeats of this solve run as a pipeline of chunks
 		// (3 chunks from 32K pairs, 2 from 8K; PA_CHUNKS overrides, up to 12); host maps use
 		// the packed offsets (checked above)
+		// (pinned buffers only: a copy from or to pageable memory holds the host thread until
+		// it is done, so a chunk's map download would wait for that chunk's DP and walk before
+		// the next chunk is queued, and the chunks would run one after the other)
 		plan.nchunks = 1;
 		if (repeatable && in.location == PA_HOST && in.form != F_DENSE && !plan.units && !want_paths) {
 			int K = B >= 32768 ? 3 : B >= 8192 ? 2 : 1;
-			if (const char *e = std::getenv("PA_CHUNKS")) K = std::atoi(e);
+			const bool pinned = host_pinned(in.a) && host_pinned(in.b) &&
+			                    (need_walk ? maps_out != nullptr && host_pinned(maps_out) : true);
+			if (!pinned) K = 1;
+			if (const char *e = std::getenv("PA_CHUNKS")) K = std::atoi(e);  // tests: any buffers
 			K = std::min(K, 12);
 			if (K > 1 && B >= (int64_t(1) << K)) plan.nchunks = K;
 		}
@@ -2517,6 +2539,34 @@ pa_status pa_solve_batch(pa_solver *s, const pa_batch *b, float *scores, int32_t
 	return PA_OK;
 }
 
+pa_status pa_solve_batch_result(pa_solver *s, const pa_batch *b, int32_t *maps, const int64_t *map_offsets,
+                                pa_result **out) {
+	if (!s || !b || !maps || !map_offsets || !out) return fail(PA_ERR_INVALID_ARGUMENT, "null argument");
+	if (b->location != PA_HOST) return fail(PA_ERR_INVALID_ARGUMENT, "pa_solve_batch_result takes host buffers");
+	if (s->goal != GOAL_ONE || s->gap == GAP_GENERAL)
+		return fail(PA_ERR_UNSUPPORTED, "pa_solve_batch_result: one optimal alignment per pair, linear, affine or DTW");
+	Input in{};
+	in.form = b->form;
+	in.location = PA_HOST;
+	in.batch = b->batch;
+	in.n_s = b->n_s;
+	in.n_t = b->n_t;
+	in.a = b->a;
+	in.b = b->b;
+	in.sim = b->sim;
+	in.table = b->table;
+	in.table_rows = b->table_rows;
+	in.table_cols = b->table_cols;
+	in.eq = b->eq;
+	in.ne = b->ne;
+	in.length = b->length;
+	pa_result *r = nullptr;
+	if (pa_status st = solve_impl(s, in, M_ALIGNMENT, nullptr, &r, maps, map_offsets)) return st;
+	r->d->maps_external = true;
+	*out = r;
+	return PA_OK;
+}
+
 pa_status pa_solve_dense_paths(pa_solver *s, const float *sim, const int64_t *offsets, int64_t stride_s,
                                int64_t stride_t, int64_t batch, int64_t n_s, int64_t n_t, const int32_t *length,
                                float *scores, int32_t *paths, const int64_t *path_offsets, int32_t *path_len) {
@@ -2673,6 +2723,7 @@ extern "C" {
 pa_status pa_result_alignment(const pa_result *r, int64_t lane, int32_t *map) {
 	if (!r || lane < 0 || lane >= r->d->batch) return fail(PA_ERR_INVALID_ARGUMENT, "bad lane");
 	const ResultData &d = *r->d;
+	if (d.maps_external) return fail(PA_ERR_INVALID_ARGUMENT, "this result's maps are in the caller's buffer");
 	const int n = std::min(d.ls[size_t(lane)], d.lt[size_t(lane)]);
 	if (!lane_walk(r, lane, nullptr, map))
 		for (int k = 0; k < n; k++) map[k] = -1;
@@ -2681,6 +2732,8 @@ pa_status pa_result_alignment(const pa_result *r, int64_t lane, int32_t *map) {
 
 pa_status pa_result_export(const pa_result *r, float *scores, int32_t *maps, const int64_t *map_offsets) {
 	if (!r) return fail(PA_ERR_INVALID_ARGUMENT, "null result");
+	if (maps && r->d->maps_external)
+		return fail(PA_ERR_INVALID_ARGUMENT, "this result's maps are in the caller's buffer");
 	for (int64_t k = 0; k < r->d->batch; k++) {
 		if (scores) scores[k] = pa_result_score(r, k);
 		if (maps) pa_result_alignment(r, k, maps + map_offsets[k]);
