@@ -1278,10 +1278,7 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 		return PA_OK;
 	};
 	std::vector<float> cand_ms(cand.size(), INFINITY);
-	// one untimed run first (clocks and caches leave their idle state), then each candidate
-	// timed twice, keeping its faster run: a single cold timing could misplace a candidate
-	for (size_t ci = 0; ci <= cand.size(); ci++) {
-		const Cand &c = cand[ci == 0 ? 0 : ci - 1];
+	auto plan_of = [&](const Cand &c) {
 		Plan pl = plan;
 		pl.G = c.G;
 		pl.units = c.units;
@@ -1289,17 +1286,52 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 		pl.C = c.C;
 		pl.blk = c.blk;
 		pl.seg = false;
-		float ms = INFINITY;
-		if (pa_status e = time_plan(pl, ci == 0 ? 1 : 2, &ms)) return e;
-		if (ci == 0) continue;  // the warm-up
-		cand_ms[ci - 1] = ms;
-		if (ms < best) {
-			best = ms;
-			bestG = pl.G;
-			bestU = pl.units;
-			bestH = pl.h16;
-			bestC = pl.C;
-			bestB = pl.blk;
+		return pl;
+	};
+	// untimed runs first, at least 3 and 30 ms of them (clocks and caches leave their idle
+	// state: a first candidate timed on a cold GPU loses to a slower one timed warm), then
+	// each candidate timed twice, keeping its faster run, and the two fastest timed twice
+	// more, alternately, so neither is judged on one stretch of clock
+	{
+		Plan pl = plan_of(cand[0]);
+		float spent = 0;
+		for (int w = 0; w < 16 && (w < 3 || spent < 30.0f); w++) {
+			float ms = INFINITY;
+			if (pa_status e = time_plan(pl, 1, &ms)) return e;
+			spent += ms;
+		}
+	}
+	for (size_t ci = 0; ci < cand.size(); ci++) {
+		Plan pl = plan_of(cand[ci]);
+		if (pa_status e = time_plan(pl, 2, &cand_ms[ci])) return e;
+	}
+	if (cand.size() >= 2) {
+		size_t a = 0, b = 1;
+		if (cand_ms[b] < cand_ms[a]) std::swap(a, b);
+		for (size_t ci = 2; ci < cand.size(); ci++) {
+			if (cand_ms[ci] < cand_ms[a]) {
+				b = a;
+				a = ci;
+			} else if (cand_ms[ci] < cand_ms[b]) {
+				b = ci;
+			}
+		}
+		for (int rep = 0; rep < 2; rep++)
+			for (size_t ci : {a, b}) {
+				Plan pl = plan_of(cand[ci]);
+				float ms = INFINITY;
+				if (pa_status e = time_plan(pl, 1, &ms)) return e;
+				cand_ms[ci] = std::min(cand_ms[ci], ms);
+			}
+	}
+	for (size_t ci = 0; ci < cand.size(); ci++) {
+		if (cand_ms[ci] < best) {
+			best = cand_ms[ci];
+			bestG = cand[ci].G;
+			bestU = cand[ci].units;
+			bestH = cand[ci].h16;
+			bestC = cand[ci].C;
+			bestB = cand[ci].blk;
 		}
 	}
 	plan.G = bestG;
@@ -1872,23 +1904,34 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			maps_host = maps_out ? maps_out : res.maps.data();
 		}
 		auto range = [&](int c, int64_t &k0, int64_t &k1) { chunk_range(B, K, c, k0, k1); };
+		// page-locked codes are all queued for upload at once; a copy from pageable codes holds
+		// this thread until the copy engine has them, so each chunk's upload is issued just
+		// before that chunk's work (the GPU computes the chunks before it meanwhile).  Maps
+		// go to a page-locked buffer chunk by chunk behind each walk; to pageable memory (or
+		// while uploads still follow on the copy stream) in one copy at the end.
+		const bool pin_in = host_pinned(in.a) && host_pinned(in.b);
+		const bool defer_maps = need_walk && (!pin_in || !host_pinned(maps_host));
+		auto upload = [&](int c) -> cudaError_t {
+			int64_t k0, k1;
+			range(c, k0, k1);
+			cudaError_t e = cudaSuccess;
+			if (in.n_s && k1 > k0)
+				e = pa_copy(s, s->d_a.as<uint32_t>() + k0 * in.n_s, in.a + k0 * in.n_s, size_t((k1 - k0) * in.n_s) * 4,
+				            cudaMemcpyHostToDevice, cs);
+			if (e == cudaSuccess && in.n_t && k1 > k0)
+				e = pa_copy(s, s->d_b.as<uint32_t>() + k0 * in.n_t, in.b + k0 * in.n_t, size_t((k1 - k0) * in.n_t) * 4,
+				            cudaMemcpyHostToDevice, cs);
+			if (e == cudaSuccess) e = cudaEventRecord(ev[c], cs);
+			return e;
+		};
 		// the copy stream and the second compute stream start after the work already queued on
 		// the solver's stream, and after this call's status reset
 		PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, st));
 		PA_CUDA(cudaEventRecord(ev_start, st));
 		PA_CUDA(cudaStreamWaitEvent(cs, ev_start, 0));
 		PA_CUDA(cudaStreamWaitEvent(s->cmp2, ev_start, 0));
-		for (int c = 0; c < K; c++) {
-			int64_t k0, k1;
-			range(c, k0, k1);
-			if (in.n_s && k1 > k0)
-				PA_CUDA(pa_copy(s, s->d_a.as<uint32_t>() + k0 * in.n_s, in.a + k0 * in.n_s, size_t((k1 - k0) * in.n_s) * 4,
-				                cudaMemcpyHostToDevice, cs));
-			if (in.n_t && k1 > k0)
-				PA_CUDA(pa_copy(s, s->d_b.as<uint32_t>() + k0 * in.n_t, in.b + k0 * in.n_t, size_t((k1 - k0) * in.n_t) * 4,
-				                cudaMemcpyHostToDevice, cs));
-			PA_CUDA(cudaEventRecord(ev[c], cs));
-		}
+		if (pin_in)
+			for (int c = 0; c < K; c++) PA_CUDA(upload(c));
 		PA_CUDA(cudaEventRecord(s->ev[1], st));
 		// even chunks on the solver's stream, odd ones on the second compute stream: a chunk's
 		// launch fills the SMs that the previous chunk's tail leaves idle
@@ -1898,6 +1941,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 			range(c, k0, k1);
 			const int side = c & 1;
 			const cudaStream_t sc = side_stream[side];
+			if (!pin_in) PA_CUDA(upload(c));
 			PA_CUDA(cudaStreamWaitEvent(sc, ev[c], 0));
 			if (in.form == F_INDEXED) {
 				uint32_t *mx = s->d_codes_max.as<uint32_t>() + 2 * c;
@@ -1931,12 +1975,14 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 				walk_kernel<<<int((k1 - k0 + 3) / 4), 128, 0, sc>>>(w);
 				PA_CUDA(cudaGetLastError());
 				launches++;
-				PA_CUDA(cudaEventRecord(ev[K + c], sc));
-				PA_CUDA(cudaStreamWaitEvent(cs, ev[K + c], 0));
-				const int64_t m0 = map_off[size_t(k0)], m1 = map_off[size_t(k1)];
-				if (m1 > m0)
-					PA_CUDA(pa_copy(s, maps_host + m0, s->d_maps.as<int32_t>() + m0, size_t(m1 - m0) * 4,
-					                cudaMemcpyDeviceToHost, cs));
+				if (!defer_maps) {
+					PA_CUDA(cudaEventRecord(ev[K + c], sc));
+					PA_CUDA(cudaStreamWaitEvent(cs, ev[K + c], 0));
+					const int64_t m0 = map_off[size_t(k0)], m1 = map_off[size_t(k1)];
+					if (m1 > m0)
+						PA_CUDA(pa_copy(s, maps_host + m0, s->d_maps.as<int32_t>() + m0, size_t(m1 - m0) * 4,
+						                cudaMemcpyDeviceToHost, cs));
+				}
 			}
 		}
 		// join: the solver's stream continues after the second compute stream and the copies
@@ -1945,6 +1991,9 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		PA_CUDA(cudaEventRecord(s->ev[2], st));
 		PA_CUDA(cudaEventRecord(ev_copy, cs));
 		PA_CUDA(cudaStreamWaitEvent(st, ev_copy, 0));
+		if (err == PA_OK && defer_maps && map_off[size_t(B)] > 0)
+			PA_CUDA(pa_copy(s, maps_host, s->d_maps.as<int32_t>(), size_t(map_off[size_t(B)]) * 4,
+			                cudaMemcpyDeviceToHost, st));
 		return err;
 	};
 
@@ -2012,16 +2061,10 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		// host buffers and many pairs: the repeats of this solve run as a pipeline of chunks
 		// (3 chunks from 32K pairs, 2 from 8K; PA_CHUNKS overrides, up to 12); host maps use
 		// the packed offsets (checked above)
-		// (pinned buffers only: a copy from or to pageable memory holds the host thread until
-		// it is done, so a chunk's map download would wait for that chunk's DP and walk before
-		// the next chunk is queued, and the chunks would run one after the other)
 		plan.nchunks = 1;
 		if (repeatable && in.location == PA_HOST && in.form != F_DENSE && !plan.units && !want_paths) {
 			int K = B >= 32768 ? 3 : B >= 8192 ? 2 : 1;
-			const bool pinned = host_pinned(in.a) && host_pinned(in.b) &&
-			                    (need_walk ? maps_out != nullptr && host_pinned(maps_out) : true);
-			if (!pinned) K = 1;
-			if (const char *e = std::getenv("PA_CHUNKS")) K = std::atoi(e);  // tests: any buffers
+			if (const char *e = std::getenv("PA_CHUNKS")) K = std::atoi(e);
 			K = std::min(K, 12);
 			if (K > 1 && B >= (int64_t(1) << K)) plan.nchunks = K;
 		}
