@@ -500,11 +500,15 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 			const int32_t *prog_in = (units && q > 0) ? p.progress + prod : nullptr;
 			int32_t avail = 0;        // columns of bin known to be written
 			int pub_next = PUB_CHUNK;  // next progress value to publish
-			V2 bnext;                  // lane 0: bin of the next column, read one step ahead
+			// lane 0: (D, P) above the next column, read one step ahead -- the top border in the
+			// first stripe, else the boundary row of the stripe above
+			V2 bnext;
 			bnext.x = NEG;
 			bnext.y = NEG;
-			if (sub == 0 && pass_active && q > 0) {
-				if (units) {
+			if (sub == 0 && pass_active) {
+				if (q == 0) {
+					bnext.x = p.top_D[1];
+				} else if (units) {
 					avail = wait_progress(prog_in, 1, p.status);
 					bnext = __ldcg(bin);
 				} else {
@@ -605,20 +609,17 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 				const uint32_t tcode = tnext;
 				if (act && brow && j + 1 < lt) tnext = brow[j + 1];
 				if (sub == 0 && act) {
-					if (q == 0) {
-						upD = p.top_D[j + 1];
-						upP = NEG;
-					} else if constexpr (units) {
-						upD = bnext.x;
-						upP = bnext.y;
-						if (j + 1 < lt) {  // prefetch the next column's boundary
+					upD = bnext.x;
+					upP = bnext.y;
+					if (j + 1 < lt) {  // prefetch the next column's
+						if (q == 0) {
+							bnext.x = p.top_D[j + 2];
+						} else if constexpr (units) {
 							if (avail < j + 2) avail = wait_progress(prog_in, j + 2, p.status);
 							bnext = __ldcg(bin + j + 1);
+						} else {
+							bnext = bin[j + 1];
 						}
-					} else {
-						upD = bnext.x;
-						upP = bnext.y;
-						if (j + 1 < lt) bnext = bin[j + 1];
 					}
 				}
 				if (act) {

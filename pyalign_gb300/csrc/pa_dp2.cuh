@@ -145,10 +145,15 @@ __global__ void __launch_bounds__(BLOCK, 4) dp2_kernel(DpParams<int32_t> p) {
 			const int32_t *prog_in = (CHAIN && q > 0) ? p.progress + prod : nullptr;
 			int32_t avail = 0;
 			int pub_next = PUB_CHUNK;
-			V2 bn0, bn1;  // lane 0: boundary of the next step's two columns, read one step ahead
+			// lane 0: (D, P) above the next step's two columns, read one step ahead -- the top
+			// border in the first stripe, else the boundary row of the stripe above
+			V2 bn0, bn1;
 			bn0.x = bn0.y = bn1.x = bn1.y = NEG;
-			if (sub == 0 && pass_active && q > 0) {
-				if (CHAIN) {
+			if (sub == 0 && pass_active) {
+				if (q == 0) {
+					bn0.x = p.top_D[1];
+					if (lt > 1) bn1.x = p.top_D[2];
+				} else if (CHAIN) {
 					avail = wait_progress(prog_in, min(2, lt), p.status);
 					bn0 = __ldcg(bin);
 					if (lt > 1) bn1 = __ldcg(bin + 1);
@@ -233,10 +238,14 @@ __global__ void __launch_bounds__(BLOCK, 4) dp2_kernel(DpParams<int32_t> p) {
 				if (act && j0 + 3 < lt) tn1 = brow[j0 + 3];
 				if (sub == 0 && act) {
 					if (q == 0) {
-						upD0 = p.top_D[j0 + 1];
+						upD0 = bn0.x;
 						upP0 = NEG;
-						upD1 = act1 ? p.top_D[j1 + 1] : NEG;
+						upD1 = act1 ? bn1.x : NEG;
 						upP1 = NEG;
+						if (j0 + 2 < lt) {  // prefetch the next step's two columns
+							bn0.x = p.top_D[j0 + 3];
+							if (j0 + 3 < lt) bn1.x = p.top_D[j0 + 4];
+						}
 					} else if constexpr (CHAIN) {
 						upD0 = bn0.x;
 						upP0 = bn0.y;
