@@ -445,6 +445,10 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
     t0 = time.perf_counter()
     res = solver.solve_indexed_for_alignment_iterator(a3[:Ba], b3[:Ba], t3, ln3)
     t_solve = time.perf_counter() - t0
+    ms4 = (ctypes.c_float * 4)()
+    nl = ctypes.c_int32(0)
+    L.pa_solver_last_timings(solver.handle, ms4, ctypes.byref(nl))
+    allopt_phases = {"upload": ms4[0], "dp": ms4[1], "traceback": ms4[2], "download": ms4[3]}
     t0 = time.perf_counter()
     counts = alg.path_counts(res[0]._res)
     t_count = time.perf_counter() - t0
@@ -475,7 +479,7 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
     cells3 = float((ls3[:Ba].astype(np.int64) * lt3[:Ba]).sum())
     out["semiglobal_affine_5000x10000_all_optimal"] = {
         "value": cells3 / t_solve / 1e9, "unit": "GCUPS", "ms": t_solve * 1000, "pairs": Ba,
-        "mask_bytes": int(2 * cells3), "plan": solver.last_plan(),
+        "mask_bytes": int(2 * cells3), "plan": solver.last_plan(), "phases_ms": allopt_phases,
         "path_counts": {"ms": t_count * 1000, "gcups": cells3 / t_count / 1e9,
                         "min": int(counts.min()), "median": float(np.median(counts.astype(np.float64))),
                         "max": int(counts.max()), "saturated": int((counts == np.iinfo(np.uint64).max).sum())},
