@@ -399,6 +399,34 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
     out["semiglobal_affine_5000x10000_score"] = dict(
         r3, parity=parity_of(n3, osc3, None, sc3, None),
         workload="256 pairs of 5000 x 10000, 20 letters, semiglobal affine 10/1, score only")
+    # length buckets: half the pairs short queries against long targets, half long pairs (local
+    # Gotoh 5/2, DNA +2/-3); the tuner's plan (a group width per length bucket of |s| where
+    # that times faster) against the one width it would use otherwise, same results required
+    rs = np.random.default_rng(seed + 5)
+    nbk, hbk = 32768, 16384
+    ls_b = np.concatenate([rs.integers(16, 49, hbk), rs.integers(600, 1001, nbk - hbk)])
+    lt_b = np.concatenate([rs.integers(800, 1001, hbk), rs.integers(600, 1001, nbk - hbk)])
+    a_b = rs.integers(0, 4, (nbk, 1000)).astype(np.uint32)
+    b_b = rs.integers(0, 4, (nbk, 1000)).astype(np.uint32)
+    t_b = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(t_b, 2.0)
+    o_b = opts(alg, "LOCAL", "ALIGNMENT", AffineGap(5.0, 2.0), nbk)
+    rb, scb, mpb = run_batch(o_b, a_b, b_b, ls_b, lt_b, table=t_b)
+    saved = os.environ.get("PA_GROUP_WIDTH")
+    os.environ["PA_GROUP_WIDTH"] = str(rb["plan"]["G"])
+    try:
+        ru, scu, mpu = run_batch(o_b, a_b, b_b, ls_b, lt_b, table=t_b)
+    finally:
+        if saved is None:
+            os.environ.pop("PA_GROUP_WIDTH", None)
+        else:
+            os.environ["PA_GROUP_WIDTH"] = saved
+    out["length_buckets_skewed"] = {
+        "tuned": rb, "one_width": ru, "tuned_over_one_width": ru["dp_ms"] / rb["dp_ms"],
+        "same_results": bool(np.array_equal(scb, scu) and np.array_equal(mpb, mpu)),
+        "workload": f"{nbk} pairs: half |s| ~ U[16, 48] x |t| ~ U[800, 1000], half |s|, |t| ~ U[600, 1000]; "
+                    "local Gotoh 5/2, DNA +2/-3, score + one traceback, device-resident codes"}
+    del a_b, b_b
     # general (logarithmic) gap costs, O(|s| |t| (|s| + |t|)): 64 pairs of 300 x 300 DNA, local,
     # score + one alignment through the native module; the first pairs against the oracle
     rw = np.random.default_rng(seed + 3)
@@ -1113,6 +1141,7 @@ def run_ours(args):
         dist.destroy_process_group()
     bad = [k for k, v in (("bench", parity), *((k, v.get("parity")) for k, v in (others or {}).items()))
            if v is not None and v["mismatches"]]
+    bad += [k for k, v in (others or {}).items() if v.get("same_results") is False]
     if bad:
         print(f"parity failure against the oracle: {bad}", file=sys.stderr)
         sys.exit(1)

@@ -1167,11 +1167,10 @@ pa_status download_wsb(pa_solver *s, ResultData &res) {
 // overrides PA_DP_MODE, PA_GROUP_WIDTH and PA_BUCKET_WIDTHS.
 //
 // When the 16-bit twin kernel wins and the pairs fall into more than one length bucket of
-// |s| (bucket_of), the tuner also tries a group width per bucket: from the timings of the
-// uniform widths it takes each width's time per computed cell (real cells plus stripe
-// padding and skew), gives every bucket the width with the lowest estimated time for its
-// own pairs, and times that plan too (one launch, the buckets in segments of one width
-// each); it is kept only when it is faster.
+// |s| (bucket_of), the tuner also tries a group width per bucket, by timing: one launch with
+// the buckets in segments of one width each, starting from the uniform width, each bucket in
+// turn at half (then a quarter ...) or twice the width, a change kept only when the launch
+// runs at least 1% faster.
 struct TuneEntry {
 	uint64_t key;
 	int G;
@@ -1341,57 +1340,47 @@ pa_status tune_plan(pa_solver *s, const std::vector<int32_t> &ls, const std::vec
 	plan.blk = bestB;
 	plan.seg = false;
 	if (bestH && !bestB && !bestU) {
-		// a width per length bucket, estimated from the uniform widths' time per computed cell
-		const int rows = R;
-		double pcells[6][PA_BUCKETS] = {};  // computed cells per (width index, bucket)
+		// a width per length bucket, by measurement: from the uniform plan, each populated
+		// bucket in turn tries half the width (and half again while that helps), else twice
+		// the width, keeping a change only when the whole launch runs at least 1% faster
 		int bpop[PA_BUCKETS] = {};
-		static const int widths[6] = {32, 16, 8, 4, 2, 1};
+		int64_t bmax[PA_BUCKETS] = {};
 		for (size_t k = 0; k < ls.size(); k++) {
 			if (ls[k] == 0 || lt[k] == 0) continue;
 			const int b = bucket_of(ls[k]);
 			bpop[b]++;
-			for (int wi = 0; wi < 6; wi++) {
-				const int64_t rpp = int64_t(widths[wi]) * rows;
-				const int64_t np = (ls[k] + rpp - 1) / rpp;
-				const int64_t steps = (bestC == 2 ? (lt[k] + 1) / 2 : lt[k]) + widths[wi] - 1;
-				pcells[wi][b] += double(np * rpp) * double(steps);
-			}
-		}
-		double per_cell[6];
-		bool have[6] = {};
-		for (size_t ci = 0; ci < cand.size(); ci++) {
-			const Cand &c = cand[ci];
-			if (!c.h16 || c.blk || c.units || c.C != bestC || !std::isfinite(cand_ms[ci])) continue;
-			for (int wi = 0; wi < 6; wi++)
-				if (widths[wi] == c.G) {
-					const double tot = pcells[wi][0] + pcells[wi][1] + pcells[wi][2] + pcells[wi][3];
-					if (tot > 0) {
-						per_cell[wi] = double(cand_ms[ci]) / tot;
-						have[wi] = true;
-					}
-				}
+			bmax[b] = std::max<int64_t>(bmax[b], ls[k]);
 		}
 		int nb = 0;
-		bool differs = false;
-		Plan pl = plan;
-		for (int b = 0; b < PA_BUCKETS; b++) {
-			pl.bucket_G[b] = bestG;
-			if (!bpop[b]) continue;
-			nb++;
-			double bt = INFINITY;
-			for (int wi = 0; wi < 6; wi++)
-				if (have[wi] && per_cell[wi] * pcells[wi][b] < bt) {
-					bt = per_cell[wi] * pcells[wi][b];
-					pl.bucket_G[b] = widths[wi];
-				}
-			differs |= pl.bucket_G[b] != bestG;
-		}
-		if (nb > 1 && differs) {
+		for (int b = 0; b < PA_BUCKETS; b++) nb += bpop[b] > 0;
+		if (nb > 1) {
+			Plan pl = plan;
 			pl.seg = true;
-			float ms = INFINITY;
-			if (pa_status e = time_plan(pl, 2, &ms)) return e;
-			if (ms < best) {
-				best = ms;
+			for (int b = 0; b < PA_BUCKETS; b++) pl.bucket_G[b] = bestG;
+			float cur = best;
+			bool changed = false;
+			for (int b = 0; b < PA_BUCKETS; b++) {
+				if (!bpop[b]) continue;
+				// the widths the uniform candidates allow for this bucket's longest pair
+				auto ok = [&](int g) {
+					return g >= 1 && g <= 32 && (g == 4 || (int64_t(g) * R <= 2 * bmax[b] && (g >= 4 || bmax[b] <= 256)));
+				};
+				for (int dir : {-1, 1}) {
+					for (int g = dir < 0 ? pl.bucket_G[b] / 2 : pl.bucket_G[b] * 2; ok(g); g = dir < 0 ? g / 2 : g * 2) {
+						Plan t = pl;
+						t.bucket_G[b] = g;
+						float ms = INFINITY;
+						if (pa_status e = time_plan(t, 2, &ms)) return e;
+						if (!(ms < cur * 0.99f)) break;
+						cur = ms;
+						pl = t;
+						changed = true;
+					}
+					if (pl.bucket_G[b] != bestG) break;  // narrower helped: no need to try wider
+				}
+			}
+			if (changed) {
+				best = cur;
 				plan.seg = true;
 				for (int b = 0; b < PA_BUCKETS; b++) plan.bucket_G[b] = pl.bucket_G[b];
 			}
