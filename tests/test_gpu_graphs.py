@@ -302,9 +302,47 @@ def test_host_maps_need_packed_offsets(env):
                                            mp.ctypes.data_as(ctypes.c_void_p), offs.ctypes.data_as(P(ctypes.c_int64))))
 
 
+def test_direct_maps_result_refuses_map_reads(env):
+    """pa_solve_batch_result writes the maps into the caller's array; the result object it
+    returns has the scores and refuses to hand out maps it does not hold."""
+    torch, alg, ag = env
+    P = ctypes.POINTER
+    rng = np.random.default_rng(8)
+    n, n_s, n_t = 40, 50, 60
+    ln = np.stack([rng.integers(0, n_s + 1, n), rng.integers(1, n_t + 1, n)]).astype(np.int32)
+    a = rng.integers(0, 4, size=(n, n_s)).astype(np.uint32)
+    b = rng.integers(0, 4, size=(n, n_t)).astype(np.uint32)
+    table = np.full((4, 4), -3.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    sizes = np.minimum(ln[0], ln[1]).astype(np.int64)
+    offs = np.zeros(n, np.int64)
+    offs[1:] = np.cumsum(sizes)[:-1]
+    maps = np.full(int(sizes.sum()), -7, np.int32)
+    bt = alg.Batch(form=1, location=0, batch=n, n_s=n_s, n_t=n_t, a=a.ctypes.data_as(P(ctypes.c_uint32)),
+                   b=b.ctypes.data_as(P(ctypes.c_uint32)), table=table.ctypes.data_as(P(ctypes.c_float)),
+                   table_rows=4, table_cols=4, length=ln.ctypes.data_as(P(ctypes.c_int32)))
+    solver = _batch_solver(alg, torch, n, n_s, n_t)
+    h = alg._P()
+    alg.check(alg.lib().pa_solve_batch_result(solver.handle, ctypes.byref(bt), alg._ip(maps),
+                                              offs.ctypes.data_as(alg._PL), ctypes.byref(h)))
+    res = alg._Result(h)
+    sc = np.zeros(n, np.float32)
+    alg.check(alg.lib().pa_result_export(res.ptr, alg._fp(sc), None, None))
+    m0 = np.zeros(max(1, int(sizes[0])), np.int32)
+    assert alg.lib().pa_result_alignment(res.ptr, 0, alg._ip(m0)) != 0
+    # the same bag through pa_solve_batch: equal scores and maps
+    sc2 = np.zeros(n, np.float32)
+    maps2 = np.full_like(maps, -9)
+    alg.check(alg.lib().pa_solve_batch(solver.handle, ctypes.byref(bt), sc2.ctypes.data_as(ctypes.c_void_p),
+                                       maps2.ctypes.data_as(ctypes.c_void_p), offs.ctypes.data_as(alg._PL)))
+    assert np.array_equal(maps, maps2)
+    has = np.array([alg.lib().pa_result_has_alignment(res.ptr, k) for k in range(n)], bool)
+    assert np.array_equal(sc[has], sc2[has])
+
+
 def test_pipelined_python_api_repeats(env, monkeypatch, oracle_alg):
     """The native module's solve_indexed_for_alignment repeated with host arrays, pipelined in
-    four chunks (maps into the result object), against the oracle."""
+    four chunks (maps straight into the results' array), against the oracle."""
     torch, alg, ag = env
     from _cases import compare, options
     monkeypatch.setenv("PA_CHUNKS", "4")
