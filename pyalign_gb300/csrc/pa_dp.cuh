@@ -102,6 +102,7 @@ struct DpParams {
 	int32_t slots_per_warp; // group slots of scratch per warp (32 / the narrowest width)
 	int32_t key_shift;      // local seeds: key = value * 2^key_shift + j
 	int32_t one, minus_one, minus_four, minus_eight, sixteen;  // IMAD multipliers (see imad)
+	int32_t two;
 	// outputs
 	float *score;           // reference-domain score
 	int32_t *seed;          // (i, j) per pair
@@ -269,6 +270,13 @@ constexpr int DENSE_RING = 4;
 __device__ __forceinline__ uint32_t gt_mask(int32_t a, int32_t b) {
 	uint32_t d;
 	asm("set.gt.u32.s32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+	return d;
+}
+
+// 0xffffffff when a == b, else 0.
+__device__ __forceinline__ uint32_t eq_mask(int32_t a, int32_t b) {
+	uint32_t d;
+	asm("set.eq.u32.s32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
 	return d;
 }
 
@@ -709,7 +717,29 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 							uint32_t cell = 0;
 							V best;
 							int code;
-							if (GAP == GAP_AFFINE) {
+							if constexpr (ISINT && TB == TB_ALL && GAP == GAP_AFFINE) {
+								// all-optimal int32: the maxima by max instructions, the eight tie
+								// flags as 0 / -1 masks folded into the cell word by IMAD (FMA
+								// pipe), highest bit first: nacc = -(flag bits)
+								const V oP = imad(uD, p.one, p.c_open_s), eP = imad(uP, p.one, p.c_ext_s);
+								P = vmax(oP, eP);
+								const V oQ = imad(old, p.one, p.c_open_t), eQ = imad(Ql[r], p.one, p.c_ext_t);
+								Q = vmax(oQ, eQ);
+								const V dg = imad(S[r], p.one, dsave);
+								best = vmax(vmax(dg, P), Q);
+								if (LOC == LOC_LOCAL) best = vmax(best, V(0));
+								D = best;
+								int32_t nacc = int32_t(eq_mask(eQ, Q));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(oQ, Q)));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(eP, P)));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(oP, P)));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(Q, best)));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(P, best)));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(dg, best)));
+								nacc = imad(nacc, p.two, LOC == LOC_LOCAL ? int32_t(eq_mask(best, 0)) : 0);
+								cell = uint32_t(imad(nacc, p.minus_one, 0));
+								code = 0;
+							} else if (GAP == GAP_AFFINE) {
 								const V oP = uD + p.c_open_s, eP = uP + p.c_ext_s;
 								const bool bP = eP > oP;
 								P = bP ? eP : oP;
@@ -734,6 +764,20 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 									       (oP == P ? 16u : 0u) | (eP == P ? 32u : 0u) |
 									       (oQ == Q ? 64u : 0u) | (eQ == Q ? 128u : 0u);
 								}
+							} else if constexpr (ISINT && TB == TB_ALL && GAP == GAP_LINEAR) {
+								// all-optimal int32, linear gaps: as the affine form above
+								const V dg = imad(S[r], p.one, dsave);
+								const V up = imad(uD, p.one, p.c_up);
+								const V lf = imad(old, p.one, p.c_left);
+								best = vmax(vmax(dg, up), lf);
+								if (LOC == LOC_LOCAL) best = vmax(best, V(0));
+								D = best;
+								int32_t nacc = int32_t(eq_mask(lf, best));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(up, best)));
+								nacc = imad(nacc, p.two, int32_t(eq_mask(dg, best)));
+								nacc = imad(nacc, p.two, LOC == LOC_LOCAL ? int32_t(eq_mask(best, 0)) : 0);
+								cell = uint32_t(imad(nacc, p.minus_one, 0));
+								code = 0;
 							} else if (GAP == GAP_LINEAR) {
 								const V dg = dsave + S[r];
 								const V up = uD + p.c_up;

@@ -268,6 +268,7 @@ extern "C" pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, con
 	p.minus_four = -4;
 	p.minus_eight = -8;
 	p.sixteen = 16;
+	p.two = 2;
 	p.score = scores;
 	p.seed = seeds;
 	p.has_seed = has;
