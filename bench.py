@@ -1012,7 +1012,8 @@ def run_ours(args):
     ln16 = np.stack([ls, lt]).astype(np.uint16)
     api_solver = mod.create_solver(1000, 1000, mod.create_options(options_dict(alg, B)))
     alg.check(L.pa_solver_set_stream(api_solver.handle, ctypes.c_void_p(stream.cuda_stream)))
-    api_res = api_solver.solve_indexed_for_alignment(a, b, table, ln16)
+    for _ in range(max(2, args.warmup)):  # the first call plans, the first repeat sets up its pipeline
+        api_res = api_solver.solve_indexed_for_alignment(a, b, table, ln16)
     barrier()
     api_steps = max(3, args.steps // 4)
     api_calls = []
