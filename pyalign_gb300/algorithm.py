@@ -825,9 +825,15 @@ class Solver:
         offs = np.zeros((n,), dtype=np.int64)
         if n > 1:
             offs[1:] = np.cumsum(sizes)[:-1]
-        maps = np.zeros((int(sizes.sum()),), dtype=np.int32)
         scores = np.zeros((n,), dtype=np.float32)
-        check(lib().pa_result_export(res.ptr, _fp(scores), _ip(maps), offs.ctypes.data_as(_PL)))
+        if self._enumerable and n:
+            # all-optimal solver: each lane's alignment is the first result of the depth-first
+            # search (solver.h:2610-2630), enumerated for every lane at once on the device
+            maps = FirstAlignments(res, 1).maps
+            check(lib().pa_result_export(res.ptr, _fp(scores), None, None))
+        else:
+            maps = np.zeros((int(sizes.sum()),), dtype=np.int32)
+            check(lib().pa_result_export(res.ptr, _fp(scores), _ip(maps), offs.ctypes.data_as(_PL)))
         batch = _AlignmentBatch(scores, maps, offs, sizes, ls, lt, self._index_dtype)
         return _Lanes(functools.partial(Alignment._lazy, batch), n)
 

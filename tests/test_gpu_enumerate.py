@@ -195,3 +195,25 @@ def test_python_iterators_resume_after_device_results(monkeypatch, gpu_alg, orac
                         assert np.array_equal(np.asarray(x.s_to_t), np.asarray(y.s_to_t)), (locality, lane, j)
                     else:
                         assert np.array_equal(np.asarray(x.path), np.asarray(y.path)), (locality, lane, j)
+
+
+@pytest.mark.parametrize("locality", ["local", "global", "semiglobal"])
+def test_alignment_codomain_of_all_optimal_solver(gpu_alg, oracle_alg, locality):
+    """solve_*_for_alignment on an all-optimal solver returns each lane's first alignment of
+    the search (taken from one device enumeration of every lane) with the lane's score, as
+    the oracle's same call does."""
+    rng = np.random.default_rng(zlib.crc32(f"first-alignment/{locality}".encode()))
+    pairs = _pairs(rng, 40)
+    n = len(pairs)
+    a, b, ln = pack(pairs, n)
+    table = np.array([[2.0, -1.0], [-1.0, 2.0]], np.float32)
+    o = dict(options(gpu_alg, locality=locality, count="all", gap=Gap("affine", 2.0, 1.0)), batch_size=n, batch=True)
+    cap = (a.shape[1], b.shape[1])
+    gs = gpu_alg.m16.create_solver(*cap, gpu_alg.m16.create_options(o))
+    os_ = oracle_alg.m16.create_solver(*cap, oracle_alg.m16.create_options(o))
+    got = gs.solve_indexed_for_alignment(a, b, table, ln)
+    want = os_.solve_indexed_for_alignment(a, b, table, ln)
+    for k in range(n):
+        assert got[k].score == want[k].score, (k, got[k].score, want[k].score)
+        assert np.array_equal(np.asarray(got[k].s_to_t), np.asarray(want[k].s_to_t)), k
+        assert np.array_equal(np.asarray(got[k].t_to_s), np.asarray(want[k].t_to_s)), k
