@@ -406,9 +406,10 @@ class Alignment:
 class Solution:
     """Solution (SolutionImpl, factory.h:284-352; core::Solution solver.h:2329-2507)."""
 
-    def __init__(self, res, lane, ls, lt, dtype, step=None, algorithm=True):
+    def __init__(self, res, lane, ls, lt, dtype, step=None, algorithm=True, first=None):
         self._res, self._lane, self._ls, self._lt, self._dtype = res, lane, ls, lt, dtype
         self._step = step  # (score, map, path) of an iterator step, or None
+        self._first = first  # all-optimal solver: () -> the result's FirstAlignments(k = 1, paths)
         self._with_algorithm = algorithm
         self._cache = {}
 
@@ -463,6 +464,13 @@ class Solution:
             L = lib()
             if not L.pa_result_has_alignment(self._res.ptr, self._lane):
                 return None
+            if self._first is not None:
+                # the first result of the lane's search, from one device enumeration of
+                # every lane of the result
+                fa = self._first()
+                if fa.counts[self._lane] > 0:
+                    mp, path = fa.alignment(self._lane, 0)
+                    return (float(L.pa_result_score(self._res.ptr, self._lane)), mp.copy(), path.copy())
             path = np.zeros((self._ls + self._lt + 4, 2), dtype=np.int32)
             n = L.pa_result_path(self._res.ptr, self._lane, _ip(path))
             mp = np.zeros((min(self._ls, self._lt),), dtype=np.int32)
@@ -847,7 +855,14 @@ class Solver:
     def _solutions(self, res):
         n, ls, lt = self._lanes(res)
         dt = self._index_dtype
-        return _Lanes(lambda k: Solution(res, k, ls[k], lt[k], dt), n)
+        first = None
+        if self._enumerable:
+            def first():
+                f = res._first.get("solution")
+                if f is None:
+                    f = res._first["solution"] = FirstAlignments(res, 1, with_paths=True)
+                return f
+        return _Lanes(lambda k: Solution(res, k, ls[k], lt[k], dt, first=first), n)
 
     def _alignment_call(self, form, args):
         """solve_*_for_alignment: the maps go straight into this call's array

@@ -217,3 +217,32 @@ def test_alignment_codomain_of_all_optimal_solver(gpu_alg, oracle_alg, locality)
         assert got[k].score == want[k].score, (k, got[k].score, want[k].score)
         assert np.array_equal(np.asarray(got[k].s_to_t), np.asarray(want[k].s_to_t)), k
         assert np.array_equal(np.asarray(got[k].t_to_s), np.asarray(want[k].t_to_s)), k
+
+
+@pytest.mark.parametrize("locality", ["local", "global", "semiglobal"])
+def test_solution_codomain_of_all_optimal_solver(gpu_alg, oracle_alg, locality):
+    """solve_*_for_solution on an all-optimal solver: each Solution's path, alignment and
+    score (the lane's first result of the search, from the device enumeration) equal the
+    oracle's."""
+    rng = np.random.default_rng(zlib.crc32(f"first-solution/{locality}".encode()))
+    pairs = _pairs(rng, 30)
+    n = len(pairs)
+    a, b, ln = pack(pairs, n)
+    table = np.array([[2.0, -1.0], [-1.0, 2.0]], np.float32)
+    o = dict(options(gpu_alg, locality=locality, detail="solution", count="all", gap=Gap("affine", 2.0, 1.0)),
+             batch_size=n, batch=True)
+    cap = (a.shape[1], b.shape[1])
+    gs = gpu_alg.m16.create_solver(*cap, gpu_alg.m16.create_options(o))
+    os_ = oracle_alg.m16.create_solver(*cap, oracle_alg.m16.create_options(o))
+    got = gs.solve_indexed_for_solution(a, b, table, ln)
+    want = os_.solve_indexed_for_solution(a, b, table, ln)
+    for k in range(n):
+        assert got[k].score == want[k].score, (k, got[k].score, want[k].score)
+        gp, wp = got[k].path, want[k].path
+        assert (gp is None) == (wp is None), k
+        if gp is not None:
+            assert np.array_equal(np.asarray(gp), np.asarray(wp)), k
+        ga, wa = got[k].alignment, want[k].alignment
+        assert (ga is None) == (wa is None), k
+        if ga is not None:
+            assert np.array_equal(np.asarray(ga.s_to_t), np.asarray(wa.s_to_t)), k
