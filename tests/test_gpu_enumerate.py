@@ -8,8 +8,10 @@ tie-rich pairs (two letters, integer scores) of every locality, linear and affin
 both directions, de-duplication on and off, the group and stripe-chained mask layouts,
 multi-stripe pairs, empty pairs and local pairs without a positive optimum; the retry
 protocol when a lane's search stack or seed list is too small (PA_ENUM_STACK,
-PA_ENUM_SEEDS force tiny ones); and the Python iterators, which serve the device results
-first and then resume the host search after them (PA_ENUM_FIRST sets how many).
+PA_ENUM_SEEDS force tiny ones); the Python iterators, which serve the device results
+first and then resume the host search after them (PA_ENUM_FIRST sets how many); and the
+alignment and solution codomains of all-optimal solvers, whose first results come from the
+same enumeration.
 """
 
 import ctypes
