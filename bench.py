@@ -261,7 +261,9 @@ def parity_of(n, sc_ref, mp_ref, sc, mp):
 
 # --------------------------------------------------------------------------- other workloads
 
-def _time_device(torch, fn, steps=3, warmup=1):
+def _time_device(torch, fn, steps=5, warmup=3):
+    """Mean device time of fn over `steps` calls after `warmup` untimed ones (the first call
+    plans, the second captures the repeat's CUDA graph)."""
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
