@@ -102,7 +102,7 @@ struct DpParams {
 	int32_t slots_per_warp; // group slots of scratch per warp (32 / the narrowest width)
 	int32_t key_shift;      // local seeds: key = value * 2^key_shift + j
 	int32_t one, minus_one, minus_four, minus_eight, sixteen;  // IMAD multipliers (see imad)
-	int32_t two;
+	int32_t two, bit16;  // 2, 65536
 	// outputs
 	float *score;           // reference-domain score
 	int32_t *seed;          // (i, j) per pair
@@ -809,7 +809,10 @@ __global__ void __launch_bounds__(BLOCK, 4) dp_kernel(DpParams<V> p) {
 							}
 							if (TB == TB_ALL) {
 								if (LOC == LOC_LOCAL && r < nvalid && best_in > V(0) && D == best_in) cell |= 256u;
-								mall[r >> 1] |= cell << (16 * (r & 1));
+								// the odd row's cell into the high half by IMAD (FMA pipe): the
+								// halves are disjoint, so the add is the OR
+								if (r & 1) mall[r >> 1] = uint32_t(imad(int32_t(cell), p.bit16, int32_t(mall[r >> 1])));
+								else mall[r >> 1] |= cell;
 							}
 						}
 

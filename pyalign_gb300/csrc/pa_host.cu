@@ -777,6 +777,7 @@ pa_status run_dp(pa_solver *s, const Input &in, const Plan &plan, int tb, const 
 	p.minus_eight = -8;
 	p.sixteen = 16;
 	p.two = 2;
+	p.bit16 = 65536;
 	p.out_sign = s->sign;
 	const int gk = s->gap;  // GAP_LINEAR / GAP_AFFINE / GAP_DTW
 	const int diag_tag = (tag && gk != GAP_DTW) ? 2 : 0;

@@ -269,6 +269,7 @@ extern "C" pa_status pa_solve_indexed_for_score_noalloc(const pa_options *o, con
 	p.minus_eight = -8;
 	p.sixteen = 16;
 	p.two = 2;
+	p.bit16 = 65536;
 	p.score = scores;
 	p.seed = seeds;
 	p.has_seed = has;
