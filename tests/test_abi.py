@@ -79,3 +79,23 @@ def test_differentiable_forms_refuse_host_tensors(libpath):
         ag.alignment_score(torch.zeros(1, 4, 5), lengths, 1.0, 0.5, "global")
     with pytest.raises(ValueError, match="CUDA"):
         ag.dtw_series_score(torch.zeros(1, 4), torch.zeros(1, 5), lengths)
+
+
+def test_result_and_report_entries_check_arguments(libpath):
+    """The result-side entry points refuse null or out-of-range arguments before touching a
+    device: the device enumeration, the direct-maps solve, and the per-bucket width report."""
+    from pyalign_gb300 import algorithm as alg
+    L = alg.lib()
+    counts = (ctypes.c_int32 * 4)()
+    assert L.pa_result_first_alignments(None, 4, counts, None, None, None) == alg.PA_ERR_INVALID_ARGUMENT
+    assert L.pa_solve_batch_result(None, None, None, None, None) == alg.PA_ERR_INVALID_ARGUMENT
+    assert L.pa_solver_last_bucket_widths(None, None) == alg.PA_ERR_INVALID_ARGUMENT
+    import types
+    opts = alg.m16.create_options({
+        "solver": alg.Type.ALIGNMENT, "direction": alg.Direction.MAXIMIZE, "batch": True, "batch_size": 4,
+        "return_dup": False, "locality": alg.Locality.LOCAL,
+        "codomain": types.SimpleNamespace(detail=alg.Detail.ALIGNMENT, count=alg.Count.ONE), "gap_cost": None})
+    solver = alg.m16.create_solver(8, 8, opts)
+    widths = (ctypes.c_int32 * 4)(7, 7, 7, 7)
+    alg.check(L.pa_solver_last_bucket_widths(solver.handle, widths))
+    assert list(widths) == [0, 0, 0, 0]  # no solve yet: one width, reported as zeros
