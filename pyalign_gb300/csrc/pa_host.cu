@@ -1060,10 +1060,12 @@ bool int_mode_ok(const pa_solver *s, const Input &in, const float *host_table, i
 	return bound < double(1 << 23);
 }
 
-// General gap costs: one CTA per pair (pa_wsb.cu); values, traceback codes and the
-// similarity of every cell come back to the host for the traceback.
+// General gap costs: one CTA per pair (pa_wsb.cu).  With `maps` (device, at the staged map
+// offsets) the one-optimal alignments are walked on the device too; otherwise the values,
+// traceback codes and similarity of every cell are downloaded for the host's traceback
+// (download_wsb).
 pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls, const std::vector<int32_t> &lt,
-                  int *launches, ResultData &res) {
+                  int *launches, ResultData &res, int32_t *maps) {
 	cudaStream_t st = s->stream;
 	const int64_t B = in.batch;
 	std::vector<int64_t> voff(size_t(B) + 1, 0), toff(size_t(B) + 1, 0);
@@ -1086,8 +1088,9 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	PA_CUDA(pa_copy(s, s->d_wsb_off.p, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, st));
 	PA_CUDA(s->d_wsb_sub_off.ensure(toff.size() * 8));
 	PA_CUDA(pa_copy(s, s->d_wsb_sub_off.p, toff.data(), toff.size() * 8, cudaMemcpyHostToDevice, st));
-	PA_CUDA(s->d_wsb_vals.ensure(size_t(voff[size_t(B)]) * 4));
-	PA_CUDA(s->d_wsb_vals_t.ensure(size_t(voff[size_t(B)]) * 4));
+	// (+64 bytes: the kernel copies the 16-byte blocks that hold a run of values)
+	PA_CUDA(s->d_wsb_vals.ensure(size_t(voff[size_t(B)]) * 4 + 64));
+	PA_CUDA(s->d_wsb_vals_t.ensure(size_t(voff[size_t(B)]) * 4 + 64));
 	PA_CUDA(s->d_wsb_tb.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
 	PA_CUDA(s->d_wsb_sub.ensure(size_t(std::max<int64_t>(toff[size_t(B)], 1)) * 4));
 	std::vector<float> tab;
@@ -1134,8 +1137,43 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	w.seed = s->d_seed.as<int32_t>();
 	w.has_seed = s->d_has.as<int32_t>();
 	w.status = s->d_status.as<int32_t>();
-	PA_CUDA(launch_wsb(w, st));
+	// a warp per cell on all but the longest diagonals; about four cells per warp on a
+	// pair's longest diagonal, 128 to 1024 threads; a cluster of 4 or 2 CTAs per pair when
+	// the clusters of all pairs fit the SMs at once and the pairs are long enough to keep
+	// them busy (PA_WSB_THREADS, PA_WSB_WARP_CELLS, PA_WSB_CLUSTER: experiments and tests)
+	int64_t diag = 0;
+	for (int64_t k = 0; k < B; k++) diag = std::max<int64_t>(diag, std::min(ls[size_t(k)], lt[size_t(k)]));
+	int threads = int(std::min<int64_t>(1024, std::max<int64_t>(128, 32 * ((diag + 3) / 4))));
+	threads = (threads + 31) / 32 * 32;
+	if (const char *e = std::getenv("PA_WSB_THREADS")) threads = std::min(1024, std::max(32, std::atoi(e) / 32 * 32));
+	int cluster = 1;
+	if (B * 4 <= s->sm_count && diag >= 512) cluster = 4;
+	else if (B * 2 <= s->sm_count && diag >= 128) cluster = 2;
+	if (const char *e = std::getenv("PA_WSB_CLUSTER")) {
+		const int c = std::atoi(e);
+		cluster = c >= 4 ? 4 : c >= 2 ? 2 : 1;
+	}
+	w.warp_cells = 64;
+	if (const char *e = std::getenv("PA_WSB_WARP_CELLS")) w.warp_cells = std::max(0, std::atoi(e));
+	PA_CUDA(launch_wsb(w, threads, cluster, st));
 	(*launches)++;
+	if (maps) {
+		WsbWalkParams wk{};
+		wk.npairs = int32_t(B);
+		wk.len_s = s->m.ls;
+		wk.len_t = s->m.lt;
+		wk.local = s->loc;
+		wk.vals = w.vals;
+		wk.vals_off = w.vals_off;
+		wk.tb = w.tb;
+		wk.tb_off = w.tb_off;
+		wk.seed = w.seed;
+		wk.has_seed = w.has_seed;
+		wk.map_off = s->m.map_off;
+		wk.maps = maps;
+		PA_CUDA(launch_wsb_walk(wk, st));
+		(*launches)++;
+	}
 	PA_CUDA(cudaStreamSynchronize(st));  // host vectors above are temporaries
 	return PA_OK;
 }
@@ -1796,6 +1834,11 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	const bool need_walk = tb == TB_ONE && s->gap != GAP_GENERAL &&
 	                       (method == M_ALIGNMENT || method == M_ALIGNMENT_ITER || method == M_SOLUTION ||
 	                        method == M_SOLUTION_ITER || method == M_PATHS);
+	// general gap costs, one alignment per pair: walked on the device (wsb_walk_kernel); the
+	// cell matrices stay there, as they do for a score-only solve (the iterators, solutions and
+	// all-optimal searches walk them on the host)
+	const bool wsb_maps = s->gap == GAP_GENERAL && tb == TB_ONE && method == M_ALIGNMENT;
+	const bool wsb_host = s->gap == GAP_GENERAL && !(goal != GOAL_ALL && (method == M_SCORE || wsb_maps));
 	// the device work after staging: status reset, DP, traceback walk, the scores of the
 	// device-resident path form.  The phase events are recorded in it; inside a capture they
 	// become external event nodes of the graph, so the timings stay exact on replays.
@@ -1843,7 +1886,16 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		PA_CUDA(cudaMemsetAsync(s->d_status.p, 0, 4, sw));
 		if (timed) PA_CUDA(record(s->ev[1], sw));
 		if (s->gap == GAP_GENERAL) {
-			if (pa_status e = run_wsb(s, in, ls, lt, &launches, res)) return e;
+			int32_t *wmaps = nullptr;
+			if (wsb_maps) {
+				if (maps_out && in.location == PA_DEVICE) {
+					wmaps = maps_out;
+				} else {
+					PA_CUDA(s->d_maps.ensure(size_t(std::max<int64_t>(map_off[size_t(B)], 1)) * 4));
+					wmaps = s->d_maps.as<int32_t>();
+				}
+			}
+			if (pa_status e = run_wsb(s, in, ls, lt, &launches, res, wmaps)) return e;
 		} else {
 			if (tb == TB_ALL && s->loc == LOC_LOCAL) {
 				// the optimum is needed to mark the seeds (solver.h:2066-2091): a score pass first
@@ -2156,7 +2208,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		res.map_off = map_off;
 		res.mask_off = mask_off;
 	}
-	if (need_walk) {
+	if (need_walk || wsb_maps) {
 		if ((maps_out && in.location == PA_DEVICE) || paths_to_user || chunked) {
 			// results stay on the device, or the pipeline downloaded them chunk by chunk
 		} else if (maps_out) {
@@ -2189,7 +2241,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 		res.values.resize(size_t(val_off[size_t(B)]));
 		PA_CUDA(pa_copy(s, res.values.data(), s->d_vals.p, res.values.size() * 4, cudaMemcpyDeviceToHost, st));
 	}
-	if (s->gap == GAP_GENERAL) {
+	if (wsb_host) {
 		if (pa_status e = download_wsb(s, res)) return e;
 	}
 	PA_CUDA(cudaEventRecord(s->ev[4], st));
@@ -2718,8 +2770,9 @@ static bool lane_walk(const pa_result *r, int64_t lane, std::vector<std::pair<in
 	}
 	if (!d.has[size_t(lane)]) return false;
 	const int n = std::min(d.ls[size_t(lane)], d.lt[size_t(lane)]);
-	if (d.gap == GAP_GENERAL) {
-		// WSB one-optimal walk over the device traceback codes (solver.h:1497-1536)
+	if (d.gap == GAP_GENERAL && !d.wsb_tb.empty()) {
+		// WSB one-optimal walk over the device traceback codes (solver.h:1497-1536); a
+		// solve for alignments walked on the device and kept only the maps
 		std::vector<std::pair<int, int>> p;
 		int u = d.seeds[size_t(2 * lane)], v = d.seeds[size_t(2 * lane + 1)];
 		p.push_back({u, v});
@@ -2789,6 +2842,7 @@ pa_status pa_result_values(const pa_result *r, int64_t lane, float *values) {
 	const int ls = d.ls[size_t(lane)], lt = d.lt[size_t(lane)];
 	const size_t n = size_t(ls + 1) * size_t(lt + 1) * size_t(pa_result_layers(r, lane));
 	if (d.gap == GAP_GENERAL) {
+		if (d.wsb_vals.empty()) return fail(PA_ERR_INVALID_ARGUMENT, "no values in this result");
 		const float *v = d.wsb_vals.data() + d.wsb_voff[size_t(lane)];
 		for (size_t k = 0; k < n; k++) values[k] = v[k] * d.sign;
 		return PA_OK;
@@ -2863,6 +2917,7 @@ extern "C" {
 
 pa_status pa_result_tb_matrix(const pa_result *r, int64_t lane, int32_t *tb) {
 	const ResultData &d = *r->d;
+	if (d.gap == GAP_GENERAL && d.wsb_tb.empty()) return fail(PA_ERR_INVALID_ARGUMENT, "no traceback matrix in this result");
 	const int ls = d.ls[size_t(lane)], lt = d.lt[size_t(lane)];
 	const int layers = pa_result_layers(r, lane);
 	for (int layer = 0; layer < layers; layer++) {
@@ -2878,6 +2933,7 @@ pa_status pa_result_tb_matrix(const pa_result *r, int64_t lane, int32_t *tb) {
 
 int64_t pa_result_tb_edges(const pa_result *r, int64_t lane, int32_t layer, int32_t *edges) {
 	const ResultData &d = *r->d;
+	if (d.gap == GAP_GENERAL && d.wsb_tb.empty()) return -1;  // no traceback matrix in this result
 	int64_t n = 0;
 	for_each_cell_tb(d, lane, layer, [&](int i, int j, const std::vector<std::pair<int, int>> &l) {
 		for (const auto &pt : l) {

@@ -1,129 +1,327 @@
 // General gap cost solve (GeneralGapCostSolver, solver.h:3056-3184): O(n m (n + m)).
 //
-// One CTA per pair sweeps anti-diagonals; every cell scans its whole column and row
-// history, so D is kept in global memory (L2-resident for the small problems this
-// cubic recurrence is used for), twice: row-major for the column scans and transposed for
-// the row scans, so that the threads of an anti-diagonal (consecutive rows u, columns
-// d - u) read consecutive words at every step k of either scan.  Candidates are pushed in
-// the reference's order -- (local zero), diagonal, vertical gaps k = -1..u-1, horizontal
-// gaps k = -1..v-1 -- and a later candidate wins only when strictly better.  The seed scans
-// (solver.h:2035-2058, 2174-2188, 2266-2294) run over the CTA with a block reduction that
-// keeps the scan order's winner.
+// A CTA, or a cluster of 2 or 4 CTAs when there are fewer pairs than SMs, per pair sweeps
+// anti-diagonals.  Cell (u, v) takes the best of its head candidates -- (local zero), the
+// diagonal -- and of u + v + 2 scan candidates: the vertical gaps k = -1..u-1,
+// D(k, v) - w_s(u - k), then the horizontal gaps k = -1..v-1, D(u, k) - w_t(v - k).  A later
+// candidate wins only when strictly better, so the winner is the first maximum in that
+// order.  Numbering the scan candidates q = 0..u+v+1 (vertical k = q - 1 while q <= u,
+// horizontal k = q - u - 2 after), the scan's winner is its largest value at the smallest q:
+// any split of the scan finds it by keeping a (value, q) pair per part and combining parts by
+// (larger value, then smaller q); the scan's winner replaces the head's only when strictly
+// better.
+//
+// D is kept in global memory (L2-resident at the sizes this cubic recurrence is used for),
+// twice: row-major and transposed.  Every cell of anti-diagonal d scans d + 2 candidates.
+// The warps of the pair split a diagonal one of two ways:
+//  * a warp per cell (diagonals of at most warp_cells cells per warp): lane l takes
+//    q = l, l + 32, ... -- the vertical scan reads a row of the transposed copy, the
+//    horizontal scan a row of the row-major copy, 32 consecutive words per step, four steps'
+//    loads in flight together -- and two warp reductions combine the lanes.  Per 32 cells of
+//    a warp, lane j loads cell j's similarity and diagonal value before the scans and stores
+//    its result after them.
+//  * a thread per cell (longer diagonals): the threads of a warp hold consecutive cells and
+//    at step k read row k of the row-major copy (vertical scans) or of the transposed copy
+//    (horizontal scans), again 32 consecutive words.
+// The CTAs of a cluster meet at a cluster barrier (release / acquire) after every diagonal
+// and read the values of D through L2, where the other CTAs' writes are.  The seed scans
+// (solver.h:2035-2058, 2174-2188, 2266-2294) run over the first CTA with a block reduction
+// that keeps the scan order's winner.
+#include <climits>
 #include <cmath>
 #include "pa_dp.cuh"
 #include "pa_wsb.h"
 
 namespace pa {
 
-__global__ void __launch_bounds__(256) wsb_kernel(WsbParams p) {
-	const int pair = blockIdx.x;
-	if (pair >= p.npairs) return;
+namespace {
+
+constexpr int32_t WSB_NO_TB = INT32_MIN;  // "no traceback" coordinates of a local zero
+
+// a value of D: through L2 when the pair's CTAs form a cluster (another SM wrote it)
+template <bool CL>
+__device__ __forceinline__ float wsb_ld(const float *a) {
+	if constexpr (CL) return __ldcg(a);
+	else return *a;
+}
+
+// every thread of the pair (its CTA, or its cluster) has finished the previous diagonal and
+// its writes are visible
+template <bool CL>
+__device__ __forceinline__ void wsb_sync() {
+	if constexpr (CL) {
+		asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+		asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+	} else {
+		__syncthreads();
+	}
+}
+
+// similarity of cell (u, v), normalised (multiplied by the direction's sign)
+__device__ __forceinline__ float wsb_similarity(const WsbParams &p, int pair, const uint32_t *arow,
+                                                const uint32_t *brow, int u, int v) {
+	if (p.sub_kind == SUB_DENSE)
+		return p.dense[int64_t(pair) + int64_t(u) * p.dense_si + int64_t(v) * p.dense_sj] * p.sign;
+	if (p.sub_kind == SUB_BINARY) return (arow[u] == brow[v] ? p.eq : p.ne) * p.sign;
+	const uint32_t x = arow[u], y = brow[v];
+	if (x >= uint32_t(p.table_rows) || y >= uint32_t(p.table_cols)) {
+		atomicOr(p.status, ST_BAD_CODE);
+		return 0.0f;
+	}
+	return p.table[size_t(x) * size_t(p.table_cols) + y] * p.sign;
+}
+
+// combine two parts of a scan: the larger value, on a tie the smaller position
+template <typename Q>
+__device__ __forceinline__ void wsb_keep(float &bv, Q &bq, float ov, Q oq) {
+	if (ov > bv || (ov == bv && oq < bq)) {
+		bv = ov;
+		bq = oq;
+	}
+}
+
+// order-preserving key of a float that is not NaN, with -0 and +0 equal
+__device__ __forceinline__ uint32_t wsb_order(float f) {
+	const uint32_t b = __float_as_uint(f == 0.0f ? 0.0f : f);
+	return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// the scan positions [qa, qb] of one phase of a warp's scan, `src` and `gap` at position qa:
+// lane l takes qa + l, qa + l + 32, ..., four at a time while whole 128-blocks remain
+// (warp-uniform bounds), then 32 at a time, then the partial block
+template <bool CL>
+__device__ __forceinline__ void wsb_phase(const float *src, const float *gap, int qa, int qb, int lane, float &bv,
+                                          int &bq) {
+	int q = qa;
+	src += lane;
+	gap -= lane;
+	for (; q + 128 <= qb + 1; q += 128, src += 128, gap -= 128) {
+		const float x0 = wsb_ld<CL>(src), x1 = wsb_ld<CL>(src + 32), x2 = wsb_ld<CL>(src + 64),
+		            x3 = wsb_ld<CL>(src + 96);
+		const float g0 = __ldg(gap), g1 = __ldg(gap - 32), g2 = __ldg(gap - 64), g3 = __ldg(gap - 96);
+		const float c0 = x0 + (-g0), c1 = x1 + (-g1), c2 = x2 + (-g2), c3 = x3 + (-g3);
+		if (c0 > bv) { bv = c0; bq = q + lane; }
+		if (c1 > bv) { bv = c1; bq = q + lane + 32; }
+		if (c2 > bv) { bv = c2; bq = q + lane + 64; }
+		if (c3 > bv) { bv = c3; bq = q + lane + 96; }
+	}
+	for (; q + 32 <= qb + 1; q += 32, src += 32, gap -= 32) {
+		const float c = wsb_ld<CL>(src) + (-__ldg(gap));
+		if (c > bv) { bv = c; bq = q + lane; }
+	}
+	if (q + lane <= qb) {
+		const float c = wsb_ld<CL>(src) + (-__ldg(gap));
+		if (c > bv) { bv = c; bq = q + lane; }
+	}
+}
+
+// the scan of cell (u, v) by one warp; every lane returns the scan's first maximum: the
+// largest key by one reduction, the smallest position holding it by another, its value
+// from the lane that scanned that position
+template <bool CL>
+__device__ __forceinline__ void wsb_scan_warp(const WsbParams &p, const float *D, const float *DT, int64_t ld,
+                                              int64_t ldt, int u, int v, int lane, float &bv, int &bq) {
+	bv = -INFINITY;
+	bq = INT_MAX;
+	// vertical, q = k + 1 in [0, u]: D(k, v) = DT[(v + 1) * ldt + q], w_s(u - k) = gap_s[u + 1 - q]
+	wsb_phase<CL>(DT + int64_t(v + 1) * ldt, p.gap_s + (u + 1), 0, u, lane, bv, bq);
+	// horizontal, q = k + u + 2 in [u + 1, u + v + 1]: D(u, k) = D[(u + 1) * ld + q - u - 1],
+	// w_t(v - k) = gap_t[u + v + 2 - q]
+	wsb_phase<CL>(D + int64_t(u + 1) * ld, p.gap_t + (v + 1), u + 1, u + v + 1, lane, bv, bq);
+	const uint32_t key = wsb_order(bv);
+	const uint32_t m = __reduce_max_sync(0xffffffffu, key);
+	const int qw = __reduce_min_sync(0xffffffffu, key == m ? bq : INT_MAX);
+	// the lane that scanned position qw: the phases start at q = 0 and q = u + 1
+	bv = __shfl_sync(0xffffffffu, bv, (qw <= u ? qw : qw - u - 1) & 31);
+	bq = qw;
+}
+
+// the scan of cell (u, v) by one thread, in order
+template <bool CL>
+__device__ __forceinline__ void wsb_scan_thread(const WsbParams &p, const float *D, const float *DT, int64_t ld,
+                                                int64_t ldt, int u, int v, float &bv, int &bq) {
+	bv = -INFINITY;
+	bq = INT_MAX;
+	const float *gs = p.gap_s + (u + 1);
+	int64_t o = v + 1;  // D(q - 1, v) = D[q * ld + v + 1]
+	for (int q = 0; q <= u; q++, o += ld) {
+		const float c = wsb_ld<CL>(D + o) + (-__ldg(gs - q));
+		if (c > bv) {
+			bv = c;
+			bq = q;
+		}
+	}
+	const float *gt = p.gap_t + (u + v + 2);
+	o = u + 1;  // D(u, q - u - 2) = DT[(q - u - 1) * ldt + u + 1]
+	for (int q = u + 1; q <= u + v + 1; q++, o += ldt) {
+		const float c = wsb_ld<CL>(DT + o) + (-__ldg(gt - q));
+		if (c > bv) {
+			bv = c;
+			bq = q;
+		}
+	}
+}
+
+// the cell's result: the head candidates -- (local zero), the diagonal (dprev = D(u-1, v-1))
+// -- then the scan's first maximum (bv at position bq), which replaces the head's only when
+// strictly better
+__device__ __forceinline__ void wsb_store(const WsbParams &p, float *D, float *DT, int32_t *T, float *SUB, int64_t ld,
+                                          int64_t ldt, int lt, int u, int v, float s, float dprev, float bv, int bq) {
+	const float dg = dprev + s;
+	float best;
+	int kind, kk = -2;
+	if (p.local == LOC_LOCAL) {
+		best = 0.0f;
+		kind = 0;
+		if (dg > best) {
+			best = dg;
+			kind = 1;
+		}
+	} else {
+		best = dg;
+		kind = 1;
+	}
+	if (bv > best) {
+		best = bv;
+		if (bq <= u) {
+			kind = 2;
+			kk = bq - 1;
+		} else {
+			kind = 3;
+			kk = bq - u - 2;
+		}
+	}
+	SUB[int64_t(u) * lt + v] = s;
+	D[int64_t(u + 1) * ld + (v + 1)] = best;
+	DT[int64_t(v + 1) * ldt + (u + 1)] = best;
+	T[int64_t(u) * lt + v] = int32_t(uint32_t(kk + 1) << 2) | kind;
+}
+
+// CL: the pair's CTAs form a cluster (its size from %cluster_nctarank, 2 or 4)
+template <bool CL>
+__global__ void __launch_bounds__(1024) wsb_kernel(WsbParams p) {
+	uint32_t rank = 0, csize = 1;
+	if constexpr (CL) {
+		asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+		asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(csize));
+	}
+	const int pair = int(blockIdx.x / csize);
+	if (pair >= p.npairs) return;  // cluster-uniform
 	const int ls = p.len_s[pair], lt = p.len_t[pair];
 	float *D = p.vals + p.vals_off[pair];
 	float *DT = p.vals_t + p.vals_off[pair];  // DT[(j + 1) * (ls + 1) + (i + 1)] = D(i, j)
 	int32_t *T = p.tb + p.tb_off[pair];
 	float *SUB = p.sub + p.tb_off[pair];
 	const int64_t ld = lt + 1, ldt = ls + 1;
-	// borders
-	for (int j = threadIdx.x; j <= lt; j += blockDim.x) {
-		D[j] = p.top_D[j];
-		DT[int64_t(j) * ldt] = p.top_D[j];
+	// borders (the first CTA's)
+	if (rank == 0) {
+		for (int j = threadIdx.x; j <= lt; j += blockDim.x) {
+			D[j] = p.top_D[j];
+			DT[int64_t(j) * ldt] = p.top_D[j];
+		}
+		for (int i = threadIdx.x; i <= ls; i += blockDim.x) {
+			D[int64_t(i) * ld] = p.left_D[i];
+			DT[i] = p.left_D[i];
+		}
 	}
-	for (int i = threadIdx.x; i <= ls; i += blockDim.x) {
-		D[int64_t(i) * ld] = p.left_D[i];
-		DT[i] = p.left_D[i];
-	}
-	__syncthreads();
+	wsb_sync<CL>();
 	const uint32_t *arow = p.a ? p.a + int64_t(pair) * p.a_stride : nullptr;
 	const uint32_t *brow = p.b ? p.b + int64_t(pair) * p.b_stride : nullptr;
+	const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+	const int gw = int(rank) * nwarps + (threadIdx.x >> 5), GW = int(csize) * nwarps;  // the pair's warps
+	const int gt = int(rank * blockDim.x + threadIdx.x), GT = int(csize * blockDim.x);  // and threads
 	for (int d = 0; d <= ls + lt - 2; d++) {
 		const int u0 = max(0, d - (lt - 1)), u1 = min(ls - 1, d);
-		for (int u = u0 + threadIdx.x; u <= u1; u += blockDim.x) {
-			const int v = d - u;
-			float s;
-			if (p.sub_kind == SUB_DENSE) {
-				s = p.dense[int64_t(pair) + int64_t(u) * p.dense_si + int64_t(v) * p.dense_sj] * p.sign;
-			} else if (p.sub_kind == SUB_BINARY) {
-				s = (arow[u] == brow[v] ? p.eq : p.ne) * p.sign;
-			} else {
-				const uint32_t x = arow[u], y = brow[v];
-				if (int(x) >= p.table_rows || int(y) >= p.table_cols) {
-					atomicOr(p.status, ST_BAD_CODE);
-					s = 0.0f;
-				} else {
-					s = p.table[x * p.table_cols + y] * p.sign;
+		const int ncell = u1 - u0 + 1;
+		if (ncell <= GW * p.warp_cells) {
+			// this warp's cells c = gw + GW * j, 32 at a time: lane l loads the similarity and
+			// D(u-1, v-1) of cell j0 + l before the scans and stores its result after them
+			const int nw = ncell > gw ? (ncell - gw + GW - 1) / GW : 0;
+			for (int j0 = 0; j0 < nw; j0 += 32) {
+				const bool mine = j0 + lane < nw;
+				const int um = u0 + gw + GW * (j0 + lane), vm = d - um;
+				float s = 0.0f, dprev = 0.0f, kv = -INFINITY;
+				int kq = INT_MAX;
+				if (mine) {
+					s = wsb_similarity(p, pair, arow, brow, um, vm);
+					dprev = wsb_ld<CL>(D + int64_t(um) * ld + vm);
 				}
+				const int jn = min(32, nw - j0);
+				for (int jj = 0; jj < jn; jj++) {  // warp-uniform
+					const int u = u0 + gw + GW * (j0 + jj);
+					float bv;
+					int bq;
+					wsb_scan_warp<CL>(p, D, DT, ld, ldt, u, d - u, lane, bv, bq);
+					if (lane == jj) {
+						kv = bv;
+						kq = bq;
+					}
+				}
+				if (mine) wsb_store(p, D, DT, T, SUB, ld, ldt, lt, um, vm, s, dprev, kv, kq);
 			}
-			SUB[int64_t(u) * lt + v] = s;
-			const float dg = D[int64_t(u) * ld + v] + s;  // D(u-1, v-1) + s(u, v)
-			float best;
-			int kind, kk = -2;
-			if (p.local == LOC_LOCAL) {
-				best = 0.0f;
-				kind = 0;
-				if (dg > best) { best = dg; kind = 1; }
-			} else {
-				best = dg;
-				kind = 1;
+		} else {
+			for (int u = u0 + gt; u <= u1; u += GT) {
+				const int v = d - u;
+				const float s = wsb_similarity(p, pair, arow, brow, u, v);
+				float bv;
+				int bq;
+				wsb_scan_thread<CL>(p, D, DT, ld, ldt, u, v, bv, bq);
+				wsb_store(p, D, DT, T, SUB, ld, ldt, lt, u, v, s, wsb_ld<CL>(D + int64_t(u) * ld + v), bv, bq);
 			}
-			for (int k = -1; k < u; k++) {
-				const float c = D[int64_t(k + 1) * ld + (v + 1)] + (-p.gap_s[u - k]);
-				if (c > best) { best = c; kind = 2; kk = k; }
-			}
-			for (int k = -1; k < v; k++) {
-				const float c = DT[int64_t(k + 1) * ldt + (u + 1)] + (-p.gap_t[v - k]);
-				if (c > best) { best = c; kind = 3; kk = k; }
-			}
-			D[int64_t(u + 1) * ld + (v + 1)] = best;
-			DT[int64_t(v + 1) * ldt + (u + 1)] = best;
-			T[int64_t(u) * lt + v] = kind | ((kk + 1) << 2);
 		}
-		__syncthreads();
+		wsb_sync<CL>();
 	}
+	if (rank != 0) return;
 	// seeds (Local 2035-2058, Global 2174-2188, Semiglobal 2266-2294): each is the first
 	// strict optimum of a scan, i.e. the optimum with the smallest scan position; every
 	// thread scans a strided share, then the block keeps (largest value, smallest position)
-	auto V = [&](int i, int j) { return D[int64_t(i + 1) * ld + (j + 1)]; };
+	auto V = [&](int i, int j) { return wsb_ld<CL>(D + int64_t(i + 1) * ld + (j + 1)); };
 	float best = -INFINITY;
-	int64_t bpos = INT64_MAX;  // scan position of this thread's optimum
-	int si = -1, sj = -1, has = 0;
+	long long bpos = LLONG_MAX;  // scan position of this thread's optimum
 	if (p.local == LOC_LOCAL) {
 		// scan i = ls-1 .. 0, j = lt-1 .. 0: position (ls-1-i) * lt + (lt-1-j)
 		const int64_t n = int64_t(ls) * lt;
 		for (int64_t x = threadIdx.x; x < n; x += blockDim.x) {
 			const int i = ls - 1 - int(x / lt), j = lt - 1 - int(x % lt);
 			const float val = V(i, j);
-			if (val > best) { best = val; bpos = x; }
+			if (val > best) {
+				best = val;
+				bpos = x;
+			}
 		}
 	} else if (p.local == LOC_SEMI) {
 		// the last row (j ascending), then the last column (i ascending)
 		for (int64_t x = threadIdx.x; x < int64_t(lt) + ls; x += blockDim.x) {
 			const float val = x < lt ? V(ls - 1, int(x)) : V(int(x - lt), lt - 1);
-			if (val > best) { best = val; bpos = x; }
-		}
-	}
-	__shared__ float rb[256];
-	__shared__ long long rp[256];
-	rb[threadIdx.x] = best;
-	rp[threadIdx.x] = bpos;
-	__syncthreads();
-	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-		if (threadIdx.x < o) {
-			const float ov = rb[threadIdx.x + o];
-			const long long op = rp[threadIdx.x + o];
-			if (ov > rb[threadIdx.x] || (ov == rb[threadIdx.x] && op < rp[threadIdx.x])) {
-				rb[threadIdx.x] = ov;
-				rp[threadIdx.x] = op;
+			if (val > best) {
+				best = val;
+				bpos = x;
 			}
 		}
-		__syncthreads();
 	}
+	for (int o = 16; o > 0; o >>= 1) {
+		const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+		const long long op = __shfl_xor_sync(0xffffffffu, bpos, o);
+		wsb_keep(best, bpos, ov, op);
+	}
+	__shared__ float rb[32];
+	__shared__ long long rp[32];
+	const int warp = threadIdx.x >> 5;
+	if (lane == 0) {
+		rb[warp] = best;
+		rp[warp] = bpos;
+	}
+	__syncthreads();
 	if (threadIdx.x != 0) return;
+	for (int w = 1; w < nwarps; w++) wsb_keep(best, bpos, rb[w], rp[w]);
+	int si = -1, sj = -1, has = 0;
 	if (p.local == LOC_GLOBAL) {
-		si = ls - 1; sj = lt - 1; has = 1; best = V(si, sj);
+		si = ls - 1;
+		sj = lt - 1;
+		has = 1;
+		best = V(si, sj);
 	} else {
-		best = rb[0];
-		const long long x = rp[0];
+		const long long x = bpos;
 		has = best > -INFINITY;
 		if (has && p.local == LOC_LOCAL) {
 			si = ls - 1 - int(x / lt);
@@ -139,9 +337,75 @@ __global__ void __launch_bounds__(256) wsb_kernel(WsbParams p) {
 	p.has_seed[pair] = has;
 }
 
-cudaError_t launch_wsb(const WsbParams &p, cudaStream_t st) {
+// a warp per pair: the lanes clear the map, lane 0 follows the codes from the seed and
+// writes the aligned pairs (a step that changes both coordinates aligns the cell it leaves)
+__global__ void __launch_bounds__(128) wsb_walk_kernel(WsbWalkParams p) {
+	const int pair = blockIdx.x * 4 + int(threadIdx.x >> 5);
+	const int lane = threadIdx.x & 31;
+	if (pair >= p.npairs) return;
+	const int ls = p.len_s[pair], lt = p.len_t[pair];
+	int32_t *map = p.maps + p.map_off[pair];
+	const int n = min(ls, lt);
+	for (int k = lane; k < n; k += 32) map[k] = -1;
+	__syncwarp();
+	if (lane != 0 || !p.has_seed[pair]) return;
+	const float *D = p.vals + p.vals_off[pair];
+	const int32_t *T = p.tb + p.tb_off[pair];
+	const int64_t ld = lt + 1;
+	int u = p.seed[2 * pair], v = p.seed[2 * pair + 1];
+	while (u >= 0 && v >= 0 && u < ls && v < lt) {
+		if (p.local == LOC_LOCAL && !(D[int64_t(u + 1) * ld + (v + 1)] > 0.0f)) break;
+		const int32_t c = T[int64_t(u) * lt + v];
+		const int kind = c & 3, kk = (c >> 2) - 1;
+		int nu = u, nv = v;
+		if (kind == 0) {
+			nu = WSB_NO_TB;
+			nv = WSB_NO_TB;
+		} else if (kind == 1) {
+			nu = u - 1;
+			nv = v - 1;
+		} else if (kind == 2 && kk < u) {
+			nu = kk;
+		} else if (kind == 3 && kk < v) {
+			nv = kk;
+		} else {
+			break;  // not a code of wsb_kernel
+		}
+		if (nu != u && nv != v) {
+			if (ls <= lt) map[u] = v;
+			else map[v] = u;
+		}
+		u = nu;
+		v = nv;
+	}
+}
+
+}  // namespace
+
+cudaError_t launch_wsb(const WsbParams &p, int threads, int cluster, cudaStream_t st) {
 	if (p.npairs == 0) return cudaSuccess;
-	wsb_kernel<<<p.npairs, 256, 0, st>>>(p);
+	if (cluster <= 1) {
+		wsb_kernel<false><<<p.npairs, threads, 0, st>>>(p);
+		return cudaGetLastError();
+	}
+	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3(unsigned(p.npairs) * unsigned(cluster));
+	cfg.blockDim = dim3(unsigned(threads));
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = st;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = unsigned(cluster);
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, wsb_kernel<true>, p);
+}
+
+cudaError_t launch_wsb_walk(const WsbWalkParams &p, cudaStream_t st) {
+	if (p.npairs == 0) return cudaSuccess;
+	wsb_walk_kernel<<<(p.npairs + 3) / 4, 128, 0, st>>>(p);
 	return cudaGetLastError();
 }
 
