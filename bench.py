@@ -444,9 +444,13 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
     sw = alg.m16.create_solver(Lw, Lw, alg.m16.create_options(ow))
     resw = sw.solve_indexed_for_alignment(aw, bw, tw, lnw)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    resw = sw.solve_indexed_for_alignment(aw, bw, tw, lnw)
-    t_w = time.perf_counter() - t0
+    calls_w, dp_w = [], []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        resw = sw.solve_indexed_for_alignment(aw, bw, tw, lnw)
+        calls_w.append(time.perf_counter() - t0)
+        dp_w.append(sw.last_timings()[0][1])
+    t_w = float(np.median(calls_w))
     kw = 4
     osw = oracle_solver(oalg, "LOCAL", "ALIGNMENT", LogGap(3.0, 1.0), Lw, Lw)
     osc_w, omp_w, offs_w, _ = oalg.batch_alignments(osw, aw[:kw], bw[:kw], tw, np.full(kw, Lw), np.full(kw, Lw))
@@ -454,11 +458,13 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
     gmp_w = np.concatenate([np.asarray(resw[k].s_to_t, np.int32) for k in range(kw)])
     cells_w = float(Bw * Lw * Lw)
     out["local_log_gap_300x300"] = {
-        "value": cells_w / t_w / 1e9, "unit": "GCUPS", "ms": t_w * 1000,
-        "candidates_per_s": cells_w * (2 * Lw) / t_w, "plan": sw.last_plan(),
+        "value": cells_w / t_w / 1e9, "unit": "GCUPS", "ms": t_w * 1000, "dp_ms": float(np.median(dp_w)),
+        "candidates_per_s": cells_w * (2 * Lw) / t_w,
+        "dp_candidates_per_s": cells_w * (2 * Lw) / (float(np.median(dp_w)) / 1000), "plan": sw.last_plan(),
         "parity": parity_of(kw, osc_w, omp_w, gsc_w, gmp_w),
         "workload": "64 pairs of 300 x 300 DNA (a query and a 15%-substituted copy), local, general gap "
-                    "3 + ln k, score + one alignment, host arrays through the native module"}
+                    "3 + ln k, score + one alignment, host arrays through the native module; median of 5 calls, "
+                    "dp_ms the general-gap kernel's CUDA-event time (a 2-CTA cluster per pair)"}
 
     # all-optimal codomain on the whole bag through the native module's iterator form:
     # one solve writes the 16-bit all-optimal masks of all 256 pairs (25.6 GB, left on the
