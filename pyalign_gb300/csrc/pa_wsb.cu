@@ -14,10 +14,10 @@
 // D is kept in global memory (L2-resident at the sizes this cubic recurrence is used for),
 // twice: row-major and transposed.  Every cell of anti-diagonal d scans d + 2 candidates.
 // The warps of the pair split a diagonal one of two ways:
-//  * a warp per cell (diagonals of at most warp_cells cells per warp): lane l takes
-//    q = l, l + 32, ... -- the vertical scan reads a row of the transposed copy, the
-//    horizontal scan a row of the row-major copy, 32 consecutive words per step, four steps'
-//    loads in flight together -- and two warp reductions combine the lanes.  Per 32 cells of
+//  * a warp per cell (diagonals of at most warp_cells cells per warp): the lanes take the
+//    positions of both scans 32 apart -- the vertical scan reads a row of the transposed
+//    copy, the horizontal scan a row of the row-major copy, 32 consecutive words per step,
+//    four steps of both in flight together -- and two warp reductions combine the lanes.  Per 32 cells of
 //    a warp, lane j loads cell j's similarity and diagonal value before the scans and stores
 //    its result after them.
 //  * a thread per cell (longer diagonals): the threads of a warp hold consecutive cells and
@@ -86,52 +86,52 @@ __device__ __forceinline__ uint32_t wsb_order(float f) {
 	return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
-// the scan positions [qa, qb] of one phase of a warp's scan, `src` and `gap` at position qa:
-// lane l takes qa + l, qa + l + 32, ..., four at a time while whole 128-blocks remain
-// (warp-uniform bounds), then 32 at a time, then the partial block
-template <bool CL>
-__device__ __forceinline__ void wsb_phase(const float *src, const float *gap, int qa, int qb, int lane, float &bv,
-                                          int &bq) {
-	int q = qa;
-	src += lane;
-	gap -= lane;
-	for (; q + 128 <= qb + 1; q += 128, src += 128, gap -= 128) {
-		const float x0 = wsb_ld<CL>(src), x1 = wsb_ld<CL>(src + 32), x2 = wsb_ld<CL>(src + 64),
-		            x3 = wsb_ld<CL>(src + 96);
-		const float g0 = __ldg(gap), g1 = __ldg(gap - 32), g2 = __ldg(gap - 64), g3 = __ldg(gap - 96);
-		const float c0 = x0 + (-g0), c1 = x1 + (-g1), c2 = x2 + (-g2), c3 = x3 + (-g3);
-		if (c0 > bv) { bv = c0; bq = q + lane; }
-		if (c1 > bv) { bv = c1; bq = q + lane + 32; }
-		if (c2 > bv) { bv = c2; bq = q + lane + 64; }
-		if (c3 > bv) { bv = c3; bq = q + lane + 96; }
-	}
-	for (; q + 32 <= qb + 1; q += 32, src += 32, gap -= 32) {
-		const float c = wsb_ld<CL>(src) + (-__ldg(gap));
-		if (c > bv) { bv = c; bq = q + lane; }
-	}
-	if (q + lane <= qb) {
-		const float c = wsb_ld<CL>(src) + (-__ldg(gap));
-		if (c > bv) { bv = c; bq = q + lane; }
-	}
-}
-
-// the scan of cell (u, v) by one warp; every lane returns the scan's first maximum: the
-// largest key by one reduction, the smallest position holding it by another, its value
-// from the lane that scanned that position
+// the scan of cell (u, v) by one warp.  The vertical positions q = p (p = 0..u) and the
+// horizontal ones q = u + 1 + p (p = 0..v) are read in the same batches: lane l takes
+// p = l, l + 32, l + 64, l + 96 of both phases, sixteen loads in flight, and keeps each
+// phase's first maximum (the vertical one wins a tie, coming first).  Every lane returns the
+// scan's first maximum: the largest key by one reduction, the smallest position holding it
+// by another, its value from the lane that scanned that position.
 template <bool CL>
 __device__ __forceinline__ void wsb_scan_warp(const WsbParams &p, const float *D, const float *DT, int64_t ld,
                                               int64_t ldt, int u, int v, int lane, float &bv, int &bq) {
-	bv = -INFINITY;
-	bq = INT_MAX;
-	// vertical, q = k + 1 in [0, u]: D(k, v) = DT[(v + 1) * ldt + q], w_s(u - k) = gap_s[u + 1 - q]
-	wsb_phase<CL>(DT + int64_t(v + 1) * ldt, p.gap_s + (u + 1), 0, u, lane, bv, bq);
-	// horizontal, q = k + u + 2 in [u + 1, u + v + 1]: D(u, k) = D[(u + 1) * ld + q - u - 1],
-	// w_t(v - k) = gap_t[u + v + 2 - q]
-	wsb_phase<CL>(D + int64_t(u + 1) * ld, p.gap_t + (v + 1), u + 1, u + v + 1, lane, bv, bq);
+	// D(p - 1, v) = DT[(v + 1) * ldt + p], w_s(u - k) = gap_s[u + 1 - p]
+	const float *xv = DT + int64_t(v + 1) * ldt + lane, *gv = p.gap_s + (u + 1) - lane;
+	// D(u, p - 1) = D[(u + 1) * ld + p], w_t(v - k) = gap_t[v + 1 - p]
+	const float *xh = D + int64_t(u + 1) * ld + lane, *gh = p.gap_t + (v + 1) - lane;
+	float bvv = -INFINITY, bvh = -INFINITY;
+	int bqv = INT_MAX, bqh = INT_MAX;
+	const int pend = max(u, v);
+	for (int p0 = 0; p0 <= pend; p0 += 128, xv += 128, gv -= 128, xh += 128, gh -= 128) {
+		float a[4], ga[4], b[4], gb[4];
+#pragma unroll
+		for (int r = 0; r < 4; r++) {
+			const int pp = p0 + lane + 32 * r;
+			a[r] = pp <= u ? wsb_ld<CL>(xv + 32 * r) : -INFINITY;
+			ga[r] = pp <= u ? __ldg(gv - 32 * r) : 0.0f;
+			b[r] = pp <= v ? wsb_ld<CL>(xh + 32 * r) : -INFINITY;
+			gb[r] = pp <= v ? __ldg(gh - 32 * r) : 0.0f;
+		}
+#pragma unroll
+		for (int r = 0; r < 4; r++) {
+			const int pp = p0 + lane + 32 * r;
+			const float cv = a[r] + (-ga[r]), ch = b[r] + (-gb[r]);
+			if (cv > bvv) {
+				bvv = cv;
+				bqv = pp;
+			}
+			if (ch > bvh) {
+				bvh = ch;
+				bqh = u + 1 + pp;
+			}
+		}
+	}
+	bv = bvh > bvv ? bvh : bvv;
+	bq = bvh > bvv ? bqh : bqv;
 	const uint32_t key = wsb_order(bv);
 	const uint32_t m = __reduce_max_sync(0xffffffffu, key);
 	const int qw = __reduce_min_sync(0xffffffffu, key == m ? bq : INT_MAX);
-	// the lane that scanned position qw: the phases start at q = 0 and q = u + 1
+	// the lane that scanned position qw: p = qw or qw - u - 1, lane p mod 32
 	bv = __shfl_sync(0xffffffffu, bv, (qw <= u ? qw : qw - u - 1) & 31);
 	bq = qw;
 }
