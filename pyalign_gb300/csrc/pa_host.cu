@@ -159,6 +159,7 @@ struct ResultData {
 	std::vector<int32_t> paths, path_len;
 	std::vector<int64_t> mask_off;
 	std::vector<uint32_t> masks_one;  // TB_ONE words (solutions)
+	bool matrices = false;  // the cell matrices (masks or general-gap codes) are readable
 	// TB_ALL: 4 words per lane-step, left on the device (the result owns the buffer) and
 	// read by the host DFS in 64 KB chunks on demand: the DFS touches the cells near the
 	// optimal paths only, a few MB of masks that can be 16 bytes per cell in total
@@ -2228,12 +2229,14 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	if (tb == TB_ALL && s->gap != GAP_GENERAL) {
 		// the result takes the mask buffer over (the solver allocates a new one next time)
 		res.dev_masks_all = s->d_masks.p;
+		res.matrices = true;
 		res.dev_masks_words = mask_off[size_t(B)] * 4;
 		s->d_masks.p = nullptr;
 		s->d_masks.cap = 0;
 	}
 	if (tb == TB_ONE && want_values && s->gap != GAP_GENERAL) {
 		res.masks_one.resize(size_t(mask_off[size_t(B)]));
+		res.matrices = true;
 		PA_CUDA(pa_copy(s, res.masks_one.data(), s->d_masks.p, res.masks_one.size() * 4, cudaMemcpyDeviceToHost, st));
 	}
 	if (want_values) {
@@ -2243,6 +2246,7 @@ pa_status solve_impl(pa_solver *s, const Input &in, int method, float *scores_ou
 	}
 	if (wsb_host) {
 		if (pa_status e = download_wsb(s, res)) return e;
+		res.matrices = true;
 	}
 	PA_CUDA(cudaEventRecord(s->ev[4], st));
 	PA_CUDA(cudaStreamSynchronize(st));
@@ -2917,7 +2921,7 @@ extern "C" {
 
 pa_status pa_result_tb_matrix(const pa_result *r, int64_t lane, int32_t *tb) {
 	const ResultData &d = *r->d;
-	if (d.gap == GAP_GENERAL && d.wsb_tb.empty()) return fail(PA_ERR_INVALID_ARGUMENT, "no traceback matrix in this result");
+	if (!d.matrices) return fail(PA_ERR_INVALID_ARGUMENT, "no traceback matrix in this result");
 	const int ls = d.ls[size_t(lane)], lt = d.lt[size_t(lane)];
 	const int layers = pa_result_layers(r, lane);
 	for (int layer = 0; layer < layers; layer++) {
@@ -2933,7 +2937,7 @@ pa_status pa_result_tb_matrix(const pa_result *r, int64_t lane, int32_t *tb) {
 
 int64_t pa_result_tb_edges(const pa_result *r, int64_t lane, int32_t layer, int32_t *edges) {
 	const ResultData &d = *r->d;
-	if (d.gap == GAP_GENERAL && d.wsb_tb.empty()) return -1;  // no traceback matrix in this result
+	if (!d.matrices) return -1;  // no traceback matrix in this result
 	int64_t n = 0;
 	for_each_cell_tb(d, lane, layer, [&](int i, int j, const std::vector<std::pair<int, int>> &l) {
 		for (const auto &pt : l) {

@@ -148,3 +148,30 @@ def test_general_gap_batch_entry_writes_maps(gpu_alg, oracle_alg):
     torch.cuda.synchronize()
     assert np.array_equal(sc_d.cpu().numpy(), want_sc)
     assert np.array_equal(mp_d.cpu().numpy(), want_mp)
+
+
+@pytest.mark.parametrize("gap", [Gap("log", 3.0, 1.0), Gap("affine", 5.0, 2.0)])
+def test_alignment_results_refuse_matrix_reads(gpu_alg, gap):
+    """An alignment result keeps no cell matrices (general gaps: walked on the device; other
+    gaps: only the maps come back): the traceback-matrix and value reads are refused with an
+    error instead of reading what was never copied."""
+    import ctypes
+    rng = np.random.default_rng(9)
+    pairs = random_pairs(rng, 3, 20, 40, alphabet=4, related=0.5)
+    a, b, ln = pack(pairs, 3)
+    table = np.full((4, 4), -1.0, np.float32)
+    np.fill_diagonal(table, 2.0)
+    o = dict(options(gpu_alg, locality="local", detail="alignment", gap=gap), batch_size=3, batch=True)
+    solver = gpu_alg.m16.create_solver(a.shape[1], b.shape[1], gpu_alg.m16.create_options(o))
+    r = solver._call("alignment", "indexed", (a, b, table, ln))  # the result object of the C ABI
+    L = gpu_alg.lib()
+    res = r.ptr
+    ls, lt = int(ln[0, 0]), int(ln[1, 0])
+    buf = np.zeros(3 * (ls + 1) * (lt + 1) * 2, np.int32)
+    assert L.pa_result_tb_matrix(res, 0, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))) != 0
+    assert L.pa_result_tb_edges(res, 0, 0, None) == -1
+    vals = np.zeros(3 * (ls + 1) * (lt + 1), np.float32)
+    assert L.pa_result_values(res, 0, vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) != 0
+    mp = np.zeros(min(ls, lt), np.int32)
+    assert L.pa_result_alignment(res, 0, mp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))) == 0  # still usable
+    assert (mp >= -1).all()
