@@ -1138,10 +1138,10 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	w.seed = s->d_seed.as<int32_t>();
 	w.has_seed = s->d_has.as<int32_t>();
 	w.status = s->d_status.as<int32_t>();
-	// a warp per cell on all but the longest diagonals; about four cells per warp on a
-	// pair's longest diagonal, 128 to 1024 threads; a cluster of 4 or 2 CTAs per pair when
-	// the clusters of all pairs fit the SMs at once and the pairs are long enough to keep
-	// them busy (PA_WSB_THREADS, PA_WSB_WARP_CELLS, PA_WSB_CLUSTER: experiments and tests)
+	// about four cells per warp on a pair's longest diagonal, 128 to 1024 threads; a cluster
+	// of 4 or 2 CTAs per pair when the clusters of all pairs fit the SMs at once and the pairs
+	// are long enough to keep them busy (PA_WSB_THREADS, PA_WSB_WARP_CELLS, PA_WSB_CLUSTER:
+	// experiments and tests)
 	int64_t diag = 0;
 	for (int64_t k = 0; k < B; k++) diag = std::max<int64_t>(diag, std::min(ls[size_t(k)], lt[size_t(k)]));
 	int threads = int(std::min<int64_t>(1024, std::max<int64_t>(128, 32 * ((diag + 3) / 4))));
@@ -1154,8 +1154,10 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 		const int c = std::atoi(e);
 		cluster = c >= 4 ? 4 : c >= 2 ? 2 : 1;
 	}
-	w.warp_cells = 64;
-	if (const char *e = std::getenv("PA_WSB_WARP_CELLS")) w.warp_cells = std::max(0, std::atoi(e));
+	// a warp per cell on every diagonal (one thread per cell measured 3.5x slower on pairs of
+	// 1000 x 1000 and only loses more as scans grow); PA_WSB_WARP_CELLS=0 keeps the thread per cell
+	w.warp_cells = 1 << 20;
+	if (const char *e = std::getenv("PA_WSB_WARP_CELLS")) w.warp_cells = std::min(1 << 20, std::max(0, std::atoi(e)));
 	PA_CUDA(launch_wsb(w, threads, cluster, st));
 	(*launches)++;
 	if (maps) {

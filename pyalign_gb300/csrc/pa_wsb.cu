@@ -17,12 +17,13 @@
 //  * a warp per cell (diagonals of at most warp_cells cells per warp): the lanes take the
 //    positions of both scans 32 apart -- the vertical scan reads a row of the transposed
 //    copy, the horizontal scan a row of the row-major copy, 32 consecutive words per step,
-//    four steps of both in flight together -- and two warp reductions combine the lanes.  Per 32 cells of
-//    a warp, lane j loads cell j's similarity and diagonal value before the scans and stores
-//    its result after them.
-//  * a thread per cell (longer diagonals): the threads of a warp hold consecutive cells and
-//    at step k read row k of the row-major copy (vertical scans) or of the transposed copy
-//    (horizontal scans), again 32 consecutive words.
+//    four steps of both in flight together -- and two warp reductions combine the lanes.
+//    Per 32 cells of a warp, lane j loads cell j's similarity and diagonal value before the
+//    scans and stores its result after them.
+//  * a thread per cell (diagonals of more than warp_cells cells per warp; the host keeps the
+//    warp per cell everywhere and this split for tests): the threads of a warp hold
+//    consecutive cells and at step k read row k of the row-major copy (vertical scans) or of
+//    the transposed copy (horizontal scans), again 32 consecutive words.
 // The CTAs of a cluster meet at a cluster barrier (release / acquire) after every diagonal
 // and read the values of D through L2, where the other CTAs' writes are.  The seed scans
 // (solver.h:2035-2058, 2174-2188, 2266-2294) run over the first CTA with a block reduction
@@ -400,6 +401,13 @@ cudaError_t launch_wsb(const WsbParams &p, int threads, int cluster, cudaStream_
 	attr[0].val.clusterDim.z = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
+	// a device (or a share of one) that cannot hold such a cluster gets a CTA per pair
+	int active = 0;
+	if (cudaOccupancyMaxActiveClusters(&active, wsb_kernel<true>, &cfg) != cudaSuccess || active < 1) {
+		cudaGetLastError();
+		wsb_kernel<false><<<p.npairs, threads, 0, st>>>(p);
+		return cudaGetLastError();
+	}
 	return cudaLaunchKernelEx(&cfg, wsb_kernel<true>, p);
 }
 
