@@ -1140,8 +1140,9 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	w.status = s->d_status.as<int32_t>();
 	// about four cells per warp on a pair's longest diagonal, 128 to 1024 threads; a cluster
 	// of 4 or 2 CTAs per pair when the clusters of all pairs fit the SMs at once and the pairs
-	// are long enough to keep them busy (PA_WSB_THREADS, PA_WSB_WARP_CELLS, PA_WSB_CLUSTER:
-	// experiments and tests)
+	// are long enough to keep them busy (pairs of 200 x 200: one CTA 1.84 ms, two 1.99 ms;
+	// 300 x 300: 4.9 and 4.2 ms).  PA_WSB_THREADS, PA_WSB_WARP_CELLS, PA_WSB_CLUSTER:
+	// experiments and tests.
 	int64_t diag = 0;
 	for (int64_t k = 0; k < B; k++) diag = std::max<int64_t>(diag, std::min(ls[size_t(k)], lt[size_t(k)]));
 	int threads = int(std::min<int64_t>(1024, std::max<int64_t>(128, 32 * ((diag + 3) / 4))));
@@ -1149,11 +1150,26 @@ pa_status run_wsb(pa_solver *s, const Input &in, const std::vector<int32_t> &ls,
 	if (const char *e = std::getenv("PA_WSB_THREADS")) threads = std::min(1024, std::max(32, std::atoi(e) / 32 * 32));
 	int cluster = 1;
 	if (B * 4 <= s->sm_count && diag >= 512) cluster = 4;
-	else if (B * 2 <= s->sm_count && diag >= 128) cluster = 2;
-	if (const char *e = std::getenv("PA_WSB_CLUSTER")) {
-		const int c = std::atoi(e);
+	else if (B * 2 <= s->sm_count && diag >= 256) cluster = 2;
+	const char *cenv = std::getenv("PA_WSB_CLUSTER");
+	if (cenv) {
+		const int c = std::atoi(cenv);
 		cluster = c >= 4 ? 4 : c >= 2 ? 2 : 1;
 	}
+	// one CTA per pair: the pair's rows in its shared memory too when they fit 200 KB (3% on
+	// 128 pairs of 200 x 200; the rows of a cluster's pair spread over its CTAs measured slower
+	// than L2).  PA_WSB_SMEM=0: global memory only, for tests.
+	int64_t max_ls = 0, max_lt = 0;
+	for (int64_t k = 0; k < B; k++) {
+		max_ls = std::max<int64_t>(max_ls, ls[size_t(k)]);
+		max_lt = std::max<int64_t>(max_lt, lt[size_t(k)]);
+	}
+	const int64_t lds = (max_lt + 1) | 1;
+	w.lds = 0;
+	w.max_ls = int32_t(max_ls);
+	const char *menv = std::getenv("PA_WSB_SMEM");
+	if (cluster == 1 && !(menv && std::strcmp(menv, "0") == 0) && (max_ls + 1) * lds * 4 <= 200 * 1024)
+		w.lds = int32_t(lds);
 	// a warp per cell on every diagonal (one thread per cell measured 3.5x slower on pairs of
 	// 1000 x 1000 and only loses more as scans grow); PA_WSB_WARP_CELLS=0 keeps the thread per cell
 	w.warp_cells = 1 << 20;

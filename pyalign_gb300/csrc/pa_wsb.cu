@@ -25,7 +25,8 @@
 //    consecutive cells and at step k read row k of the row-major copy (vertical scans) or of
 //    the transposed copy (horizontal scans), again 32 consecutive words.
 // The CTAs of a cluster meet at a cluster barrier (release / acquire) after every diagonal
-// and read the values of D through L2, where the other CTAs' writes are.  The seed scans
+// and read the values of D through L2, where the other CTAs' writes are.  With one CTA per
+// pair and rows that fit (at most 200 KB), the scans read D from a copy in shared memory.  The seed scans
 // (solver.h:2035-2058, 2174-2188, 2266-2294) run over the first CTA with a block reduction
 // that keeps the scan order's winner.
 #include <climits>
@@ -166,7 +167,8 @@ __device__ __forceinline__ void wsb_scan_thread(const WsbParams &p, const float 
 // the cell's result: the head candidates -- (local zero), the diagonal (dprev = D(u-1, v-1))
 // -- then the scan's first maximum (bv at position bq), which replaces the head's only when
 // strictly better
-__device__ __forceinline__ void wsb_store(const WsbParams &p, float *D, float *DT, int32_t *T, float *SUB, int64_t ld,
+template <bool WRITE_DT = true>
+__device__ __forceinline__ float wsb_store(const WsbParams &p, float *D, float *DT, int32_t *T, float *SUB, int64_t ld,
                                           int64_t ldt, int lt, int u, int v, float s, float dprev, float bv, int bq) {
 	const float dg = dprev + s;
 	float best;
@@ -194,13 +196,63 @@ __device__ __forceinline__ void wsb_store(const WsbParams &p, float *D, float *D
 	}
 	SUB[int64_t(u) * lt + v] = s;
 	D[int64_t(u + 1) * ld + (v + 1)] = best;
-	DT[int64_t(v + 1) * ldt + (u + 1)] = best;
+	if (WRITE_DT) DT[int64_t(v + 1) * ldt + (u + 1)] = best;
 	T[int64_t(u) * lt + v] = int32_t(uint32_t(kk + 1) << 2) | kind;
+	return best;
 }
 
-// CL: the pair's CTAs form a cluster (its size from %cluster_nctarank, 2 or 4)
-template <bool CL>
+// The scan of cell (u, v) by one warp with the pair's D in the CTA's shared memory (bordered
+// row i, i.e. D(i - 1, .), at sD[i * lds]): the same lane split and reductions as
+// wsb_scan_warp.  Position p of the vertical scan is col[p * lds] (col: column v + 1), of the
+// horizontal scan row[p] (row: bordered row u + 1).  lds is odd, so the lanes' column reads
+// fall in distinct banks.
+__device__ __forceinline__ void wsb_scan_warp_sm(const WsbParams &p, const float *col, const float *row, int lds,
+                                                 int u, int v, int lane, float &bv, int &bq) {
+	const float *gv = p.gap_s + (u + 1) - lane, *gh = p.gap_t + (v + 1) - lane;
+	float bvv = -INFINITY, bvh = -INFINITY;
+	int bqv = INT_MAX, bqh = INT_MAX;
+	const int pend = max(u, v);
+	for (int p0 = 0; p0 <= pend; p0 += 128, gv -= 128, gh -= 128) {
+		float a[4], ga[4], b[4], gb[4];
+#pragma unroll
+		for (int r = 0; r < 4; r++) {
+			const int pp = p0 + lane + 32 * r;
+			a[r] = pp <= u ? col[pp * lds] : -INFINITY;
+			ga[r] = pp <= u ? __ldg(gv - 32 * r) : 0.0f;
+			b[r] = pp <= v ? row[pp] : -INFINITY;
+			gb[r] = pp <= v ? __ldg(gh - 32 * r) : 0.0f;
+		}
+#pragma unroll
+		for (int r = 0; r < 4; r++) {
+			const int pp = p0 + lane + 32 * r;
+			const float cv = a[r] + (-ga[r]), ch = b[r] + (-gb[r]);
+			if (cv > bvv) {
+				bvv = cv;
+				bqv = pp;
+			}
+			if (ch > bvh) {
+				bvh = ch;
+				bqh = u + 1 + pp;
+			}
+		}
+	}
+	bv = bvh > bvv ? bvh : bvv;
+	bq = bvh > bvv ? bqh : bqv;
+	const uint32_t key = wsb_order(bv);
+	const uint32_t m = __reduce_max_sync(0xffffffffu, key);
+	const int qw = __reduce_min_sync(0xffffffffu, key == m ? bq : INT_MAX);
+	bv = __shfl_sync(0xffffffffu, bv, (qw <= u ? qw : qw - u - 1) & 31);
+	bq = qw;
+}
+
+// CL: the pair's CTAs form a cluster (its size from %cluster_nctarank, 2 or 4).  SM (one CTA
+// per pair): the pair's D is also held in the CTA's shared memory (p.lds floats a row) and the
+// scans read it there; the global copy serves the walk, the seeds and the host.
+template <bool CL, bool SM>
 __global__ void __launch_bounds__(1024) wsb_kernel(WsbParams p) {
+	static_assert(!(CL && SM), "shared-memory rows: one CTA per pair");
+	extern __shared__ float4 wsb_smem4[];
+	float *sD = reinterpret_cast<float *>(wsb_smem4);
 	uint32_t rank = 0, csize = 1;
 	if constexpr (CL) {
 		asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
@@ -214,15 +266,21 @@ __global__ void __launch_bounds__(1024) wsb_kernel(WsbParams p) {
 	int32_t *T = p.tb + p.tb_off[pair];
 	float *SUB = p.sub + p.tb_off[pair];
 	const int64_t ld = lt + 1, ldt = ls + 1;
-	// borders (the first CTA's)
+	const int lds = p.lds;
+	// borders (the first CTA's; in shared memory too with SM)
 	if (rank == 0) {
 		for (int j = threadIdx.x; j <= lt; j += blockDim.x) {
 			D[j] = p.top_D[j];
-			DT[int64_t(j) * ldt] = p.top_D[j];
+			if (SM) sD[j] = p.top_D[j];
+			else DT[int64_t(j) * ldt] = p.top_D[j];
 		}
 		for (int i = threadIdx.x; i <= ls; i += blockDim.x) {
 			D[int64_t(i) * ld] = p.left_D[i];
-			DT[i] = p.left_D[i];
+			if (SM) {
+				if (i > 0) sD[i * lds] = p.left_D[i];
+			} else {
+				DT[i] = p.left_D[i];
+			}
 		}
 	}
 	wsb_sync<CL>();
@@ -234,7 +292,34 @@ __global__ void __launch_bounds__(1024) wsb_kernel(WsbParams p) {
 	for (int d = 0; d <= ls + lt - 2; d++) {
 		const int u0 = max(0, d - (lt - 1)), u1 = min(ls - 1, d);
 		const int ncell = u1 - u0 + 1;
-		if (ncell <= GW * p.warp_cells) {
+		if constexpr (SM) {
+			// the same split as below over the CTA's warps, D read from shared memory
+			const int w = threadIdx.x >> 5;
+			const int nw = ncell > w ? (ncell - w + nwarps - 1) / nwarps : 0;
+			for (int j0 = 0; j0 < nw; j0 += 32) {
+				const bool mine = j0 + lane < nw;
+				const int um = u0 + w + nwarps * (j0 + lane), vm = d - um;
+				float s = 0.0f, dprev = 0.0f, kv = -INFINITY;
+				int kq = INT_MAX;
+				if (mine) {
+					s = wsb_similarity(p, pair, arow, brow, um, vm);
+					dprev = sD[um * lds + vm];
+				}
+				const int jn = min(32, nw - j0);
+				for (int jj = 0; jj < jn; jj++) {  // warp-uniform
+					const int u = u0 + w + nwarps * (j0 + jj), v = d - u;
+					float bv;
+					int bq;
+					wsb_scan_warp_sm(p, sD + (v + 1), sD + (u + 1) * lds, lds, u, v, lane, bv, bq);
+					if (lane == jj) {
+						kv = bv;
+						kq = bq;
+					}
+				}
+				if (mine)
+					sD[(um + 1) * lds + (vm + 1)] = wsb_store<false>(p, D, DT, T, SUB, ld, ldt, lt, um, vm, s, dprev, kv, kq);
+			}
+		} else if (ncell <= GW * p.warp_cells) {
 			// this warp's cells c = gw + GW * j, 32 at a time: lane l loads the similarity and
 			// D(u-1, v-1) of cell j0 + l before the scans and stores its result after them
 			const int nw = ncell > gw ? (ncell - gw + GW - 1) / GW : 0;
@@ -381,18 +466,28 @@ __global__ void __launch_bounds__(128) wsb_walk_kernel(WsbWalkParams p) {
 	}
 }
 
-}  // namespace
+// opens a kernel for `smem` bytes of dynamic shared memory (once per size)
+template <bool CL, bool SM>
+cudaError_t wsb_open(int smem) {
+	static int opened = 0;
+	if (smem <= opened) return cudaSuccess;
+	cudaError_t e = cudaFuncSetAttribute(wsb_kernel<CL, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+	if (e == cudaSuccess) opened = smem;
+	return e;
+}
 
-cudaError_t launch_wsb(const WsbParams &p, int threads, int cluster, cudaStream_t st) {
-	if (p.npairs == 0) return cudaSuccess;
-	if (cluster <= 1) {
-		wsb_kernel<false><<<p.npairs, threads, 0, st>>>(p);
+template <bool SM>
+cudaError_t launch_wsb_as(const WsbParams &p, int threads, int cluster, int smem, cudaStream_t st) {
+	if (SM || cluster <= 1) {
+		if (cudaError_t e = wsb_open<false, SM>(smem)) return e;
+		wsb_kernel<false, SM><<<p.npairs, threads, smem, st>>>(p);
 		return cudaGetLastError();
 	}
+	if (cudaError_t e = wsb_open<true, false>(smem)) return e;
 	cudaLaunchConfig_t cfg{};
 	cfg.gridDim = dim3(unsigned(p.npairs) * unsigned(cluster));
 	cfg.blockDim = dim3(unsigned(threads));
-	cfg.dynamicSmemBytes = 0;
+	cfg.dynamicSmemBytes = size_t(smem);
 	cfg.stream = st;
 	cudaLaunchAttribute attr[1];
 	attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -401,14 +496,23 @@ cudaError_t launch_wsb(const WsbParams &p, int threads, int cluster, cudaStream_
 	attr[0].val.clusterDim.z = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	// a device (or a share of one) that cannot hold such a cluster gets a CTA per pair
 	int active = 0;
-	if (cudaOccupancyMaxActiveClusters(&active, wsb_kernel<true>, &cfg) != cudaSuccess || active < 1) {
+	if (cudaOccupancyMaxActiveClusters(&active, wsb_kernel<true, false>, &cfg) != cudaSuccess || active < 1) {
 		cudaGetLastError();
-		wsb_kernel<false><<<p.npairs, threads, 0, st>>>(p);
-		return cudaGetLastError();
+		return cudaErrorNotSupported;
 	}
-	return cudaLaunchKernelEx(&cfg, wsb_kernel<true>, p);
+	return cudaLaunchKernelEx(&cfg, wsb_kernel<true, false>, p);
+}
+
+}  // namespace
+
+cudaError_t launch_wsb(const WsbParams &p, int threads, int cluster, cudaStream_t st) {
+	if (p.npairs == 0) return cudaSuccess;
+	if (p.lds > 0)  // the pair's rows in the CTA's shared memory: max |s| + 1 rows
+		return launch_wsb_as<true>(p, threads, 1, (p.max_ls + 1) * p.lds * int(sizeof(float)), st);
+	const cudaError_t e = launch_wsb_as<false>(p, threads, cluster, 0, st);
+	if (e != cudaErrorNotSupported) return e;
+	return launch_wsb_as<false>(p, threads, 1, 0, st);  // one CTA per pair
 }
 
 cudaError_t launch_wsb_walk(const WsbWalkParams &p, cudaStream_t st) {

@@ -35,6 +35,8 @@ struct WsbParams {
 	int32_t *has_seed;
 	int32_t *status;
 	int32_t warp_cells;    // a warp per cell on diagonals of at most warp_cells x warps cells
+	int32_t lds;           // > 0 (one CTA per pair): the rows also in shared memory, lds (odd) floats a row
+	int32_t max_ls;        // the launch's largest |s| (sizes that shared memory)
 };
 
 // One optimal alignment per pair from the traceback codes (TracebackIterators<false>,

@@ -175,3 +175,34 @@ def test_alignment_results_refuse_matrix_reads(gpu_alg, gap):
     mp = np.zeros(min(ls, lt), np.int32)
     assert L.pa_result_alignment(res, 0, mp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))) == 0  # still usable
     assert (mp >= -1).all()
+
+
+@pytest.mark.parametrize("form", ["smem_1", "global_1", "global_2", "global_4"])
+@pytest.mark.parametrize("locality", ["local", "global", "semiglobal"])
+def test_general_gap_shared_memory_rows(gpu_alg, oracle_alg, monkeypatch, form, locality):
+    """Pairs of up to 220 x 200, whose rows fit a CTA's shared memory: one CTA with the rows
+    in shared memory (the default for one CTA per pair), one CTA from global memory
+    (PA_WSB_SMEM=0), and clusters of 2 and 4 CTAs (global memory), each against the oracle bit
+    for bit, with |s| > |t| and |s| < |t| pairs and a one-letter query."""
+    kind, c = form.split("_")
+    monkeypatch.setenv("PA_WSB_CLUSTER", c)
+    if kind == "global":
+        monkeypatch.setenv("PA_WSB_SMEM", "0")
+    rng = np.random.default_rng(zlib.crc32(f"wsb-smem/{locality}".encode()))
+    pairs = random_pairs(rng, 10, 90, 200, alphabet=4, related=0.7)
+    pairs[1] = (rng.integers(0, 4, 220).astype(np.uint32), pairs[1][1][:57])
+    pairs[2] = (pairs[2][0][:1], pairs[2][1])
+    n = len(pairs)
+    a, b, ln = pack(pairs, n)
+    table = rng.integers(-3, 4, size=(4, 4)).astype(np.float32)
+    np.fill_diagonal(table, 3.0)
+    o = dict(options(gpu_alg, locality=locality, detail="alignment", gap=Gap("log", 2.0, 1.5)),
+             batch_size=n, batch=True)
+    cap = (a.shape[1], b.shape[1])
+    g = gpu_alg.m16.create_solver(*cap, gpu_alg.m16.create_options(o)).solve_indexed_for_alignment(a, b, table, ln)
+    r = oracle_alg.m16.create_solver(*cap, oracle_alg.m16.create_options(o)).solve_indexed_for_alignment(
+        a, b, table, ln)
+    for k in range(n):
+        assert g[k].score == r[k].score, (k, g[k].score, r[k].score)
+        assert np.array_equal(np.asarray(g[k].s_to_t), np.asarray(r[k].s_to_t)), k
+        assert np.array_equal(np.asarray(g[k].t_to_s), np.asarray(r[k].t_to_s)), k
