@@ -378,7 +378,7 @@ def other_configs(torch, alg, L, seed, allopt_pairs=256):
                 "codomain": types.SimpleNamespace(detail=alg_.Detail.__members__[detail], count=alg_.Count.__members__[count]),
                 "gap_cost": gap}
 
-    import oracle.algorithm as oalg   # the checker of the sampled pairs' results
+    import oracle.algorithm as oalg   # the oracle that checks the sampled pairs' results
 
     # config 1: every pair against the oracle (eq/ne as a 20 x 20 table of the indexed form)
     a1, b1, l1, _ = make_global_linear_64(seed)

@@ -466,9 +466,7 @@ pa_status pa_measure_f32_peak(float *gops, float *ms);
  * complete when the stream is.  The call blocks the calling thread until `stream` has run
  * the check that every code indexes the table (it synchronises `stream` once, after the
  * two index-range kernels, and then queues the DP without waiting for it), so an out-of-
- * range code is reported by the call itself (PA_ERR_INVALID_ARGUMENT).  That wait also
- * means a call cannot be recorded into a CUDA graph: under stream capture it fails with
- * PA_ERR_CUDA (and the capture is invalidated).
+ * range code is reported by the call itself (PA_ERR_INVALID_ARGUMENT).
  * All scratch lives in one static device array of PA_NOALLOC_SCRATCH_BYTES per device
  * (held until the process exits): batch <= PA_NOALLOC_MAX_BATCH, n_s, n_t <=
  * PA_NOALLOC_MAX_LEN and a table of at most 64 x 64; larger sizes are rejected with

@@ -559,7 +559,7 @@ m16 = _IndexModule(16)
 m32 = _IndexModule(32)
 
 
-# --- threaded batch helpers of the checker (indexed form) ---
+# --- threaded batch helpers of the oracle (indexed form) ---
 
 def _batch_args(a, b, ls, lt, table):
     a = np.ascontiguousarray(a, dtype=np.uint32)

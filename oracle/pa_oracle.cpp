@@ -2,7 +2,7 @@
 //
 // A plain scalar C++ restatement of the recurrences, tie rules, seeds, traceback walk,
 // path compression and all-optimal DFS of pyalign's DP core (pyalign/algorithm/solver.h,
-// pyalign 0.4.4).  It is the checker for the CUDA path: only tests/, the smoke check and
+// pyalign 0.4.4).  It checks the CUDA path: only tests/, the smoke check and
 // the CPU-baseline leg of bench.py load it.  Nothing in the product links or calls it.
 //
 // Parity pin: the reference's own known-answer tests (pyalign/tests/*.py) run on this

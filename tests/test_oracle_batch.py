@@ -1,6 +1,6 @@
 """The oracle's threaded batch helpers against its one-pair solver (CPU only).
 
-The checker at full workload sizes uses three batch forms of the oracle: scores and
+Parity checks at full workload sizes use three batch forms of the oracle: scores and
 alignment maps on host threads (batch_alignments), a two-rows-per-layer score for pairs of
 5000 x 10000 cells (batch_scores_lean), and the FP64 twin over float32 matrices
 (batch_f64).  Each must give what the oracle's own per-pair solver gives -- the solver that
