@@ -31,6 +31,7 @@
 // that keeps the scan order's winner.
 #include <climits>
 #include <cmath>
+#include <mutex>
 #include "pa_dp.cuh"
 #include "pa_wsb.h"
 
@@ -466,13 +467,20 @@ __global__ void __launch_bounds__(128) wsb_walk_kernel(WsbWalkParams p) {
 	}
 }
 
-// opens a kernel for `smem` bytes of dynamic shared memory (once per size)
+// opens a kernel for `smem` bytes of dynamic shared memory on the current device (the
+// attribute belongs to the device's copy of the kernel): once per device and larger size,
+// under a lock so that threads solving at once each see an opened kernel
 template <bool CL, bool SM>
 cudaError_t wsb_open(int smem) {
-	static int opened = 0;
-	if (smem <= opened) return cudaSuccess;
-	cudaError_t e = cudaFuncSetAttribute(wsb_kernel<CL, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-	if (e == cudaSuccess) opened = smem;
+	static std::mutex mu;
+	static int opened[64] = {};
+	int dev = 0;
+	if (cudaError_t e = cudaGetDevice(&dev)) return e;
+	const bool known = dev >= 0 && dev < 64;
+	std::lock_guard<std::mutex> lock(mu);
+	if (known && smem <= opened[dev]) return cudaSuccess;
+	const cudaError_t e = cudaFuncSetAttribute(wsb_kernel<CL, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+	if (e == cudaSuccess && known) opened[dev] = smem;
 	return e;
 }
 
