@@ -7,8 +7,10 @@ layer consumes that sequence like the tuple the reference's methods return
 (factory.h:130-193: the shorter side's map is stored, the other one is its inverse, -1
 where unaligned).  `prepare.bag_batches` replaces `ProblemBag.batches`
 (instance.py:230-275): every problem in exactly one batch, each batch's master shape
-covering its members.  These checks need no device: they build the exported arrays by
-hand.
+covering its members.  Options map pyalign's gap costs to the native special cases
+(factory.h:33-90: affine (u, v) flipped to Gotoh's form, linear, none, general vectors,
+per-side dicts).  These checks need no device: they build the exported arrays and the
+gap objects by hand.
 """
 
 import sys
@@ -138,3 +140,71 @@ def test_bag_batches_cover_every_problem_once(fake_instance, batch_size):
         seen.extend(batch.indices)
     assert sorted(seen) == list(range(len(problems)))
     assert list(prepare.bag_batches(types.SimpleNamespace(problems=[]), batch_size)) == []
+
+
+class _Gap:
+    """A gap cost as pyalign.gaps presents it to the native module: to_special_case() and
+    costs(n) (gaps.py:13-17)."""
+
+    def __init__(self, special, costs=None):
+        self._special, self._costs = special, costs
+
+    def to_special_case(self):
+        return dict(self._special)
+
+    def costs(self, n):
+        return self._costs(n)
+
+
+def _options(gap_cost, **extra):
+    d = {"solver": alg.Type.ALIGNMENT, "direction": alg.Direction.MAXIMIZE, "batch": True,
+         "return_dup": False, "locality": alg.Locality.GLOBAL, "gap_cost": gap_cost,
+         "codomain": types.SimpleNamespace(detail=alg.Detail.ALIGNMENT, count=alg.Count.ONE)}
+    d.update(extra)
+    return alg.m16.create_options(d)
+
+
+def test_gap_costs_map_to_the_native_special_cases():
+    # affine (u, v) of w(k) = u + v k becomes Gotoh's (u', v') = (v, u) (factory.h:42-52)
+    o = _options(_Gap({"affine": (3.0, 2.0)}))
+    assert o.gap_s == o.gap_t
+    kind, (ext, opn) = o.gap_s
+    assert kind == "affine" and (float(ext), float(opn)) == (2.0, 3.0)
+    w = alg._general_costs(o.gap_s, 6)
+    assert w.dtype == np.float32 and w.tolist() == [0.0, 5.0, 7.0, 9.0, 11.0, 13.0]
+    # linear, and no gap cost at all (linear 0, factory.h:37-38)
+    o = _options(_Gap({"linear": 1.5}))
+    assert o.gap_s[0] == "linear" and float(o.gap_s[1]) == 1.5
+    assert alg._general_costs(o.gap_s, 4).tolist() == [0.0, 1.5, 3.0, 4.5]
+    o = _options(None)
+    assert o.gap_s[0] == "linear" and float(o.gap_s[1]) == 0.0
+    # a gap cost with no special case is general: its cost vector, length-checked
+    g = _Gap({}, lambda n: np.log(np.arange(n, dtype=np.float64) + 1.0))
+    o = _options(g)
+    assert o.gap_s == ("general", g)
+    np.testing.assert_array_equal(alg._general_costs(o.gap_s, 5), np.log(np.arange(5) + 1.0).astype(np.float32))
+    with pytest.raises(ValueError):
+        alg._general_costs(("general", _Gap({}, lambda n: np.zeros(n + 1))), 5)
+
+
+def test_per_side_gap_costs_and_option_defaults():
+    # a dict gives each side its own cost; a missing side has none (factory.h:70-86)
+    o = _options({"s": _Gap({"linear": 2.0}), "t": _Gap({"affine": (1.0, 0.5)})})
+    assert o.gap_s[0] == "linear" and float(o.gap_s[1]) == 2.0
+    assert o.gap_t[0] == "affine" and tuple(map(float, o.gap_t[1])) == (0.5, 1.0)
+    o = _options({"t": _Gap({"linear": 2.0})})
+    assert o.gap_s[0] == "linear" and float(o.gap_s[1]) == 0.0
+    assert o.remove_dup and o.locality == alg.Locality.GLOBAL and o.index_bits == 16
+    o = _options(None, return_dup=True, batch_size=77)
+    assert not o.remove_dup and o.batch_size == 77
+    d = _options(None).to_dict()
+    del d["locality"]
+    assert alg.m32.create_options(d).locality == alg.Locality.LOCAL
+    assert alg.m32.create_options(d).index_bits == 32
+    # DTW options carry no gap costs and are global, one optimum
+    dtw = alg.m16.create_options({"solver": alg.Type.DTW, "direction": alg.Direction.MINIMIZE,
+                                  "batch": True, "return_dup": False})
+    assert dtw.locality == alg.Locality.GLOBAL and dtw.count == alg.Count.ONE
+    # illegal enum values are refused, as pybind11 refuses them
+    with pytest.raises(ValueError):
+        _options(None, direction=7)
