@@ -99,3 +99,64 @@ def test_result_and_report_entries_check_arguments(libpath):
     widths = (ctypes.c_int32 * 4)(7, 7, 7, 7)
     alg.check(L.pa_solver_last_bucket_widths(solver.handle, widths))
     assert list(widths) == [0, 0, 0, 0]  # no solve yet: one width, reported as zeros
+
+
+_LAYOUT_C = r"""
+#include <stdio.h>
+#include "pyalign_gb300.h"
+#define F(T, f) printf("%s.%s %zu %zu\n", #T, #f, offsetof(T, f), sizeof(((T *)0)->f));
+#define C(x) printf("%s %ld\n", #x, (long)(x));
+int main(void) {
+	printf("pa_options %zu\npa_batch %zu\n", sizeof(pa_options), sizeof(pa_batch));
+	F(pa_options, type) F(pa_options, direction) F(pa_options, detail) F(pa_options, count)
+	F(pa_options, locality) F(pa_options, remove_dup) F(pa_options, batch) F(pa_options, batch_size)
+	F(pa_options, index_bits) F(pa_options, gap_kind) F(pa_options, linear_s) F(pa_options, linear_t)
+	F(pa_options, affine_u_s) F(pa_options, affine_v_s) F(pa_options, affine_u_t) F(pa_options, affine_v_t)
+	F(pa_options, general_s) F(pa_options, general_t)
+	F(pa_batch, form) F(pa_batch, location) F(pa_batch, batch) F(pa_batch, n_s) F(pa_batch, n_t)
+	F(pa_batch, a) F(pa_batch, b) F(pa_batch, sim) F(pa_batch, table) F(pa_batch, table_rows)
+	F(pa_batch, table_cols) F(pa_batch, eq) F(pa_batch, ne) F(pa_batch, length)
+	C(PA_OK) C(PA_ERR_INVALID_ARGUMENT) C(PA_ERR_LENGTH) C(PA_ERR_UNSUPPORTED)
+	C(PA_TYPE_ALIGNMENT) C(PA_TYPE_DTW) C(PA_MINIMIZE) C(PA_MAXIMIZE)
+	C(PA_DETAIL_SCORE) C(PA_DETAIL_ALIGNMENT) C(PA_DETAIL_SOLUTION) C(PA_COUNT_ONE) C(PA_COUNT_ALL)
+	C(PA_LOCAL) C(PA_GLOBAL) C(PA_SEMIGLOBAL)
+	return 0;
+}
+"""
+
+
+def test_python_binding_matches_the_header_layout(tmp_path):
+    """The ctypes structures and constants of the Python binding are the header's: a C
+    program compiled against include/pyalign_gb300.h prints every field's offset and size of
+    pa_options and pa_batch and the enum values, and the binding must agree with each (a
+    drifted field would pass garbage through the C ABI without any error)."""
+    import shutil
+    import subprocess
+    from pyalign_gb300 import algorithm as alg
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text(_LAYOUT_C)
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    c = {}
+    for line in filter(None, out):
+        k, *v = line.split()
+        c[k] = tuple(int(x) for x in v) if len(v) > 1 else int(v[0])
+    for name, cls in (("pa_options", alg._Options), ("pa_batch", alg.Batch)):
+        assert ctypes.sizeof(cls) == c[name], name
+        fields = [f[0] for f in cls._fields_]
+        assert fields == [k.split(".", 1)[1] for k in c if k.startswith(name + ".")], name
+        for f in fields:
+            desc = getattr(cls, f)
+            assert (desc.offset, desc.size) == c[f"{name}.{f}"], (name, f)
+    assert (alg.PA_OK, alg.PA_ERR_INVALID_ARGUMENT, alg.PA_ERR_LENGTH, alg.PA_ERR_UNSUPPORTED) == (
+        c["PA_OK"], c["PA_ERR_INVALID_ARGUMENT"], c["PA_ERR_LENGTH"], c["PA_ERR_UNSUPPORTED"])
+    assert (alg.Type.ALIGNMENT, alg.Type.DTW) == (c["PA_TYPE_ALIGNMENT"], c["PA_TYPE_DTW"])
+    assert (alg.Direction.MINIMIZE, alg.Direction.MAXIMIZE) == (c["PA_MINIMIZE"], c["PA_MAXIMIZE"])
+    assert (alg.Detail.SCORE, alg.Detail.ALIGNMENT, alg.Detail.SOLUTION) == (
+        c["PA_DETAIL_SCORE"], c["PA_DETAIL_ALIGNMENT"], c["PA_DETAIL_SOLUTION"])
+    assert (alg.Count.ONE, alg.Count.ALL) == (c["PA_COUNT_ONE"], c["PA_COUNT_ALL"])
+    assert (alg.Locality.LOCAL, alg.Locality.GLOBAL, alg.Locality.SEMIGLOBAL) == (
+        c["PA_LOCAL"], c["PA_GLOBAL"], c["PA_SEMIGLOBAL"])
