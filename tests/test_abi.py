@@ -160,3 +160,66 @@ def test_python_binding_matches_the_header_layout(tmp_path):
     assert (alg.Count.ONE, alg.Count.ALL) == (c["PA_COUNT_ONE"], c["PA_COUNT_ALL"])
     assert (alg.Locality.LOCAL, alg.Locality.GLOBAL, alg.Locality.SEMIGLOBAL) == (
         c["PA_LOCAL"], c["PA_GLOBAL"], c["PA_SEMIGLOBAL"])
+
+
+def _prototypes():
+    """{name: (return type, [parameter types])} of every function include/*.h declares, each
+    type reduced to 'ptr' or its fixed-width scalar name."""
+    scal = {"int64_t": "i64", "int32_t": "i32", "uint32_t": "u32", "uint64_t": "u64", "float": "f32",
+            "double": "f64", "pa_status": "i32", "void": "void"}
+
+    def kind(decl):
+        decl = decl.strip()
+        if "*" in decl:
+            return "ptr"
+        words = [w for w in re.findall(r"[A-Za-z_][A-Za-z0-9_]*", decl) if w not in ("const", "struct")]
+        return scal[words[0]]
+
+    protos = {}
+    inc = os.path.join(REPO, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        src = re.sub(r"/\*.*?\*/", "", open(os.path.join(inc, f)).read(), flags=re.S)
+        src = re.sub(r"^\s*#.*$", "", src, flags=re.M)
+        for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(pa_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", src):
+            ret, name, params = m.group(1), m.group(2), m.group(3).strip()
+            args = [] if params in ("", "void") else [kind(p) for p in params.split(",")]
+            protos[name] = (kind(ret + (" *" if ret.rstrip().endswith("*") else "")), args)
+    return protos
+
+
+def test_ctypes_prototypes_match_the_header(libpath):
+    """Every argtypes/restype the package's bindings give a C function (algorithm.py,
+    prepare.py, autograd.py) agrees with its declaration in include/*.h, parameter by
+    parameter: a pointer where the header has a pointer, the same fixed-width scalar
+    elsewhere, and a return type that does not truncate (int64 results, float, strings)."""
+    pytest.importorskip("torch")
+    from pyalign_gb300 import algorithm as alg
+    from pyalign_gb300 import autograd as ag
+    from pyalign_gb300 import prepare
+    L = alg.lib()
+    prepare._lib()
+    ag._lib()
+    protos = _prototypes()
+    assert len(protos) == len(_declared())
+
+    def kind(t):
+        if t is None:
+            return "i32"     # ctypes' default int return
+        if t in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(t, ctypes._Pointer):
+            return "ptr"
+        return {ctypes.c_int64: "i64", ctypes.c_int32: "i32", ctypes.c_uint32: "u32",
+                ctypes.c_uint64: "u64", ctypes.c_float: "f32", ctypes.c_double: "f64"}[t]
+
+    checked = 0
+    for name, (ret, args) in sorted(protos.items()):
+        fn = getattr(L, name)
+        at = getattr(fn, "argtypes", None)
+        if at is None and args:
+            continue         # not bound by the package (diagnostics, the allocation-free entry)
+        assert [kind(t) for t in (at or [])] == args, name
+        if ret != "void":
+            assert kind(fn.restype) == ret, (name, ret)
+        checked += 1
+    assert checked >= 55
