@@ -45,14 +45,17 @@ def gather_results(index, scores, maps, map_sizes, n, group=None):
     world = dist.get_world_size(group)
     parts = [None] * world
     dist.all_gather_object(parts, part, group=group)
-    all_scores = np.zeros(n, dtype=np.asarray(scores).dtype)
+    # element types from the ranks that solved pairs (a rank with none may pass empty lists)
+    dt_s = [p[1].dtype for p in parts if p[1].size] or [part[1].dtype]
+    dt_m = [p[2].dtype for p in parts if p[2].size] or [part[2].dtype]
+    all_scores = np.zeros(n, dtype=np.result_type(*dt_s))
     sizes = np.zeros(n, dtype=np.int64)
     for idx, _, _, ms in parts:
         sizes[idx] = ms
     offs = np.zeros(n, dtype=np.int64)
     if n > 1:
         np.cumsum(sizes[:-1], out=offs[1:])
-    all_maps = np.zeros(int(sizes.sum()), dtype=np.asarray(maps).dtype)
+    all_maps = np.zeros(int(sizes.sum()), dtype=np.result_type(*dt_m))
     seen = np.zeros(n, dtype=bool)
     for idx, sc, mp, ms in parts:
         if seen[idx].any():

@@ -1,7 +1,7 @@
-"""One bag over several ranks (CPU, torch.distributed gloo, world size 2).
+"""One bag over several ranks (CPU, torch.distributed gloo, world sizes 2 and 3).
 
 shard_pairs splits a bag by cells with no communication and gather_results puts every
-rank's scores and maps back in bag order.  Here two gloo ranks each solve their share of a
+rank's scores and maps back in bag order.  Here gloo ranks each solve their share of a
 bag of small pairs with the oracle (standing in for each rank's GPU) and the gathered
 results must equal the oracle's solve of the whole bag; the split itself must cover every
 pair once and balance the cells.
@@ -55,7 +55,7 @@ def test_split_covers_every_pair_once_and_balances_cells():
         shard_pairs(ls, lt, 2, 2)
 
 
-def _rank(rank, world, port, out):
+def _rank(rank, world, port, out, n):
     import sys
     sys.path.insert(0, os.path.dirname(__file__))
     import torch.distributed as dist
@@ -63,31 +63,40 @@ def _rank(rank, world, port, out):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        a, b, ls, lt, table = _bag()
+        a, b, ls, lt, table = _bag(n=n)
         idx = shard_pairs(ls, lt, world, rank)
-        sc, mp_, sizes = _oracle_solve(a[idx], b[idx], ls[idx], lt[idx], table)
+        if len(idx):
+            sc, mp_, sizes = _oracle_solve(a[idx], b[idx], ls[idx], lt[idx], table)
+        else:
+            sc, mp_, sizes = [], [], []   # a rank with no pairs (more ranks than pairs)
         all_sc, all_mp, offs = gather_results(idx, sc, mp_, sizes, len(ls))
-        out.put((rank, all_sc, all_mp, offs))
+        out.put((rank, len(idx), all_sc, all_mp, offs))
     finally:
         dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_gather_the_whole_bag():
+@pytest.mark.parametrize("world,n", [(2, 57), (3, 2)])
+def test_gloo_ranks_gather_the_whole_bag(world, n):
+    """Two ranks over 57 pairs, and three ranks over 2 pairs (one rank solves nothing and
+    passes empty lists): every rank ends with the whole bag's results in bag order."""
     pytest.importorskip("torch")
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
         port = s.getsockname()[1]
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank, args=(r, world, port, q, n)) for r in range(world)]
     for p in procs:
         p.start()
     got = [q.get(timeout=120) for _ in procs]
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    a, b, ls, lt, table = _bag()
-    want_sc, want_mp, _ = _oracle_solve(a, b, ls, lt, table)
-    for rank, sc, mp_, offs in got:
+    a, b, ls, lt, table = _bag(n=n)
+    want_sc, want_mp, want_sizes = _oracle_solve(a, b, ls, lt, table)
+    assert sum(k for _, k, _, _, _ in got) == n
+    for rank, _, sc, mp_, offs in got:
+        assert sc.dtype == want_sc.dtype and mp_.dtype == want_mp.dtype, rank
         assert np.array_equal(sc, want_sc), rank
         assert np.array_equal(mp_, want_mp), rank
+        assert np.array_equal(offs, np.concatenate([[0], np.cumsum(want_sizes)[:-1]])), rank
